@@ -1,0 +1,153 @@
+/*
+ * jaxabm_gb300 — C ABI of the GB300 agent-step engine.
+ *
+ * Every entry point:
+ *   - returns an int status (ABM_OK = 0, else one of the ABM_ERR_* codes below);
+ *   - takes a `void* stream` that is a cudaStream_t (NULL = legacy default stream);
+ *   - borrows the device pointers it is given for the duration of the call (work is
+ *     enqueued on `stream`; the caller keeps the buffers alive until the stream has
+ *     finished it) and keeps no pointer after return;
+ *   - allocates no device memory: scratch comes from a caller-provided workspace whose
+ *     size the matching *_workspace_bytes() query returns.
+ *
+ * PRNG keys are uint32 pairs in device memory, laid out exactly like a JAX raw key
+ * (`jax.random.PRNGKey(seed)` = [seed >> 32, seed & 0xffffffff]).
+ * `mode` selects the `jax_threefry_partitionable` behaviour: ABM_RNG_PARTITIONABLE (the
+ * JAX >= 0.5 default) or ABM_RNG_LEGACY (the original mode).  Model kernels use the
+ * partitionable mode.
+ *
+ * Reference interfaces are cited as path:line inside the JaxABM 0.1.5 source tree.
+ */
+#ifndef JAXABM_GB300_H
+#define JAXABM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ABM_API __attribute__((visibility("default")))
+#else
+#define ABM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define ABM_OK 0
+#define ABM_ERR_BADARG 1       /* null pointer, non-positive size, bad mode, misalignment */
+#define ABM_ERR_OOM 2          /* request does not fit the free device memory            */
+#define ABM_ERR_TIMEOUT 3      /* a bounded device-side wait ran out                      */
+#define ABM_ERR_BOUNDS 4       /* a checked gather/scatter index was out of range         */
+#define ABM_ERR_UNREGISTERED 5 /* no step kernel registered for the agent class           */
+#define ABM_ERR_CUDA 6         /* a CUDA runtime call or kernel launch failed             */
+#define ABM_ERR_WORKSPACE 7    /* caller workspace is null or smaller than required       */
+
+#define ABM_RNG_LEGACY 0
+#define ABM_RNG_PARTITIONABLE 1
+
+/* Library version (major*10000 + minor*100 + patch). */
+ABM_API int abm_version(void);
+
+/* Static string naming a status code. */
+ABM_API const char* abm_status_string(int status);
+
+/* Text of the last CUDA error seen by the library on this host thread ("" if none). */
+ABM_API const char* abm_last_cuda_error(void);
+
+/* SM count and compute capability of the current device. */
+ABM_API int abm_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* ---- K1: threefry2x32-20 and jax.random -------------------------------------------- */
+
+/* vmap(lambda k: jax.random.split(k, num))(keys): keys uint32[nkeys][2] ->
+ * out uint32[nkeys][num][2].  Replaces jax.random.split at jaxabm/model.py:129,156,164,183
+ * and jaxabm/agent.py:115,156. */
+ABM_API int abm_rng_split(const uint32_t* keys, int64_t nkeys, int64_t num, uint32_t* out, int mode,
+                  void* stream);
+
+/* vmap(lambda k: jax.random.bits(k, (count,), uint32))(keys) -> out uint32[nkeys][count]. */
+ABM_API int abm_rng_bits(const uint32_t* keys, int64_t nkeys, int64_t count, uint32_t* out, int mode,
+                 void* stream);
+
+/* vmap(lambda k: jax.random.uniform(k, (count,), float32, minval, maxval))(keys). */
+ABM_API int abm_rng_uniform(const uint32_t* keys, int64_t nkeys, int64_t count, float minval,
+                    float maxval, float* out, int mode, void* stream);
+
+/* vmap(lambda k: jax.random.normal(k, (count,), float32))(keys).  The inverse error
+ * function is Giles' single-precision approximation (GPU Computing Gems, 2011). */
+ABM_API int abm_rng_normal(const uint32_t* keys, int64_t nkeys, int64_t count, float* out, int mode,
+                   void* stream);
+
+/* vmap(lambda k: jax.random.bernoulli(k, p, (count,)))(keys) -> out uint8 0/1. */
+ABM_API int abm_rng_bernoulli(const uint32_t* keys, int64_t nkeys, int64_t count, float p,
+                      uint8_t* out, int mode, void* stream);
+
+/* vmap(lambda k: jax.random.randint(k, (count,), minval, maxval, int32))(keys): two bit
+ * draws from split(key) combined modulo the span, as jax.random.randint does.  Used by
+ * Grid.position_agents (jaxabm/agentpy.py:509-512). */
+ABM_API int abm_rng_randint(const uint32_t* keys, int64_t nkeys, int64_t count, int32_t minval,
+                            int32_t maxval, int32_t* out, int mode, void* stream);
+
+/* Key chain of Model.step (jaxabm/model.py:155-190) for `steps` steps of `ninst`
+ * independent models with `ncoll` agent collections each:
+ *   rng, step_key = split(rng); for c: step_key, coll_key[c] = split(step_key)
+ * rng uint32[ninst][2] is read and overwritten with the advanced key;
+ * coll_keys uint32[ninst][steps][ncoll][2] receives the per-step collection keys and
+ * update_keys (nullable) uint32[ninst][steps][2] the key handed to update_state_fn
+ * (split(step_key)[1] after the collections, jaxabm/model.py:183).
+ * Partitionable mode. */
+ABM_API int abm_keychain(uint32_t* rng, int64_t ninst, int32_t ncoll, int32_t steps,
+                         uint32_t* coll_keys, uint32_t* update_keys, void* stream);
+
+/* ---- random walk (quick-start model) ----------------------------------------------- */
+/* Agent init: agent_key_i = split(init_key, n)[i]; kx, ky = split(agent_key_i);
+ * x_i = uniform(kx), y_i = uniform(ky).  Replaces AgentCollection.init
+ * (jaxabm/agent.py:92-130) for the random-walk agent. */
+ABM_API int abm_randomwalk_init(float* x, float* y, int64_t n, const uint32_t* init_key, void* stream);
+
+ABM_API size_t abm_randomwalk_workspace_bytes(int64_t n, int32_t steps);
+
+/* `steps` synchronous steps of the random walk: for step t with collection key
+ * coll_keys[t] (uint32[steps][2], as written by abm_keychain with ncoll = 1):
+ *   agent_key_i = split(coll_key, n)[i]; kx, ky = split(agent_key_i);
+ *   x_i = (x_i + sigma * normal(kx)) mod 1.0; y_i likewise with ky;
+ *   means[t] = (mean x, mean y) after the update (float32[steps][2]).
+ * Replaces the Python loop of JaxModel.run (jaxabm/model.py:240-241) over
+ * AgentCollection.update (jaxabm/agent.py:132-179) and the metrics reduction
+ * (jaxabm/model.py:193-200). */
+ABM_API int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* coll_keys, int32_t steps,
+                       float sigma, float* means, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* ---- K6: stable compaction (AgentList.select / AgentCollection.filter) -------------- */
+ABM_API size_t abm_select_workspace_bytes(int64_t n);
+
+/* Indices i (ascending) with mask[i] != 0 -> out_idx int32[n]; *count (device int64)
+ * receives how many.  Replaces `int(jnp.sum(mask))` and the boolean-mask gather of
+ * AgentCollection.filter (jaxabm/agent.py:227-242) / AgentList.select
+ * (jaxabm/agentpy.py:316-345).  n <= 2^31 - 1. */
+ABM_API int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t* count,
+                               void* workspace, size_t workspace_bytes, void* stream);
+
+/* dst[r] = src[idx[r]] for `count` rows of `row_bytes` bytes (the per-attribute
+ * `v[mask]` of jaxabm/agent.py:242). */
+ABM_API int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes,
+                            const int32_t* idx, int64_t count, void* dst, void* stream);
+
+/* ---- K7: reductions (AgentCollection.aggregate, jaxabm/agent.py:198-211) ------------ */
+#define ABM_REDUCE_SUM 0
+#define ABM_REDUCE_MEAN 1
+#define ABM_REDUCE_MIN 2
+#define ABM_REDUCE_MAX 3
+ABM_API size_t abm_reduce_workspace_bytes(int64_t n);
+/* *out (device float) = op over x[0..n); sums accumulate in float64. */
+ABM_API int abm_reduce_f32(const float* x, int64_t n, int op, float* out, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JAXABM_GB300_H */

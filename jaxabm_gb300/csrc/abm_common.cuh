@@ -1,0 +1,161 @@
+// Shared device helpers: threefry2x32-20, jax.random key derivation and sampling,
+// launch/status plumbing.  All kernels of the library include this header.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/jaxabm_gb300.h"
+
+namespace abm {
+
+constexpr uint32_t kThreefryParity = 0x1BD11BDAu;
+
+// Threefry-2x32 with 20 rounds (Salmon et al., SC'11 / Random123): rotation schedule
+// 13,15,26,6 then 17,29,16,24, key injection after every fourth round.
+#define ABM_TF_ROUND(r)                  \
+  x0 += x1;                              \
+  x1 = __funnelshift_l(x1, x1, (r));     \
+  x1 ^= x0;
+
+__device__ __forceinline__ uint2 threefry(uint2 key, uint32_t c0, uint32_t c1) {
+  const uint32_t ks0 = key.x, ks1 = key.y, ks2 = key.x ^ key.y ^ kThreefryParity;
+  uint32_t x0 = c0 + ks0, x1 = c1 + ks1;
+  ABM_TF_ROUND(13) ABM_TF_ROUND(15) ABM_TF_ROUND(26) ABM_TF_ROUND(6)
+  x0 += ks1; x1 += ks2 + 1u;
+  ABM_TF_ROUND(17) ABM_TF_ROUND(29) ABM_TF_ROUND(16) ABM_TF_ROUND(24)
+  x0 += ks2; x1 += ks0 + 2u;
+  ABM_TF_ROUND(13) ABM_TF_ROUND(15) ABM_TF_ROUND(26) ABM_TF_ROUND(6)
+  x0 += ks0; x1 += ks1 + 3u;
+  ABM_TF_ROUND(17) ABM_TF_ROUND(29) ABM_TF_ROUND(16) ABM_TF_ROUND(24)
+  x0 += ks1; x1 += ks2 + 4u;
+  ABM_TF_ROUND(13) ABM_TF_ROUND(15) ABM_TF_ROUND(26) ABM_TF_ROUND(6)
+  x0 += ks2; x1 += ks0 + 5u;
+  return make_uint2(x0, x1);
+}
+#undef ABM_TF_ROUND
+
+// ---- partitionable-mode jax.random (JAX >= 0.5 default) ---------------------------
+// split(key, n)[i] = threefry(key, (hi(i), lo(i)))
+__device__ __forceinline__ uint2 split_at(uint2 key, uint64_t i) {
+  return threefry(key, (uint32_t)(i >> 32), (uint32_t)i);
+}
+// bits(key, shape)[i] = y0 ^ y1 of threefry(key, (hi(i), lo(i)))
+__device__ __forceinline__ uint32_t bits_at(uint2 key, uint64_t i) {
+  uint2 y = threefry(key, (uint32_t)(i >> 32), (uint32_t)i);
+  return y.x ^ y.y;
+}
+
+// ---- legacy-mode jax.random --------------------------------------------------------
+// threefry_2x32(key, iota(m)) with the counter array zero-padded to even length and its
+// first half paired with its second half; element j of the concatenated output.
+__device__ __forceinline__ uint32_t legacy_word(uint2 key, uint64_t m, uint64_t j) {
+  const uint64_t padded = m + (m & 1u);
+  const uint64_t h = padded >> 1;
+  const bool second = j >= h;
+  const uint64_t p = second ? j - h : j;       // pair index
+  const uint32_t c0 = (uint32_t)p;              // counters are iota values (pad = 0)
+  const uint64_t hi_idx = p + h;
+  const uint32_t c1 = hi_idx < m ? (uint32_t)hi_idx : 0u;
+  uint2 y = threefry(key, c0, c1);
+  return second ? y.y : y.x;
+}
+__device__ __forceinline__ uint2 legacy_split_at(uint2 key, uint64_t num, uint64_t i) {
+  const uint64_t m = 2 * num;
+  return make_uint2(legacy_word(key, m, 2 * i), legacy_word(key, m, 2 * i + 1));
+}
+__device__ __forceinline__ uint32_t legacy_bits_at(uint2 key, uint64_t count, uint64_t i) {
+  return legacy_word(key, count, i);
+}
+
+// ---- float conversions (exactly jax.random._uniform) -------------------------------
+// top 23 bits as the mantissa of a float in [1, 2), minus one: exactly k * 2^-23.
+__device__ __forceinline__ float unit_float(uint32_t b) {
+  return __uint_as_float((b >> 9) | 0x3F800000u) - 1.0f;
+}
+__device__ __forceinline__ float uniform_from_bits(uint32_t b, float lo, float hi) {
+  const float span = __fsub_rn(hi, lo);
+  const float v = __fadd_rn(__fmul_rn(unit_float(b), span), lo);
+  return fmaxf(lo, v);
+}
+
+// Inverse error function: Giles, "Approximating the erfinv function" (GPU Computing
+// Gems Jade, 2011), single-precision variant with w = -log1p(-x^2).
+__device__ __forceinline__ float erfinv_giles(float x) {
+  float w = -log1pf(-__fmul_rn(x, x));
+  float p;
+  if (w < 5.0f) {
+    w = w - 2.5f;
+    p = 2.81022636e-08f;
+    p = fmaf(p, w, 3.43273939e-07f);
+    p = fmaf(p, w, -3.5233877e-06f);
+    p = fmaf(p, w, -4.39150654e-06f);
+    p = fmaf(p, w, 0.00021858087f);
+    p = fmaf(p, w, -0.00125372503f);
+    p = fmaf(p, w, -0.00417768164f);
+    p = fmaf(p, w, 0.246640727f);
+    p = fmaf(p, w, 1.50140941f);
+  } else {
+    w = sqrtf(w) - 3.0f;
+    p = -0.000200214257f;
+    p = fmaf(p, w, 0.000100950558f);
+    p = fmaf(p, w, 0.00134934322f);
+    p = fmaf(p, w, -0.00367342844f);
+    p = fmaf(p, w, 0.00573950773f);
+    p = fmaf(p, w, -0.0076224613f);
+    p = fmaf(p, w, 0.00943887047f);
+    p = fmaf(p, w, 1.00167406f);
+    p = fmaf(p, w, 2.83297682f);
+  }
+  return p * x;
+}
+
+// nextafter(-1.0f, 0.0f)
+constexpr float kNormalLo = -0.99999994039535522461f;
+constexpr float kSqrt2 = 1.41421353816986083984f;  // float32(sqrt(2))
+
+__device__ __forceinline__ float normal_from_bits(uint32_t b) {
+  const float u = uniform_from_bits(b, kNormalLo, 1.0f);
+  return __fmul_rn(kSqrt2, erfinv_giles(u));
+}
+
+__device__ __forceinline__ uint2 load_key(const uint32_t* p) {
+  return make_uint2(p[0], p[1]);
+}
+
+// jnp.remainder(x, 1.0) for float32: truncated fmod, shifted into [0, 1) when negative
+// (the +1 can round to exactly 1.0 for tiny negative remainders, as in JAX).
+__device__ __forceinline__ float mod1(float v) {
+  float r = fmodf(v, 1.0f);
+  if (r != 0.0f && r < 0.0f) r = __fadd_rn(r, 1.0f);
+  return r;
+}
+
+// ---- warp / block reductions (fixed order => deterministic) ------------------------
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace abm
+
+// ---- host-side helpers --------------------------------------------------------------
+namespace abm_host {
+// Records the last CUDA error for abm_last_cuda_error(); returns ABM_ERR_CUDA or ABM_OK.
+int check_launch(const char* where);
+int record_cuda_error(cudaError_t e, const char* where);
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+int sm_count();
+inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+}  // namespace abm_host

@@ -1,0 +1,147 @@
+// Random-walk model (the quick-start agent with jax.random noise).
+//
+// Per agent and step (partitionable jax.random):
+//   agent_key = split(coll_key, n)[i]; kx, ky = split(agent_key)
+//   x = (x + sigma * normal(kx)) % 1.0 ; y likewise with ky
+// followed by the metrics reduction mean(x), mean(y).
+//
+// Replaces JaxModel.run's Python loop (jaxabm/model.py:240-241) over
+// AgentCollection.update (jaxabm/agent.py:156-177) and metrics_fn (jaxabm/model.py:193-200).
+// The whole run is one launch: agents are independent between steps, so every thread keeps
+// its agent's (x, y) in registers for all steps and only the per-step reductions leave it.
+
+#include "abm_common.cuh"
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kWarps = kBlock / 32;
+constexpr int kChunk = 64;  // steps whose keys / warp sums are staged in shared memory
+
+__global__ void __launch_bounds__(kBlock) rw_init_kernel(float* __restrict__ x,
+                                                         float* __restrict__ y, int64_t n,
+                                                         const uint32_t* __restrict__ init_key) {
+  const uint2 key = abm::load_key(init_key);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 ak = abm::split_at(key, (uint64_t)i);
+    const uint2 kx = abm::split_at(ak, 0), ky = abm::split_at(ak, 1);
+    x[i] = abm::unit_float(abm::bits_at(kx, 0));
+    y[i] = abm::unit_float(abm::bits_at(ky, 0));
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) rw_run_kernel(float* __restrict__ x,
+                                                        float* __restrict__ y, int64_t n,
+                                                        const uint32_t* __restrict__ coll_keys,
+                                                        int32_t steps, float sigma,
+                                                        float2* __restrict__ partial) {
+  __shared__ uint2 skeys[kChunk];
+  __shared__ float2 swarp[kChunk][kWarps];
+  const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
+  const bool active = i < n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float xi = active ? x[i] : 0.f;
+  float yi = active ? y[i] : 0.f;
+  for (int32_t t0 = 0; t0 < steps; t0 += kChunk) {
+    const int nt = min(kChunk, steps - t0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nt; k += kBlock) skeys[k] = abm::load_key(coll_keys + 2 * (int64_t)(t0 + k));
+    __syncthreads();
+#pragma unroll 2
+    for (int k = 0; k < nt; ++k) {
+      const uint2 ak = abm::split_at(skeys[k], (uint64_t)i);
+      const uint2 kx = abm::split_at(ak, 0), ky = abm::split_at(ak, 1);
+      const float nx = abm::normal_from_bits(abm::bits_at(kx, 0));
+      const float ny = abm::normal_from_bits(abm::bits_at(ky, 0));
+      xi = abm::mod1(__fadd_rn(xi, __fmul_rn(sigma, nx)));
+      yi = abm::mod1(__fadd_rn(yi, __fmul_rn(sigma, ny)));
+      const float sx = abm::warp_sum(active ? xi : 0.f);
+      const float sy = abm::warp_sum(active ? yi : 0.f);
+      if (lane == 0) swarp[k][warp] = make_float2(sx, sy);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nt; k += kBlock) {
+      float sx = 0.f, sy = 0.f;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        sx += swarp[k][w].x;
+        sy += swarp[k][w].y;
+      }
+      partial[(int64_t)(t0 + k) * gridDim.x + blockIdx.x] = make_float2(sx, sy);
+    }
+  }
+  if (active) {
+    x[i] = xi;
+    y[i] = yi;
+  }
+}
+
+// means[t] = (sum_b partial[t][b]) / n, one block per step, fixed reduction tree.
+__global__ void rw_means_kernel(const float2* __restrict__ partial, int nblocks, int64_t n,
+                                float2* __restrict__ means) {
+  __shared__ float2 s[kBlock];
+  const int t = blockIdx.x;
+  float sx = 0.f, sy = 0.f;
+  for (int b = threadIdx.x; b < nblocks; b += kBlock) {
+    const float2 p = partial[(int64_t)t * nblocks + b];
+    sx += p.x;
+    sy += p.y;
+  }
+  s[threadIdx.x] = make_float2(sx, sy);
+  __syncthreads();
+  for (int o = kBlock / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s[threadIdx.x].x += s[threadIdx.x + o].x;
+      s[threadIdx.x].y += s[threadIdx.x + o].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float fn = (float)n;
+    means[t] = make_float2(s[0].x / fn, s[0].y / fn);
+  }
+}
+
+int64_t rw_blocks(int64_t n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+extern "C" {
+
+int abm_randomwalk_init(float* x, float* y, int64_t n, const uint32_t* init_key, void* stream) {
+  if (!x || !y || !init_key || n <= 0) return ABM_ERR_BADARG;
+  int64_t blocks = rw_blocks(n);
+  const int64_t cap = (int64_t)abm_host::sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  rw_init_kernel<<<(unsigned)blocks, kBlock, 0, abm_host::as_stream(stream)>>>(x, y, n, init_key);
+  return abm_host::check_launch("abm_randomwalk_init");
+}
+
+size_t abm_randomwalk_workspace_bytes(int64_t n, int32_t steps) {
+  if (n <= 0 || steps <= 0) return 0;
+  return (size_t)rw_blocks(n) * (size_t)steps * sizeof(float2);
+}
+
+int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* coll_keys, int32_t steps,
+                       float sigma, float* means, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  if (!x || !y || !coll_keys || !means || n <= 0 || steps < 0) return ABM_ERR_BADARG;
+  if (!abm_host::aligned(means, 8)) return ABM_ERR_BADARG;
+  if (steps == 0) return ABM_OK;
+  const int64_t blocks = rw_blocks(n);
+  if (blocks > 0x7FFFFFFF) return ABM_ERR_BADARG;
+  const size_t need = abm_randomwalk_workspace_bytes(n, steps);
+  if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 8))
+    return ABM_ERR_WORKSPACE;
+  cudaStream_t s = abm_host::as_stream(stream);
+  float2* partial = static_cast<float2*>(workspace);
+  rw_run_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(x, y, n, coll_keys, steps, sigma, partial);
+  int st = abm_host::check_launch("abm_randomwalk_run");
+  if (st) return st;
+  rw_means_kernel<<<(unsigned)steps, kBlock, 0, s>>>(partial, (int)blocks, n,
+                                                     reinterpret_cast<float2*>(means));
+  return abm_host::check_launch("abm_randomwalk_means");
+}
+
+}  // extern "C"

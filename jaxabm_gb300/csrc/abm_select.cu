@@ -1,0 +1,265 @@
+// K6: stable stream compaction of a boolean mask (AgentCollection.filter / AgentList.select)
+// and K7-style single-pass reductions for AgentCollection.aggregate.
+//
+// Replaces `int(jnp.sum(mask))` + `{k: v[mask]}` at jaxabm/agent.py:227-242 and
+// jaxabm/agentpy.py:330-343, and `jnp.mean(states[var])` at jaxabm/agent.py:198-211.
+//
+// Compaction is three launches over tiles of 4096 mask bytes (one 128-bit load per thread
+// per 16 bytes): (1) per-tile counts, (2) one-block exclusive scan of the tile counts,
+// (3) per-tile rank = tile offset + warp offset + lane prefix (warp shuffles) + position
+// inside the thread's 16 bytes, so output order is ascending index order.
+
+#include "abm_common.cuh"
+
+namespace {
+
+constexpr int kSelThreads = 256;
+constexpr int kSelPerThread = 16;
+constexpr int kTile = kSelThreads * kSelPerThread;  // 4096 mask bytes per block
+
+// 16 mask bytes of thread `tid` in tile `tile` (bytes past n read as 0).
+__device__ __forceinline__ uint32_t load_flags(const uint8_t* __restrict__ mask, int64_t n,
+                                               int64_t base, bool vec_ok) {
+  uint32_t bits = 0;
+  if (vec_ok && base + kSelPerThread <= n) {
+    const uint4 v = *reinterpret_cast<const uint4*>(mask + base);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if ((w[q] >> (8 * b)) & 0xFFu) bits |= 1u << (4 * q + b);
+  } else {
+#pragma unroll
+    for (int j = 0; j < kSelPerThread; ++j)
+      if (base + j < n && mask[base + j]) bits |= 1u << j;
+  }
+  return bits;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+select_count_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
+                    int32_t* __restrict__ tile_counts) {
+  __shared__ int swarp[kSelThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kSelPerThread;
+  const int c = __popc(load_flags(mask, n, base, vec_ok));
+  const int wsum = abm::warp_sum(c);
+  if ((threadIdx.x & 31) == 0) swarp[threadIdx.x >> 5] = wsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kSelThreads / 32; ++w) s += swarp[w];
+    tile_counts[blockIdx.x] = s;
+  }
+}
+
+// Single block: exclusive scan of tile_counts into tile_offsets (int64), total -> *count.
+__global__ void __launch_bounds__(1024)
+select_scan_kernel(const int32_t* __restrict__ tile_counts, int64_t ntiles,
+                   int64_t* __restrict__ tile_offsets, int64_t* __restrict__ count) {
+  __shared__ int64_t swarp[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t b0 = 0; b0 < ntiles; b0 += 1024) {
+    const int64_t b = b0 + threadIdx.x;
+    const int64_t v = b < ntiles ? tile_counts[b] : 0;
+    int64_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) swarp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = swarp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t u = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += u;
+      }
+      swarp[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int64_t warp_excl = warp > 0 ? swarp[warp - 1] : 0;
+    if (b < ntiles) tile_offsets[b] = carry + warp_excl + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += swarp[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = carry;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+select_scatter_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
+                      const int64_t* __restrict__ tile_offsets, int32_t* __restrict__ out_idx) {
+  __shared__ int swarp[kSelThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kSelPerThread;
+  const uint32_t bits = load_flags(mask, n, base, vec_ok);
+  const int c = __popc(bits);
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) swarp[warp] = incl;
+  __syncthreads();
+  int warp_excl = 0;
+  for (int w = 0; w < warp; ++w) warp_excl += swarp[w];
+  int64_t pos = tile_offsets[blockIdx.x] + warp_excl + (incl - c);
+  uint32_t rest = bits;
+  while (rest) {
+    const int j = __ffs(rest) - 1;
+    rest &= rest - 1;
+    out_idx[pos++] = (int32_t)(base + j);
+  }
+}
+
+// out[r] = src[idx[r]] for rows of `row_bytes` bytes, copied in 4-byte words when possible.
+__global__ void gather_rows_words(const uint32_t* __restrict__ src, const int32_t* __restrict__ idx,
+                                  int64_t count, int64_t row_words, uint32_t* __restrict__ dst) {
+  const int64_t total = count * row_words;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = g / row_words, w = g - r * row_words;
+    dst[g] = src[(int64_t)idx[r] * row_words + w];
+  }
+}
+__global__ void gather_rows_bytes(const uint8_t* __restrict__ src, const int32_t* __restrict__ idx,
+                                  int64_t count, int64_t row_bytes, uint8_t* __restrict__ dst) {
+  const int64_t total = count * row_bytes;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = g / row_bytes, b = g - r * row_bytes;
+    dst[g] = src[(int64_t)idx[r] * row_bytes + b];
+  }
+}
+
+// ---- reductions -------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+
+// op: 0 sum, 1 mean, 2 min, 3 max.  Sums accumulate in double in a fixed tree.
+__global__ void __launch_bounds__(kRedThreads)
+reduce_partial_kernel(const float* __restrict__ x, int64_t n, int op, double* __restrict__ part) {
+  __shared__ double s[kRedThreads];
+  double acc = (op == 2) ? INFINITY : (op == 3 ? -INFINITY : 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)kRedThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kRedThreads) {
+    const double v = x[i];
+    acc = op == 2 ? fmin(acc, v) : (op == 3 ? fmax(acc, v) : acc + v);
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double a = s[threadIdx.x], b = s[threadIdx.x + o];
+      s[threadIdx.x] = op == 2 ? fmin(a, b) : (op == 3 ? fmax(a, b) : a + b);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+__global__ void reduce_final_kernel(const double* __restrict__ part, int nparts, int64_t n, int op,
+                                    float* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = (op == 2) ? INFINITY : (op == 3 ? -INFINITY : 0.0);
+  for (int b = 0; b < nparts; ++b)
+    acc = op == 2 ? fmin(acc, part[b]) : (op == 3 ? fmax(acc, part[b]) : acc + part[b]);
+  if (op == 1) acc /= (double)n;
+  *out = (float)acc;
+}
+
+int reduce_blocks(int64_t n) {
+  int64_t b = (n + kRedThreads - 1) / kRedThreads;
+  const int64_t cap = (int64_t)abm_host::sm_count() * 4;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+extern "C" {
+
+size_t abm_select_workspace_bytes(int64_t n) {
+  if (n <= 0) return 0;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  return align_up((size_t)tiles * sizeof(int32_t), 256) + (size_t)tiles * sizeof(int64_t);
+}
+
+int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t* count,
+                       void* workspace, size_t workspace_bytes, void* stream) {
+  if (!mask || !out_idx || !count || n < 0 || n > 0x7FFFFFFFll) return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  if (n == 0) {
+    return abm_host::record_cuda_error(cudaMemsetAsync(count, 0, sizeof(int64_t), s),
+                                       "abm_select_indices");
+  }
+  const size_t need = abm_select_workspace_bytes(n);
+  if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 256))
+    return ABM_ERR_WORKSPACE;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  int32_t* tile_counts = static_cast<int32_t*>(workspace);
+  int64_t* tile_offsets = reinterpret_cast<int64_t*>(
+      static_cast<char*>(workspace) + align_up((size_t)tiles * sizeof(int32_t), 256));
+  const bool vec_ok = abm_host::aligned(mask, 16);
+  select_count_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(mask, n, vec_ok, tile_counts);
+  int st = abm_host::check_launch("abm_select_indices/count");
+  if (st) return st;
+  select_scan_kernel<<<1, 1024, 0, s>>>(tile_counts, tiles, tile_offsets, count);
+  st = abm_host::check_launch("abm_select_indices/scan");
+  if (st) return st;
+  select_scatter_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(mask, n, vec_ok, tile_offsets,
+                                                                out_idx);
+  return abm_host::check_launch("abm_select_indices/scatter");
+}
+
+int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes, const int32_t* idx,
+                    int64_t count, void* dst, void* stream) {
+  if (!src || !dst || row_bytes <= 0 || count < 0 || nrows_src < 0) return ABM_ERR_BADARG;
+  if (count == 0) return ABM_OK;
+  if (!idx) return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int threads = 256;
+  const bool words = row_bytes % 4 == 0 && abm_host::aligned(src, 4) && abm_host::aligned(dst, 4);
+  const int64_t total = words ? count * (row_bytes / 4) : count * row_bytes;
+  int64_t blocks = (total + threads - 1) / threads;
+  const int64_t cap = (int64_t)abm_host::sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  if (words)
+    gather_rows_words<<<(unsigned)blocks, threads, 0, s>>>(
+        static_cast<const uint32_t*>(src), idx, count, row_bytes / 4, static_cast<uint32_t*>(dst));
+  else
+    gather_rows_bytes<<<(unsigned)blocks, threads, 0, s>>>(
+        static_cast<const uint8_t*>(src), idx, count, row_bytes, static_cast<uint8_t*>(dst));
+  return abm_host::check_launch("abm_gather_rows");
+}
+
+size_t abm_reduce_workspace_bytes(int64_t n) {
+  if (n <= 0) return 0;
+  return (size_t)reduce_blocks(n) * sizeof(double);
+}
+
+int abm_reduce_f32(const float* x, int64_t n, int op, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  if (!x || !out || n <= 0 || op < 0 || op > 3) return ABM_ERR_BADARG;
+  const size_t need = abm_reduce_workspace_bytes(n);
+  if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 8))
+    return ABM_ERR_WORKSPACE;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int blocks = reduce_blocks(n);
+  double* part = static_cast<double*>(workspace);
+  reduce_partial_kernel<<<blocks, kRedThreads, 0, s>>>(x, n, op, part);
+  int st = abm_host::check_launch("abm_reduce_f32/partial");
+  if (st) return st;
+  reduce_final_kernel<<<1, 32, 0, s>>>(part, blocks, n, op, out);
+  return abm_host::check_launch("abm_reduce_f32/final");
+}
+
+}  // extern "C"

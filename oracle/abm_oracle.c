@@ -1,0 +1,229 @@
+/*
+ * CPU oracle of the agent-step path, plain C + OpenMP.
+ *
+ * TEST INFRASTRUCTURE ONLY: linked by tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py as the checker, never by the shipped library.
+ *
+ * Parity status: the threefry2x32 / jax.random layer is pinned against published
+ * known-answer values (see oracle/threefry.py and tests/test_oracle_threefry.py);
+ * model trajectories are UNPINNED against the reference, because the reference runs on
+ * the third-party package `jax` (absent here) and ships no golden trajectories.  The
+ * models follow the reference call sites cited at each function.
+ *
+ * Build: oracle/build.py (gcc -O2 -fopenmp -ffp-contract=off).  -ffp-contract=off keeps
+ * every float32 multiply and add separately rounded, like the JAX expressions restated.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- threefry2x32-20 (Salmon et al., SC'11) ---------------------------------------- */
+static inline uint32_t rotl32(uint32_t x, int r) { return (x << r) | (x >> (32 - r)); }
+
+#define RND(r)         \
+  x0 += x1;            \
+  x1 = rotl32(x1, r);  \
+  x1 ^= x0;
+
+static inline void tf(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t* o0,
+                      uint32_t* o1) {
+  const uint32_t ks0 = k0, ks1 = k1, ks2 = k0 ^ k1 ^ 0x1BD11BDAu;
+  uint32_t x0 = c0 + ks0, x1 = c1 + ks1;
+  RND(13) RND(15) RND(26) RND(6)
+  x0 += ks1; x1 += ks2 + 1u;
+  RND(17) RND(29) RND(16) RND(24)
+  x0 += ks2; x1 += ks0 + 2u;
+  RND(13) RND(15) RND(26) RND(6)
+  x0 += ks0; x1 += ks1 + 3u;
+  RND(17) RND(29) RND(16) RND(24)
+  x0 += ks1; x1 += ks2 + 4u;
+  RND(13) RND(15) RND(26) RND(6)
+  x0 += ks2; x1 += ks0 + 5u;
+  *o0 = x0;
+  *o1 = x1;
+}
+#undef RND
+
+typedef struct { uint32_t a, b; } key_t2;
+
+/* partitionable split(key, n)[i] */
+static inline key_t2 split_at(key_t2 k, uint64_t i) {
+  key_t2 r;
+  tf(k.a, k.b, (uint32_t)(i >> 32), (uint32_t)i, &r.a, &r.b);
+  return r;
+}
+/* partitionable bits(key, shape)[i] */
+static inline uint32_t bits_at(key_t2 k, uint64_t i) {
+  uint32_t y0, y1;
+  tf(k.a, k.b, (uint32_t)(i >> 32), (uint32_t)i, &y0, &y1);
+  return y0 ^ y1;
+}
+
+static inline float as_float(uint32_t u) {
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+static inline float unit_float(uint32_t b) { return as_float((b >> 9) | 0x3F800000u) - 1.0f; }
+
+static inline float uniform_from_bits(uint32_t b, float lo, float hi) {
+  const float span = hi - lo;
+  float v = unit_float(b) * span;
+  v = v + lo;
+  return v > lo ? v : lo;
+}
+
+/* Giles (2011) single-precision erfinv, Horner with fused multiply-add. */
+static inline float erfinv_giles(float x) {
+  float w = -log1pf(-(x * x));
+  float p;
+  if (w < 5.0f) {
+    w = w - 2.5f;
+    p = 2.81022636e-08f;
+    p = fmaf(p, w, 3.43273939e-07f);
+    p = fmaf(p, w, -3.5233877e-06f);
+    p = fmaf(p, w, -4.39150654e-06f);
+    p = fmaf(p, w, 0.00021858087f);
+    p = fmaf(p, w, -0.00125372503f);
+    p = fmaf(p, w, -0.00417768164f);
+    p = fmaf(p, w, 0.246640727f);
+    p = fmaf(p, w, 1.50140941f);
+  } else {
+    w = sqrtf(w) - 3.0f;
+    p = -0.000200214257f;
+    p = fmaf(p, w, 0.000100950558f);
+    p = fmaf(p, w, 0.00134934322f);
+    p = fmaf(p, w, -0.00367342844f);
+    p = fmaf(p, w, 0.00573950773f);
+    p = fmaf(p, w, -0.0076224613f);
+    p = fmaf(p, w, 0.00943887047f);
+    p = fmaf(p, w, 1.00167406f);
+    p = fmaf(p, w, 2.83297682f);
+  }
+  return p * x;
+}
+
+static const float kNormalLo = -0.99999994039535522461f;
+static const float kSqrt2f = 1.41421353816986083984f;
+
+static inline float normal_from_bits(uint32_t b) {
+  return kSqrt2f * erfinv_giles(uniform_from_bits(b, kNormalLo, 1.0f));
+}
+
+/* float64 draw from the same bits: erfinv by Newton iteration on erf in double. */
+static double erfinv_f64(double y) {
+  if (y <= -1.0) return -INFINITY;
+  if (y >= 1.0) return INFINITY;
+  double x = (double)erfinv_giles((float)y);
+  for (int it = 0; it < 4; ++it) {
+    const double err = erf(x) - y;
+    x -= err / (1.1283791670955126 * exp(-x * x));
+  }
+  return x;
+}
+static inline double normal_from_bits_f64(uint32_t b) {
+  return 1.4142135623730951 * erfinv_f64((double)uniform_from_bits(b, kNormalLo, 1.0f));
+}
+
+static inline float mod1f(float v) {
+  float r = fmodf(v, 1.0f);
+  if (r != 0.0f && r < 0.0f) r = r + 1.0f;
+  return r;
+}
+static inline double mod1d(double v) {
+  double r = fmod(v, 1.0);
+  if (r != 0.0 && r < 0.0) r = r + 1.0;
+  return r;
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+/* ---- jax.random primitives ---------------------------------------------------------- */
+void orc_threefry(const uint32_t* k, const uint32_t* c0, const uint32_t* c1, int64_t n,
+                  uint32_t* y0, uint32_t* y1) {
+  for (int64_t i = 0; i < n; ++i) tf(k[0], k[1], c0[i], c1[i], &y0[i], &y1[i]);
+}
+
+/* Model.step key chain (jaxabm/model.py:155-168), partitionable mode. */
+void orc_keychain(uint32_t* rng, int32_t ncoll, int32_t steps, uint32_t* coll_keys) {
+  key_t2 r = {rng[0], rng[1]};
+  for (int32_t t = 0; t < steps; ++t) {
+    key_t2 step_key = split_at(r, 1);
+    r = split_at(r, 0);
+    for (int32_t c = 0; c < ncoll; ++c) {
+      key_t2 ck = split_at(step_key, 1);
+      step_key = split_at(step_key, 0);
+      coll_keys[2 * ((int64_t)t * ncoll + c)] = ck.a;
+      coll_keys[2 * ((int64_t)t * ncoll + c) + 1] = ck.b;
+    }
+  }
+  rng[0] = r.a;
+  rng[1] = r.b;
+}
+
+/* ---- random walk -------------------------------------------------------------------- */
+/* AgentCollection.init (jaxabm/agent.py:113-128) of the random-walk agent. */
+void orc_randomwalk_init(float* x, float* y, int64_t n, const uint32_t* init_key) {
+  const key_t2 k = {init_key[0], init_key[1]};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const key_t2 ak = split_at(k, (uint64_t)i);
+    x[i] = unit_float(bits_at(split_at(ak, 0), 0));
+    y[i] = unit_float(bits_at(split_at(ak, 1), 0));
+  }
+}
+
+/* JaxModel.run loop (jaxabm/model.py:240-241) over AgentCollection.update
+ * (jaxabm/agent.py:156-177) of the random-walk agent, float32 state, plus the float64
+ * means of the float32 states after every step.  xd/yd (optional) carry the same walk in
+ * float64 arithmetic with float64 normals from the same bits. */
+void orc_randomwalk_run(float* x, float* y, double* xd, double* yd, int64_t n,
+                        const uint32_t* coll_keys, int32_t steps, float sigma, double* means,
+                        double* means_f64) {
+  for (int32_t t = 0; t < steps; ++t) {
+    const key_t2 ck = {coll_keys[2 * t], coll_keys[2 * t + 1]};
+    double sx = 0.0, sy = 0.0, sxd = 0.0, syd = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : sx, sy, sxd, syd)
+    for (int64_t i = 0; i < n; ++i) {
+      const key_t2 ak = split_at(ck, (uint64_t)i);
+      const uint32_t bx = bits_at(split_at(ak, 0), 0);
+      const uint32_t by = bits_at(split_at(ak, 1), 0);
+      float dx = sigma * normal_from_bits(bx);
+      float dy = sigma * normal_from_bits(by);
+      x[i] = mod1f(x[i] + dx);
+      y[i] = mod1f(y[i] + dy);
+      sx += x[i];
+      sy += y[i];
+      if (xd) {
+        xd[i] = mod1d(xd[i] + (double)sigma * normal_from_bits_f64(bx));
+        yd[i] = mod1d(yd[i] + (double)sigma * normal_from_bits_f64(by));
+        sxd += xd[i];
+        syd += yd[i];
+      }
+    }
+    means[2 * t] = sx / (double)n;
+    means[2 * t + 1] = sy / (double)n;
+    if (means_f64) {
+      means_f64[2 * t] = sxd / (double)n;
+      means_f64[2 * t + 1] = syd / (double)n;
+    }
+  }
+}

@@ -1,0 +1,72 @@
+"""ctypes wrappers of the C oracle (oracle/abm_oracle.c).  TEST INFRASTRUCTURE ONLY."""
+
+import ctypes
+
+import numpy as np
+
+from . import build as _build
+from . import models as _models
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def lib():
+    L = _build.load()
+    return L
+
+
+def set_threads(n):
+    lib().orc_set_threads(ctypes.c_int(int(n)))
+
+
+def num_threads():
+    L = lib()
+    L.orc_num_threads.restype = ctypes.c_int
+    return L.orc_num_threads()
+
+
+def threefry(key, c0, c1):
+    key = np.ascontiguousarray(key, dtype=np.uint32)
+    c0 = np.ascontiguousarray(c0, dtype=np.uint32)
+    c1 = np.ascontiguousarray(c1, dtype=np.uint32)
+    y0 = np.empty_like(c0)
+    y1 = np.empty_like(c1)
+    lib().orc_threefry(_p(key), _p(c0), _p(c1), ctypes.c_int64(c0.size), _p(y0), _p(y1))
+    return y0, y1
+
+
+def keychain(rng, steps, ncoll=1):
+    rng = np.array(rng, dtype=np.uint32, copy=True)
+    out = np.zeros((steps, ncoll, 2), dtype=np.uint32)
+    lib().orc_keychain(_p(rng), ctypes.c_int32(ncoll), ctypes.c_int32(steps), _p(out))
+    return out, rng
+
+
+def randomwalk_init(init_key, n):
+    x = np.empty(n, np.float32)
+    y = np.empty(n, np.float32)
+    k = np.ascontiguousarray(init_key, dtype=np.uint32)
+    lib().orc_randomwalk_init(_p(x), _p(y), ctypes.c_int64(n), _p(k))
+    return x, y
+
+
+def randomwalk_run(seed, n, steps, sigma=0.01, f64=False):
+    """Full run from a seed.  Returns dict with x, y (float32), means (float64[steps,2]
+    of the float32 states) and, with f64=True, x64/y64/means64 from float64 arithmetic."""
+    rng, (ik,) = _models.model_keys(seed, 1)
+    x, y = randomwalk_init(ik, n)
+    ck, rng = keychain(rng, steps, 1)
+    ck = np.ascontiguousarray(ck.reshape(steps, 2))
+    means = np.zeros((steps, 2))
+    xd = x.astype(np.float64) if f64 else None
+    yd = y.astype(np.float64) if f64 else None
+    means64 = np.zeros((steps, 2)) if f64 else None
+    lib().orc_randomwalk_run(_p(x), _p(y), _p(xd), _p(yd), ctypes.c_int64(n), _p(ck),
+                             ctypes.c_int32(steps), ctypes.c_float(sigma), _p(means),
+                             _p(means64))
+    out = {"x": x, "y": y, "means": means, "rng": rng}
+    if f64:
+        out.update(x64=xd, y64=yd, means64=means64)
+    return out

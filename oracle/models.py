@@ -1,0 +1,92 @@
+"""NumPy restatement of the reference's step semantics for the workload models.
+
+TEST INFRASTRUCTURE ONLY (the checker; never imported by the shipped package).
+
+Parity status: model trajectories are UNPINNED against the reference (JAX absent, no
+reference golden trajectories exist); the key chain and samplers come from
+``oracle/threefry.py``, which is pinned against published known-answer values.
+
+The reference semantics restated here:
+
+* ``Model.initialize`` (jaxabm/model.py:118-144): ``keys = split(PRNGKey(seed), C + 1)``,
+  ``rng = keys[0]``, collection ``i`` initialises from ``keys[i + 1]``.
+* ``AgentCollection.init`` (jaxabm/agent.py:113-128): per-agent keys ``split(key, N)``.
+* ``Model.step`` (jaxabm/model.py:155-168): ``rng, step_key = split(rng)``; per collection
+  ``step_key, coll_key = split(step_key)``; ``AgentCollection.update`` gives agent ``i``
+  the key ``split(coll_key, N)[i]`` (jaxabm/agent.py:156) and updates all agents from the
+  pre-step states (synchronous ``vmap``, jaxabm/agent.py:168-177).
+"""
+
+import numpy as np
+
+from . import threefry as tfy
+
+
+def model_keys(seed, ncoll=1):
+    """(rng after initialize, [collection init keys])."""
+    keys = tfy.split(tfy.PRNGKey(seed), ncoll + 1)
+    return keys[0].copy(), [keys[i + 1].copy() for i in range(ncoll)]
+
+
+def keychain(rng, steps, ncoll=1):
+    """Collection keys uint32[steps, ncoll, 2] of ``steps`` Model.step calls, and the
+    advanced rng."""
+    rng = np.asarray(rng, dtype=np.uint32).copy()
+    out = np.zeros((steps, ncoll, 2), dtype=np.uint32)
+    for t in range(steps):
+        k = tfy.split(rng, 2)
+        rng, step_key = k[0], k[1]
+        for c in range(ncoll):
+            k = tfy.split(step_key, 2)
+            step_key, out[t, c] = k[0], k[1]
+    return out, rng
+
+
+def agent_keys(coll_key, n):
+    return tfy.split(coll_key, n)
+
+
+# ---- random walk ------------------------------------------------------------------------
+# Agent (jx.Agent form):
+#   setup(key):  kx, ky = split(key); {'x': uniform(kx), 'y': uniform(ky)}
+#   step(model_state, key): kx, ky = split(key)
+#       x = (x + sigma * normal(kx)) % 1.0 ; y likewise
+
+
+def randomwalk_init(init_key, n):
+    ak = agent_keys(init_key, n)
+    sub = tfy.split_batched(ak, 2)                 # [n, 2, 2]
+    x = tfy.bits_to_unit_float(tfy.bits_batched(sub[:, 0], 1)[:, 0])
+    y = tfy.bits_to_unit_float(tfy.bits_batched(sub[:, 1], 1)[:, 0])
+    return x, y
+
+
+def _mod1_f32(v):
+    r = np.fmod(v, np.float32(1.0)).astype(np.float32)
+    neg = (r != 0) & (r < 0)
+    r[neg] = (r[neg] + np.float32(1.0)).astype(np.float32)
+    return r
+
+
+def randomwalk_step(x, y, coll_key, sigma=0.01):
+    n = x.shape[0]
+    ak = agent_keys(coll_key, n)
+    sub = tfy.split_batched(ak, 2)
+    nx = tfy.normal_from_bits(tfy.bits_batched(sub[:, 0], 1)[:, 0])
+    ny = tfy.normal_from_bits(tfy.bits_batched(sub[:, 1], 1)[:, 0])
+    s = np.float32(sigma)
+    x = _mod1_f32((x + (s * nx).astype(np.float32)).astype(np.float32))
+    y = _mod1_f32((y + (s * ny).astype(np.float32)).astype(np.float32))
+    return x, y
+
+
+def randomwalk_run(seed, n, steps, sigma=0.01):
+    """Full run from a seed: returns (x, y, means float64[steps, 2])."""
+    rng, (ik,) = model_keys(seed, 1)
+    x, y = randomwalk_init(ik, n)
+    ck, rng = keychain(rng, steps, 1)
+    means = np.zeros((steps, 2))
+    for t in range(steps):
+        x, y = randomwalk_step(x, y, ck[t, 0], sigma)
+        means[t] = (x.astype(np.float64).mean(), y.astype(np.float64).mean())
+    return x, y, means

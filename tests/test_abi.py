@@ -1,0 +1,45 @@
+"""The C-ABI library builds, loads without a GPU and exports every declared symbol."""
+
+import ctypes
+import os
+import re
+
+from jaxabm_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "jaxabm_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"ABM_API\s+[\w\s\*]+?\b(abm_\w+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "abm_rng_split" in syms and "abm_randomwalk_run" in syms
+    assert len(syms) >= 15
+
+
+def test_every_declared_symbol_is_exported(lib):
+    raw = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [s for s in declared_symbols() if not hasattr(raw, s)]
+    assert not missing, missing
+
+
+def test_every_declared_symbol_is_bound(lib):
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_status_strings(lib):
+    assert lib.abm_status_string(0) == b"ok"
+    assert lib.abm_status_string(_lib.ABM_ERR_WORKSPACE) == b"workspace too small"
+    assert lib.abm_version() >= 100
+
+
+def test_bad_arguments_rejected_without_gpu(lib):
+    # argument validation happens before any CUDA call
+    assert lib.abm_rng_split(None, 1, 2, None, 1, None) == _lib.ABM_ERR_BADARG
+    assert lib.abm_randomwalk_run(None, None, 10, None, 5, 0.01, None, None, 0, None) == \
+        _lib.ABM_ERR_BADARG
+    assert lib.abm_randomwalk_workspace_bytes(10_000, 100) > 0

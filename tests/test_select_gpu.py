@@ -1,0 +1,81 @@
+"""K6 compaction and K7 reductions vs NumPy (bit-exact indices, stable order)."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [1, 15, 16, 17, 4095, 4096, 4097, 100_003, 1 << 20])
+@pytest.mark.parametrize("density", [0.0, 0.01, 0.5, 1.0])
+def test_select_indices(cuda, n, density):
+    from jaxabm_gb300.select import select_indices
+    rs = np.random.RandomState(n)
+    m = rs.rand(n) < density
+    idx, c = select_indices(torch.from_numpy(m).cuda())
+    ref = np.nonzero(m)[0]
+    assert c == len(ref)
+    assert np.array_equal(idx.cpu().numpy(), ref)
+
+
+def test_select_unaligned_mask(cuda):
+    from jaxabm_gb300.select import select_indices
+    m = torch.from_numpy(np.random.RandomState(1).rand(5001) < 0.3).cuda()
+    sub = m[3:]  # data pointer not 16-byte aligned: scalar path
+    idx, c = select_indices(sub)
+    assert np.array_equal(idx.cpu().numpy(), np.nonzero(sub.cpu().numpy())[0])
+
+
+def test_compact_states_rows(cuda):
+    from jaxabm_gb300.select import compact_states
+    n = 3001
+    rs = np.random.RandomState(2)
+    st = {"a": torch.from_numpy(rs.rand(n).astype(np.float32)).cuda(),
+          "b": torch.from_numpy(rs.randint(0, 100, size=(n, 3)).astype(np.int8)).cuda(),
+          "c": torch.from_numpy(rs.randint(0, 9, size=(n, 2)).astype(np.int64)).cuda()}
+    mask = st["a"] > 0.5
+    out, c = compact_states(st, mask)
+    mk = mask.cpu().numpy()
+    for k in st:
+        assert np.array_equal(out[k].cpu().numpy(), st[k].cpu().numpy()[mk])
+    assert c == mk.sum()
+
+
+def test_agent_collection_filter_and_aggregate(cuda):
+    import jaxabm_gb300 as jx
+    m = jx.JaxModel(config=jx.ModelConfig(seed=1))
+    coll = jx.AgentCollection(jx.agentpy.AgentWrapper(jx.RandomWalker), 5000)
+    m.add_agent_collection("w", coll)
+    m.initialize()
+    f = coll.filter(lambda s: s["x"] > 0.5)
+    x = coll.states["x"].cpu().numpy()
+    assert f.num_agents == int((x > 0.5).sum())
+    assert np.array_equal(f.states["x"].cpu().numpy(), x[x > 0.5])
+    np.testing.assert_allclose(float(coll.aggregate("x")), x.astype(np.float64).mean(), rtol=1e-6)
+    with pytest.raises(ValueError):
+        coll.aggregate("nope")
+
+
+@pytest.mark.parametrize("op", [0, 1, 2, 3])
+def test_reduce(cuda, op):
+    from jaxabm_gb300.select import reduce
+    x = np.random.RandomState(op).randn(123_457).astype(np.float32)
+    out = float(reduce(torch.from_numpy(x).cuda(), op))
+    ref = [x.astype(np.float64).sum(), x.astype(np.float64).mean(), x.min(), x.max()][op]
+    np.testing.assert_allclose(out, ref, rtol=1e-6)
+
+
+def test_select_agentlist_api(cuda):
+    import jaxabm_gb300 as jx
+
+    class M(jx.Model):
+        def setup(self):
+            self.walkers = self.add_agents(2000, jx.RandomWalker, name="walkers")
+
+    m = M({"steps": 3, "seed": 4})
+    m.run()
+    sel = m.walkers.select(lambda s: s["y"] < 0.25)
+    y = m.walkers.y.cpu().numpy()
+    assert len(sel) == int((y < 0.25).sum())
+    assert np.array_equal(sel.y.cpu().numpy(), y[y < 0.25])
