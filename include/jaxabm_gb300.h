@@ -121,6 +121,79 @@ ABM_API int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* co
                        float sigma, float* means, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* ---- Network construction (HOST memory; native setup code) ------------------------- */
+/* Directed-entry count 2*m*(n-m) of a Barabasi-Albert graph, or -1 for bad sizes. */
+ABM_API int64_t abm_graph_ba_num_edges(int64_t n, int32_t m);
+
+/* Barabasi-Albert preferential attachment (star on nodes 0..m, then each new node links
+ * to m distinct nodes drawn from the degree-weighted node list), written as symmetric CSR
+ * with rows sorted ascending into HOST buffers row_ptr int32[n+1] and col int32[capacity].
+ * Replaces building the graph with Network.add_edge (jaxabm/agentpy.py:559-582). */
+ABM_API int abm_graph_barabasi_albert(int64_t n, int32_t m, uint64_t seed, int32_t* row_ptr,
+                                      int32_t* col, int64_t col_capacity);
+
+/* Simple d-regular graph (d even) as the union of d/2 edge-disjoint random Hamiltonian
+ * cycles; symmetric CSR into HOST buffers (col holds n*d entries). */
+ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_t* row_ptr,
+                                     int32_t* col, int64_t col_capacity);
+
+/* ---- K5: SIR contagion on a Network ------------------------------------------------- */
+/* Device-side descriptor of one SIR model instance (80 bytes, 8-byte aligned).
+ * state holds 2*n int8 compartments (0 S, 1 I, 2 R); buffer (t & 1) is current.
+ * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
+ * NULL, else it is derived from rng, the instance's Model.step key-chain state
+ * (jaxabm/model.py:156,164), which is advanced once per step either way.  counts receives
+ * S, I, R after each step (int32[steps][3], zeroed by the caller); done_flag (nullable,
+ * may be host-mapped) is set to 1 after the last step. */
+typedef struct abm_sir_instance {
+  const int32_t* row_ptr;
+  const int32_t* col;
+  int8_t* state;
+  int32_t* counts;
+  int32_t* done_flag;
+  const uint32_t* coll_keys;
+  uint32_t rng[2];
+  int32_t n;
+  int32_t t;
+  int32_t steps;
+  float beta;
+  float gamma;
+  int32_t reserved;
+} abm_sir_instance;
+
+/* A tile of agents [begin, end) of instance `inst` (end - begin <= 256). */
+typedef struct abm_work_item {
+  int32_t inst;
+  int32_t begin;
+  int32_t end;
+  int32_t reserved;
+} abm_work_item;
+
+ABM_API size_t abm_sir_instance_size(void);
+
+/* nsteps synchronous SIR steps of every instance with t < steps, over the tiles `work`
+ * (persistent grid of `grid` CTAs; 0 = 8 per SM).  Per step and agent i of an instance:
+ * agent_key = split(coll_key, n)[i], k_inf, k_rec = split(agent_key);
+ *   S -> I if some neighbour slot k with an I neighbour has uniform(k_inf,(deg,))[k] < beta;
+ *   I -> R if uniform(k_rec) < gamma.
+ * Replaces Model.step's AgentCollection.update (jaxabm/model.py:163-171,
+ * jaxabm/agent.py:132-179) for the SIR agent, batched over instances (the serial loops of
+ * Model.batch_run, jaxabm/agentpy.py:1116-1152).  Descriptors and tiles are device memory
+ * and may be rewritten between calls (e.g. to admit instances) without re-capturing a
+ * CUDA graph of this call. */
+ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
+                          int32_t nwork, int32_t nsteps, int32_t grid, void* stream);
+
+ABM_API size_t abm_sir_run_workspace_bytes(int64_t n);
+
+/* One SIR model for `steps` steps (the plain engine: one simulation per launch sequence)
+ * with the per-step collection keys coll_keys uint32[steps][2] (abm_keychain, ncoll = 1).
+ * state int8[2*n]: the current compartments are read from state[0..n) and the final ones
+ * are in buffer (steps & 1); counts int32[steps][3] (zeroed by the call). */
+ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* state,
+                        const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
+                        int32_t* counts, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- K6: stable compaction (AgentList.select / AgentCollection.filter) -------------- */
 ABM_API size_t abm_select_workspace_bytes(int64_t n);
 

@@ -22,6 +22,8 @@ from .utils import convert_to_numpy, format_time
 
 from . import randomwalk  # noqa: E402  registers RandomWalker
 from .randomwalk import RandomWalker, RandomWalkModel  # noqa: E402
+from . import sir  # noqa: E402  registers SIRAgent
+from .sir import SIRAgent, SIRModel  # noqa: E402
 
 
 def build(force: bool = False) -> str:

@@ -46,6 +46,13 @@ SIGNATURES = {
     "abm_randomwalk_init": (_int, [_p, _p, _i64, _p, _p]),
     "abm_randomwalk_workspace_bytes": (_sz, [_i64, _i32]),
     "abm_randomwalk_run": (_int, [_p, _p, _i64, _p, _i32, _f32, _p, _p, _sz, _p]),
+    "abm_graph_ba_num_edges": (_i64, [_i64, _i32]),
+    "abm_graph_barabasi_albert": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
+    "abm_graph_random_regular": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
+    "abm_sir_instance_size": (_sz, []),
+    "abm_sir_steps": (_int, [_p, _i32, _p, _i32, _i32, _i32, _p]),
+    "abm_sir_run_workspace_bytes": (_sz, [_i64]),
+    "abm_sir_run": (_int, [_p, _p, _i64, _p, _p, _i32, _f32, _f32, _p, _p, _sz, _p]),
     "abm_select_workspace_bytes": (_sz, [_i64]),
     "abm_select_indices": (_int, [_p, _i64, _p, _p, _p, _sz, _p]),
     "abm_gather_rows": (_int, [_p, _i64, _i64, _p, _i64, _p, _p]),

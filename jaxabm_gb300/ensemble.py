@@ -1,0 +1,213 @@
+"""Batched SIR ensembles: many independent SIR models stepped by one launch sequence.
+
+The reference runs ensembles as serial Python loops of ``model.run()``
+(``Model.batch_run``, jaxabm/agentpy.py:1116-1152; ``SensitivityAnalysis.run``,
+jaxabm/analysis.py:97-165).  Here every member is an *instance*: its CSR, compartments and
+per-step counts live in packed device buffers, a device descriptor (``abm_sir_instance``)
+points into them, and ``abm_sir_steps`` advances all live instances over a persistent grid
+of (instance, 256-agent tile) work items.  The whole multi-step launch sequence is captured
+once in a CUDA graph and replayed.
+
+Each instance follows exactly the single-model key chain (``PRNGKey(seed)`` ->
+``initialize`` -> ``Model.step``), so its result is identical to running it alone.
+"""
+
+import math
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import torch
+
+from . import _dev
+from . import _lib
+from . import random as jrandom
+from .sir import barabasi_albert, initial_states
+
+TILE = 256
+
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 80 bytes
+INSTANCE_DTYPE = np.dtype([
+    ("row_ptr", "<u8"), ("col", "<u8"), ("state", "<u8"), ("counts", "<u8"),
+    ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)), ("n", "<i4"),
+    ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("reserved", "<i4"),
+])
+assert INSTANCE_DTYPE.itemsize == 80
+RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
+
+
+def check_layout():
+    size = _lib.load().abm_sir_instance_size()
+    if size != INSTANCE_DTYPE.itemsize:
+        raise RuntimeError(f"abm_sir_instance is {size} bytes, host layout expects "
+                           f"{INSTANCE_DTYPE.itemsize}")
+
+
+def tiles_for(inst, n):
+    b = np.arange(0, n, TILE, dtype=np.int64)
+    out = np.zeros((b.size, 4), dtype=np.int32)
+    out[:, 0] = inst
+    out[:, 1] = b
+    out[:, 2] = np.minimum(b + TILE, n)
+    return out
+
+
+def model_rngs(seeds):
+    """Device rng after ``Model.initialize`` for each seed: split(PRNGKey(s), 2)[0]."""
+    seeds = np.asarray(seeds, dtype=np.uint64)
+    keys = np.zeros((seeds.size, 2), dtype=np.uint32)
+    keys[:, 0] = (seeds >> np.uint64(32)).astype(np.uint32)
+    keys[:, 1] = (seeds & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    dk = _dev.keys_from_numpy(keys)
+    return jrandom.split(dk, 2)[:, 0].contiguous()
+
+
+class SIRBatch:
+    """A fixed set of SIR instances packed into device buffers.
+
+    Args:
+        graphs: list of (row_ptr, col) host CSR arrays
+        init_states: list of int8 host compartment arrays
+        betas, gammas: per-instance parameters
+        seeds: per-instance model seeds (key chain of ``Model.initialize``/``step``)
+        steps: number of steps every instance runs
+    """
+
+    def __init__(self, graphs, init_states, betas, gammas, seeds, steps):
+        check_layout()
+        dev = _dev.device()
+        k = len(graphs)
+        self.k = k
+        self.steps = int(steps)
+        self.n = np.array([len(rp) - 1 for rp, _ in graphs], dtype=np.int64)
+        self.e = np.array([len(c) for _, c in graphs], dtype=np.int64)
+        # packed host buffers -> one device buffer each
+        rp_off = np.concatenate([[0], np.cumsum(self.n + 1)])
+        col_off = np.concatenate([[0], np.cumsum(self.e)])
+        st_off = np.concatenate([[0], np.cumsum(2 * self.n)])
+        cnt_off = np.arange(k + 1, dtype=np.int64) * self.steps * 3
+        h_rp = np.empty(rp_off[-1], dtype=np.int32)
+        h_col = np.empty(col_off[-1], dtype=np.int32)
+        h_st = np.zeros(st_off[-1], dtype=np.int8)
+        for i, ((rp, col), st) in enumerate(zip(graphs, init_states)):
+            h_rp[rp_off[i]:rp_off[i + 1]] = rp
+            h_col[col_off[i]:col_off[i + 1]] = col
+            h_st[st_off[i]:st_off[i] + self.n[i]] = st
+        self.row_ptr = torch.from_numpy(h_rp).to(dev)
+        self.col = torch.from_numpy(h_col).to(dev)
+        self.state = torch.from_numpy(h_st).to(dev)
+        self.h_state0 = h_st
+        self.counts = torch.zeros(int(cnt_off[-1]), dtype=torch.int32, device=dev)
+        self._offsets = (rp_off, col_off, st_off, cnt_off)
+        desc = np.zeros(k, dtype=INSTANCE_DTYPE)
+        desc["row_ptr"] = self.row_ptr.data_ptr() + 4 * rp_off[:-1]
+        desc["col"] = self.col.data_ptr() + 4 * col_off[:-1]
+        desc["state"] = self.state.data_ptr() + st_off[:-1]
+        desc["counts"] = self.counts.data_ptr() + 4 * cnt_off[:-1]
+        desc["n"] = self.n
+        desc["t"] = 0
+        desc["steps"] = self.steps
+        desc["beta"] = np.asarray(betas, dtype=np.float32)
+        desc["gamma"] = np.asarray(gammas, dtype=np.float32)
+        self.h_desc0 = desc
+        self.desc = torch.from_numpy(desc.view(np.int32).reshape(k, 20).copy()).to(dev)
+        self.rng0 = model_rngs(seeds)
+        self.desc[:, RNG_WORD:RNG_WORD + 2] = self.rng0
+        self.desc0 = self.desc.clone()
+        self.work = torch.from_numpy(
+            np.concatenate([tiles_for(i, int(n)) for i, n in enumerate(self.n)])).to(dev)
+        self.state0 = self.state.clone()
+        self.grid = 0
+        self._graph = None
+        self._graph_steps = None
+
+    @property
+    def agent_steps(self):
+        return int(self.n.sum()) * self.steps
+
+    def reset(self):
+        """Back to step 0 (state, counters, key chains) without reallocating."""
+        self.state.copy_(self.state0)
+        self.desc.copy_(self.desc0)
+        self.counts.zero_()
+
+    def launch(self, nsteps, stream=None):
+        """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps``)."""
+        _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
+                  self.work.shape[0], int(nsteps), int(self.grid), _dev.stream_handle(stream))
+
+    def capture(self, nsteps):
+        """Capture ``nsteps`` steps into a CUDA graph (replayed by :meth:`replay`)."""
+        torch.cuda.synchronize()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.launch(nsteps, s)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self._graph, self._graph_steps = g, nsteps
+        return g
+
+    def replay(self):
+        self._graph.replay()
+
+    def run(self, use_graph=True):
+        """All ``steps`` steps of every instance."""
+        if use_graph:
+            if self._graph is None or self._graph_steps != self.steps:
+                self.capture(self.steps)
+            self.replay()
+        else:
+            self.launch(self.steps)
+
+    def final_state(self, i):
+        st_off = self._offsets[2]
+        n = int(self.n[i])
+        buf = self.steps & 1
+        return self.state[st_off[i] + buf * n: st_off[i] + (buf + 1) * n]
+
+    def counts_of(self, i):
+        c = self._offsets[3]
+        return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
+
+    def launches_per_run(self):
+        return 2 * self.steps
+
+
+# ---- the batched-ensemble workload (4,096 SIR instances) -------------------------------
+
+def ensemble_spec(count=4096, n_lo=1_000, n_hi=100_000, seed=2, rate=200.0):
+    """Per-instance sizes, parameters, seeds and Poisson arrival times.
+
+    Sizes are log-uniform in [n_lo, n_hi] (``RandomState(seed)``); (beta, gamma) come from a
+    scrambled 2-D Sobol sequence seeded with ``seed``, scaled to [0.01, 0.2] x [0.05, 0.3];
+    arrivals are a Poisson stream of ``rate`` requests/s (exponential gaps,
+    ``RandomState(seed + 1)``)."""
+    from scipy.stats import qmc
+    rs = np.random.RandomState(seed)
+    n = np.rint(np.exp(rs.uniform(math.log(n_lo), math.log(n_hi), size=count))).astype(np.int64)
+    try:
+        sob = qmc.Sobol(d=2, scramble=True, rng=np.random.default_rng(seed))
+    except TypeError:  # older SciPy spells the argument `seed`
+        sob = qmc.Sobol(d=2, scramble=True, seed=seed)
+    u = sob.random(count)
+    beta = (0.01 + 0.19 * u[:, 0]).astype(np.float32)
+    gamma = (0.05 + 0.25 * u[:, 1]).astype(np.float32)
+    gaps = np.random.RandomState(seed + 1).exponential(1.0 / rate, size=count)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    seeds = np.arange(count, dtype=np.int64)
+    return {"n": n, "beta": beta, "gamma": gamma, "arrival_s": arrivals, "seed": seeds}
+
+
+def build_instances(spec, m=4, initial_infected=0.001, workers=None):
+    """Host CSR graphs and initial compartments of every instance (native generator,
+    threads across instances)."""
+    def one(i):
+        n = int(spec["n"][i])
+        s = int(spec["seed"][i])
+        g = barabasi_albert(n, m, s)
+        return g, initial_states(n, initial_infected, s)
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        res = list(ex.map(one, range(len(spec["n"]))))
+    return [r[0] for r in res], [r[1] for r in res]

@@ -72,7 +72,7 @@ def bits(key: torch.Tensor, shape=()) -> torch.Tensor:
     out = _dev.empty((flat.shape[0], count), torch.int32)
     _lib.call("abm_rng_bits", _dev.ptr(flat), flat.shape[0], count, _dev.ptr(out), _MODE[0],
               _dev.stream_handle())
-    return out.reshape(*lead, *shape)
+    return out.reshape(lead + shape)
 
 
 def uniform(key: torch.Tensor, shape=(), minval=0.0, maxval=1.0) -> torch.Tensor:
@@ -82,7 +82,7 @@ def uniform(key: torch.Tensor, shape=(), minval=0.0, maxval=1.0) -> torch.Tensor
     out = _dev.empty((flat.shape[0], count), torch.float32)
     _lib.call("abm_rng_uniform", _dev.ptr(flat), flat.shape[0], count, float(minval),
               float(maxval), _dev.ptr(out), _MODE[0], _dev.stream_handle())
-    return out.reshape(*lead, *shape)
+    return out.reshape(lead + shape)
 
 
 def normal(key: torch.Tensor, shape=()) -> torch.Tensor:
@@ -92,7 +92,7 @@ def normal(key: torch.Tensor, shape=()) -> torch.Tensor:
     out = _dev.empty((flat.shape[0], count), torch.float32)
     _lib.call("abm_rng_normal", _dev.ptr(flat), flat.shape[0], count, _dev.ptr(out), _MODE[0],
               _dev.stream_handle())
-    return out.reshape(*lead, *shape)
+    return out.reshape(lead + shape)
 
 
 def bernoulli(key: torch.Tensor, p=0.5, shape=()) -> torch.Tensor:
@@ -102,7 +102,7 @@ def bernoulli(key: torch.Tensor, p=0.5, shape=()) -> torch.Tensor:
     out = _dev.empty((flat.shape[0], count), torch.uint8)
     _lib.call("abm_rng_bernoulli", _dev.ptr(flat), flat.shape[0], count, float(p), _dev.ptr(out),
               _MODE[0], _dev.stream_handle())
-    return out.reshape(*lead, *shape).bool()
+    return out.reshape(lead + shape).bool()
 
 
 def randint(key: torch.Tensor, shape, minval, maxval) -> torch.Tensor:
@@ -112,7 +112,7 @@ def randint(key: torch.Tensor, shape, minval, maxval) -> torch.Tensor:
     out = _dev.empty((flat.shape[0], count), torch.int32)
     _lib.call("abm_rng_randint", _dev.ptr(flat), flat.shape[0], count, int(minval), int(maxval),
               _dev.ptr(out), _MODE[0], _dev.stream_handle())
-    return out.reshape(*lead, *shape)
+    return out.reshape(lead + shape)
 
 
 def keychain(rng: torch.Tensor, steps: int, ncoll: int = 1, update_keys: bool = False):

@@ -227,3 +227,64 @@ void orc_randomwalk_run(float* x, float* y, double* xd, double* yd, int64_t n,
     }
   }
 }
+
+/* ---- SIR on a network ----------------------------------------------------------------
+ * One Model.step per iteration (jaxabm/model.py:146-216) with the SIR agent update:
+ * coll_key = split(split(rng)[1])[1]; agent_key_i = split(coll_key, n)[i];
+ * k_inf, k_rec = split(agent_key_i); S -> I if any I-neighbour slot k has
+ * uniform(k_inf, (deg,))[k] < beta; I -> R if uniform(k_rec) < gamma; rng = split(rng)[0].
+ * state int8[n] in/out; counts int32[steps][3] (S, I, R after each step). */
+void orc_sir_run(const int32_t* rp, const int32_t* col, int64_t n, int8_t* state, uint32_t* rng,
+                 int32_t steps, float beta, float gamma, int32_t* counts) {
+  int8_t* cur = state;
+  int8_t* nxt = (int8_t*)malloc((size_t)n);
+  key_t2 r = {rng[0], rng[1]};
+  for (int32_t t = 0; t < steps; ++t) {
+    const key_t2 coll = split_at(split_at(r, 1), 1);
+    int64_t cs = 0, ci = 0, cr = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : cs, ci, cr)
+    for (int64_t i = 0; i < n; ++i) {
+      const int8_t s = cur[i];
+      int8_t ns = s;
+      if (s == 0) {
+        const int32_t row0 = rp[i], deg = rp[i + 1] - rp[i];
+        int have = 0;
+        key_t2 kinf = {0, 0};
+        for (int32_t k = 0; k < deg; ++k) {
+          if (cur[col[row0 + k]] == 1) {
+            if (!have) {
+              kinf = split_at(split_at(coll, (uint64_t)i), 0);
+              have = 1;
+            }
+            if (unit_float(bits_at(kinf, (uint64_t)k)) < beta) {
+              ns = 1;
+              break;
+            }
+          }
+        }
+      } else if (s == 1) {
+        const key_t2 krec = split_at(split_at(coll, (uint64_t)i), 1);
+        if (unit_float(bits_at(krec, 0)) < gamma) ns = 2;
+      }
+      nxt[i] = ns;
+      cs += ns == 0;
+      ci += ns == 1;
+      cr += ns == 2;
+    }
+    counts[3 * t] = (int32_t)cs;
+    counts[3 * t + 1] = (int32_t)ci;
+    counts[3 * t + 2] = (int32_t)cr;
+    int8_t* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    r = split_at(r, 0);
+  }
+  if (cur != state) {
+    memcpy(state, cur, (size_t)n);
+    free(cur);
+  } else {
+    free(nxt);
+  }
+  rng[0] = r.a;
+  rng[1] = r.b;
+}

@@ -70,3 +70,17 @@ def randomwalk_run(seed, n, steps, sigma=0.01, f64=False):
     if f64:
         out.update(x64=xd, y64=yd, means64=means64)
     return out
+
+
+def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
+    """SIR run from the given compartments and rng.  Returns (final state, counts
+    int32[steps, 3], advanced rng)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    st = np.array(state, dtype=np.int8, copy=True)
+    r = np.array(rng, dtype=np.uint32, copy=True)
+    counts = np.zeros((steps, 3), dtype=np.int32)
+    lib().orc_sir_run(_p(rp), _p(cl), ctypes.c_int64(st.size), _p(st), _p(r),
+                      ctypes.c_int32(steps), ctypes.c_float(beta), ctypes.c_float(gamma),
+                      _p(counts))
+    return st, counts, r

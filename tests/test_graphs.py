@@ -1,0 +1,71 @@
+"""Host-side network builders and ensemble specification (CPU only)."""
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from jaxabm_gb300 import ensemble, sir
+
+
+def _check_simple_symmetric(rp, col):
+    n = len(rp) - 1
+    a = sp.csr_matrix((np.ones(col.size, np.int32), col, rp), shape=(n, n))
+    assert (a != a.T).nnz == 0
+    assert a.diagonal().sum() == 0
+    assert a.max() == 1
+    for i in range(0, n, max(1, n // 50)):
+        row = col[rp[i]:rp[i + 1]]
+        assert np.all(np.diff(row) > 0)
+
+
+@pytest.mark.parametrize("n,m", [(10, 2), (1000, 4), (50_000, 4), (3000, 7)])
+def test_barabasi_albert(lib, n, m):
+    rp, col = sir.barabasi_albert(n, m, 5)
+    assert col.size == 2 * m * (n - m)
+    _check_simple_symmetric(rp, col)
+    deg = np.diff(rp)
+    assert deg.min() >= 1 and deg[m + 1:].min() >= m
+    # deterministic in the seed
+    rp2, col2 = sir.barabasi_albert(n, m, 5)
+    assert np.array_equal(col, col2)
+    assert not np.array_equal(col, sir.barabasi_albert(n, m, 6)[1])
+
+
+def test_barabasi_albert_bad_sizes(lib):
+    with pytest.raises(ValueError):
+        sir.barabasi_albert(3, 4)
+
+
+@pytest.mark.parametrize("n,d", [(40, 4), (1000, 16), (1 << 16, 16)])
+def test_random_regular(lib, n, d):
+    rp, col = sir.random_regular(n, d, 3)
+    assert np.all(np.diff(rp) == d)
+    _check_simple_symmetric(rp, col)
+
+
+def test_initial_states():
+    st = sir.initial_states(1 << 20, 0.001, 0)
+    assert (st == 1).sum() == 1048 and (st == 0).sum() == (1 << 20) - 1048
+    assert (sir.initial_states(500, 0.001, 0) == 1).sum() == 1
+
+
+def test_instance_layout(lib):
+    ensemble.check_layout()
+    assert ensemble.INSTANCE_DTYPE.itemsize == lib.abm_sir_instance_size()
+
+
+def test_tiles_cover_instance():
+    t = ensemble.tiles_for(3, 1000)
+    assert t[0].tolist() == [3, 0, 256, 0] and t[-1].tolist() == [3, 768, 1000, 0]
+    assert (t[:, 2] - t[:, 1]).sum() == 1000
+
+
+def test_ensemble_spec():
+    s = ensemble.ensemble_spec(4096)
+    assert s["n"].min() >= 1000 and s["n"].max() <= 100_000
+    assert 15_000 < s["n"].mean() < 28_000
+    assert s["beta"].min() >= 0.01 and s["beta"].max() <= 0.2
+    assert s["gamma"].min() >= 0.05 and s["gamma"].max() <= 0.3
+    assert s["arrival_s"][0] == 0.0 and np.all(np.diff(s["arrival_s"]) >= 0)
+    assert 15.0 < s["arrival_s"][-1] < 26.0
+    assert np.array_equal(s["n"], ensemble.ensemble_spec(4096)["n"])

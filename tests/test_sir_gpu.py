@@ -1,0 +1,140 @@
+"""SIR parity: bit-exact compartments and per-step S/I/R counts vs the C oracle, through the
+C ABI (plain single-model run and batched instances) and the jx.Model API."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import coracle, models
+
+pytestmark = pytest.mark.gpu
+
+
+def _graph(kind, n, seed=0):
+    from jaxabm_gb300 import sir
+    if kind == "ba":
+        return sir.barabasi_albert(n, 4, seed)
+    if kind == "ba2":
+        return sir.barabasi_albert(n, 2, seed)
+    if kind == "star":  # one hub of degree n-1 (warp-cooperative path), leaves of degree 1
+        rp = np.zeros(n + 1, np.int32)
+        rp[1] = n - 1
+        rp[2:] = n - 1 + np.arange(1, n)
+        col = np.concatenate([np.arange(1, n), np.zeros(n - 1)]).astype(np.int32)
+        return rp, col
+    if kind == "rr":
+        return sir.random_regular(n, 16, seed)
+    if kind == "clique":  # every row 63 long: every S agent takes the warp path
+        rp = (np.arange(n + 1) * (n - 1)).astype(np.int32)
+        col = np.concatenate([np.delete(np.arange(n), i) for i in range(n)]).astype(np.int32)
+        return rp, col
+    raise ValueError(kind)
+
+
+def _run_abi(rp, col, st0, seed, steps, beta, gamma):
+    from jaxabm_gb300 import _dev, _lib
+    import jaxabm_gb300.random as jr
+    rng, _ = models.model_keys(seed, 1)
+    ck = jr.keychain(_dev.keys_from_numpy(rng), steps, 1).reshape(steps, 2).contiguous()
+    n = st0.size
+    buf = torch.zeros(2 * n, dtype=torch.int8, device="cuda")
+    buf[:n] = torch.from_numpy(st0).cuda()
+    drp = torch.from_numpy(rp).cuda()
+    dcol = torch.from_numpy(col).cuda()
+    counts = torch.empty((steps, 3), dtype=torch.int32, device="cuda")
+    wsb = _lib.load().abm_sir_run_workspace_bytes(n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(buf), _dev.ptr(ck), steps,
+              beta, gamma, _dev.ptr(counts), _dev.ptr(ws), wsb, None)
+    torch.cuda.synchronize()
+    fin = buf[(steps & 1) * n:(steps & 1) * n + n].cpu().numpy()
+    return fin, counts.cpu().numpy()
+
+
+@pytest.mark.parametrize("kind,n,steps,beta,gamma", [
+    ("ba2", 200, 30, 0.3, 0.1),
+    ("ba", 5000, 60, 0.05, 0.1),
+    ("star", 3000, 25, 0.02, 0.05),
+    ("clique", 64, 20, 0.01, 0.2),
+    ("rr", 4096, 40, 0.1, 0.2),
+])
+def test_sir_abi_bit_exact(cuda, kind, n, steps, beta, gamma):
+    from jaxabm_gb300 import sir
+    rp, col = _graph(kind, n)
+    st0 = sir.initial_states(n, 0.01, 1)
+    fin, counts = _run_abi(rp, col, st0, 7, steps, beta, gamma)
+    rng, _ = models.model_keys(7, 1)
+    ref_st, ref_counts, _ = coracle.sir_run(rp, col, st0, rng, steps, beta, gamma)
+    assert np.array_equal(fin, ref_st)
+    assert np.array_equal(counts, ref_counts)
+
+
+def test_sir_full_config_bit_exact(cuda):
+    """N = 2^20 Barabasi-Albert (m=4), 0.1% infected, beta 0.05, gamma 0.1, 365 steps."""
+    from jaxabm_gb300 import sir
+    n = 1 << 20
+    rp, col = sir.barabasi_albert(n, 4, 0)
+    st0 = sir.initial_states(n, 0.001, 0)
+    fin, counts = _run_abi(rp, col, st0, 0, 365, 0.05, 0.1)
+    rng, _ = models.model_keys(0, 1)
+    ref_st, ref_counts, _ = coracle.sir_run(rp, col, st0, rng, 365, 0.05, 0.1)
+    assert np.array_equal(counts, ref_counts)
+    assert np.array_equal(fin, ref_st)
+    # size-independent properties: conservation and monotone R
+    assert np.all(counts.sum(axis=1) == n)
+    assert np.all(np.diff(counts[:, 2]) >= 0) and np.all(np.diff(counts[:, 0]) <= 0)
+
+
+def test_sir_model_api(cuda):
+    import jaxabm_gb300 as jx
+    from jaxabm_gb300 import sir
+    n = 20_000
+    model = jx.SIRModel({"n": n, "steps": 50, "seed": 3, "beta": 0.08, "gamma": 0.15})
+    res = model.run()
+    rp, col = sir.barabasi_albert(n, 4, 3)
+    st0 = sir.initial_states(n, 0.001, 3)
+    rng, _ = models.model_keys(3, 1)
+    ref_st, ref_counts, _ = coracle.sir_run(rp, col, st0, rng, 50, 0.08, 0.15)
+    assert np.array_equal(np.array([res["S"], res["I"], res["R"]]).T, ref_counts)
+    assert np.array_equal(res["agents.people.state"], ref_st)
+    # select the infected through the warp-ballot compaction
+    inf = model.agents.select(lambda s: s["state"] == 1)
+    assert len(inf) == int((ref_st == 1).sum())
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_sir_batched_equals_alone(cuda, use_graph):
+    """Each instance of a batch is bit-identical to the instance run alone."""
+    from jaxabm_gb300 import ensemble, sir
+    sizes = [300, 1000, 4097, 257, 256, 70_000]
+    seeds = [11, 12, 13, 14, 15, 16]
+    betas = [0.2, 0.05, 0.1, 0.15, 0.01, 0.06]
+    gammas = [0.05, 0.1, 0.3, 0.2, 0.1, 0.08]
+    graphs = [sir.barabasi_albert(n, 4, s) for n, s in zip(sizes, seeds)]
+    inits = [sir.initial_states(n, 0.002, s) for n, s in zip(sizes, seeds)]
+    steps = 45
+    b = ensemble.SIRBatch(graphs, inits, betas, gammas, seeds, steps)
+    b.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    for i in range(len(sizes)):
+        rng, _ = models.model_keys(seeds[i], 1)
+        ref_st, ref_counts, ref_rng = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng,
+                                                      steps, betas[i], gammas[i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), i
+        assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st), i
+        d = b.desc[i].cpu().numpy().view(np.uint32)
+        assert np.array_equal(d[ensemble.RNG_WORD:ensemble.RNG_WORD + 2], ref_rng)
+    # replay after reset reproduces the run
+    c0 = b.counts.clone()
+    b.reset()
+    b.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    assert torch.equal(c0, b.counts)
+
+
+def test_sir_bad_args(cuda):
+    from jaxabm_gb300 import _lib
+    L = _lib.load()
+    assert L.abm_sir_steps(None, 1, None, 0, 1, 0, None) == _lib.ABM_ERR_BADARG
+    assert L.abm_sir_run(None, None, 10, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
+        _lib.ABM_ERR_BADARG
