@@ -1,8 +1,18 @@
-"""Benchmark of the agent-step engine on one GB300 (agent-steps/s).
+"""Benchmark of the agent-step engine on one GB300: agent-steps/s, plain vs batched+served.
 
-Prints ONE JSON line on rank 0.  ``--impl reference`` times the CPU oracle port of the
-same workload on the host cores instead (the reference runs on JAX, which is not
-available on the GPU host).
+Default workload: the batched and served SIR ensemble -- 4,096 SIR instances on
+Barabasi-Albert graphs (m=4), agent counts log-uniform in [1e3, 1e5], (beta, gamma) from a
+scrambled Sobol sequence (seed 2), 365 steps each.  One bench step = the whole ensemble
+(all instances, all 365 steps) in one captured CUDA-graph launch; inputs (~3 GB of CSR)
+are larger than L2.  Reported beside it: ``e2e`` (same step through the public batch API
+with pinned host buffers: inputs H2D, counts D2H), ``plain`` (one simulation per launch
+sequence, the JaxModel.run path, on a sample of the instances), ``served`` (the Poisson
+request stream at 200 requests/s replayed in real time through the continuous-batching
+server: p50/p99 latency and throughput), and ``cpu_baseline`` (the C/OpenMP oracle on a
+sample of the instances, host cores).
+
+Prints ONE JSON line on rank 0.  ``--impl reference`` times the CPU port of the same
+workload (the reference itself runs on JAX, which the GPU host does not have).
 """
 
 import argparse
@@ -87,10 +97,8 @@ class ClockSampler:
 
 
 def _dist():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 def _barrier(world):
@@ -98,109 +106,152 @@ def _barrier(world):
         torch.distributed.barrier()
 
 
-def _max_over_ranks(v, world):
+def _reduce(v, world, op):
     if world == 1:
         return v
     t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    return float(t.item())
-
-
-def _sum_over_ranks(v, world):
-    if world == 1:
-        return v
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    torch.distributed.all_reduce(t, op=op)
     return float(t.item())
 
 
 # --------------------------------------------------------------------------------------
-# workloads
+# SIR ensemble (default workload)
 # --------------------------------------------------------------------------------------
 
-class RandomWalkBench:
-    """Quick-start random walk: N=10,000 agents, 100 steps, PRNGKey(0); one bench step is
-    one full 100-step run (1e6 agent-steps)."""
+class SIREnsembleBench:
+    name = "sir_ensemble_4096_ba_m4_n1e3_1e5_t365"
 
-    name = "randomwalk_n10000_t100"
-
-    def __init__(self, rank, n=10_000, steps=100, sigma=0.01):
-        from jaxabm_gb300 import _dev, _lib
-        import jaxabm_gb300.random as jr
-        from oracle import models
-        self._lib, self._dev, self.jr = _lib, _dev, jr
-        self.n, self.T, self.sigma = n, steps, sigma
-        rng, (ik,) = models.model_keys(rank, 1)
-        self.rng0 = rng
-        self.x = torch.empty(n, dtype=torch.float32, device="cuda")
-        self.y = torch.empty(n, dtype=torch.float32, device="cuda")
-        _lib.call("abm_randomwalk_init", _dev.ptr(self.x), _dev.ptr(self.y), n,
-                  _dev.ptr(_dev.keys_from_numpy(ik)), None)
-        self.x0 = self.x.clone()
-        self.y0 = self.y.clone()
-        self.rng = _dev.keys_from_numpy(rng)
-        self.ck = torch.empty((steps, 1, 2), dtype=torch.int32, device="cuda")
-        self.means = torch.empty((steps, 2), dtype=torch.float32, device="cuda")
-        wsb = _lib.load().abm_randomwalk_workspace_bytes(n, steps)
-        self.ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
-        self.launches_per_step = 3
-        self.units_per_step = n * steps
-        self.bytes_per_unit = 16  # read + write x, y per agent-step (keys live in registers)
-        self.h_x = torch.empty(n, dtype=torch.float32).pin_memory()
-        self.h_y = torch.empty(n, dtype=torch.float32).pin_memory()
-        self.h_x.copy_(self.x0.cpu())
-        self.h_y.copy_(self.y0.cpu())
-        self.h_means = torch.empty((steps, 2), dtype=torch.float32).pin_memory()
+    def __init__(self, rank, count=4096, steps=365):
+        from jaxabm_gb300 import ensemble
+        self.ensemble = ensemble
+        self.count, self.T = count, steps
+        spec = ensemble.ensemble_spec(count)
+        spec["seed"] = spec["seed"] + rank * count  # each rank its own members
+        self.spec = spec
+        t0 = time.perf_counter()
+        self.graphs, self.inits = ensemble.build_instances(spec)
+        self.build_s = time.perf_counter() - t0
+        self.batch = ensemble.SIRBatch(self.graphs, self.inits, spec["beta"], spec["gamma"],
+                                       spec["seed"], steps)
+        self.batch.capture(steps)
+        self.units_per_step = self.batch.agent_steps
+        self.launches_per_step = self.batch.launches_per_run()
+        # pinned host copies of the packed inputs for the end-to-end leg
+        b = self.batch
+        self.h_rp = torch.from_numpy(b.row_ptr.cpu().numpy()).pin_memory()
+        self.h_col = torch.from_numpy(b.col.cpu().numpy()).pin_memory()
+        self.h_state = torch.from_numpy(b.h_state0).pin_memory()
+        self.h_counts = torch.empty(b.counts.numel(), dtype=torch.int32).pin_memory()
 
     def reset(self):
-        self.x.copy_(self.x0)
-        self.y.copy_(self.y0)
+        self.batch.reset()
 
-    def step(self, stream, dom_events=None):
-        L, D = self._lib, self._dev
-        s = stream.cuda_stream
-        L.call("abm_keychain", D.ptr(self.rng), 1, 1, self.T, D.ptr(self.ck), None, s)
-        if dom_events:
-            dom_events[0].record(stream)
-        L.call("abm_randomwalk_run", D.ptr(self.x), D.ptr(self.y), self.n, D.ptr(self.ck), self.T,
-               self.sigma, D.ptr(self.means), D.ptr(self.ws), self.ws.numel(), s)
-        if dom_events:
-            dom_events[1].record(stream)
+    def step(self, stream, dom=None):
+        if dom:
+            dom[0].record(stream)
+        self.batch.replay()
+        if dom:
+            dom[1].record(stream)
 
     def e2e_step(self, stream):
-        """Same step through the C ABI with host buffers: H2D of the states, run, D2H of
-        the per-step means."""
-        self.x.copy_(self.h_x, non_blocking=True)
-        self.y.copy_(self.h_y, non_blocking=True)
-        self.step(stream)
-        self.h_means.copy_(self.means, non_blocking=True)
+        b = self.batch
+        b.row_ptr.copy_(self.h_rp, non_blocking=True)
+        b.col.copy_(self.h_col, non_blocking=True)
+        b.state.copy_(self.h_state, non_blocking=True)
+        b.desc.copy_(b.desc0)
+        b.counts.zero_()
+        b.replay()
+        self.h_counts.copy_(b.counts, non_blocking=True)
 
     @property
     def e2e_bytes(self):
-        return 8 * self.n, 8 * self.T
+        h2d = (self.h_rp.numel() + self.h_col.numel()) * 4 + self.h_state.numel()
+        return h2d, self.h_counts.numel() * 4
 
-    def cpu_baseline(self, threads):
-        from oracle import coracle
+    def algorithmic_bytes(self):
+        self.batch.reset()
+        self.batch.replay()
+        torch.cuda.synchronize()
+        return self.batch.algorithmic_bytes()
+
+    def plain(self, sample=48):
+        """One simulation per launch sequence (abm_sir_run, the JaxModel.run path), on the
+        first ``sample`` instances, each from device-resident inputs."""
+        from jaxabm_gb300 import _dev, _lib
+        import jaxabm_gb300.random as jr
+        L = _lib.load()
+        units, secs = 0, 0.0
+        for i in range(min(sample, self.count)):
+            rp, col = self.graphs[i]
+            n = len(rp) - 1
+            drp = torch.from_numpy(rp).cuda()
+            dcol = torch.from_numpy(col).cuda()
+            buf = torch.zeros(2 * n, dtype=torch.int8, device="cuda")
+            buf[:n] = torch.from_numpy(self.inits[i]).cuda()
+            counts = torch.empty((self.T, 3), dtype=torch.int32, device="cuda")
+            ws = torch.empty(L.abm_sir_run_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            rng = self.ensemble.model_rngs([int(self.spec["seed"][i])])[0].contiguous()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ck = jr.keychain(rng, self.T, 1).reshape(self.T, 2).contiguous()
+            _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(buf), _dev.ptr(ck),
+                      self.T, float(self.spec["beta"][i]), float(self.spec["gamma"][i]),
+                      _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
+            torch.cuda.synchronize()
+            secs += time.perf_counter() - t0
+            units += n * self.T
+        return {"value": units / secs, "unit": "agent-steps/s",
+                "sample": f"first {min(sample, self.count)} instances, one simulation per "
+                          f"launch sequence (keychain + 2 launches per step)"}
+
+    def served(self, rate_scale=1.0):
+        """Real-time replay of the Poisson request stream through the server."""
+        from jaxabm_gb300.serving import Request, SIRServer
+        reqs = []
+        for i in range(self.count):
+            rp, col = self.graphs[i]
+            reqs.append(Request(i, torch.from_numpy(rp).pin_memory(),
+                                torch.from_numpy(col).pin_memory(),
+                                torch.from_numpy(self.inits[i]).pin_memory(),
+                                self.spec["beta"][i], self.spec["gamma"][i],
+                                int(self.spec["seed"][i]), self.T))
+        srv = SIRServer(max_slots=1024, max_tiles=1 << 17, steps_per_tick=32)
+        torch.cuda.synchronize()
+        wall = srv.serve(reqs, self.spec["arrival_s"] / rate_scale)
+        lat = srv.latencies()
+        units = sum(r.n for r in reqs) * self.T
+        # spot-check a few results against the batched run (bit-identical by design)
+        self.batch.reset()
+        self.batch.replay()
+        torch.cuda.synchronize()
+        same = all(np.array_equal(r.counts.numpy(), self.batch.counts_of(r.rid).cpu().numpy())
+                   for r in sorted(srv.completed, key=lambda r: r.rid)[:: max(1, self.count // 16)])
+        return {"value": units / wall, "unit": "agent-steps/s",
+                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "requests": len(lat), "rate_per_s": 200.0 * rate_scale, "wall_s": wall,
+                "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
+                "results_match_batched": bool(same)}
+
+    def cpu_baseline(self, threads, budget_s=12.0):
+        from oracle import coracle, models
         coracle.set_threads(threads)
-        n, T = self.n, self.T
-        reps = 0
-        t0 = time.perf_counter()
-        while True:
-            coracle.randomwalk_run(0, n, T, self.sigma)
-            reps += 1
-            if time.perf_counter() - t0 > 10.0 or reps >= 200:
-                break
-        dt = time.perf_counter() - t0
-        return {"value": reps * n * T / dt, "unit": "agent-steps/s", "cores": threads,
-                "kind": "port", "sample": f"{reps} full runs of N={n}, T={T} (C oracle, OpenMP)"}
+        units, secs, k = 0, 0.0, 0
+        while k < self.count and secs < budget_s:
+            rp, col = self.graphs[k]
+            rng, _ = models.model_keys(int(self.spec["seed"][k]), 1)
+            t0 = time.perf_counter()
+            coracle.sir_run(rp, col, self.inits[k], rng, self.T, float(self.spec["beta"][k]),
+                            float(self.spec["gamma"][k]))
+            secs += time.perf_counter() - t0
+            units += (len(rp) - 1) * self.T
+            k += 1
+        return {"value": units / secs, "unit": "agent-steps/s", "cores": threads, "kind": "port",
+                "sample": f"first {k} of {self.count} instances, 365 steps each, C/OpenMP oracle"}
 
 
-WORKLOADS = {"randomwalk": RandomWalkBench}
-DEFAULT_WORKLOAD = "randomwalk"
-
-
-def _flush_l2(buf):
-    buf.add_(1)
+WORKLOADS = {"sir_ensemble": SIREnsembleBench}
+DEFAULT_WORKLOAD = "sir_ensemble"
 
 
 def run_ours(args):
@@ -213,70 +264,75 @@ def run_ours(args):
     jx.build()
     wl = WORKLOADS[args.workload](rank)
     stream = torch.cuda.current_stream()
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         wl.reset()
         wl.step(stream)
     torch.cuda.synchronize()
 
-    # device-resident timed region: per-step events, L2 flushed between steps
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    dom = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
     _barrier(world)
     torch.cuda.synchronize()
     for i in range(args.steps):
         wl.reset()
-        _flush_l2(flush)
-        starts[i].record(stream)
-        wl.step(stream, dom[i])
-        ends[i].record(stream)
+        wl.step(stream, (starts[i], ends[i]))
     torch.cuda.synchronize()
     _barrier(world)
     clk = clocks.stop()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
-    dom_ms = sum(a.elapsed_time(b) for a, b in dom) / args.steps
-    ms = _max_over_ranks(ms, world)
+    ms_local = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    ms = _reduce(ms_local, world, torch.distributed.ReduceOp.MAX if world > 1 else None)
 
-    # end-to-end through the C ABI with host buffers
+    # end-to-end through the batch API with pinned host buffers
     for _ in range(2):
         wl.e2e_step(stream)
     torch.cuda.synchronize()
     _barrier(world)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
         wl.e2e_step(stream)
     e1.record(stream)
     torch.cuda.synchronize()
     _barrier(world)
-    e2e_ms = _max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    e2e_ms = _reduce(e0.elapsed_time(e1) / args.steps, world,
+                     torch.distributed.ReduceOp.MAX if world > 1 else None)
 
-    units = _sum_over_ranks(wl.units_per_step, world)
+    units = _reduce(wl.units_per_step, world, torch.distributed.ReduceOp.SUM if world > 1 else None)
     value = units / (ms / 1e3)
     hbm_peak, peak_kind = _peaks()
-    achieved = wl.units_per_step * wl.bytes_per_unit / (dom_ms / 1e3) / 1e9
+    alg_bytes = wl.algorithmic_bytes()
+    achieved = alg_bytes / (ms_local / 1e3) / 1e9
     h2d, d2h = wl.e2e_bytes
     out = {
         "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8",
         "data": "synthetic",
-        "config": {"workload": wl.name, "l2": "flushed between timed steps (256 MiB write)",
-                   "parallelism": f"replicas{world}"},
+        "config": {"workload": wl.name, "instances": wl.count, "steps_per_instance": wl.T,
+                   "agents": int(wl.batch.n.sum()), "directed_edges": int(wl.batch.e.sum()),
+                   "l2": "inputs larger than L2 (CSR %.2f GB)" % (wl.batch.e.sum() * 4 / 1e9),
+                   "parallelism": f"instances sharded over {world} GPU(s)"},
         "e2e": {"value": units / (e2e_ms / 1e3), "unit": "agent-steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": wl.launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind},
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                     if peak_kind == "measured" else "fallback",
+                     "kernel": "sir_step_kernel (+ per-step finalize) in one graph replay",
+                     "algorithmic_bytes_per_step": alg_bytes},
         "clocks": clk,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if not args.quick:
+        out["plain"] = wl.plain()
+        out["plain"]["batched_over_plain"] = value / out["plain"]["value"]
+        out["served"] = wl.served()
+        out["served"]["served_over_plain"] = out["served"]["value"] / out["plain"]["value"]
+    if rank == 0 and world == 1 and not args.quick:
         out["cpu_baseline"] = wl.cpu_baseline(os.cpu_count() or 1)
+    out["setup_s"] = {"graph_build": wl.build_s}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -284,33 +340,44 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """CPU port of the same workload on all host cores: each step runs a bounded sample of
+    the ensemble's instances (the first ``sample`` members, 365 steps each)."""
     world, rank, _ = _dist()
     if rank != 0:
         return
-    sys.path.insert(0, ROOT)
-    from oracle import coracle
+    from jaxabm_gb300 import ensemble
+    from oracle import coracle, models
     cores = os.cpu_count() or 1
     coracle.set_threads(cores)
-    wl_cls = WORKLOADS[args.workload]
-    name = wl_cls.name
-    times = []
-    n, T = 10_000, 100
-    for i in range(args.warmup + args.steps):
+    count, T, sample = 4096, 365, 64
+    spec = ensemble.ensemble_spec(count)
+    sub = {k: v[:sample] for k, v in spec.items()}
+    graphs, inits = ensemble.build_instances(sub)
+    times, units = [], 0
+    for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        coracle.randomwalk_run(0, n, T)
+        u = 0
+        for k in range(sample):
+            rp, col = graphs[k]
+            rng, _ = models.model_keys(int(sub["seed"][k]), 1)
+            coracle.sir_run(rp, col, inits[k], rng, T, float(sub["beta"][k]), float(sub["gamma"][k]))
+            u += (len(rp) - 1) * T
         dt = time.perf_counter() - t0
-        if i >= args.warmup:
+        if it >= args.warmup:
             times.append(dt)
+            units = u
     ms = 1e3 * sum(times) / len(times)
-    value = n * T / (ms / 1e3)
+    value = units / (ms / 1e3)
     out = {"metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8",
            "data": "synthetic", "impl": "reference",
-           "config": {"workload": name, "parallelism": "host cores"},
+           "config": {"workload": SIREnsembleBench.name, "parallelism": "host cores"},
            "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": cores,
                             "kind": "port",
-                            "sample": f"full N={n}, T={T} runs (C oracle, OpenMP)"},
+                            "sample": f"first {sample} of {count} ensemble instances per step, "
+                                      f"{T} steps each (C/OpenMP port; the reference needs JAX, "
+                                      f"absent on this host)"},
            "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
@@ -319,14 +386,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the batched value and e2e (no plain/served/cpu legs)")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -138,13 +138,14 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
                                      int32_t* col, int64_t col_capacity);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (80 bytes, 8-byte aligned).
+/* Device-side descriptor of one SIR model instance (88 bytes, 8-byte aligned).
  * state holds 2*n int8 compartments (0 S, 1 I, 2 R); buffer (t & 1) is current.
  * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
  * NULL, else it is derived from rng, the instance's Model.step key-chain state
  * (jaxabm/model.py:156,164), which is advanced once per step either way.  counts receives
  * S, I, R after each step (int32[steps][3], zeroed by the caller); done_flag (nullable,
- * may be host-mapped) is set to 1 after the last step. */
+ * may be host-mapped) is set to 1 after the last step; edges_scanned accumulates the CSR
+ * slots the step kernel examined (the algorithmic gather volume). */
 typedef struct abm_sir_instance {
   const int32_t* row_ptr;
   const int32_t* col;
@@ -159,6 +160,7 @@ typedef struct abm_sir_instance {
   float beta;
   float gamma;
   int32_t reserved;
+  unsigned long long edges_scanned;
 } abm_sir_instance;
 
 /* A tile of agents [begin, end) of instance `inst` (end - begin <= 256). */

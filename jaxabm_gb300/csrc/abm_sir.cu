@@ -29,16 +29,16 @@ constexpr int kSirWarps = kSirThreads / 32;
 constexpr int kHeavyDeg = 32;
 constexpr unsigned kFull = 0xffffffffu;
 
-static_assert(sizeof(abm_sir_instance) == 80, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 88, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
 __global__ void __launch_bounds__(kSirThreads)
 sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work, int nwork) {
-  __shared__ int scount[3][kSirWarps];
+  __shared__ int scount[4][kSirWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
-    const abm_sir_instance* I = insts + item.x;
+    abm_sir_instance* I = insts + item.x;
     const int t = I->t;
     if (t >= I->steps) continue;  // uniform over the CTA
     const int n = I->n;
@@ -58,7 +58,7 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
     const int8_t s = valid ? cur[i] : (int8_t)2;
     int8_t ns = s;
     bool heavy = false;
-    int row0 = 0, deg = 0;
+    int row0 = 0, deg = 0, scanned = 0;
     if (s == 0) {
       row0 = rp[i];
       deg = rp[i + 1] - row0;
@@ -67,7 +67,8 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
       } else {
         bool have = false;
         uint2 kinf = make_uint2(0, 0);
-        for (int k = 0; k < deg; ++k) {
+        int k = 0;
+        for (; k < deg; ++k) {
           const int j = col[row0 + k];
           if (cur[j] == 1) {
             if (!have) {
@@ -76,10 +77,12 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
             }
             if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
               ns = 1;
+              ++k;
               break;
             }
           }
         }
+        scanned = k;
       }
     } else if (s == 1) {
       const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
@@ -95,7 +98,8 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
       const int hdeg = __shfl_sync(kFull, deg, src);
       const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
       bool fired = false;
-      for (int c = 0; c < hdeg && !fired; c += 32) {
+      int c = 0;
+      for (; c < hdeg && !fired; c += 32) {
         const int k = c + lane;
         bool f = false;
         if (k < hdeg) {
@@ -104,24 +108,34 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
         }
         fired = __any_sync(kFull, f);
       }
-      if (lane == src && fired) ns = 1;
+      if (lane == src) {
+        if (fired) ns = 1;
+        scanned = min(c, hdeg);
+      }
     }
 
     if (valid) nxt[i] = ns;
     const int cs = abm::warp_sum((int)(valid && ns == 0));
     const int ci = abm::warp_sum((int)(valid && ns == 1));
     const int cr = abm::warp_sum((int)(valid && ns == 2));
+    const int ce = abm::warp_sum(scanned);
     if (lane == 0) {
       scount[0][warp] = cs;
       scount[1][warp] = ci;
       scount[2][warp] = cr;
+      scount[3][warp] = ce;
     }
     __syncthreads();
-    if (threadIdx.x < 3) {
+    if (threadIdx.x < 4) {
       int sum = 0;
 #pragma unroll
       for (int q = 0; q < kSirWarps; ++q) sum += scount[threadIdx.x][q];
-      if (sum) atomicAdd(&I->counts[3 * t + threadIdx.x], sum);
+      if (sum) {
+        if (threadIdx.x < 3)
+          atomicAdd(&I->counts[3 * t + threadIdx.x], sum);
+        else
+          atomicAdd(&I->edges_scanned, (unsigned long long)sum);
+      }
     }
     __syncthreads();
   }
@@ -167,6 +181,7 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->beta = beta;
     d->gamma = gamma;
     d->reserved = 0;
+    d->edges_scanned = 0;
   }
   for (int b = g; b < ntiles; b += gridDim.x * blockDim.x) {
     const int begin = b * kSirThreads;

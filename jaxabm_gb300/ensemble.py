@@ -25,13 +25,14 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 256
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 80 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 88 bytes
 INSTANCE_DTYPE = np.dtype([
     ("row_ptr", "<u8"), ("col", "<u8"), ("state", "<u8"), ("counts", "<u8"),
     ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)), ("n", "<i4"),
     ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("reserved", "<i4"),
+    ("edges_scanned", "<u8"),
 ])
-assert INSTANCE_DTYPE.itemsize == 80
+assert INSTANCE_DTYPE.itemsize == 88
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
 
@@ -96,6 +97,7 @@ class SIRBatch:
         self.col = torch.from_numpy(h_col).to(dev)
         self.state = torch.from_numpy(h_st).to(dev)
         self.h_state0 = h_st
+        self.s0 = np.array([int((st == 0).sum()) for st in init_states], dtype=np.int64)
         self.counts = torch.zeros(int(cnt_off[-1]), dtype=torch.int32, device=dev)
         self._offsets = (rp_off, col_off, st_off, cnt_off)
         desc = np.zeros(k, dtype=INSTANCE_DTYPE)
@@ -109,7 +111,8 @@ class SIRBatch:
         desc["beta"] = np.asarray(betas, dtype=np.float32)
         desc["gamma"] = np.asarray(gammas, dtype=np.float32)
         self.h_desc0 = desc
-        self.desc = torch.from_numpy(desc.view(np.int32).reshape(k, 20).copy()).to(dev)
+        words = INSTANCE_DTYPE.itemsize // 4
+        self.desc = torch.from_numpy(desc.view(np.int32).reshape(k, words).copy()).to(dev)
         self.rng0 = model_rngs(seeds)
         self.desc[:, RNG_WORD:RNG_WORD + 2] = self.rng0
         self.desc0 = self.desc.clone()
@@ -170,6 +173,19 @@ class SIRBatch:
     def counts_of(self, i):
         c = self._offsets[3]
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
+
+    def edges_scanned(self):
+        """CSR slots examined by the step kernel, summed over instances since reset."""
+        d = self.desc.cpu().numpy().view(INSTANCE_DTYPE).reshape(-1)
+        return int(d["edges_scanned"].sum())
+
+    def algorithmic_bytes(self):
+        """Bytes the run must move (after it completed): per step and instance 2 bytes of
+        state per agent (read + write), 4 bytes of row offset per susceptible agent, and
+        4 + 1 bytes (column index + neighbour state) per CSR slot examined."""
+        counts = self.counts.reshape(self.k, self.steps, 3).cpu().numpy().astype(np.int64)
+        s_pre = np.concatenate([self.s0[:, None], counts[:, :-1, 0]], axis=1)
+        return int(2 * self.n.sum() * self.steps + 4 * s_pre.sum() + 5 * self.edges_scanned())
 
     def launches_per_run(self):
         return 2 * self.steps

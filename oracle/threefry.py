@@ -225,7 +225,8 @@ def randint(key, shape, minval, maxval, mode=PARTITIONABLE):
     hi = bits(k[0], shape, mode).astype(np.uint64)
     lo = bits(k[1], shape, mode).astype(np.uint64)
     span = 1 if maxval <= minval else (int(maxval) - int(minval)) & 0xFFFFFFFF
-    mult = (65536 % span) ** 2 % span
+    mult = 65536 % span
+    mult = ((mult * mult) & 0xFFFFFFFF) % span  # the square wraps in uint32, as in JAX
     r = (((hi % span) * np.uint64(mult)) & np.uint64(0xFFFFFFFF)) + (lo % span)
     r = (r & np.uint64(0xFFFFFFFF)) % np.uint64(span)
     return ((np.int64(minval) + r.astype(np.int64)) & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
