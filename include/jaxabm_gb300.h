@@ -196,6 +196,74 @@ ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, i
                         const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
                         int32_t* counts, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- K3/K4: Schelling segregation on a torus Grid ----------------------------------- */
+/* Cell (x, y) of a W x H grid has index x*H + y; grid int8[W*H] holds -1 (empty) or the
+ * occupant's type, cell_agent int32[W*H] the occupant id or -1. */
+ABM_API size_t abm_schelling_workspace_bytes(int64_t n, int32_t W, int32_t H);
+
+/* Build grid and cell_agent from agent positions pos int32[n] (cell indices) and types
+ * int8[n] (>= 0).  *status (device int32) becomes 1 if a position is out of range or two
+ * agents share a cell.  Replaces Grid.position_agents + the grid fill of the Schelling
+ * example (jaxabm/agentpy.py:496-527, examples/models/schelling_model.py:118-133). */
+ABM_API int abm_schelling_place(const int32_t* pos, const int8_t* type, int64_t n, int32_t W,
+                                int32_t H, int8_t* grid, int32_t* cell_agent, int32_t* status,
+                                void* stream);
+
+/* `steps` synchronous Schelling steps with per-step collection keys coll_keys
+ * uint32[steps][2]: an agent is unhappy iff 8*same < 3*occupied over its Moore-8 torus
+ * neighbours; each unhappy agent draws idx = min(floor(uniform(agent_key) * e), e - 1)
+ * into the ascending list of the e pre-step empty cells and claims that cell; the lowest
+ * claiming id moves.  pos, grid and cell_agent are updated in place; stats int32[steps][2]
+ * receives (unhappy, moved) per step.  Replaces the vmapped Agent.step of the Schelling
+ * model (examples/models/schelling_model.py:33-68, jaxabm/agent.py:168-177) with the
+ * neighbourhood rule and relocation it leaves as placeholders. */
+ABM_API int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, int32_t H,
+                              int8_t* grid, int32_t* cell_agent, const uint32_t* coll_keys,
+                              int32_t steps, int32_t* stats, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
+/* ---- K8: differentiable bounded-confidence opinion model ---------------------------- */
+/* B instances (B a power of two, 4 <= B <= 128) share one symmetric CSR graph; opinions
+ * are interleaved o float32[n][B] (16-byte aligned); mu, eps, tau are float32[B].
+ * Per step: o_i += mu * (sum_j sigmoid((eps - |o_j - o_i|) / tau) (o_j - o_i)) / deg_i.
+ * The reference trains such models with jit(grad(loss)) through its whole run loop
+ * (jaxabm/analysis.py:494-522); these entry points give the forward pass, checkpoints and
+ * the hand-written reverse pass. */
+
+/* `steps` forward steps in place (o_tmp: scratch of the same shape).  When checkpoints is
+ * not NULL, the state before step t is stored at checkpoints[t / ckpt_every] for every t
+ * that is a multiple of ckpt_every. */
+ABM_API int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, const int32_t* col,
+                            int64_t n, int32_t B, const float* mu, const float* eps,
+                            const float* tau, int32_t steps, int32_t ckpt_every,
+                            float* checkpoints, void* stream);
+
+ABM_API size_t abm_opinion_moments_workspace_bytes(int64_t n, int32_t B);
+
+/* Raw moments m_k = mean_i o_i^k, k = 1..4, per instance -> moments float64[B][4]. */
+ABM_API int abm_opinion_moments(const float* o, int64_t n, int32_t B, double* moments,
+                                void* workspace, size_t workspace_bytes, void* stream);
+
+/* Terminal adjoint lambda_i = sum_k dloss_dmoments[b][k-1] * k * o_i^(k-1) / n. */
+ABM_API int abm_opinion_adjoint_init(const float* o, int64_t n, int32_t B,
+                                     const double* dloss_dmoments, float* lam, void* stream);
+
+/* Bytes of the per-CTA parameter-gradient partials (float64) of abm_opinion_adjoint_step;
+ * the caller zeroes them once before the reverse sweep. */
+ABM_API size_t abm_opinion_grad_workspace_bytes(int64_t n, int32_t B);
+
+/* One reverse step at forward state o (= o^t): lam_out = lambda^t from lam_in =
+ * lambda^{t+1}, and grad_partials += lambda^{t+1} . dF/d(mu, eps, tau). */
+ABM_API int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out,
+                                     const int32_t* row_ptr, const int32_t* col, int64_t n,
+                                     int32_t B, const float* mu, const float* eps,
+                                     const float* tau, double* grad_partials,
+                                     size_t grad_partials_bytes, void* stream);
+
+/* grads float64[B][3] (d/dmu, d/deps, d/dtau) from the accumulated partials. */
+ABM_API int abm_opinion_grad_reduce(const double* grad_partials, int64_t n, int32_t B,
+                                    double* grads, void* stream);
+
 /* ---- K6: stable compaction (AgentList.select / AgentCollection.filter) -------------- */
 ABM_API size_t abm_select_workspace_bytes(int64_t n);
 

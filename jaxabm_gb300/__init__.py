@@ -24,6 +24,8 @@ from . import randomwalk  # noqa: E402  registers RandomWalker
 from .randomwalk import RandomWalker, RandomWalkModel  # noqa: E402
 from . import sir  # noqa: E402  registers SIRAgent
 from .sir import SIRAgent, SIRModel  # noqa: E402
+from . import schelling  # noqa: E402  registers SchellingAgent
+from .schelling import SchellingAgent, SchellingModel  # noqa: E402
 
 
 def build(force: bool = False) -> str:

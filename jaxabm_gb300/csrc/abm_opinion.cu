@@ -1,0 +1,354 @@
+// Differentiable bounded-confidence opinion model on a symmetric network (K8).
+//
+// B calibration instances share one CSR graph; their opinions are interleaved o[N][B]
+// (float32), so a neighbour's B values are one contiguous 4*B-byte row: a group of B/4
+// lanes reads it with 128-bit loads.  Per step, for node i and instance b:
+//   d_j = o_j - o_i;  s_j = sigmoid((eps_b - |d_j|) * (1/tau_b))
+//   o_i' = o_i + mu_b * (sum_j s_j d_j) / deg_i                (fused multiply-adds)
+// which is the model o_i += mu * mean_j sigmoid((eps - |o_j - o_i|)/tau) (o_j - o_i).
+//
+// Adjoint (reverse mode, the gradient jax.grad of the reference's run loop would give,
+// jaxabm/analysis.py:494-522): with g(d) = s d and g'(d) = s - |d| s (1 - s) / tau,
+//   lambda_i^t = lambda_i + mu * sum_{j in N(i)} g'(d_ij) (lambda_j / deg_j - lambda_i / deg_i)
+// (valid because the graph is symmetric and g' is even), and the parameter gradients
+// accumulate lambda_i^{t+1} dF_i/dtheta at o^t:
+//   dF_i/dmu  = (1/deg_i) sum_j g(d_ij)
+//   dF_i/deps = (mu/deg_i) sum_j s(1-s) d_ij / tau
+//   dF_i/dtau = (mu/deg_i) sum_j s(1-s) (-z_ij / tau) d_ij,   z = (eps - |d|) / tau
+// The per-CTA partial sums of the parameter gradients are kept per CTA across all steps
+// and reduced in a fixed order, so gradients are deterministic.
+
+#include "abm_common.cuh"
+
+namespace {
+
+constexpr int kOpThreads = 256;
+
+__device__ __forceinline__ float comp(const float4& v, int c) {
+  return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void set_comp(float4& v, int c, float x) {
+  if (c == 0) v.x = x;
+  else if (c == 1) v.y = x;
+  else if (c == 2) v.z = x;
+  else v.w = x;
+}
+
+__device__ __forceinline__ float sigmoid_of(float eps, float itau, float d) {
+  const float z = (eps - fabsf(d)) * itau;
+  return 1.0f / (1.0f + expf(-z));
+}
+
+template <int LPN>
+__global__ void __launch_bounds__(kOpThreads)
+opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
+                    const int32_t* __restrict__ rp, const int32_t* __restrict__ col, int n, int B,
+                    const float* __restrict__ mu, const float* __restrict__ eps,
+                    const float* __restrict__ tau) {
+  const long long g = (long long)blockIdx.x * kOpThreads + threadIdx.x;
+  const int node = (int)(g / LPN);
+  const int sub = (int)(g % LPN);
+  if (node >= n) return;
+  const float4 m4 = reinterpret_cast<const float4*>(mu)[sub];
+  const float4 e4 = reinterpret_cast<const float4*>(eps)[sub];
+  const float4 t4 = reinterpret_cast<const float4*>(tau)[sub];
+  const float4 it4 = make_float4(1.0f / t4.x, 1.0f / t4.y, 1.0f / t4.z, 1.0f / t4.w);
+  const float4 oi = reinterpret_cast<const float4*>(o + (size_t)node * B)[sub];
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int r0 = rp[node], r1 = rp[node + 1];
+  for (int e = r0; e < r1; ++e) {
+    const int j = col[e];
+    const float4 oj = reinterpret_cast<const float4*>(o + (size_t)j * B)[sub];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float d = comp(oj, c) - comp(oi, c);
+      const float s = sigmoid_of(comp(e4, c), comp(it4, c), d);
+      set_comp(acc, c, fmaf(s, d, comp(acc, c)));
+    }
+  }
+  float4 res = oi;
+  const int deg = r1 - r0;
+  if (deg > 0) {
+    const float fdeg = (float)deg;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) set_comp(res, c, fmaf(comp(m4, c), comp(acc, c) / fdeg, comp(oi, c)));
+  }
+  reinterpret_cast<float4*>(out + (size_t)node * B)[sub] = res;
+}
+
+// One adjoint step: lam_out from lam_in (= lambda^{t+1}) at the forward state o (= o^t);
+// gpart[cta][b][3] += this CTA's lambda * dF/d(mu, eps, tau).
+template <int LPN>
+__global__ void __launch_bounds__(kOpThreads)
+opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ lam_in,
+                       float* __restrict__ lam_out, const int32_t* __restrict__ rp,
+                       const int32_t* __restrict__ col, int n, int B, const float* __restrict__ mu,
+                       const float* __restrict__ eps, const float* __restrict__ tau,
+                       double* __restrict__ gpart) {
+  extern __shared__ double sg[];  // [kOpThreads / LPN][B/4 groups -> per thread 12 values]
+  const long long g = (long long)blockIdx.x * kOpThreads + threadIdx.x;
+  const int node = (int)(g / LPN);
+  const int sub = (int)(g % LPN);
+  float gm[4] = {0.f, 0.f, 0.f, 0.f}, ge[4] = {0.f, 0.f, 0.f, 0.f}, gt[4] = {0.f, 0.f, 0.f, 0.f};
+  if (node < n) {
+    const float4 m4 = reinterpret_cast<const float4*>(mu)[sub];
+    const float4 e4 = reinterpret_cast<const float4*>(eps)[sub];
+    const float4 t4 = reinterpret_cast<const float4*>(tau)[sub];
+    const float4 it4 = make_float4(1.0f / t4.x, 1.0f / t4.y, 1.0f / t4.z, 1.0f / t4.w);
+    const float4 oi = reinterpret_cast<const float4*>(o + (size_t)node * B)[sub];
+    const float4 li = reinterpret_cast<const float4*>(lam_in + (size_t)node * B)[sub];
+    const int r0 = rp[node], r1 = rp[node + 1];
+    const float fdeg_i = (float)(r1 - r0);
+    float4 li_d = li;
+    float sl[4] = {0.f, 0.f, 0.f, 0.f};  // sum_j g'(d) (lam_j/deg_j - lam_i/deg_i)
+    float sgd[4] = {0.f, 0.f, 0.f, 0.f}, sse[4] = {0.f, 0.f, 0.f, 0.f}, sst[4] = {0.f, 0.f, 0.f, 0.f};
+    if (r1 > r0) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) set_comp(li_d, c, comp(li, c) / fdeg_i);
+    }
+    for (int e = r0; e < r1; ++e) {
+      const int j = col[e];
+      const float4 oj = reinterpret_cast<const float4*>(o + (size_t)j * B)[sub];
+      const float4 lj = reinterpret_cast<const float4*>(lam_in + (size_t)j * B)[sub];
+      const float fdeg_j = (float)(rp[j + 1] - rp[j]);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float d = comp(oj, c) - comp(oi, c);
+        const float a = fabsf(d);
+        const float itau = comp(it4, c);
+        const float z = (comp(e4, c) - a) * itau;
+        const float s = 1.0f / (1.0f + expf(-z));
+        const float sp = s * (1.0f - s);
+        const float gprime = s - a * sp * itau;
+        sl[c] = fmaf(gprime, comp(lj, c) / fdeg_j - comp(li_d, c), sl[c]);
+        sgd[c] = fmaf(s, d, sgd[c]);
+        sse[c] = fmaf(sp * itau, d, sse[c]);
+        sst[c] = fmaf(-sp * z * itau, d, sst[c]);
+      }
+    }
+    float4 lo;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      set_comp(lo, c, fmaf(comp(m4, c), sl[c], comp(li, c)));
+      if (r1 > r0) {
+        gm[c] = comp(li, c) * (sgd[c] / fdeg_i);
+        ge[c] = comp(li, c) * comp(m4, c) * (sse[c] / fdeg_i);
+        gt[c] = comp(li, c) * comp(m4, c) * (sst[c] / fdeg_i);
+      }
+    }
+    reinterpret_cast<float4*>(lam_out + (size_t)node * B)[sub] = lo;
+  }
+  // per-CTA reduction of the parameter gradients per instance column (fixed order)
+  constexpr int kNodes = kOpThreads / LPN;
+  double* mine = sg + (size_t)threadIdx.x * 12;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    mine[c] = gm[c];
+    mine[4 + c] = ge[c];
+    mine[8 + c] = gt[c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < LPN * 12; q += kOpThreads) {
+    const int s_ = q / 12, v = q % 12;
+    double acc = 0.0;
+    for (int k = 0; k < kNodes; ++k) acc += sg[(size_t)(k * LPN + s_) * 12 + v];
+    // v: param*4 + component; instance b = 4*s_ + component
+    const int param = v / 4, c = v % 4;
+    const int b = 4 * s_ + c;
+    gpart[((size_t)blockIdx.x * B + b) * 3 + param] += acc;
+  }
+}
+
+// lambda^T_i = sum_k dL/dm_k * k * o_i^(k-1) / N for the raw moments m_k, k = 1..4.
+__global__ void opinion_adjoint_init_kernel(const float* __restrict__ o, int n, int B,
+                                            const double* __restrict__ dldm,
+                                            float* __restrict__ lam) {
+  const long long total = (long long)n * B;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(g % B);
+    const double x = o[g];
+    const double* w = dldm + 4 * b;
+    lam[g] = (float)((w[0] + 2.0 * w[1] * x + 3.0 * w[2] * x * x + 4.0 * w[3] * x * x * x) / n);
+  }
+}
+
+// Raw moments: per-CTA partials in double, then a fixed-order final sum.
+__global__ void __launch_bounds__(kOpThreads)
+opinion_moments_partial_kernel(const float* __restrict__ o, int n, int B, int rows_per_cta,
+                               double* __restrict__ part) {
+  // thread t handles instance column b = t % B for rows r0 + t / B, stepping kOpThreads / B rows
+  extern __shared__ double sm[];  // [kOpThreads][4]
+  const int per = kOpThreads / B;  // B <= kOpThreads and divides it
+  const int b = threadIdx.x % B, r = threadIdx.x / B;
+  double a1 = 0, a2 = 0, a3 = 0, a4 = 0;
+  const int r0 = blockIdx.x * rows_per_cta;
+  const int r1 = min(n, r0 + rows_per_cta);
+  for (int i = r0 + r; i < r1; i += per) {
+    const double x = o[(size_t)i * B + b];
+    const double x2 = x * x;
+    a1 += x;
+    a2 += x2;
+    a3 += x2 * x;
+    a4 += x2 * x2;
+  }
+  double* mine = sm + 4 * threadIdx.x;
+  mine[0] = a1;
+  mine[1] = a2;
+  mine[2] = a3;
+  mine[3] = a4;
+  __syncthreads();
+  if (threadIdx.x < B) {
+    double s[4] = {0, 0, 0, 0};
+    for (int k = 0; k < per; ++k)
+      for (int q = 0; q < 4; ++q) s[q] += sm[4 * (k * B + threadIdx.x) + q];
+    for (int q = 0; q < 4; ++q) part[((size_t)blockIdx.x * B + threadIdx.x) * 4 + q] = s[q];
+  }
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ part, int nparts, int width,
+                                    double scale, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= width) return;
+  double s = 0.0;
+  for (int p = 0; p < nparts; ++p) s += part[(size_t)p * width + k];
+  out[k] = s * scale;
+}
+
+bool valid_batch(int B) { return B >= 4 && B <= 128 && (B & (B - 1)) == 0; }
+
+int step_blocks(int64_t n, int B) {
+  const long long threads = n * (long long)(B / 4);
+  return (int)((threads + kOpThreads - 1) / kOpThreads);
+}
+
+}  // namespace
+
+#define ABM_OP_DISPATCH(KERNEL, LPN_, GRID, SMEM, STREAM, ...)                         \
+  switch (LPN_) {                                                                     \
+    case 1: KERNEL<1><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 2: KERNEL<2><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 4: KERNEL<4><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 8: KERNEL<8><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 16: KERNEL<16><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;        \
+    default: KERNEL<32><<<GRID, kOpThreads, SMEM, STREAM>>>(__VA_ARGS__); break;        \
+  }
+
+extern "C" {
+
+int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, const int32_t* col, int64_t n,
+                    int32_t B, const float* mu, const float* eps, const float* tau,
+                    int32_t steps, int32_t ckpt_every, float* checkpoints, void* stream) {
+  if (!o || !o_tmp || !row_ptr || !col || !mu || !eps || !tau || n <= 0 || n > 0x7FFFFFFFll ||
+      steps < 0 || !valid_batch(B) || (checkpoints && ckpt_every <= 0))
+    return ABM_ERR_BADARG;
+  if (!abm_host::aligned(o, 16) || !abm_host::aligned(o_tmp, 16) || !abm_host::aligned(mu, 16) ||
+      !abm_host::aligned(eps, 16) || !abm_host::aligned(tau, 16) ||
+      (checkpoints && !abm_host::aligned(checkpoints, 16)))
+    return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const size_t bytes = (size_t)n * B * sizeof(float);
+  const int lpn = B / 4;
+  const int blocks = step_blocks(n, B);
+  float* cur = o;
+  float* nxt = o_tmp;
+  for (int32_t t = 0; t < steps; ++t) {
+    if (checkpoints && t % ckpt_every == 0) {
+      int st = abm_host::record_cuda_error(
+          cudaMemcpyAsync(checkpoints + (size_t)(t / ckpt_every) * n * B, cur, bytes,
+                          cudaMemcpyDeviceToDevice, s),
+          "abm_opinion_run/checkpoint");
+      if (st) return st;
+    }
+    ABM_OP_DISPATCH(opinion_step_kernel, lpn, blocks, 0, s, cur, nxt, row_ptr, col, (int)n, B, mu,
+                    eps, tau);
+    int st = abm_host::check_launch("abm_opinion_run/step");
+    if (st) return st;
+    float* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  if (cur != o) {
+    return abm_host::record_cuda_error(
+        cudaMemcpyAsync(o, cur, bytes, cudaMemcpyDeviceToDevice, s), "abm_opinion_run/final");
+  }
+  return ABM_OK;
+}
+
+size_t abm_opinion_moments_workspace_bytes(int64_t n, int32_t B) {
+  if (n <= 0 || !valid_batch(B)) return 0;
+  const int rows_per_cta = 1024;
+  const int64_t parts = (n + rows_per_cta - 1) / rows_per_cta;
+  return (size_t)parts * B * 4 * sizeof(double);
+}
+
+int abm_opinion_moments(const float* o, int64_t n, int32_t B, double* moments, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+  if (!o || !moments || n <= 0 || n > 0x7FFFFFFFll || !valid_batch(B)) return ABM_ERR_BADARG;
+  if (!workspace || workspace_bytes < abm_opinion_moments_workspace_bytes(n, B) ||
+      !abm_host::aligned(workspace, 8))
+    return ABM_ERR_WORKSPACE;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int rows_per_cta = 1024;
+  const int parts = (int)((n + rows_per_cta - 1) / rows_per_cta);
+  double* part = static_cast<double*>(workspace);
+  opinion_moments_partial_kernel<<<parts, kOpThreads, kOpThreads * 4 * sizeof(double), s>>>(
+      o, (int)n, B, rows_per_cta, part);
+  int st = abm_host::check_launch("abm_opinion_moments/partial");
+  if (st) return st;
+  sum_partials_kernel<<<(B * 4 + 127) / 128, 128, 0, s>>>(part, parts, B * 4, 1.0 / (double)n,
+                                                          moments);
+  return abm_host::check_launch("abm_opinion_moments/sum");
+}
+
+int abm_opinion_adjoint_init(const float* o, int64_t n, int32_t B, const double* dloss_dmoments,
+                             float* lam, void* stream) {
+  if (!o || !dloss_dmoments || !lam || n <= 0 || n > 0x7FFFFFFFll || !valid_batch(B))
+    return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const long long total = n * (long long)B;
+  long long blocks = (total + 255) / 256;
+  const long long cap = (long long)abm_host::sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  opinion_adjoint_init_kernel<<<(unsigned)blocks, 256, 0, s>>>(o, (int)n, B, dloss_dmoments, lam);
+  return abm_host::check_launch("abm_opinion_adjoint_init");
+}
+
+size_t abm_opinion_grad_workspace_bytes(int64_t n, int32_t B) {
+  if (n <= 0 || !valid_batch(B)) return 0;
+  return (size_t)step_blocks(n, B) * B * 3 * sizeof(double);
+}
+
+int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out,
+                             const int32_t* row_ptr, const int32_t* col, int64_t n, int32_t B,
+                             const float* mu, const float* eps, const float* tau,
+                             double* grad_partials, size_t grad_partials_bytes, void* stream) {
+  if (!o || !lam_in || !lam_out || !row_ptr || !col || !mu || !eps || !tau || n <= 0 ||
+      n > 0x7FFFFFFFll || !valid_batch(B) || lam_in == lam_out)
+    return ABM_ERR_BADARG;
+  if (!abm_host::aligned(o, 16) || !abm_host::aligned(lam_in, 16) ||
+      !abm_host::aligned(lam_out, 16) || !abm_host::aligned(mu, 16) ||
+      !abm_host::aligned(eps, 16) || !abm_host::aligned(tau, 16))
+    return ABM_ERR_BADARG;
+  if (!grad_partials || grad_partials_bytes < abm_opinion_grad_workspace_bytes(n, B) ||
+      !abm_host::aligned(grad_partials, 8))
+    return ABM_ERR_WORKSPACE;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int lpn = B / 4;
+  const int blocks = step_blocks(n, B);
+  const size_t smem = (size_t)kOpThreads * 12 * sizeof(double);
+  ABM_OP_DISPATCH(opinion_adjoint_kernel, lpn, blocks, smem, s, o, lam_in, lam_out, row_ptr, col,
+                  (int)n, B, mu, eps, tau, grad_partials);
+  return abm_host::check_launch("abm_opinion_adjoint_step");
+}
+
+int abm_opinion_grad_reduce(const double* grad_partials, int64_t n, int32_t B, double* grads,
+                            void* stream) {
+  if (!grad_partials || !grads || n <= 0 || !valid_batch(B)) return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int parts = step_blocks(n, B);
+  sum_partials_kernel<<<(B * 3 + 127) / 128, 128, 0, s>>>(grad_partials, parts, B * 3, 1.0, grads);
+  return abm_host::check_launch("abm_opinion_grad_reduce");
+}
+
+}  // extern "C"

@@ -11,19 +11,21 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "abm_oracle.c")
+SRCS = sorted(os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".c"))
+HDRS = sorted(os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".h"))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-FLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
+FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+         "-fno-fast-math"]
 
 
 def build(force=False):
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(__file__))):
+    newest = max(os.path.getmtime(p) for p in SRCS + HDRS + [__file__])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp"
-    cmd = ["gcc"] + FLAGS + [SRC, "-o", tmp, "-lm"]
+    cmd = ["gcc"] + FLAGS + SRCS + ["-o", tmp, "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + res.stderr)

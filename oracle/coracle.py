@@ -84,3 +84,16 @@ def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
                       ctypes.c_int32(steps), ctypes.c_float(beta), ctypes.c_float(gamma),
                       _p(counts))
     return st, counts, r
+
+
+def schelling_run(pos, types, W, H, coll_keys):
+    """Schelling steps with the given per-step collection keys uint32[steps, 2].
+    Returns (final positions, stats int32[steps, 2] = (unhappy, moved))."""
+    p = np.array(pos, dtype=np.int32, copy=True)
+    ty = np.ascontiguousarray(types, dtype=np.int8)
+    ck = np.ascontiguousarray(coll_keys, dtype=np.uint32).reshape(-1, 2)
+    steps = ck.shape[0]
+    stats = np.zeros((steps, 2), dtype=np.int32)
+    lib().orc_schelling_run(_p(p), _p(ty), ctypes.c_int64(p.size), ctypes.c_int32(W),
+                            ctypes.c_int32(H), _p(ck), ctypes.c_int32(steps), _p(stats))
+    return p, stats
