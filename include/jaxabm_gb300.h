@@ -274,6 +274,20 @@ ABM_API size_t abm_select_workspace_bytes(int64_t n);
 ABM_API int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t* count,
                                void* workspace, size_t workspace_bytes, void* stream);
 
+/* Same result as abm_select_indices, without any workspace and without allocating.
+ * No counterpart in the reference (it allocates through JAX for every selection).
+ * For callers that cannot allocate device memory when they select: a host application
+ * that gives the engine a fixed device-memory budget, or a latency-critical loop that must
+ * not risk the device-wide synchronisation cudaMalloc/cudaFree can cause.  Its scratch is a
+ * fixed 192 KiB array inside the library's device image, held by every GPU that loads the
+ * library until the process exits.  Limit: n <= 67,108,864 (2^26); larger n returns
+ * ABM_ERR_BADARG (use abm_select_indices).  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress, with that device current); make that first
+ * call before any stream capture.  All calls share the one array, so calls that overlap
+ * on the GPU (other streams, other host threads) race: serialise them on one stream. */
+ABM_API int abm_select_indices_noalloc(const uint8_t* mask, int64_t n, int32_t* out_idx,
+                                       int64_t* count, void* stream);
+
 /* dst[r] = src[idx[r]] for `count` rows of `row_bytes` bytes (the per-attribute
  * `v[mask]` of jaxabm/agent.py:242). */
 ABM_API int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes,

@@ -65,6 +65,7 @@ SIGNATURES = {
     "abm_opinion_grad_reduce": (_int, [_p, _i64, _i32, _p, _p]),
     "abm_select_workspace_bytes": (_sz, [_i64]),
     "abm_select_indices": (_int, [_p, _i64, _p, _p, _p, _sz, _p]),
+    "abm_select_indices_noalloc": (_int, [_p, _i64, _p, _p, _p]),
     "abm_gather_rows": (_int, [_p, _i64, _i64, _p, _i64, _p, _p]),
     "abm_reduce_workspace_bytes": (_sz, [_i64]),
     "abm_reduce_f32": (_int, [_p, _i64, _int, _p, _p, _sz, _p]),

@@ -263,3 +263,85 @@ int abm_reduce_f32(const float* x, int64_t n, int op, float* out, void* workspac
 }
 
 }  // extern "C"
+
+// ---- compaction without any allocation ---------------------------------------------------
+// abm_select_indices needs a workspace, which most callers take from their allocator.  Some
+// callers cannot allocate device memory at the moment they need a selection: a host
+// application that hands the engine a fixed device-memory budget and forbids growth, or a
+// latency-critical loop that must not pay the implicit device synchronisation that
+// cudaMalloc/cudaFree can cause.  For them the per-tile scratch lives in a fixed array in
+// the library's own device image instead.  Every GPU that loads the library holds this
+// array (192 KiB) until the process exits.
+#include <mutex>
+
+namespace {
+
+constexpr int64_t kNoAllocMaxN = int64_t(1) << 26;              // 67,108,864 mask entries
+constexpr int64_t kNoAllocMaxTiles = kNoAllocMaxN / kTile;       // 16,384 tiles
+constexpr size_t kNoAllocCountsBytes = (size_t)kNoAllocMaxTiles * sizeof(int32_t);
+constexpr size_t kNoAllocScratchBytes =
+    kNoAllocCountsBytes + (size_t)kNoAllocMaxTiles * sizeof(int64_t);
+
+// tile counts (int32[kNoAllocMaxTiles]) followed by tile offsets (int64[kNoAllocMaxTiles])
+static __device__ __align__(256) unsigned char g_select_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_select_scratch on the current device.  In host code the symbol names
+// a host-side stand-in, so the address must come from the runtime: looked up once per
+// device (with that device current) and cached.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return abm_host::record_cuda_error(e, "abm_select_indices_noalloc/device");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return ABM_ERR_BADARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_select_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return abm_host::record_cuda_error(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                                         "abm_select_indices_noalloc/cudaGetSymbolAddress");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return ABM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int abm_select_indices_noalloc(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t* count,
+                               void* stream) {
+  if ((!mask && n > 0) || !out_idx || !count || n < 0) return ABM_ERR_BADARG;
+  if (n > kNoAllocMaxN) return ABM_ERR_BADARG;  // beyond the fixed scratch: use abm_select_indices
+  cudaStream_t s = abm_host::as_stream(stream);
+  if (n == 0) {
+    return abm_host::record_cuda_error(cudaMemsetAsync(count, 0, sizeof(int64_t), s),
+                                       "abm_select_indices_noalloc");
+  }
+  void* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
+  if (st) return st;
+  // Nothing in the scratch has to start at zero: each call writes every tile count and
+  // offset it later reads.
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  int32_t* tile_counts = static_cast<int32_t*>(scratch);
+  int64_t* tile_offsets =
+      reinterpret_cast<int64_t*>(static_cast<char*>(scratch) + kNoAllocCountsBytes);
+  const bool vec_ok = abm_host::aligned(mask, 16);
+  select_count_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(mask, n, vec_ok, tile_counts);
+  st = abm_host::check_launch("abm_select_indices_noalloc/count");
+  if (st) return st;
+  select_scan_kernel<<<1, 1024, 0, s>>>(tile_counts, tiles, tile_offsets, count);
+  st = abm_host::check_launch("abm_select_indices_noalloc/scan");
+  if (st) return st;
+  select_scatter_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(mask, n, vec_ok, tile_offsets,
+                                                                out_idx);
+  return abm_host::check_launch("abm_select_indices_noalloc/scatter");
+}
+
+}  // extern "C"
