@@ -26,6 +26,8 @@ from . import sir  # noqa: E402  registers SIRAgent
 from .sir import SIRAgent, SIRModel  # noqa: E402
 from . import schelling  # noqa: E402  registers SchellingAgent
 from .schelling import SchellingAgent, SchellingModel  # noqa: E402
+from . import opinion  # noqa: E402  registers OpinionAgent
+from .opinion import OpinionAgent, OpinionModel  # noqa: E402
 
 
 def build(force: bool = False) -> str:

@@ -1,0 +1,241 @@
+"""Differentiable bounded-confidence opinion model and its calibration gradient.
+
+Model (per step, every agent reads the pre-step opinions)::
+
+    o_i += mu * mean_j sigmoid((eps - |o_j - o_i|) / tau) * (o_j - o_i)
+
+on a symmetric network (``Network``, CSR).  ``OpinionBatch`` evaluates B parameter sets at
+once on one graph (opinions interleaved ``[N][B]``), stores a checkpoint every ``k`` steps
+on the forward pass, and computes d loss / d (mu, eps, tau) with the hand-written reverse
+sweep: each segment of ``k`` steps is recomputed from its checkpoint, then the adjoint
+kernel walks it backwards.  ``OpinionLoss`` wraps this as a ``torch.autograd.Function``.
+
+The reference calibrates by ``jit(grad(loss_fn))`` through its whole Python run loop
+(jaxabm/analysis.py:494-522, ``ModelCalibrator._calibrate_gradient``); the loss here is the
+mean squared error of the first four raw opinion moments at step T against a target.
+"""
+
+import numpy as np
+import torch
+
+from . import _dev
+from . import _lib
+from . import random as jrandom
+from .agentpy import Agent, Model, Network
+from .registry import StepKernel, register_step
+
+
+def _pow2_at_least(b, lo=4):
+    p = lo
+    while p < b:
+        p *= 2
+    return p
+
+
+def initial_opinions(n, seed=0):
+    """o_i = uniform(split(init_key, n)[i]) with the collection init key of
+    ``Model.initialize`` for ``seed`` (one collection)."""
+    keys = jrandom.split(jrandom.PRNGKey(seed), 2)
+    agent_keys = jrandom.split(keys[1].contiguous(), n)
+    return jrandom.uniform(agent_keys)
+
+
+class OpinionBatch:
+    """B opinion models (one parameter set each) on one graph.
+
+    Args:
+        row_ptr, col: symmetric CSR (host arrays or device tensors)
+        o0: initial opinions, float32[N] (shared) or [N, B]
+        mu, eps, tau: float32[B]
+    """
+
+    def __init__(self, row_ptr, col, o0, mu, eps, tau):
+        dev = _dev.device()
+        self.rp = torch.as_tensor(np.asarray(row_ptr) if not isinstance(row_ptr, torch.Tensor)
+                                  else row_ptr, dtype=torch.int32).to(dev).contiguous()
+        self.col = torch.as_tensor(np.asarray(col) if not isinstance(col, torch.Tensor)
+                                   else col, dtype=torch.int32).to(dev).contiguous()
+        self.n = self.rp.numel() - 1
+        mu = torch.as_tensor(mu, dtype=torch.float32).reshape(-1)
+        self.B_user = mu.numel()
+        self.B = _pow2_at_least(self.B_user)
+        if self.B > 128:
+            raise ValueError("at most 128 instances per batch")
+        self.set_params(mu, eps, tau)
+        o0 = torch.as_tensor(o0, dtype=torch.float32).to(dev)
+        if o0.dim() == 1:
+            o0 = o0[:, None].expand(self.n, self.B_user)
+        self.o0 = self._pad_cols(o0).contiguous()
+        self.o = self.o0.clone()
+        self.tmp = torch.empty_like(self.o)
+        self.ckpts = None
+        self.ckpt_every = None
+        self.steps_done = 0
+
+    def _pad_cols(self, x):
+        if x.shape[-1] == self.B:
+            return x.contiguous()
+        pad = x[..., :1].expand(*x.shape[:-1], self.B - x.shape[-1])
+        return torch.cat([x, pad], dim=-1).contiguous()
+
+    def set_params(self, mu, eps, tau):
+        dev = _dev.device()
+        vals = [torch.as_tensor(v, dtype=torch.float32).reshape(-1).to(dev) for v in (mu, eps, tau)]
+        self.mu, self.eps, self.tau = (self._pad_cols(v[None])[0] for v in vals)
+
+    def reset(self):
+        self.o.copy_(self.o0)
+        self.steps_done = 0
+
+    def forward(self, steps, ckpt_every=None):
+        """Run ``steps`` steps from the initial state; keep checkpoints every
+        ``ckpt_every`` steps for :meth:`backward`."""
+        self.reset()
+        ck = None
+        if ckpt_every:
+            nck = (steps + ckpt_every - 1) // ckpt_every
+            ck = torch.empty((nck, self.n, self.B), dtype=torch.float32, device=self.o.device)
+        _lib.call("abm_opinion_run", _dev.ptr(self.o), _dev.ptr(self.tmp), _dev.ptr(self.rp),
+                  _dev.ptr(self.col), self.n, self.B, _dev.ptr(self.mu), _dev.ptr(self.eps),
+                  _dev.ptr(self.tau), int(steps), int(ckpt_every or 0),
+                  _dev.ptr(ck) if ck is not None else None, _dev.stream_handle())
+        self.ckpts, self.ckpt_every, self.steps_done = ck, ckpt_every, steps
+        return self.o
+
+    def moments(self, o=None):
+        """Raw moments float64[B_user, 4] of the current (or given) state."""
+        o = self.o if o is None else o
+        out = torch.empty((self.B, 4), dtype=torch.float64, device=o.device)
+        ws = _dev.workspace(_lib.load().abm_opinion_moments_workspace_bytes(self.n, self.B))
+        _lib.call("abm_opinion_moments", _dev.ptr(o), self.n, self.B, _dev.ptr(out), _dev.ptr(ws),
+                  ws.numel(), _dev.stream_handle())
+        return out[:self.B_user]
+
+    @staticmethod
+    def loss_of(moments, target):
+        t = torch.as_tensor(target, dtype=torch.float64, device=moments.device).reshape(-1, 4)
+        return 0.25 * ((moments - t) ** 2).sum(dim=1)
+
+    def backward(self, target, grad_loss=None):
+        """d loss_b / d (mu_b, eps_b, tau_b) -> float64[B_user, 3] after :meth:`forward`
+        with checkpoints; ``grad_loss`` (float64[B_user]) scales each instance."""
+        if self.ckpts is None:
+            raise RuntimeError("forward(steps, ckpt_every) must run first")
+        dev = self.o.device
+        T, k = self.steps_done, self.ckpt_every
+        m = self.moments()
+        t = torch.as_tensor(target, dtype=torch.float64, device=dev).reshape(-1, 4)
+        dldm = 0.5 * (m - t)
+        if grad_loss is not None:
+            dldm = dldm * torch.as_tensor(grad_loss, dtype=torch.float64, device=dev).reshape(-1, 1)
+        dl = torch.zeros((self.B, 4), dtype=torch.float64, device=dev)
+        dl[:self.B_user] = dldm
+        lam = torch.empty_like(self.o)
+        lam2 = torch.empty_like(self.o)
+        _lib.call("abm_opinion_adjoint_init", _dev.ptr(self.o), self.n, self.B, _dev.ptr(dl),
+                  _dev.ptr(lam), _dev.stream_handle())
+        gws = torch.zeros(_lib.load().abm_opinion_grad_workspace_bytes(self.n, self.B) // 8,
+                          dtype=torch.float64, device=dev)
+        seg = torch.empty((k, self.n, self.B), dtype=torch.float32, device=dev)
+        scratch = torch.empty_like(self.o)
+        nseg = self.ckpts.shape[0]
+        for s in range(nseg - 1, -1, -1):
+            t0 = s * k
+            length = min(k, T - t0)
+            # recompute o^{t0} .. o^{t0+length-1} from the checkpoint
+            seg[0].copy_(self.ckpts[s])
+            for q in range(1, length):
+                seg[q].copy_(seg[q - 1])
+                _lib.call("abm_opinion_run", _dev.ptr(seg[q]), _dev.ptr(scratch), _dev.ptr(self.rp),
+                          _dev.ptr(self.col), self.n, self.B, _dev.ptr(self.mu), _dev.ptr(self.eps),
+                          _dev.ptr(self.tau), 1, 0, None, _dev.stream_handle())
+            for q in range(length - 1, -1, -1):
+                _lib.call("abm_opinion_adjoint_step", _dev.ptr(seg[q]), _dev.ptr(lam),
+                          _dev.ptr(lam2), _dev.ptr(self.rp), _dev.ptr(self.col), self.n, self.B,
+                          _dev.ptr(self.mu), _dev.ptr(self.eps), _dev.ptr(self.tau),
+                          _dev.ptr(gws), gws.numel() * 8, _dev.stream_handle())
+                lam, lam2 = lam2, lam
+        grads = torch.empty((self.B, 3), dtype=torch.float64, device=dev)
+        _lib.call("abm_opinion_grad_reduce", _dev.ptr(gws), self.n, self.B, _dev.ptr(grads),
+                  _dev.stream_handle())
+        return grads[:self.B_user]
+
+
+class OpinionLoss(torch.autograd.Function):
+    """loss[b] = 0.25 * sum_k (m_k(T; mu_b, eps_b, tau_b) - target_k)^2 with the adjoint
+    kernel as its backward.  ``OpinionLoss.apply(mu, eps, tau, batch, target, steps, k)``."""
+
+    @staticmethod
+    def forward(ctx, mu, eps, tau, batch, target, steps, ckpt_every):
+        batch.set_params(mu.detach(), eps.detach(), tau.detach())
+        batch.forward(int(steps), int(ckpt_every))
+        m = batch.moments()
+        ctx.batch, ctx.target = batch, target
+        return OpinionBatch.loss_of(m, target).to(mu.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_loss):
+        g = ctx.batch.backward(ctx.target, grad_loss.detach().to(torch.float64))
+        gm, ge, gt = (g[:, i].to(grad_loss.dtype) for i in range(3))
+        return gm, ge, gt, None, None, None, None
+
+
+# ---- single-model API --------------------------------------------------------------------
+
+class OpinionKernel(StepKernel):
+    name = "opinion"
+    attributes = ("opinion",)
+    metrics = ()
+    params = {"mu": 0.3, "eps": 0.2, "tau": 0.02}
+
+    def init(self, n, init_key, params, env):
+        agent_keys = jrandom.split(init_key.contiguous(), n)
+        return {"opinion": jrandom.uniform(agent_keys)}
+
+    def run(self, states, coll_keys, params, env):
+        steps = coll_keys.reshape(-1, 2).shape[0]
+        b = OpinionBatch(env["network_row_ptr"], env["network_col"], states["opinion"],
+                         [params["mu"]], [params["eps"]], [params["tau"]])
+        b.forward(steps)
+        return {"opinion": b.o[:, 0].contiguous()}, None
+
+    def step(self, states, coll_key, params, env):
+        return self.run(states, coll_key.reshape(1, 2), params, env)
+
+
+class OpinionAgent(Agent):
+    """Bounded-confidence opinion agent on a Network (registered: ``abm_opinion_*``)."""
+
+    def setup(self, key=None):
+        return {"opinion": jrandom.uniform(key)}
+
+
+register_step(OpinionAgent, OpinionKernel())
+
+
+class OpinionModel(Model):
+    """Parameters: ``n`` (2^18), ``degree`` (16, random regular graph), ``mu``, ``eps``,
+    ``tau``, ``steps`` (200), ``seed``."""
+
+    def setup(self):
+        from .sir import random_regular
+        n = int(self.p.get("n", 1 << 18))
+        rp, col = random_regular(n, int(self.p.get("degree", 16)), int(self.seed))
+        self.network = Network(self)
+        self.network.from_csr(rp, col)
+        self.agents = self.add_agents(n, OpinionAgent, name="people",
+                                      mu=float(self.p.get("mu", 0.3)),
+                                      eps=float(self.p.get("eps", 0.2)),
+                                      tau=float(self.p.get("tau", 0.02)))
+
+
+def calibration_params(count=64, base=(0.3, 0.2, 0.02), spread=0.2, seed=0):
+    """``count`` parameter sets base * (1 + spread * U[-1, 1]) (RandomState(seed)); set 0 is
+    the base point."""
+    u = np.random.RandomState(seed).uniform(-1.0, 1.0, size=(count, 3))
+    u[0] = 0.0
+    p = np.asarray(base)[None, :] * (1.0 + spread * u)
+    return p.astype(np.float32)
+
+
+HIDDEN_PARAMS = (0.25, 0.15, 0.025)

@@ -97,3 +97,51 @@ def schelling_run(pos, types, W, H, coll_keys):
     lib().orc_schelling_run(_p(p), _p(ty), ctypes.c_int64(p.size), ctypes.c_int32(W),
                             ctypes.c_int32(H), _p(ck), ctypes.c_int32(steps), _p(stats))
     return p, stats
+
+
+def _params(dtype, *arrs):
+    return [np.ascontiguousarray(a, dtype=dtype) for a in arrs]
+
+
+def opinion_run_f32(o, row_ptr, col, mu, eps, tau, steps):
+    """Float32 forward (GPU operation order); o float32[n, B]."""
+    x = np.array(o, dtype=np.float32, copy=True, order="C")
+    n, B = x.shape
+    rp, cl = _params(np.int32, row_ptr, col)
+    m, e, t = _params(np.float32, mu, eps, tau)
+    lib().orc_opinion_run_f32(_p(x), _p(rp), _p(cl), ctypes.c_int64(n), ctypes.c_int32(B),
+                              _p(m), _p(e), _p(t), ctypes.c_int32(steps))
+    return x
+
+
+def opinion_run_f64(o, row_ptr, col, mu, eps, tau, steps):
+    x = np.array(o, dtype=np.float64, copy=True, order="C")
+    n, B = x.shape
+    rp, cl = _params(np.int32, row_ptr, col)
+    m, e, t = _params(np.float64, mu, eps, tau)
+    lib().orc_opinion_run_f64(_p(x), _p(rp), _p(cl), ctypes.c_int64(n), ctypes.c_int32(B),
+                              _p(m), _p(e), _p(t), ctypes.c_int32(steps))
+    return x
+
+
+def opinion_moments_f64(o):
+    x = np.ascontiguousarray(o, dtype=np.float64)
+    n, B = x.shape
+    m = np.zeros((B, 4))
+    lib().orc_opinion_moments_f64(_p(x), ctypes.c_int64(n), ctypes.c_int32(B), _p(m))
+    return m
+
+
+def opinion_grad_f64(o0, row_ptr, col, mu, eps, tau, steps, target):
+    """(loss float64[B], grads float64[B, 3]) by the float64 reverse sweep."""
+    x = np.ascontiguousarray(o0, dtype=np.float64)
+    n, B = x.shape
+    rp, cl = _params(np.int32, row_ptr, col)
+    m, e, t = _params(np.float64, mu, eps, tau)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    loss = np.zeros(B)
+    grads = np.zeros((B, 3))
+    lib().orc_opinion_grad_f64(_p(x), _p(rp), _p(cl), ctypes.c_int64(n), ctypes.c_int32(B),
+                               _p(m), _p(e), _p(t), ctypes.c_int32(steps), _p(tg), _p(loss),
+                               _p(grads))
+    return loss, grads

@@ -1,0 +1,149 @@
+"""Opinion model on the GPU: FP32 forward vs the FP32/FP64 oracles (1e-5), the adjoint
+gradient vs the FP64 adjoint oracle, checkpoint invariance and torch.autograd."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import coracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _graph(n, seed=1):
+    from jaxabm_gb300 import sir
+    return sir.random_regular(n, 16, seed)
+
+
+def _params(B, seed=0):
+    from jaxabm_gb300.opinion import calibration_params
+    p = calibration_params(B, seed=seed)
+    return p[:, 0], p[:, 1], p[:, 2]
+
+
+@pytest.mark.parametrize("n,B,T", [(64, 4, 10), (4096, 4, 200), (4096, 64, 50), (2000, 8, 30)])
+def test_forward_vs_oracle(cuda, n, B, T):
+    from jaxabm_gb300.opinion import OpinionBatch
+    rp, col = _graph(n)
+    o0 = np.random.RandomState(n).rand(n, B).astype(np.float32)
+    mu, eps, tau = _params(B)
+    b = OpinionBatch(rp, col, torch.from_numpy(o0), mu, eps, tau)
+    got = b.forward(T)[:, :B].cpu().numpy()
+    ref32 = coracle.opinion_run_f32(o0, rp, col, mu, eps, tau, T)
+    ref64 = coracle.opinion_run_f64(o0.astype(np.float64), rp, col, mu.astype(np.float64),
+                                    eps.astype(np.float64), tau.astype(np.float64), T)
+    # opinions are O(1), so absolute errors are relative errors.  Per instance: states
+    # within 1e-5 of the FP64 oracle; where the dynamics amplify rounding (steep sigmoid,
+    # small tau) so much that the independent FP32 oracle is itself more than 1e-5 from
+    # FP64, the bar applies to the four moments (1e-5 relative) instead.
+    e_gpu64 = np.abs(got.astype(np.float64) - ref64).max(axis=0)
+    e_ora64 = np.abs(ref32.astype(np.float64) - ref64).max(axis=0)
+    e_gpu32 = np.abs(got - ref32).max(axis=0)
+    m_gpu = coracle.opinion_moments_f64(got.astype(np.float64))
+    m_64 = coracle.opinion_moments_f64(ref64)
+    e_mom = (np.abs(m_gpu - m_64) / np.abs(m_64)).max(axis=1)
+    ill = e_ora64 >= 5e-6
+    print(f"opinion n={n} B={B} T={T}: max|gpu-f32 oracle|={e_gpu32.max():.2e} "
+          f"max|gpu-f64|={e_gpu64.max():.2e} max|f32 oracle-f64|={e_ora64.max():.2e} "
+          f"ill-conditioned instances {ill.sum()}/{B}, max moment rel err {e_mom.max():.2e}")
+    for q in np.argsort(-e_gpu64)[:6]:
+        print(f"  instance {q}: gpu-f64 {e_gpu64[q]:.2e} f32oracle-f64 {e_ora64[q]:.2e} "
+              f"gpu-f32oracle {e_gpu32[q]:.2e} moments {e_mom[q]:.2e}")
+    assert np.all(e_gpu64[~ill] < 1e-5)
+    assert np.all(e_mom < 1e-5)
+    assert np.median(e_gpu32) < 1e-6
+    m = b.moments().cpu().numpy()
+    np.testing.assert_allclose(m, coracle.opinion_moments_f64(got.astype(np.float64)), rtol=1e-9)
+
+
+def test_full_size_properties(cuda):
+    """N = 2^18, 16-regular, 64 instances, 200 steps: mean opinion conserved, opinions stay
+    in the initial range, and column b equals the same instance run in a batch of 4."""
+    from jaxabm_gb300.opinion import OpinionBatch, initial_opinions
+    n = 1 << 18
+    rp, col = _graph(n, 0)
+    o0 = initial_opinions(n, 0)
+    mu, eps, tau = _params(64)
+    b = OpinionBatch(rp, col, o0, mu, eps, tau)
+    oT = b.forward(200).clone()
+    m = b.moments()
+    m0 = float(o0.double().mean())
+    assert torch.all(torch.abs(m[:, 0] - m0) < 1e-6)
+    assert float(oT.min()) >= float(o0.min()) - 1e-6 and float(oT.max()) <= float(o0.max()) + 1e-6
+    small = OpinionBatch(rp, col, o0, mu[5:9], eps[5:9], tau[5:9])
+    assert torch.equal(small.forward(200), oT[:, 5:9])
+
+
+@pytest.mark.parametrize("B,T,k", [(4, 60, 20), (8, 45, 7), (64, 40, 20)])
+def test_adjoint_vs_f64_oracle(cuda, B, T, k):
+    from jaxabm_gb300.opinion import OpinionBatch
+    n = 2048
+    rp, col = _graph(n, 3)
+    o0 = np.random.RandomState(7).rand(n, B).astype(np.float32)
+    mu, eps, tau = _params(B, seed=1)
+    target = coracle.opinion_moments_f64(coracle.opinion_run_f64(
+        o0[:, :1].astype(np.float64), rp, col, [0.25], [0.15], [0.025], T))[0]
+    b = OpinionBatch(rp, col, torch.from_numpy(o0), mu, eps, tau)
+    b.forward(T, k)
+    g = b.backward(target).cpu().numpy()
+    loss_ref, g_ref = coracle.opinion_grad_f64(o0.astype(np.float64), rp, col,
+                                               mu.astype(np.float64), eps.astype(np.float64),
+                                               tau.astype(np.float64), T, target)
+    rel = np.abs(g - g_ref).max(axis=1) / np.maximum(np.abs(g_ref).max(axis=1), 1e-12)
+    print(f"adjoint B={B} T={T} k={k}: max normwise rel err vs FP64 = {rel.max():.2e}")
+    # float32 states and adjoints (float64 parameter-gradient accumulation) against the
+    # float64 reverse sweep: a few 1e-3 at most, where the gradient is small
+    assert rel.max() < 5e-3 and np.median(rel) < 5e-4
+    loss = b.loss_of(b.moments(), target).cpu().numpy()
+    np.testing.assert_allclose(loss, loss_ref, rtol=1e-4, atol=1e-12)
+
+
+def test_checkpoint_interval_invariance(cuda):
+    from jaxabm_gb300.opinion import OpinionBatch
+    n, B, T = 1024, 4, 33
+    rp, col = _graph(n, 2)
+    o0 = np.random.RandomState(1).rand(n, B).astype(np.float32)
+    mu, eps, tau = _params(B, seed=2)
+    target = np.array([0.5, 0.3, 0.2, 0.15])
+    grads = []
+    for k in (1, 5, 20, 33):
+        b = OpinionBatch(rp, col, torch.from_numpy(o0), mu, eps, tau)
+        b.forward(T, k)
+        grads.append(b.backward(target).cpu().numpy())
+    for g in grads[1:]:
+        assert np.array_equal(g, grads[0])
+
+
+def test_autograd_function(cuda):
+    from jaxabm_gb300.opinion import OpinionBatch, OpinionLoss
+    n, B, T = 1024, 4, 30
+    rp, col = _graph(n, 4)
+    o0 = np.random.RandomState(2).rand(n).astype(np.float32)
+    mu0, eps0, tau0 = _params(B, seed=3)
+    target = np.array([0.5, 0.3, 0.2, 0.15])
+    b = OpinionBatch(rp, col, torch.from_numpy(o0), mu0, eps0, tau0)
+    mu = torch.tensor(mu0, device="cuda", requires_grad=True)
+    eps = torch.tensor(eps0, device="cuda", requires_grad=True)
+    tau = torch.tensor(tau0, device="cuda", requires_grad=True)
+    loss = OpinionLoss.apply(mu, eps, tau, b, target, T, 10)
+    w = torch.tensor([1.0, 2.0, 0.5, 3.0], device="cuda")
+    (loss * w).sum().backward()
+    b2 = OpinionBatch(rp, col, torch.from_numpy(o0), mu0, eps0, tau0)
+    b2.forward(T, 10)
+    g = b2.backward(target, w.double()).cpu().numpy()
+    np.testing.assert_allclose(mu.grad.cpu().numpy(), g[:, 0], rtol=1e-6)
+    np.testing.assert_allclose(eps.grad.cpu().numpy(), g[:, 1], rtol=1e-6)
+    np.testing.assert_allclose(tau.grad.cpu().numpy(), g[:, 2], rtol=1e-6)
+
+
+def test_opinion_model_api(cuda):
+    import jaxabm_gb300 as jx
+    from jaxabm_gb300 import sir
+    m = jx.OpinionModel({"n": 4096, "steps": 40, "seed": 5})
+    res = m.run()
+    x = res["agents.people.opinion"]
+    rp, col = sir.random_regular(4096, 16, 5)
+    from jaxabm_gb300.opinion import initial_opinions
+    o0 = initial_opinions(4096, 5).cpu().numpy()
+    ref = coracle.opinion_run_f32(o0[:, None], rp, col, [0.3], [0.2], [0.02], 40)[:, 0]
+    assert np.abs(x - ref).max() < 1e-5
