@@ -125,7 +125,8 @@ class SIREnsembleBench:
         from jaxabm_gb300 import ensemble
         self.ensemble = ensemble
         self.count, self.T = count, steps
-        spec = ensemble.ensemble_spec(count)
+        spec = ensemble.ensemble_spec(4096)
+        spec = {k: v[:count] for k, v in spec.items()}
         spec["seed"] = spec["seed"] + rank * count  # each rank its own members
         self.spec = spec
         t0 = time.perf_counter()
@@ -262,7 +263,7 @@ def run_ours(args):
     import jaxabm_gb300 as jx
     jx.set_verbose(False)
     jx.build()
-    wl = WORKLOADS[args.workload](rank)
+    wl = WORKLOADS[args.workload](rank, count=args.instances)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         wl.reset()
@@ -392,6 +393,9 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--quick", action="store_true",
                     help="only the batched value and e2e (no plain/served/cpu legs)")
+    ap.add_argument("--instances", type=int, default=4096,
+                    help="ensemble members (the first K of the 4,096-member specification); "
+                         "smaller values are for profiling captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
