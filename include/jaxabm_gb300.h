@@ -138,18 +138,21 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
                                      int32_t* col, int64_t col_capacity);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (88 bytes, 8-byte aligned).
- * state holds 2*n int8 compartments (0 S, 1 I, 2 R); buffer (t & 1) is current.
+/* Device-side descriptor of one SIR model instance (112 bytes, 8-byte aligned).
+ * state holds one int32 word per agent, (infected neighbours << 2) | compartment
+ * (0 S, 1 I, 2 R), built by abm_sir_pack and read back by abm_sir_unpack.
  * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
  * NULL, else it is derived from rng, the instance's Model.step key-chain state
- * (jaxabm/model.py:156,164), which is advanced once per step either way.  counts receives
- * S, I, R after each step (int32[steps][3], zeroed by the caller); done_flag (nullable,
- * may be host-mapped) is set to 1 after the last step; edges_scanned accumulates the CSR
- * slots the step kernel examined (the algorithmic gather volume). */
+ * (jaxabm/model.py:156,164), which is advanced once per step either way.  num_s/num_i/num_r
+ * are the current compartment sizes (set by the caller before step 0); counts receives
+ * S, I, R after each step (int32[steps][3]); step_si/step_ir are the transitions of the
+ * step in flight (zero before step 0); done_flag (nullable, may be host-mapped) is set to
+ * 1 after the last step; edges_scanned / edges_pushed accumulate the CSR slots read by
+ * the decide and push phases (zero before step 0). */
 typedef struct abm_sir_instance {
   const int32_t* row_ptr;
   const int32_t* col;
-  int8_t* state;
+  int32_t* state;
   int32_t* counts;
   int32_t* done_flag;
   const uint32_t* coll_keys;
@@ -159,8 +162,13 @@ typedef struct abm_sir_instance {
   int32_t steps;
   float beta;
   float gamma;
-  int32_t reserved;
+  int32_t num_s;
+  int32_t num_i;
+  int32_t num_r;
+  int32_t step_si;
+  int32_t step_ir;
   unsigned long long edges_scanned;
+  unsigned long long edges_pushed;
 } abm_sir_instance;
 
 /* A tile of agents [begin, end) of instance `inst` (end - begin <= 256). */
@@ -173,25 +181,52 @@ typedef struct abm_work_item {
 
 ABM_API size_t abm_sir_instance_size(void);
 
+/* Per-agent words of one instance from int8 compartments state[n] (n < 2^29): the number
+ * of infected neighbours over the CSR is counted; sizes (device int32[3]) receives the
+ * S, I, R totals; *status (device int32) becomes 1 on a compartment outside 0..2. */
+ABM_API int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col,
+                         int64_t n, int32_t* words, int32_t* sizes, int32_t* status,
+                         void* stream);
+
+/* abm_sir_pack for every tile of `work` at once: the int8 compartments of an instance are
+ * read from states8 at the same element offset as its words (insts[i].state) from
+ * words_base.  Descriptors must already point at their CSR and words. */
+ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
+                               int32_t nwork, const int8_t* states8, const int32_t* words_base,
+                               int32_t* status, void* stream);
+
+/* int8 compartments of n packed words. */
+ABM_API int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream);
+
+/* Bytes of the change-list workspace of abm_sir_steps for up to max_agents live agents
+ * (16-byte header {count, overflow, 0, 0}, zeroed once by the caller, then 8 bytes per
+ * agent). */
+ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
+
 /* nsteps synchronous SIR steps of every instance with t < steps, over the tiles `work`
  * (persistent grid of `grid` CTAs; 0 = 8 per SM).  Per step and agent i of an instance:
  * agent_key = split(coll_key, n)[i], k_inf, k_rec = split(agent_key);
  *   S -> I if some neighbour slot k with an I neighbour has uniform(k_inf,(deg,))[k] < beta;
  *   I -> R if uniform(k_rec) < gamma.
+ * A susceptible agent whose word says it has no infected neighbour reads nothing else;
+ * changes are pushed to the neighbours' words after all decisions (three launches per
+ * step: decide, push, finalize).  `changes` must hold abm_sir_changes_bytes(total agents
+ * of all live instances); its overflow flag is set (and changes dropped) if it is smaller.
  * Replaces Model.step's AgentCollection.update (jaxabm/model.py:163-171,
  * jaxabm/agent.py:132-179) for the SIR agent, batched over instances (the serial loops of
  * Model.batch_run, jaxabm/agentpy.py:1116-1152).  Descriptors and tiles are device memory
  * and may be rewritten between calls (e.g. to admit instances) without re-capturing a
  * CUDA graph of this call. */
 ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                          int32_t nwork, int32_t nsteps, int32_t grid, void* stream);
+                          int32_t nwork, int32_t nsteps, int32_t grid, void* changes,
+                          size_t changes_bytes, void* stream);
 
 ABM_API size_t abm_sir_run_workspace_bytes(int64_t n);
 
 /* One SIR model for `steps` steps (the plain engine: one simulation per launch sequence)
  * with the per-step collection keys coll_keys uint32[steps][2] (abm_keychain, ncoll = 1).
- * state int8[2*n]: the current compartments are read from state[0..n) and the final ones
- * are in buffer (steps & 1); counts int32[steps][3] (zeroed by the call). */
+ * state int8[n] holds the compartments before the run and receives them after it;
+ * counts int32[steps][3]. */
 ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* state,
                         const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
                         int32_t* counts, void* workspace, size_t workspace_bytes, void* stream);

@@ -9,74 +9,94 @@
 // All agents read the pre-step states (synchronous update, jaxabm/agent.py:168-177); the
 // S/I/R counts after each step are the metrics (jaxabm/model.py:193-200).
 //
-// Layout: each instance has a descriptor (abm_sir_instance) with its CSR, a 2*n int8 state
-// double buffer (buffer t&1 is current), its rng (Model.step key chain state) and step
-// counter.  Work items are (instance, agent range) tiles of <= 256 agents; one CTA runs one
-// tile at a time over a persistent grid.  Per step: the step kernel over all work items,
-// then a one-thread-per-instance kernel that advances rng and t.  Kernels never wait on
-// anything, so a step can neither hang nor deadlock.
-//
-// Load balance on heavy-tailed (Barabasi-Albert) degrees: a thread scans its own row when
-// deg <= 32; longer rows are scanned by the whole warp, 32 slots per pass, with a warp vote
-// ending the scan at the first firing draw ("any" is order-free, so results are exact).
+// Work-efficient ("frontier") formulation.  Each agent has one int32 word
+//     word = (number of infected neighbours << 2) | compartment
+// and a step is three launches:
+//   decide   one thread per agent over (instance, 256-agent tile) work items: reads its
+//            own word; only a susceptible agent with infected neighbours scans its CSR row
+//            (stopping at the first firing draw or once all its infected neighbours were
+//            seen); an infected agent draws its recovery.  Agents whose compartment
+//            changes are appended to a change list (warp-aggregated atomics).  Nothing is
+//            written to the words, so every decision sees the pre-step states.
+//   push     one warp per change: adds +-4 to the word of every neighbour (infected-
+//            neighbour count) and +1 to the agent's own compartment; counts the instance's
+//            S->I and I->R transitions.
+//   finalize one thread per instance: S/I/R counts of the step from the transitions,
+//            rng = split(rng)[0], t += 1, done flag after the last step; clears the list.
+// Rows longer than 32 slots are scanned by the whole warp, 32 slots per pass, with warp
+// votes.  Integer atomics commute, so every result is exact and independent of scheduling.
+// No kernel waits on anything.
 
 #include "abm_common.cuh"
 
 namespace {
 
 constexpr int kSirThreads = 256;
-constexpr int kSirWarps = kSirThreads / 32;
 constexpr int kHeavyDeg = 32;
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kS = 0, kI = 1;
 
-static_assert(sizeof(abm_sir_instance) == 88, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 112, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
+// change-list workspace: header {count, overflow, pad, pad} then int2 entries
+struct ChangeHeader {
+  int32_t count;
+  int32_t overflow;
+  int32_t pad[2];
+};
+
+__device__ __forceinline__ uint2 coll_key_of(const abm_sir_instance* I, int t) {
+  // coll_key of step t: given per step, or from the instance's own key chain
+  // (step_key = split(rng)[1]; coll_key = split(step_key)[1], jaxabm/model.py:156,164)
+  return I->coll_keys != nullptr
+             ? abm::load_key(I->coll_keys + 2 * (size_t)t)
+             : abm::split_at(abm::split_at(make_uint2(I->rng[0], I->rng[1]), 1), 1);
+}
+
 __global__ void __launch_bounds__(kSirThreads)
-sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work, int nwork) {
-  __shared__ int scount[4][kSirWarps];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+sir_decide_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work, int nwork,
+                  ChangeHeader* __restrict__ hdr, int2* __restrict__ changes, int capacity) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long scanned_acc = 0;
+  int scanned_inst = -1;
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
     abm_sir_instance* I = insts + item.x;
     const int t = I->t;
     if (t >= I->steps) continue;  // uniform over the CTA
-    const int n = I->n;
-    const int8_t* __restrict__ cur = I->state + (size_t)(t & 1) * n;
-    int8_t* __restrict__ nxt = I->state + (size_t)((t + 1) & 1) * n;
-    const int32_t* __restrict__ rp = I->row_ptr;
-    const int32_t* __restrict__ col = I->col;
-    const float beta = I->beta, gamma = I->gamma;
-    // coll_key of step t: given per step, or from the instance's own key chain
-    // (step_key = split(rng)[1]; coll_key = split(step_key)[1], jaxabm/model.py:156,164)
-    const uint2 coll = I->coll_keys != nullptr
-                           ? abm::load_key(I->coll_keys + 2 * (size_t)t)
-                           : abm::split_at(abm::split_at(make_uint2(I->rng[0], I->rng[1]), 1), 1);
-
+    const int32_t* __restrict__ word = I->state;
     const int i = item.y + threadIdx.x;
     const bool valid = i < item.z;
-    const int8_t s = valid ? cur[i] : (int8_t)2;
-    int8_t ns = s;
+    const int32_t wi = valid ? word[i] : 2;
+    const int s = wi & 3;
+    int cnt = wi >> 2;
+    int ns = s;
     bool heavy = false;
     int row0 = 0, deg = 0, scanned = 0;
-    if (s == 0) {
+    const bool scan = (s == kS) && cnt > 0;
+    const bool recover = (s == kI);
+    uint2 coll = make_uint2(0, 0);
+    if (__any_sync(kFull, scan || recover)) coll = coll_key_of(I, t);
+    if (scan) {
+      const int32_t* __restrict__ rp = I->row_ptr;
       row0 = rp[i];
       deg = rp[i + 1] - row0;
       if (deg > kHeavyDeg) {
         heavy = true;
       } else {
-        bool have = false;
-        uint2 kinf = make_uint2(0, 0);
+        const int32_t* __restrict__ col = I->col;
+        const float beta = I->beta;
+        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
         int k = 0;
         for (; k < deg; ++k) {
-          const int j = col[row0 + k];
-          if (cur[j] == 1) {
-            if (!have) {
-              kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-              have = true;
-            }
+          if ((word[col[row0 + k]] & 3) == kI) {
             if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
-              ns = 1;
+              ns = kI;
+              ++k;
+              break;
+            }
+            if (--cnt == 0) {
               ++k;
               break;
             }
@@ -84,71 +104,111 @@ sir_step_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ w
         }
         scanned = k;
       }
-    } else if (s == 1) {
+    } else if (recover) {
       const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
-      if (abm::unit_float(abm::bits_at(krec, 0)) < gamma) ns = 2;
+      if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
     }
 
     unsigned hmask = __ballot_sync(kFull, heavy);
-    while (hmask) {
-      const int src = __ffs(hmask) - 1;
-      hmask &= hmask - 1;
-      const int hi = __shfl_sync(kFull, i, src);
-      const int hrow = __shfl_sync(kFull, row0, src);
-      const int hdeg = __shfl_sync(kFull, deg, src);
-      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
-      bool fired = false;
-      int c = 0;
-      for (; c < hdeg && !fired; c += 32) {
-        const int k = c + lane;
-        bool f = false;
-        if (k < hdeg) {
-          const int j = col[hrow + k];
-          if (cur[j] == 1) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta;
+    if (hmask) {
+      const int32_t* __restrict__ col = I->col;
+      const float beta = I->beta;
+      while (hmask) {
+        const int src = __ffs(hmask) - 1;
+        hmask &= hmask - 1;
+        const int hi = __shfl_sync(kFull, i, src);
+        const int hrow = __shfl_sync(kFull, row0, src);
+        const int hdeg = __shfl_sync(kFull, deg, src);
+        int remaining = __shfl_sync(kFull, cnt, src);
+        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
+        bool fired = false;
+        int c = 0;
+        for (; c < hdeg && !fired && remaining > 0; c += 32) {
+          const int k = c + lane;
+          bool isI = false, f = false;
+          if (k < hdeg) {
+            isI = (word[col[hrow + k]] & 3) == kI;
+            if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta;
+          }
+          fired = __any_sync(kFull, f);
+          remaining -= __popc(__ballot_sync(kFull, isI));
         }
-        fired = __any_sync(kFull, f);
-      }
-      if (lane == src) {
-        if (fired) ns = 1;
-        scanned = min(c, hdeg);
+        if (lane == src) {
+          if (fired) ns = kI;
+          scanned = min(c, hdeg);
+        }
       }
     }
 
-    if (valid) nxt[i] = ns;
-    const int cs = abm::warp_sum((int)(valid && ns == 0));
-    const int ci = abm::warp_sum((int)(valid && ns == 1));
-    const int cr = abm::warp_sum((int)(valid && ns == 2));
-    const int ce = abm::warp_sum(scanned);
-    if (lane == 0) {
-      scount[0][warp] = cs;
-      scount[1][warp] = ci;
-      scount[2][warp] = cr;
-      scount[3][warp] = ce;
-    }
-    __syncthreads();
-    if (threadIdx.x < 4) {
-      int sum = 0;
-#pragma unroll
-      for (int q = 0; q < kSirWarps; ++q) sum += scount[threadIdx.x][q];
-      if (sum) {
-        if (threadIdx.x < 3)
-          atomicAdd(&I->counts[3 * t + threadIdx.x], sum);
-        else
-          atomicAdd(&I->edges_scanned, (unsigned long long)sum);
+    // warp-aggregated append of the agents whose compartment changes
+    const bool changed = valid && ns != s;
+    const unsigned cmask = __ballot_sync(kFull, changed);
+    if (cmask) {
+      const int leader = __ffs(cmask) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&hdr->count, __popc(cmask));
+      base = __shfl_sync(kFull, base, leader);
+      if (changed) {
+        const int pos = base + __popc(cmask & ((1u << lane) - 1u));
+        if (pos < capacity) changes[pos] = make_int2(item.x, (i << 2) | ns);
+        else hdr->overflow = 1;
       }
     }
-    __syncthreads();
+    if (scanned) {
+      if (scanned_inst != item.x && scanned_acc) {
+        atomicAdd(&insts[scanned_inst].edges_scanned, scanned_acc);
+        scanned_acc = 0;
+      }
+      scanned_inst = item.x;
+      scanned_acc += scanned;
+    }
+  }
+  if (scanned_acc) atomicAdd(&insts[scanned_inst].edges_scanned, scanned_acc);
+}
+
+// One warp per change: neighbours' infected counts +-1, own compartment +1.
+__global__ void __launch_bounds__(kSirThreads)
+sir_push_kernel(abm_sir_instance* __restrict__ insts, const ChangeHeader* __restrict__ hdr,
+                const int2* __restrict__ changes, int capacity) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (kSirThreads / 32);
+  const int count = min(hdr->count, capacity);
+  for (int e = blockIdx.x * (kSirThreads / 32) + (threadIdx.x >> 5); e < count; e += warps) {
+    const int2 ent = changes[e];
+    abm_sir_instance* I = insts + ent.x;
+    const int agent = ent.y >> 2;
+    const int ns = ent.y & 3;
+    int32_t* __restrict__ word = I->state;
+    const int32_t* __restrict__ col = I->col;
+    const int r0 = I->row_ptr[agent], r1 = I->row_ptr[agent + 1];
+    const int delta = ns == kI ? 4 : -4;
+    for (int k = r0 + lane; k < r1; k += 32) atomicAdd(&word[col[k]], delta);
+    if (lane == 0) {
+      atomicAdd(&word[agent], 1);  // S(0) -> I(1) and I(1) -> R(2) both add one
+      atomicAdd(ns == kI ? &I->step_si : &I->step_ir, 1);
+      atomicAdd(&I->edges_pushed, (unsigned long long)(r1 - r0));
+    }
   }
 }
 
-// Advance every live instance by one step: rng = split(rng)[0]; t += 1; raise the
-// (host-mapped) done flag when the last step has been applied.
-__global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst) {
+// Counts after the step, key chain, step counter, done flag; clears the change list.
+__global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
+                                    ChangeHeader* __restrict__ hdr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0) hdr->count = 0;
   if (k >= ninst) return;
   abm_sir_instance* I = insts + k;
   const int t = I->t;
   if (t >= I->steps) return;
+  const int si = I->step_si, ir = I->step_ir;
+  I->num_s -= si;
+  I->num_i += si - ir;
+  I->num_r += ir;
+  I->step_si = 0;
+  I->step_ir = 0;
+  I->counts[3 * t] = I->num_s;
+  I->counts[3 * t + 1] = I->num_i;
+  I->counts[3 * t + 2] = I->num_r;
   const uint2 r = abm::split_at(make_uint2(I->rng[0], I->rng[1]), 0);
   I->rng[0] = r.x;
   I->rng[1] = r.y;
@@ -159,17 +219,71 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   }
 }
 
-// Single-instance descriptor and tile list written on the device (keeps abm_sir_run
-// free of host-to-device copies, so it can be captured in a CUDA graph).
+// word[i] = (infected neighbours << 2) | state[i]; compartment sizes into *sizes.
+__global__ void sir_pack_kernel(const int8_t* __restrict__ state, const int32_t* __restrict__ rp,
+                                const int32_t* __restrict__ col, int n, int32_t* __restrict__ word,
+                                int32_t* __restrict__ sizes, int32_t* __restrict__ bad) {
+  __shared__ int sc[3];
+  if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const int s = state[i];
+    if (s < 0 || s > 2) {
+      atomicExch(bad, 1);
+    } else {
+      int c = 0;
+      for (int k = rp[i]; k < rp[i + 1]; ++k) c += state[col[k]] == kI;
+      word[i] = (c << 2) | s;
+      atomicAdd(&sc[s], 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3 && sc[threadIdx.x]) atomicAdd(&sizes[threadIdx.x], sc[threadIdx.x]);
+}
+
+// The same over the tiles of many instances: the int8 compartments of an instance sit in
+// states8 at the same element offset as its words from words_base.
+__global__ void sir_pack_tiles_kernel(const abm_sir_instance* __restrict__ insts,
+                                      const int4* __restrict__ work, int nwork,
+                                      const int8_t* __restrict__ states8,
+                                      const int32_t* __restrict__ words_base,
+                                      int32_t* __restrict__ bad) {
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int4 item = work[w];
+    const abm_sir_instance* I = insts + item.x;
+    const int i = item.y + threadIdx.x;
+    if (i >= item.z) continue;
+    int32_t* word = I->state;
+    const int8_t* st = states8 + (word - words_base);
+    const int s = st[i];
+    if (s < 0 || s > 2) {
+      atomicExch(bad, 1);
+      continue;
+    }
+    int c = 0;
+    for (int k = I->row_ptr[i]; k < I->row_ptr[i + 1]; ++k) c += st[I->col[k]] == kI;
+    word[i] = (c << 2) | s;
+  }
+}
+
+__global__ void sir_unpack_kernel(const int32_t* __restrict__ word, int n, int8_t* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int8_t)(word[i] & 3);
+}
+
+// Single-instance descriptor and tile list written on the device, so abm_sir_run makes
+// no host-to-device copy and can be captured in a CUDA graph.
 __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int ntiles,
-                                       const int32_t* row_ptr, const int32_t* col, int8_t* state,
+                                       const int32_t* row_ptr, const int32_t* col, int32_t* words,
                                        int32_t* counts, const uint32_t* coll_keys, int32_t n,
-                                       int32_t steps, float beta, float gamma) {
+                                       int32_t steps, float beta, float gamma,
+                                       const int32_t* sizes) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g == 0) {
     d->row_ptr = row_ptr;
     d->col = col;
-    d->state = state;
+    d->state = words;
     d->counts = counts;
     d->done_flag = nullptr;
     d->coll_keys = coll_keys;
@@ -180,8 +294,13 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->steps = steps;
     d->beta = beta;
     d->gamma = gamma;
-    d->reserved = 0;
+    d->num_s = sizes[0];
+    d->num_i = sizes[1];
+    d->num_r = sizes[2];
+    d->step_si = 0;
+    d->step_ir = 0;
     d->edges_scanned = 0;
+    d->edges_pushed = 0;
   }
   for (int b = g; b < ntiles; b += gridDim.x * blockDim.x) {
     const int begin = b * kSirThreads;
@@ -203,22 +322,76 @@ extern "C" {
 
 size_t abm_sir_instance_size(void) { return sizeof(abm_sir_instance); }
 
-int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                  int32_t nwork, int32_t nsteps, int32_t grid, void* stream) {
-  if (!insts || ninst <= 0 || nwork < 0 || nsteps < 0 || (nwork > 0 && !work))
-    return ABM_ERR_BADARG;
-  if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)))
+size_t abm_sir_changes_bytes(int64_t max_agents) {
+  if (max_agents <= 0) return 0;
+  return sizeof(ChangeHeader) + (size_t)max_agents * sizeof(int2);
+}
+
+int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
+                 int32_t* words, int32_t* sizes, int32_t* status, void* stream) {
+  if (!state || !row_ptr || !col || !words || !sizes || !status || n <= 0 || n >= (1ll << 29))
     return ABM_ERR_BADARG;
   cudaStream_t s = abm_host::as_stream(stream);
+  int st = abm_host::record_cuda_error(cudaMemsetAsync(sizes, 0, 3 * sizeof(int32_t), s),
+                                       "abm_sir_pack/sizes");
+  if (st) return st;
+  st = abm_host::record_cuda_error(cudaMemsetAsync(status, 0, sizeof(int32_t), s),
+                                   "abm_sir_pack/status");
+  if (st) return st;
+  sir_pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(state, row_ptr, col, (int)n, words,
+                                                             sizes, status);
+  return abm_host::check_launch("abm_sir_pack");
+}
+
+int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work, int32_t nwork,
+                       const int8_t* states8, const int32_t* words_base, int32_t* status,
+                       void* stream) {
+  if (!insts || !work || nwork <= 0 || !states8 || !words_base || !status) return ABM_ERR_BADARG;
+  if (!abm_host::aligned(insts, 8) || !abm_host::aligned(work, 16)) return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  int st = abm_host::record_cuda_error(cudaMemsetAsync(status, 0, sizeof(int32_t), s),
+                                       "abm_sir_pack_batch/status");
+  if (st) return st;
+  sir_pack_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(
+      insts, reinterpret_cast<const int4*>(work), nwork, states8, words_base, status);
+  return abm_host::check_launch("abm_sir_pack_batch");
+}
+
+int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream) {
+  if (!words || !state || n <= 0 || n >= (1ll << 29)) return ABM_ERR_BADARG;
+  sir_unpack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, abm_host::as_stream(stream)>>>(
+      words, (int)n, state);
+  return abm_host::check_launch("abm_sir_unpack");
+}
+
+int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
+                  int32_t nwork, int32_t nsteps, int32_t grid, void* changes,
+                  size_t changes_bytes, void* stream) {
+  if (!insts || ninst <= 0 || nwork < 0 || nsteps < 0 || (nwork > 0 && !work) || !changes)
+    return ABM_ERR_BADARG;
+  if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)) ||
+      !abm_host::aligned(changes, 16))
+    return ABM_ERR_BADARG;
+  if (changes_bytes < sizeof(ChangeHeader) + sizeof(int2)) return ABM_ERR_WORKSPACE;
+  const size_t cap_sz = (changes_bytes - sizeof(ChangeHeader)) / sizeof(int2);
+  const int capacity = cap_sz > 0x7FFFFFFF ? 0x7FFFFFFF : (int)cap_sz;
+  ChangeHeader* hdr = static_cast<ChangeHeader*>(changes);
+  int2* list = reinterpret_cast<int2*>(hdr + 1);
+  cudaStream_t s = abm_host::as_stream(stream);
   const int g = grid > 0 ? grid : default_grid(nwork);
+  const int push_grid = abm_host::sm_count() * 8;
   const int fin_blocks = (ninst + 255) / 256;
   for (int32_t k = 0; k < nsteps; ++k) {
     if (nwork > 0) {
-      sir_step_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work), nwork);
-      int st = abm_host::check_launch("abm_sir_steps/step");
+      sir_decide_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work),
+                                                  nwork, hdr, list, capacity);
+      int st = abm_host::check_launch("abm_sir_steps/decide");
+      if (st) return st;
+      sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, hdr, list, capacity);
+      st = abm_host::check_launch("abm_sir_steps/push");
       if (st) return st;
     }
-    sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst);
+    sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, hdr);
     int st = abm_host::check_launch("abm_sir_steps/finalize");
     if (st) return st;
   }
@@ -228,13 +401,14 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
 size_t abm_sir_run_workspace_bytes(int64_t n) {
   if (n <= 0) return 0;
   const int64_t tiles = (n + kSirThreads - 1) / kSirThreads;
-  return align256(sizeof(abm_sir_instance)) + (size_t)tiles * sizeof(int4);
+  return align256(sizeof(abm_sir_instance)) + align256((size_t)tiles * sizeof(int4)) +
+         align256((size_t)n * sizeof(int32_t)) + 256 + align256(abm_sir_changes_bytes(n));
 }
 
 int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* state,
                 const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
                 int32_t* counts, void* workspace, size_t workspace_bytes, void* stream) {
-  if (!row_ptr || !col || !state || !coll_keys || !counts || n <= 0 || n > 0x7FFFFFFFll ||
+  if (!row_ptr || !col || !state || !coll_keys || !counts || n <= 0 || n >= (1ll << 29) ||
       steps < 0)
     return ABM_ERR_BADARG;
   if (!abm_host::aligned(coll_keys, 8)) return ABM_ERR_BADARG;
@@ -243,19 +417,31 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
     return ABM_ERR_WORKSPACE;
   if (steps == 0) return ABM_OK;
   cudaStream_t s = abm_host::as_stream(stream);
-  abm_sir_instance* d = static_cast<abm_sir_instance*>(workspace);
-  int4* work = reinterpret_cast<int4*>(static_cast<char*>(workspace) +
-                                       align256(sizeof(abm_sir_instance)));
+  char* p = static_cast<char*>(workspace);
+  abm_sir_instance* d = reinterpret_cast<abm_sir_instance*>(p);
+  p += align256(sizeof(abm_sir_instance));
   const int ntiles = (int)((n + kSirThreads - 1) / kSirThreads);
-  int st = abm_host::record_cuda_error(
-      cudaMemsetAsync(counts, 0, sizeof(int32_t) * 3 * (size_t)steps, s), "abm_sir_run/memset");
+  int4* work = reinterpret_cast<int4*>(p);
+  p += align256((size_t)ntiles * sizeof(int4));
+  int32_t* words = reinterpret_cast<int32_t*>(p);
+  p += align256((size_t)n * sizeof(int32_t));
+  int32_t* misc = reinterpret_cast<int32_t*>(p);  // sizes[3], status
+  p += 256;
+  void* changes = p;
+  int st = abm_sir_pack(state, row_ptr, col, n, words, misc, misc + 3, stream);
+  if (st) return st;
+  st = abm_host::record_cuda_error(cudaMemsetAsync(changes, 0, sizeof(ChangeHeader), s),
+                                   "abm_sir_run/changes");
   if (st) return st;
   sir_setup_single_kernel<<<(ntiles + 255) / 256, 256, 0, s>>>(
-      d, work, ntiles, row_ptr, col, state, counts, coll_keys, (int32_t)n, steps, beta, gamma);
+      d, work, ntiles, row_ptr, col, words, counts, coll_keys, (int32_t)n, steps, beta, gamma,
+      misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
-  return abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, steps, 0,
-                       stream);
+  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, steps, 0,
+                     changes, align256(abm_sir_changes_bytes(n)), stream);
+  if (st) return st;
+  return abm_sir_unpack(words, n, state, stream);
 }
 
 }  // extern "C"

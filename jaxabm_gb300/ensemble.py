@@ -2,11 +2,11 @@
 
 The reference runs ensembles as serial Python loops of ``model.run()``
 (``Model.batch_run``, jaxabm/agentpy.py:1116-1152; ``SensitivityAnalysis.run``,
-jaxabm/analysis.py:97-165).  Here every member is an *instance*: its CSR, compartments and
-per-step counts live in packed device buffers, a device descriptor (``abm_sir_instance``)
-points into them, and ``abm_sir_steps`` advances all live instances over a persistent grid
-of (instance, 256-agent tile) work items.  The whole multi-step launch sequence is captured
-once in a CUDA graph and replayed.
+jaxabm/analysis.py:97-165).  Here every member is an *instance*: its CSR, per-agent words
+and per-step counts live in packed device buffers, a device descriptor
+(``abm_sir_instance``) points into them, and ``abm_sir_steps`` advances all live instances
+over a persistent grid of (instance, 256-agent tile) work items.  The whole multi-step
+launch sequence is captured once in a CUDA graph and replayed.
 
 Each instance follows exactly the single-model key chain (``PRNGKey(seed)`` ->
 ``initialize`` -> ``Model.step``), so its result is identical to running it alone.
@@ -25,14 +25,16 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 256
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 88 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 112 bytes
 INSTANCE_DTYPE = np.dtype([
     ("row_ptr", "<u8"), ("col", "<u8"), ("state", "<u8"), ("counts", "<u8"),
     ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)), ("n", "<i4"),
-    ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("reserved", "<i4"),
-    ("edges_scanned", "<u8"),
+    ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("num_s", "<i4"),
+    ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"), ("step_ir", "<i4"),
+    ("edges_scanned", "<u8"), ("edges_pushed", "<u8"),
 ])
-assert INSTANCE_DTYPE.itemsize == 88
+assert INSTANCE_DTYPE.itemsize == 112
+WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
 
@@ -62,6 +64,32 @@ def model_rngs(seeds):
     return jrandom.split(dk, 2)[:, 0].contiguous()
 
 
+def changes_workspace(max_agents, device=None):
+    """Zeroed change-list workspace of ``abm_sir_steps`` for ``max_agents`` live agents."""
+    nbytes = _lib.load().abm_sir_changes_bytes(int(max_agents))
+    return torch.zeros(max(nbytes, 32), dtype=torch.uint8, device=device or _dev.device())
+
+
+def changes_overflowed(ws):
+    return int(ws[4:8].view(torch.int32).item()) != 0
+
+
+def pack_words(state_i8, row_ptr, col, words, stream=None):
+    """Per-agent words (infected-neighbour count << 2 | compartment) of one instance."""
+    n = state_i8.numel()
+    scratch = torch.zeros(4, dtype=torch.int32, device=words.device)
+    _lib.call("abm_sir_pack", _dev.ptr(state_i8), _dev.ptr(row_ptr), _dev.ptr(col), n,
+              _dev.ptr(words), _dev.ptr(scratch), _dev.ptr(scratch[3:]), _dev.stream_handle(stream))
+    return scratch
+
+
+def unpack_words(words, stream=None):
+    out = torch.empty(words.numel(), dtype=torch.int8, device=words.device)
+    _lib.call("abm_sir_unpack", _dev.ptr(words), words.numel(), _dev.ptr(out),
+              _dev.stream_handle(stream))
+    return out
+
+
 class SIRBatch:
     """A fixed set of SIR instances packed into device buffers.
 
@@ -81,62 +109,82 @@ class SIRBatch:
         self.steps = int(steps)
         self.n = np.array([len(rp) - 1 for rp, _ in graphs], dtype=np.int64)
         self.e = np.array([len(c) for _, c in graphs], dtype=np.int64)
-        # packed host buffers -> one device buffer each
         rp_off = np.concatenate([[0], np.cumsum(self.n + 1)])
         col_off = np.concatenate([[0], np.cumsum(self.e)])
-        st_off = np.concatenate([[0], np.cumsum(2 * self.n)])
+        w_off = np.concatenate([[0], np.cumsum(self.n)])
         cnt_off = np.arange(k + 1, dtype=np.int64) * self.steps * 3
         h_rp = np.empty(rp_off[-1], dtype=np.int32)
         h_col = np.empty(col_off[-1], dtype=np.int32)
-        h_st = np.zeros(st_off[-1], dtype=np.int8)
+        h_st = np.empty(w_off[-1], dtype=np.int8)
         for i, ((rp, col), st) in enumerate(zip(graphs, init_states)):
             h_rp[rp_off[i]:rp_off[i + 1]] = rp
             h_col[col_off[i]:col_off[i + 1]] = col
-            h_st[st_off[i]:st_off[i] + self.n[i]] = st
+            h_st[w_off[i]:w_off[i + 1]] = st
+        self.h_state0 = h_st
         self.row_ptr = torch.from_numpy(h_rp).to(dev)
         self.col = torch.from_numpy(h_col).to(dev)
-        self.state = torch.from_numpy(h_st).to(dev)
-        self.h_state0 = h_st
-        self.s0 = np.array([int((st == 0).sum()) for st in init_states], dtype=np.int64)
+        self.state8 = torch.from_numpy(h_st).to(dev)
+        self.words = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
         self.counts = torch.zeros(int(cnt_off[-1]), dtype=torch.int32, device=dev)
-        self._offsets = (rp_off, col_off, st_off, cnt_off)
+        self._offsets = (rp_off, col_off, w_off, cnt_off)
+        sizes = np.array([[int((st == c).sum()) for c in (0, 1, 2)] for st in init_states],
+                         dtype=np.int32).reshape(k, 3)
+        self.s0 = sizes[:, 0].astype(np.int64)
         desc = np.zeros(k, dtype=INSTANCE_DTYPE)
         desc["row_ptr"] = self.row_ptr.data_ptr() + 4 * rp_off[:-1]
         desc["col"] = self.col.data_ptr() + 4 * col_off[:-1]
-        desc["state"] = self.state.data_ptr() + st_off[:-1]
+        desc["state"] = self.words.data_ptr() + 4 * w_off[:-1]
         desc["counts"] = self.counts.data_ptr() + 4 * cnt_off[:-1]
         desc["n"] = self.n
-        desc["t"] = 0
         desc["steps"] = self.steps
         desc["beta"] = np.asarray(betas, dtype=np.float32)
         desc["gamma"] = np.asarray(gammas, dtype=np.float32)
-        self.h_desc0 = desc
-        words = INSTANCE_DTYPE.itemsize // 4
-        self.desc = torch.from_numpy(desc.view(np.int32).reshape(k, words).copy()).to(dev)
+        desc["num_s"], desc["num_i"], desc["num_r"] = sizes[:, 0], sizes[:, 1], sizes[:, 2]
+        self.desc = torch.from_numpy(desc.view(np.int32).reshape(k, WORDS).copy()).to(dev)
         self.rng0 = model_rngs(seeds)
         self.desc[:, RNG_WORD:RNG_WORD + 2] = self.rng0
         self.desc0 = self.desc.clone()
         self.work = torch.from_numpy(
             np.concatenate([tiles_for(i, int(n)) for i, n in enumerate(self.n)])).to(dev)
-        self.state0 = self.state.clone()
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.pack()
+        if int(self._status.item()) != 0:
+            raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
+        self.words0 = self.words.clone()
+        self.changes = changes_workspace(int(self.n.sum()))
         self.grid = 0
         self._graph = None
         self._graph_steps = None
+
+    def pack(self, stream=None):
+        """Words of every instance from the int8 compartments in ``state8`` (one launch)."""
+        _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(self.work),
+                  self.work.shape[0], _dev.ptr(self.state8), _dev.ptr(self.words),
+                  _dev.ptr(self._status), _dev.stream_handle(stream))
+
+    def load_host(self, h_row_ptr, h_col, h_state8, stream=None):
+        """Inputs from (pinned) host buffers laid out like ``row_ptr``/``col``/``state8``:
+        copy them in, rebuild the words and rewind every instance to step 0."""
+        self.row_ptr.copy_(h_row_ptr, non_blocking=True)
+        self.col.copy_(h_col, non_blocking=True)
+        self.state8.copy_(h_state8, non_blocking=True)
+        self.pack(stream)
+        self.desc.copy_(self.desc0, non_blocking=True)
 
     @property
     def agent_steps(self):
         return int(self.n.sum()) * self.steps
 
     def reset(self):
-        """Back to step 0 (state, counters, key chains) without reallocating."""
-        self.state.copy_(self.state0)
+        """Back to step 0 (words, counters, key chains) without reallocating."""
+        self.words.copy_(self.words0)
         self.desc.copy_(self.desc0)
-        self.counts.zero_()
 
     def launch(self, nsteps, stream=None):
         """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps``)."""
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
-                  self.work.shape[0], int(nsteps), int(self.grid), _dev.stream_handle(stream))
+                  self.work.shape[0], int(nsteps), int(self.grid), _dev.ptr(self.changes),
+                  self.changes.numel(), _dev.stream_handle(stream))
 
     def capture(self, nsteps):
         """Capture ``nsteps`` steps into a CUDA graph (replayed by :meth:`replay`)."""
@@ -164,31 +212,36 @@ class SIRBatch:
         else:
             self.launch(self.steps)
 
+    def check(self):
+        if changes_overflowed(self.changes):
+            raise RuntimeError("SIR change list overflowed (workspace smaller than live agents)")
+
     def final_state(self, i):
-        st_off = self._offsets[2]
-        n = int(self.n[i])
-        buf = self.steps & 1
-        return self.state[st_off[i] + buf * n: st_off[i] + (buf + 1) * n]
+        w_off = self._offsets[2]
+        return unpack_words(self.words[w_off[i]:w_off[i + 1]])
 
     def counts_of(self, i):
         c = self._offsets[3]
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
-    def edges_scanned(self):
-        """CSR slots examined by the step kernel, summed over instances since reset."""
+    def launches_per_run(self):
+        return 3 * self.steps
+
+    def edge_stats(self):
+        """(CSR slots read by decide, CSR slots read by push, compartment changes) since
+        the last reset, summed over instances."""
         d = self.desc.cpu().numpy().view(INSTANCE_DTYPE).reshape(-1)
-        return int(d["edges_scanned"].sum())
+        changes = int((d["num_i"] + 2 * d["num_r"]).sum() - (self.h_state0 == 1).sum()
+                      - 2 * (self.h_state0 == 2).sum())
+        return int(d["edges_scanned"].sum()), int(d["edges_pushed"].sum()), changes
 
     def algorithmic_bytes(self):
-        """Bytes the run must move (after it completed): per step and instance 2 bytes of
-        state per agent (read + write), 4 bytes of row offset per susceptible agent, and
-        4 + 1 bytes (column index + neighbour state) per CSR slot examined."""
-        counts = self.counts.reshape(self.k, self.steps, 3).cpu().numpy().astype(np.int64)
-        s_pre = np.concatenate([self.s0[:, None], counts[:, :-1, 0]], axis=1)
-        return int(2 * self.n.sum() * self.steps + 4 * s_pre.sum() + 5 * self.edges_scanned())
-
-    def launches_per_run(self):
-        return 2 * self.steps
+        """Bytes the run must move (after it completed): per step and agent its 4-byte word;
+        per CSR slot read by decide 8 bytes (column index + neighbour word); per slot read
+        by push 12 bytes (column index + atomic read-modify-write); per compartment change
+        32 bytes (list entry write and read, row offsets, own word update)."""
+        scanned, pushed, changes = self.edge_stats()
+        return int(4 * self.n.sum() * self.steps + 8 * scanned + 12 * pushed + 32 * changes)
 
 
 # ---- the batched-ensemble workload (4,096 SIR instances) -------------------------------

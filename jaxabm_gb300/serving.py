@@ -27,7 +27,8 @@ import torch
 
 from . import _dev
 from . import _lib
-from .ensemble import INSTANCE_DTYPE, RNG_WORD, TILE, check_layout, model_rngs
+from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, changes_workspace,
+                       check_layout, model_rngs, pack_words, unpack_words)
 
 
 class Request:
@@ -56,7 +57,7 @@ class Request:
 
     def device_bytes(self):
         n, e = self.n, len(self.col)
-        return 4 * (n + 1) + 4 * e + 2 * n + 12 * self.steps
+        return 4 * (n + 1) + 4 * e + 5 * n + 12 * self.steps
 
     @property
     def latency(self):
@@ -91,6 +92,7 @@ class SIRServer:
         self.h_work[:, 0] = self.dummy
         self.work = torch.zeros((self.max_tiles, 4), dtype=torch.int32, device=dev)
         self.work.copy_(self.h_work)
+        self.changes = changes_workspace(self.max_tiles * TILE)
         self.done = torch.zeros(self.max_slots, dtype=torch.int32).pin_memory()
         self.stream = torch.cuda.Stream()
         self.free_slots = list(range(self.max_slots - 1, -1, -1))
@@ -107,7 +109,8 @@ class SIRServer:
     # -- graph ------------------------------------------------------------------------
     def _launch(self):
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.max_slots + 1, _dev.ptr(self.work),
-                  self.max_tiles, self.steps_per_tick, self.grid, self.stream.cuda_stream)
+                  self.max_tiles, self.steps_per_tick, self.grid, _dev.ptr(self.changes),
+                  self.changes.numel(), self.stream.cuda_stream)
 
     def _capture(self):
         torch.cuda.synchronize()
@@ -127,11 +130,21 @@ class SIRServer:
     def _tiles(self, req):
         return (req.n + TILE - 1) // TILE
 
+    @staticmethod
+    def free_bytes():
+        """Device memory available to new requests: free in the driver plus what the caching
+        allocator holds but does not use."""
+        free, _ = torch.cuda.mem_get_info()
+        return free + torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
+
+    def check(self):
+        if changes_overflowed(self.changes):
+            raise RuntimeError("SIR change list overflowed")
+
     def _try_admit(self, req) -> bool:
         if not self.free_slots or self._tiles_used + self._tiles(req) > self.max_tiles:
             return False
-        free, _ = torch.cuda.mem_get_info()
-        if free - self.reserve < req.device_bytes():
+        if self.free_bytes() - self.reserve < req.device_bytes():
             return False
         slot = self.free_slots.pop()
         dev = self.desc.device
@@ -139,10 +152,12 @@ class SIRServer:
         with torch.cuda.stream(s):
             rp = torch.as_tensor(req.row_ptr).to(dev, non_blocking=True)
             col = torch.as_tensor(req.col).to(dev, non_blocking=True)
-            st = torch.empty(2 * req.n, dtype=torch.int8, device=dev)
-            st[:req.n].copy_(torch.as_tensor(req.state), non_blocking=True)
+            st8 = torch.as_tensor(req.state).to(dev, non_blocking=True)
+            st = torch.empty(req.n, dtype=torch.int32, device=dev)
+            pack_words(st8, rp, col, st, s)
             counts = torch.zeros(req.steps * 3, dtype=torch.int32, device=dev)
             rng = model_rngs([req.seed])
+        host_state = np.asarray(req.state)
         row = np.zeros(1, dtype=INSTANCE_DTYPE)
         row["row_ptr"] = rp.data_ptr()
         row["col"] = col.data_ptr()
@@ -154,6 +169,9 @@ class SIRServer:
         row["steps"] = req.steps
         row["beta"] = req.beta
         row["gamma"] = req.gamma
+        row["num_s"] = int((host_state == 0).sum())
+        row["num_i"] = int((host_state == 1).sum())
+        row["num_r"] = int((host_state == 2).sum())
         self.done[slot] = 0
         self.h_desc[slot] = torch.from_numpy(row.view(np.int32).copy())
         with torch.cuda.stream(s):
@@ -193,9 +211,8 @@ class SIRServer:
                 req.counts = torch.empty((req.steps, 3), dtype=torch.int32).pin_memory()
                 req.counts.copy_(counts.view(req.steps, 3), non_blocking=True)
                 if req.keep_state:
-                    buf = req.steps & 1
                     req.final_state = torch.empty(req.n, dtype=torch.int8).pin_memory()
-                    req.final_state.copy_(st[buf * req.n:(buf + 1) * req.n], non_blocking=True)
+                    req.final_state.copy_(unpack_words(st, self.stream), non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
             req._event = ev

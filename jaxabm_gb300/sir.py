@@ -81,26 +81,21 @@ class SIRKernel(StepKernel):
         init = env.get("sir_initial_state")
         if init is None:
             init = initial_states(n, params["initial_infected"], params["infection_seed"])
-        buf = torch.empty(2 * n, dtype=torch.int8, device=_dev.device())
-        buf[:n].copy_(torch.as_tensor(np.asarray(init, dtype=np.int8)).to(buf.device))
-        return {"state": buf[:n], "_sir_buffer": buf}
+        st = torch.as_tensor(np.asarray(init, dtype=np.int8)).to(_dev.device())
+        return {"state": st.contiguous()}
 
     def run(self, states, coll_keys, params, env):
         coll_keys = coll_keys.reshape(-1, 2).contiguous()
         steps = coll_keys.shape[0]
-        buf = states["_sir_buffer"]
-        n = buf.numel() // 2
-        if states["state"].data_ptr() != buf.data_ptr():
-            buf[:n].copy_(states["state"])
+        st = states["state"].contiguous()
+        n = st.numel()
         rp, col = env["network_row_ptr"], env["network_col"]
-        counts = torch.empty((steps, 3), dtype=torch.int32, device=buf.device)
+        counts = torch.empty((steps, 3), dtype=torch.int32, device=st.device)
         ws = _dev.workspace(_lib.load().abm_sir_run_workspace_bytes(n))
-        _lib.call("abm_sir_run", _dev.ptr(rp), _dev.ptr(col), n, _dev.ptr(buf),
+        _lib.call("abm_sir_run", _dev.ptr(rp), _dev.ptr(col), n, _dev.ptr(st),
                   _dev.ptr(coll_keys), steps, float(params["beta"]), float(params["gamma"]),
                   _dev.ptr(counts), _dev.ptr(ws), ws.numel(), _dev.stream_handle())
-        if steps & 1:
-            buf[:n].copy_(buf[n:])
-        return {"state": buf[:n], "_sir_buffer": buf}, counts
+        return {"state": st}, counts
 
     def step(self, states, coll_key, params, env):
         states, counts = self.run(states, coll_key.reshape(1, 2), params, env)

@@ -1,0 +1,88 @@
+"""Continuous-batching server: every request's result is identical alone and in the mix,
+admission respects slots/tiles/memory, and requests arriving while others run overlap."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import coracle, models
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(k, seed0=100, steps=60):
+    from jaxabm_gb300 import sir
+    from jaxabm_gb300.serving import Request
+    rs = np.random.RandomState(seed0)
+    reqs = []
+    for i in range(k):
+        n = int(rs.randint(300, 20_000))
+        s = seed0 + i
+        rp, col = sir.barabasi_albert(n, 4, s)
+        st = sir.initial_states(n, 0.005, s)
+        reqs.append(Request(i, rp, col, st, float(rs.uniform(0.02, 0.2)),
+                            float(rs.uniform(0.05, 0.3)), s, steps, keep_state=True))
+    return reqs
+
+
+def test_results_identical_alone_and_in_mix(cuda):
+    from jaxabm_gb300.serving import SIRServer
+    reqs = _requests(24)
+    # mix: all submitted at once into a small server (forces queueing + slot reuse)
+    srv = SIRServer(max_slots=6, max_tiles=256, steps_per_tick=7)
+    for r in reqs:
+        srv.submit(r)
+    srv.drain()
+    srv.check()
+    assert len(srv.completed) == len(reqs)
+    mixed = {r.rid: (r.counts.numpy().copy(), r.final_state.numpy().copy()) for r in srv.completed}
+    # alone: each request by itself through a fresh server
+    for r in _requests(24)[::5]:
+        solo = SIRServer(max_slots=1, max_tiles=128, steps_per_tick=13)
+        solo.submit(r)
+        solo.drain()
+        c, fs = mixed[r.rid]
+        assert np.array_equal(solo.completed[0].counts.numpy(), c)
+        assert np.array_equal(solo.completed[0].final_state.numpy(), fs)
+    # and against the oracle
+    for r in _requests(24)[:4]:
+        rng, _ = models.model_keys(r.seed, 1)
+        ref_st, ref_counts, _ = coracle.sir_run(r.row_ptr, r.col, r.state, rng, r.steps,
+                                                r.beta, r.gamma)
+        c, fs = mixed[r.rid]
+        assert np.array_equal(c, ref_counts)
+        assert np.array_equal(fs, ref_st)
+
+
+def test_overlap_and_slot_limit(cuda):
+    from jaxabm_gb300.serving import SIRServer
+    reqs = _requests(10, seed0=7, steps=40)
+    srv = SIRServer(max_slots=3, max_tiles=512, steps_per_tick=4)
+    for r in reqs:
+        srv.submit(r)
+    max_active = 0
+    while not srv.idle():
+        srv.tick()
+        max_active = max(max_active, len(srv.active))
+        assert len(srv.active) <= 3
+    assert max_active == 3  # several requests were on the device together
+    assert len(srv.completed) == 10
+    adm = sorted(r.admitted for r in srv.completed)
+    fin = sorted(r.finished for r in srv.completed)
+    assert adm[3] < fin[-1]  # later requests were admitted while others were running
+
+
+def test_admission_by_free_memory(cuda, monkeypatch):
+    from jaxabm_gb300.serving import SIRServer
+    reqs = _requests(3, seed0=11, steps=10)
+    srv = SIRServer(max_slots=4, max_tiles=256, steps_per_tick=5, reserve_bytes=0)
+    # pretend the device has room for exactly one request
+    budget = reqs[0].device_bytes() + 1
+    monkeypatch.setattr(SIRServer, "free_bytes",
+                        staticmethod(lambda: budget - sum(r.device_bytes() for r in srv.active.values())))
+    for r in reqs:
+        srv.submit(r)
+    srv.tick()
+    assert len(srv.active) == 1 and len(srv.queue) == 2
+    srv.drain()
+    assert len(srv.completed) == 3

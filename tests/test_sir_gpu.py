@@ -37,8 +37,7 @@ def _run_abi(rp, col, st0, seed, steps, beta, gamma):
     rng, _ = models.model_keys(seed, 1)
     ck = jr.keychain(_dev.keys_from_numpy(rng), steps, 1).reshape(steps, 2).contiguous()
     n = st0.size
-    buf = torch.zeros(2 * n, dtype=torch.int8, device="cuda")
-    buf[:n] = torch.from_numpy(st0).cuda()
+    buf = torch.from_numpy(st0).cuda()
     drp = torch.from_numpy(rp).cuda()
     dcol = torch.from_numpy(col).cuda()
     counts = torch.empty((steps, 3), dtype=torch.int32, device="cuda")
@@ -47,7 +46,7 @@ def _run_abi(rp, col, st0, seed, steps, beta, gamma):
     _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(buf), _dev.ptr(ck), steps,
               beta, gamma, _dev.ptr(counts), _dev.ptr(ws), wsb, None)
     torch.cuda.synchronize()
-    fin = buf[(steps & 1) * n:(steps & 1) * n + n].cpu().numpy()
+    fin = buf.cpu().numpy()
     return fin, counts.cpu().numpy()
 
 
@@ -135,6 +134,6 @@ def test_sir_batched_equals_alone(cuda, use_graph):
 def test_sir_bad_args(cuda):
     from jaxabm_gb300 import _lib
     L = _lib.load()
-    assert L.abm_sir_steps(None, 1, None, 0, 1, 0, None) == _lib.ABM_ERR_BADARG
+    assert L.abm_sir_steps(None, 1, None, 0, 1, 0, None, 0, None) == _lib.ABM_ERR_BADARG
     assert L.abm_sir_run(None, None, 10, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
         _lib.ABM_ERR_BADARG
