@@ -51,7 +51,8 @@ def test_forward_vs_oracle(cuda, n, B, T):
               f"gpu-f32oracle {e_gpu32[q]:.2e} moments {e_mom[q]:.2e}")
     assert np.all(e_gpu64[~ill] < 1e-5)
     assert np.all(e_mom < 1e-5)
-    assert np.median(e_gpu32) < 1e-6
+    if (~ill).any():
+        assert np.median(e_gpu32[~ill]) < 1e-6
     m = b.moments().cpu().numpy()
     np.testing.assert_allclose(m, coracle.opinion_moments_f64(got.astype(np.float64)), rtol=1e-9)
 
