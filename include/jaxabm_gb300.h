@@ -171,7 +171,7 @@ typedef struct abm_sir_instance {
   unsigned long long edges_pushed;
 } abm_sir_instance;
 
-/* A tile of agents [begin, end) of instance `inst` (end - begin <= 256). */
+/* A tile of agents [begin, end) of instance `inst` (end - begin <= abm_sir_tile_agents()). */
 typedef struct abm_work_item {
   int32_t inst;
   int32_t begin;
@@ -180,6 +180,9 @@ typedef struct abm_work_item {
 } abm_work_item;
 
 ABM_API size_t abm_sir_instance_size(void);
+
+/* Largest tile (agents per work item) of the SIR kernels: 1024. */
+ABM_API int32_t abm_sir_tile_agents(void);
 
 /* Per-agent words of one instance from int8 compartments state[n] (n < 2^29): the number
  * of infected neighbours over the CSR is counted; sizes (device int32[3]) receives the
@@ -204,7 +207,9 @@ ABM_API int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void*
 ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
 
 /* nsteps synchronous SIR steps of every instance with t < steps, over the tiles `work`
- * (persistent grid of `grid` CTAs; 0 = 8 per SM).  Per step and agent i of an instance:
+ * (persistent grid of `grid` CTAs; 0 = 8 per SM).  When live_work (device int32) is not
+ * NULL, only the first min(*live_work, nwork) tiles are read, so a CUDA graph of this call
+ * stays valid while the number of live tiles changes.  Per step and agent i of an instance:
  * agent_key = split(coll_key, n)[i], k_inf, k_rec = split(agent_key);
  *   S -> I if some neighbour slot k with an I neighbour has uniform(k_inf,(deg,))[k] < beta;
  *   I -> R if uniform(k_rec) < gamma.
@@ -218,8 +223,8 @@ ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
  * and may be rewritten between calls (e.g. to admit instances) without re-capturing a
  * CUDA graph of this call. */
 ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                          int32_t nwork, int32_t nsteps, int32_t grid, void* changes,
-                          size_t changes_bytes, void* stream);
+                          int32_t nwork, const int32_t* live_work, int32_t nsteps, int32_t grid,
+                          void* changes, size_t changes_bytes, void* stream);
 
 ABM_API size_t abm_sir_run_workspace_bytes(int64_t n);
 

@@ -12,8 +12,9 @@
 // Work-efficient ("frontier") formulation.  Each agent has one int32 word
 //     word = (number of infected neighbours << 2) | compartment
 // and a step is three launches:
-//   decide   one thread per agent over (instance, 256-agent tile) work items: reads its
-//            own word; only a susceptible agent with infected neighbours scans its CSR row
+//   decide   over (instance, 1024-agent tile) work items, four agents per thread (their
+//            four words are loaded before any is used, so each thread keeps four loads in
+//            flight): only a susceptible agent with infected neighbours scans its CSR row
 //            (stopping at the first firing draw or once all its infected neighbours were
 //            seen); an infected agent draws its recovery.  Agents whose compartment
 //            changes are appended to a change list (warp-aggregated atomics).  Nothing is
@@ -32,6 +33,8 @@
 namespace {
 
 constexpr int kSirThreads = 256;
+constexpr int kPerThread = 4;
+constexpr int kTile = kSirThreads * kPerThread;  // agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kS = 0, kI = 1;
@@ -54,116 +57,141 @@ __device__ __forceinline__ uint2 coll_key_of(const abm_sir_instance* I, int t) {
              : abm::split_at(abm::split_at(make_uint2(I->rng[0], I->rng[1]), 1), 1);
 }
 
+__device__ __forceinline__ int live_count(const int32_t* live, int nwork) {
+  return live != nullptr ? min(*live, nwork) : nwork;
+}
+
+// Decision for one agent slot of the warp; all 32 lanes call it together.  Returns the
+// CSR slots this lane's agent scanned.
+__device__ __forceinline__ int decide_one(const abm_sir_instance* I, int inst, int t,
+                                          const int32_t* __restrict__ word, int i, bool valid,
+                                          int32_t wi, uint2& coll, bool& have_coll, int lane,
+                                          ChangeHeader* __restrict__ hdr,
+                                          int2* __restrict__ changes, int capacity) {
+  const int s = wi & 3;
+  int cnt = wi >> 2;
+  int ns = s;
+  bool heavy = false;
+  int row0 = 0, deg = 0, scanned = 0;
+  const bool scan = valid && s == kS && cnt > 0;
+  const bool recover = valid && s == kI;
+  const bool any = __any_sync(kFull, scan || recover);
+  if (!any) return 0;  // warp-uniform: nothing to decide in this slot
+  if (!have_coll) {
+    coll = coll_key_of(I, t);
+    have_coll = true;
+  }
+  if (scan) {
+    const int32_t* __restrict__ rp = I->row_ptr;
+    row0 = rp[i];
+    deg = rp[i + 1] - row0;
+    if (deg > kHeavyDeg) {
+      heavy = true;
+    } else {
+      const int32_t* __restrict__ col = I->col;
+      const float beta = I->beta;
+      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
+      int k = 0;
+      for (; k < deg; ++k) {
+        if ((word[col[row0 + k]] & 3) == kI) {
+          if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
+            ns = kI;
+            ++k;
+            break;
+          }
+          if (--cnt == 0) {
+            ++k;
+            break;
+          }
+        }
+      }
+      scanned = k;
+    }
+  } else if (recover) {
+    const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
+    if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
+  }
+
+  unsigned hmask = __ballot_sync(kFull, heavy);
+  if (hmask) {
+    const int32_t* __restrict__ col = I->col;
+    const float beta = I->beta;
+    while (hmask) {
+      const int src = __ffs(hmask) - 1;
+      hmask &= hmask - 1;
+      const int hi = __shfl_sync(kFull, i, src);
+      const int hrow = __shfl_sync(kFull, row0, src);
+      const int hdeg = __shfl_sync(kFull, deg, src);
+      int remaining = __shfl_sync(kFull, cnt, src);
+      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
+      bool fired = false;
+      int c = 0;
+      for (; c < hdeg && !fired && remaining > 0; c += 32) {
+        const int k = c + lane;
+        bool isI = false, f = false;
+        if (k < hdeg) {
+          isI = (word[col[hrow + k]] & 3) == kI;
+          if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta;
+        }
+        fired = __any_sync(kFull, f);
+        remaining -= __popc(__ballot_sync(kFull, isI));
+      }
+      if (lane == src) {
+        if (fired) ns = kI;
+        scanned = min(c, hdeg);
+      }
+    }
+  }
+
+  // warp-aggregated append of the agents whose compartment changes
+  const bool changed = valid && ns != s;
+  const unsigned cmask = __ballot_sync(kFull, changed);
+  if (cmask) {
+    const int leader = __ffs(cmask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&hdr->count, __popc(cmask));
+    base = __shfl_sync(kFull, base, leader);
+    if (changed) {
+      const int pos = base + __popc(cmask & ((1u << lane) - 1u));
+      if (pos < capacity) changes[pos] = make_int2(inst, (i << 2) | ns);
+      else hdr->overflow = 1;
+    }
+  }
+  return scanned;
+}
+
 __global__ void __launch_bounds__(kSirThreads)
-sir_decide_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work, int nwork,
-                  ChangeHeader* __restrict__ hdr, int2* __restrict__ changes, int capacity) {
+sir_decide_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
+                  int nwork_max, const int32_t* __restrict__ live, ChangeHeader* __restrict__ hdr,
+                  int2* __restrict__ changes, int capacity) {
   const int lane = threadIdx.x & 31;
-  unsigned long long scanned_acc = 0;
-  int scanned_inst = -1;
+  const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
     abm_sir_instance* I = insts + item.x;
     const int t = I->t;
     if (t >= I->steps) continue;  // uniform over the CTA
     const int32_t* __restrict__ word = I->state;
-    const int i = item.y + threadIdx.x;
-    const bool valid = i < item.z;
-    const int32_t wi = valid ? word[i] : 2;
-    const int s = wi & 3;
-    int cnt = wi >> 2;
-    int ns = s;
-    bool heavy = false;
-    int row0 = 0, deg = 0, scanned = 0;
-    const bool scan = (s == kS) && cnt > 0;
-    const bool recover = (s == kI);
+    int32_t wv[kPerThread];
+#pragma unroll
+    for (int j = 0; j < kPerThread; ++j) {
+      const int i = item.y + threadIdx.x + j * kSirThreads;
+      wv[j] = i < item.z ? word[i] : 2;
+    }
     uint2 coll = make_uint2(0, 0);
-    if (__any_sync(kFull, scan || recover)) coll = coll_key_of(I, t);
-    if (scan) {
-      const int32_t* __restrict__ rp = I->row_ptr;
-      row0 = rp[i];
-      deg = rp[i + 1] - row0;
-      if (deg > kHeavyDeg) {
-        heavy = true;
-      } else {
-        const int32_t* __restrict__ col = I->col;
-        const float beta = I->beta;
-        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-        int k = 0;
-        for (; k < deg; ++k) {
-          if ((word[col[row0 + k]] & 3) == kI) {
-            if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
-              ns = kI;
-              ++k;
-              break;
-            }
-            if (--cnt == 0) {
-              ++k;
-              break;
-            }
-          }
-        }
-        scanned = k;
-      }
-    } else if (recover) {
-      const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
-      if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
+    bool have_coll = false;
+    int tile_scanned = 0;
+#pragma unroll 1
+    for (int j = 0; j < kPerThread; ++j) {
+      const int i = item.y + threadIdx.x + j * kSirThreads;
+      tile_scanned += decide_one(I, item.x, t, word, i, i < item.z, wv[j], coll, have_coll, lane,
+                                 hdr, changes, capacity);
     }
-
-    unsigned hmask = __ballot_sync(kFull, heavy);
-    if (hmask) {
-      const int32_t* __restrict__ col = I->col;
-      const float beta = I->beta;
-      while (hmask) {
-        const int src = __ffs(hmask) - 1;
-        hmask &= hmask - 1;
-        const int hi = __shfl_sync(kFull, i, src);
-        const int hrow = __shfl_sync(kFull, row0, src);
-        const int hdeg = __shfl_sync(kFull, deg, src);
-        int remaining = __shfl_sync(kFull, cnt, src);
-        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
-        bool fired = false;
-        int c = 0;
-        for (; c < hdeg && !fired && remaining > 0; c += 32) {
-          const int k = c + lane;
-          bool isI = false, f = false;
-          if (k < hdeg) {
-            isI = (word[col[hrow + k]] & 3) == kI;
-            if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta;
-          }
-          fired = __any_sync(kFull, f);
-          remaining -= __popc(__ballot_sync(kFull, isI));
-        }
-        if (lane == src) {
-          if (fired) ns = kI;
-          scanned = min(c, hdeg);
-        }
-      }
-    }
-
-    // warp-aggregated append of the agents whose compartment changes
-    const bool changed = valid && ns != s;
-    const unsigned cmask = __ballot_sync(kFull, changed);
-    if (cmask) {
-      const int leader = __ffs(cmask) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(&hdr->count, __popc(cmask));
-      base = __shfl_sync(kFull, base, leader);
-      if (changed) {
-        const int pos = base + __popc(cmask & ((1u << lane) - 1u));
-        if (pos < capacity) changes[pos] = make_int2(item.x, (i << 2) | ns);
-        else hdr->overflow = 1;
-      }
-    }
-    if (scanned) {
-      if (scanned_inst != item.x && scanned_acc) {
-        atomicAdd(&insts[scanned_inst].edges_scanned, scanned_acc);
-        scanned_acc = 0;
-      }
-      scanned_inst = item.x;
-      scanned_acc += scanned;
+    if (__any_sync(kFull, tile_scanned != 0)) {
+      const int ws = abm::warp_sum(tile_scanned);
+      if (lane == 0) atomicAdd(&I->edges_scanned, (unsigned long long)ws);
     }
   }
-  if (scanned_acc) atomicAdd(&insts[scanned_inst].edges_scanned, scanned_acc);
 }
 
 // One warp per change: neighbours' infected counts +-1, own compartment +1.
@@ -219,6 +247,14 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   }
 }
 
+__device__ __forceinline__ int32_t pack_word(const int8_t* __restrict__ st,
+                                             const int32_t* __restrict__ rp,
+                                             const int32_t* __restrict__ col, int i, int s) {
+  int c = 0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k) c += st[col[k]] == kI;
+  return (c << 2) | s;
+}
+
 // word[i] = (infected neighbours << 2) | state[i]; compartment sizes into *sizes.
 __global__ void sir_pack_kernel(const int8_t* __restrict__ state, const int32_t* __restrict__ rp,
                                 const int32_t* __restrict__ col, int n, int32_t* __restrict__ word,
@@ -232,9 +268,7 @@ __global__ void sir_pack_kernel(const int8_t* __restrict__ state, const int32_t*
     if (s < 0 || s > 2) {
       atomicExch(bad, 1);
     } else {
-      int c = 0;
-      for (int k = rp[i]; k < rp[i + 1]; ++k) c += state[col[k]] == kI;
-      word[i] = (c << 2) | s;
+      word[i] = pack_word(state, rp, col, i, s);
       atomicAdd(&sc[s], 1);
     }
   }
@@ -252,18 +286,16 @@ __global__ void sir_pack_tiles_kernel(const abm_sir_instance* __restrict__ insts
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
     const abm_sir_instance* I = insts + item.x;
-    const int i = item.y + threadIdx.x;
-    if (i >= item.z) continue;
     int32_t* word = I->state;
     const int8_t* st = states8 + (word - words_base);
-    const int s = st[i];
-    if (s < 0 || s > 2) {
-      atomicExch(bad, 1);
-      continue;
+    for (int i = item.y + threadIdx.x; i < item.z; i += blockDim.x) {
+      const int s = st[i];
+      if (s < 0 || s > 2) {
+        atomicExch(bad, 1);
+        continue;
+      }
+      word[i] = pack_word(st, I->row_ptr, I->col, i, s);
     }
-    int c = 0;
-    for (int k = I->row_ptr[i]; k < I->row_ptr[i + 1]; ++k) c += st[I->col[k]] == kI;
-    word[i] = (c << 2) | s;
   }
 }
 
@@ -303,8 +335,8 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->edges_pushed = 0;
   }
   for (int b = g; b < ntiles; b += gridDim.x * blockDim.x) {
-    const int begin = b * kSirThreads;
-    const int end = min(begin + kSirThreads, n);
+    const int begin = b * kTile;
+    const int end = min(begin + kTile, n);
     work[b] = make_int4(0, begin, end, 0);
   }
 }
@@ -321,6 +353,8 @@ size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 extern "C" {
 
 size_t abm_sir_instance_size(void) { return sizeof(abm_sir_instance); }
+
+int32_t abm_sir_tile_agents(void) { return kTile; }
 
 size_t abm_sir_changes_bytes(int64_t max_agents) {
   if (max_agents <= 0) return 0;
@@ -365,12 +399,12 @@ int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream)
 }
 
 int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                  int32_t nwork, int32_t nsteps, int32_t grid, void* changes,
-                  size_t changes_bytes, void* stream) {
+                  int32_t nwork, const int32_t* live_work, int32_t nsteps, int32_t grid,
+                  void* changes, size_t changes_bytes, void* stream) {
   if (!insts || ninst <= 0 || nwork < 0 || nsteps < 0 || (nwork > 0 && !work) || !changes)
     return ABM_ERR_BADARG;
   if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)) ||
-      !abm_host::aligned(changes, 16))
+      !abm_host::aligned(changes, 16) || (live_work && !abm_host::aligned(live_work, 4)))
     return ABM_ERR_BADARG;
   if (changes_bytes < sizeof(ChangeHeader) + sizeof(int2)) return ABM_ERR_WORKSPACE;
   const size_t cap_sz = (changes_bytes - sizeof(ChangeHeader)) / sizeof(int2);
@@ -384,7 +418,7 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   for (int32_t k = 0; k < nsteps; ++k) {
     if (nwork > 0) {
       sir_decide_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work),
-                                                  nwork, hdr, list, capacity);
+                                                  nwork, live_work, hdr, list, capacity);
       int st = abm_host::check_launch("abm_sir_steps/decide");
       if (st) return st;
       sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, hdr, list, capacity);
@@ -400,7 +434,7 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
 
 size_t abm_sir_run_workspace_bytes(int64_t n) {
   if (n <= 0) return 0;
-  const int64_t tiles = (n + kSirThreads - 1) / kSirThreads;
+  const int64_t tiles = (n + kTile - 1) / kTile;
   return align256(sizeof(abm_sir_instance)) + align256((size_t)tiles * sizeof(int4)) +
          align256((size_t)n * sizeof(int32_t)) + 256 + align256(abm_sir_changes_bytes(n));
 }
@@ -420,7 +454,7 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
   char* p = static_cast<char*>(workspace);
   abm_sir_instance* d = reinterpret_cast<abm_sir_instance*>(p);
   p += align256(sizeof(abm_sir_instance));
-  const int ntiles = (int)((n + kSirThreads - 1) / kSirThreads);
+  const int ntiles = (int)((n + kTile - 1) / kTile);
   int4* work = reinterpret_cast<int4*>(p);
   p += align256((size_t)ntiles * sizeof(int4));
   int32_t* words = reinterpret_cast<int32_t*>(p);
@@ -438,7 +472,7 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
       misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
-  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, steps, 0,
+  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps, 0,
                      changes, align256(abm_sir_changes_bytes(n)), stream);
   if (st) return st;
   return abm_sir_unpack(words, n, state, stream);

@@ -23,7 +23,7 @@ from . import _lib
 from . import random as jrandom
 from .sir import barabasi_albert, initial_states
 
-TILE = 256
+TILE = 1024  # agents per work item (abm_sir_tile_agents)
 
 # numpy view of abm_sir_instance (include/jaxabm_gb300.h), 112 bytes
 INSTANCE_DTYPE = np.dtype([
@@ -43,6 +43,9 @@ def check_layout():
     if size != INSTANCE_DTYPE.itemsize:
         raise RuntimeError(f"abm_sir_instance is {size} bytes, host layout expects "
                            f"{INSTANCE_DTYPE.itemsize}")
+    tile = _lib.load().abm_sir_tile_agents()
+    if tile != TILE:
+        raise RuntimeError(f"SIR kernels take {tile}-agent tiles, host layout expects {TILE}")
 
 
 def tiles_for(inst, n):
@@ -183,7 +186,7 @@ class SIRBatch:
     def launch(self, nsteps, stream=None):
         """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps``)."""
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
-                  self.work.shape[0], int(nsteps), int(self.grid), _dev.ptr(self.changes),
+                  self.work.shape[0], None, int(nsteps), int(self.grid), _dev.ptr(self.changes),
                   self.changes.numel(), _dev.stream_handle(stream))
 
     def capture(self, nsteps):

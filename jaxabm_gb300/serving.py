@@ -93,6 +93,9 @@ class SIRServer:
         self.work = torch.zeros((self.max_tiles, 4), dtype=torch.int32, device=dev)
         self.work.copy_(self.h_work)
         self.changes = changes_workspace(self.max_tiles * TILE)
+        # number of live work items, read by the kernels on every replay
+        self.live = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.h_live = torch.zeros(1, dtype=torch.int32).pin_memory()
         self.done = torch.zeros(self.max_slots, dtype=torch.int32).pin_memory()
         self.stream = torch.cuda.Stream()
         self.free_slots = list(range(self.max_slots - 1, -1, -1))
@@ -105,11 +108,15 @@ class SIRServer:
         self._work_dirty = False
         self._graph = None
         self._tiles_used = 0
+        self._work_event = None
+        self._in_flight = collections.deque()  # events of replayed ticks
+        self.max_ticks_in_flight = 2
 
     # -- graph ------------------------------------------------------------------------
     def _launch(self):
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.max_slots + 1, _dev.ptr(self.work),
-                  self.max_tiles, self.steps_per_tick, self.grid, _dev.ptr(self.changes),
+                  self.max_tiles, _dev.ptr(self.live), self.steps_per_tick, self.grid,
+                  _dev.ptr(self.changes),
                   self.changes.numel(), self.stream.cuda_stream)
 
     def _capture(self):
@@ -186,6 +193,9 @@ class SIRServer:
         return True
 
     def _rebuild_work(self):
+        # the pinned staging buffers may still feed the previous rebuild's copies
+        if self._work_event is not None:
+            self._work_event.synchronize()
         w = self.h_work
         w[:, 0] = self.dummy
         w[:, 1:] = 0
@@ -198,7 +208,11 @@ class SIRServer:
             w[k:k + m, 2] = torch.clamp(b + TILE, max=req.n)
             k += m
         with torch.cuda.stream(self.stream):
-            self.work.copy_(w, non_blocking=True)
+            self.work[:max(k, 1)].copy_(w[:max(k, 1)], non_blocking=True)
+            self.h_live[0] = k
+            self.live.copy_(self.h_live, non_blocking=True)
+            self._work_event = torch.cuda.Event()
+            self._work_event.record(self.stream)
         self._work_dirty = False
 
     def _harvest(self):
@@ -243,8 +257,13 @@ class SIRServer:
                 self._capture()
             with torch.cuda.stream(self.stream):
                 self._graph.replay()
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+            self._in_flight.append(ev)
+            while len(self._in_flight) > self.max_ticks_in_flight:
+                self._in_flight.popleft().synchronize()
             self.ticks += 1
-            self.launches += 2 * self.steps_per_tick
+            self.launches += 3 * self.steps_per_tick
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)

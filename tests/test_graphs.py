@@ -54,10 +54,12 @@ def test_instance_layout(lib):
     assert ensemble.INSTANCE_DTYPE.itemsize == lib.abm_sir_instance_size()
 
 
-def test_tiles_cover_instance():
-    t = ensemble.tiles_for(3, 1000)
-    assert t[0].tolist() == [3, 0, 256, 0] and t[-1].tolist() == [3, 768, 1000, 0]
-    assert (t[:, 2] - t[:, 1]).sum() == 1000
+def test_tiles_cover_instance(lib):
+    assert ensemble.TILE == lib.abm_sir_tile_agents()
+    t = ensemble.tiles_for(3, 2500)
+    assert t[0].tolist() == [3, 0, 1024, 0] and t[-1].tolist() == [3, 2048, 2500, 0]
+    assert (t[:, 2] - t[:, 1]).sum() == 2500
+    assert ensemble.tiles_for(0, 1000).tolist() == [[0, 0, 1000, 0]]
 
 
 def test_ensemble_spec():

@@ -134,6 +134,6 @@ def test_sir_batched_equals_alone(cuda, use_graph):
 def test_sir_bad_args(cuda):
     from jaxabm_gb300 import _lib
     L = _lib.load()
-    assert L.abm_sir_steps(None, 1, None, 0, 1, 0, None, 0, None) == _lib.ABM_ERR_BADARG
+    assert L.abm_sir_steps(None, 1, None, 0, None, 1, 0, None, 0, None) == _lib.ABM_ERR_BADARG
     assert L.abm_sir_run(None, None, 10, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
         _lib.ABM_ERR_BADARG
