@@ -91,21 +91,33 @@ __device__ __forceinline__ int decide_one(const abm_sir_instance* I, int inst, i
       const int32_t* __restrict__ col = I->col;
       const float beta = I->beta;
       const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-      int k = 0;
-      for (; k < deg; ++k) {
-        if ((word[col[row0 + k]] & 3) == kI) {
-          if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
-            ns = kI;
-            ++k;
-            break;
-          }
-          if (--cnt == 0) {
-            ++k;
-            break;
+      // eight slots per pass: the eight column loads, then the eight neighbour-word loads,
+      // are issued together before any is used
+      constexpr int kChunk = 8;
+      scanned = deg;
+      bool done = false;
+      for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
+        int nb[kChunk];
+        int32_t wn[kChunk];
+#pragma unroll
+        for (int q = 0; q < kChunk; ++q) nb[q] = k0 + q < deg ? col[row0 + k0 + q] : -1;
+#pragma unroll
+        for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? word[nb[q]] : 0;
+#pragma unroll
+        for (int q = 0; q < kChunk; ++q) {
+          if (!done && nb[q] >= 0 && (wn[q] & 3) == kI) {
+            const int k = k0 + q;
+            if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
+              ns = kI;
+              done = true;
+              scanned = k + 1;
+            } else if (--cnt == 0) {
+              done = true;
+              scanned = k + 1;
+            }
           }
         }
       }
-      scanned = k;
     }
   } else if (recover) {
     const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
