@@ -181,7 +181,9 @@ typedef struct abm_work_item {
 
 ABM_API size_t abm_sir_instance_size(void);
 
-/* Largest tile (agents per work item) of the SIR kernels: 1024. */
+/* Largest tile (agents per work item) of the SIR kernels: 4096.  Words are read with
+ * 128-bit loads when an instance's word array is 16-byte aligned and tiles start at
+ * multiples of 4 agents (scalar loads otherwise). */
 ABM_API int32_t abm_sir_tile_agents(void);
 
 /* Per-agent words of one instance from int8 compartments state[n] (n < 2^29): the number

@@ -33,8 +33,10 @@
 namespace {
 
 constexpr int kSirThreads = 256;
-constexpr int kPerThread = 4;
-constexpr int kTile = kSirThreads * kPerThread;  // agents per work item
+constexpr int kVec = 4;                            // words per 128-bit load
+constexpr int kVecsPerThread = 4;
+constexpr int kPerThread = kVec * kVecsPerThread;  // 16 agents per thread
+constexpr int kTile = kSirThreads * kPerThread;    // 4096 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kS = 0, kI = 1;
@@ -184,18 +186,30 @@ sir_decide_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__
     const int t = I->t;
     if (t >= I->steps) continue;  // uniform over the CTA
     const int32_t* __restrict__ word = I->state;
+    // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
+    // words are 16-byte aligned, scalar loads for a partial last vector
+    const bool vec_ok = ((reinterpret_cast<uintptr_t>(word) & 15) == 0) && ((item.y & 3) == 0);
     int32_t wv[kPerThread];
 #pragma unroll
-    for (int j = 0; j < kPerThread; ++j) {
-      const int i = item.y + threadIdx.x + j * kSirThreads;
-      wv[j] = i < item.z ? word[i] : 2;
+    for (int v = 0; v < kVecsPerThread; ++v) {
+      const int base = item.y + v * (kSirThreads * kVec) + kVec * threadIdx.x;
+      if (vec_ok && base + kVec <= item.z) {
+        const int4 q = *reinterpret_cast<const int4*>(word + base);
+        wv[kVec * v] = q.x;
+        wv[kVec * v + 1] = q.y;
+        wv[kVec * v + 2] = q.z;
+        wv[kVec * v + 3] = q.w;
+      } else {
+#pragma unroll
+        for (int c = 0; c < kVec; ++c) wv[kVec * v + c] = base + c < item.z ? word[base + c] : 2;
+      }
     }
     uint2 coll = make_uint2(0, 0);
     bool have_coll = false;
     int tile_scanned = 0;
 #pragma unroll 1
     for (int j = 0; j < kPerThread; ++j) {
-      const int i = item.y + threadIdx.x + j * kSirThreads;
+      const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
       tile_scanned += decide_one(I, item.x, t, word, i, i < item.z, wv[j], coll, have_coll, lane,
                                  hdr, changes, capacity);
     }
@@ -358,6 +372,17 @@ int default_grid(int nwork) {
   return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
 }
 
+// Persistent grid of the decide kernel: as many CTAs as can be resident at once.
+int decide_grid(int nwork) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sir_decide_kernel, kSirThreads, 0) !=
+          cudaSuccess ||
+      per_sm <= 0)
+    per_sm = 4;
+  const int cap = abm_host::sm_count() * per_sm;
+  return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
+}
+
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
 }  // namespace
@@ -424,7 +449,7 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   ChangeHeader* hdr = static_cast<ChangeHeader*>(changes);
   int2* list = reinterpret_cast<int2*>(hdr + 1);
   cudaStream_t s = abm_host::as_stream(stream);
-  const int g = grid > 0 ? grid : default_grid(nwork);
+  const int g = grid > 0 ? grid : decide_grid(nwork);
   const int push_grid = abm_host::sm_count() * 8;
   const int fin_blocks = (ninst + 255) / 256;
   for (int32_t k = 0; k < nsteps; ++k) {

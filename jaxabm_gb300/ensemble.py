@@ -23,7 +23,7 @@ from . import _lib
 from . import random as jrandom
 from .sir import barabasi_albert, initial_states
 
-TILE = 1024  # agents per work item (abm_sir_tile_agents)
+TILE = 4096  # agents per work item (abm_sir_tile_agents)
 
 # numpy view of abm_sir_instance (include/jaxabm_gb300.h), 112 bytes
 INSTANCE_DTYPE = np.dtype([
@@ -114,15 +114,16 @@ class SIRBatch:
         self.e = np.array([len(c) for _, c in graphs], dtype=np.int64)
         rp_off = np.concatenate([[0], np.cumsum(self.n + 1)])
         col_off = np.concatenate([[0], np.cumsum(self.e)])
-        w_off = np.concatenate([[0], np.cumsum(self.n)])
+        # word arrays start 16-byte aligned (128-bit loads): pad each to a multiple of 4
+        w_off = np.concatenate([[0], np.cumsum((self.n + 3) // 4 * 4)])
         cnt_off = np.arange(k + 1, dtype=np.int64) * self.steps * 3
         h_rp = np.empty(rp_off[-1], dtype=np.int32)
         h_col = np.empty(col_off[-1], dtype=np.int32)
-        h_st = np.empty(w_off[-1], dtype=np.int8)
+        h_st = np.zeros(w_off[-1], dtype=np.int8)
         for i, ((rp, col), st) in enumerate(zip(graphs, init_states)):
             h_rp[rp_off[i]:rp_off[i + 1]] = rp
             h_col[col_off[i]:col_off[i + 1]] = col
-            h_st[w_off[i]:w_off[i + 1]] = st
+            h_st[w_off[i]:w_off[i] + self.n[i]] = st
         self.h_state0 = h_st
         self.row_ptr = torch.from_numpy(h_rp).to(dev)
         self.col = torch.from_numpy(h_col).to(dev)
@@ -221,7 +222,7 @@ class SIRBatch:
 
     def final_state(self, i):
         w_off = self._offsets[2]
-        return unpack_words(self.words[w_off[i]:w_off[i + 1]])
+        return unpack_words(self.words[w_off[i]:w_off[i] + int(self.n[i])])
 
     def counts_of(self, i):
         c = self._offsets[3]
