@@ -203,9 +203,9 @@ ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_ite
 /* int8 compartments of n packed words. */
 ABM_API int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream);
 
-/* Bytes of the change-list workspace of abm_sir_steps for up to max_agents live agents
- * (16-byte header {count, overflow, 0, 0}, zeroed once by the caller, then 8 bytes per
- * agent). */
+/* Bytes of the list workspace of abm_sir_steps for up to max_agents live agents (16-byte
+ * header {changes, overflow, candidates, 0}, zeroed once by the caller, then 24 bytes per
+ * agent: a change list and a candidate list). */
 ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
 
 /* nsteps synchronous SIR steps of every instance with t < steps, over the tiles `work`
@@ -216,8 +216,8 @@ ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
  *   S -> I if some neighbour slot k with an I neighbour has uniform(k_inf,(deg,))[k] < beta;
  *   I -> R if uniform(k_rec) < gamma.
  * A susceptible agent whose word says it has no infected neighbour reads nothing else;
- * changes are pushed to the neighbours' words after all decisions (three launches per
- * step: decide, push, finalize).  `changes` must hold abm_sir_changes_bytes(total agents
+ * changes are pushed to the neighbours' words after all decisions (four launches per
+ * step: sweep, candidates, push, finalize).  `changes` must hold abm_sir_changes_bytes(total agents
  * of all live instances); its overflow flag is set (and changes dropped) if it is smaller.
  * Replaces Model.step's AgentCollection.update (jaxabm/model.py:163-171,
  * jaxabm/agent.py:132-179) for the SIR agent, batched over instances (the serial loops of

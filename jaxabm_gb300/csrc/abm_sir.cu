@@ -11,44 +11,57 @@
 //
 // Work-efficient ("frontier") formulation.  Each agent has one int32 word
 //     word = (number of infected neighbours << 2) | compartment
-// and a step is three launches:
-//   decide   over (instance, 1024-agent tile) work items, four agents per thread (their
-//            four words are loaded before any is used, so each thread keeps four loads in
-//            flight): only a susceptible agent with infected neighbours scans its CSR row
-//            (stopping at the first firing draw or once all its infected neighbours were
-//            seen); an infected agent draws its recovery.  Agents whose compartment
-//            changes are appended to a change list (warp-aggregated atomics).  Nothing is
-//            written to the words, so every decision sees the pre-step states.
-//   push     one warp per change: adds +-4 to the word of every neighbour (infected-
-//            neighbour count) and +1 to the agent's own compartment; counts the instance's
-//            S->I and I->R transitions.
-//   finalize one thread per instance: S/I/R counts of the step from the transitions,
-//            rng = split(rng)[0], t += 1, done flag after the last step; clears the list.
-// Rows longer than 32 slots are scanned by the whole warp, 32 slots per pass, with warp
-// votes.  Integer atomics commute, so every result is exact and independent of scheduling.
-// No kernel waits on anything.
+// and a step is four launches:
+//   sweep      over (instance, 4096-agent tile) work items, 16 agents per thread read with
+//              128-bit loads: the agents that need a decision -- susceptible with infected
+//              neighbours, and infected -- are appended to a candidate list (warp-aggregated
+//              atomics).  Everyone else (most agents) costs one 4-byte read.
+//   candidates one lane per candidate: a susceptible candidate scans its CSR row, eight
+//              column/neighbour loads in flight per pass, stopping at the first firing draw
+//              or once all its infected neighbours were seen (rows longer than 32 slots are
+//              scanned by the whole warp, 32 slots per pass, with warp votes); an infected
+//              candidate draws its recovery.  Changes go to a change list.  Nothing is
+//              written to the words, so every decision sees the pre-step states.
+//   push       one warp per change: adds +-4 to the word of every neighbour (infected-
+//              neighbour count) and +1 to the agent's own compartment; counts the
+//              instance's S->I and I->R transitions.
+//   finalize   one thread per instance: S/I/R counts of the step from the transitions,
+//              rng = split(rng)[0], t += 1, done flag after the last step; clears the lists.
+// Integer atomics commute, so every result is exact and independent of scheduling.  No
+// kernel waits on anything.
 
 #include "abm_common.cuh"
 
 namespace {
 
 constexpr int kSirThreads = 256;
+constexpr int kWarpsPerCta = kSirThreads / 32;
 constexpr int kVec = 4;                            // words per 128-bit load
 constexpr int kVecsPerThread = 4;
 constexpr int kPerThread = kVec * kVecsPerThread;  // 16 agents per thread
 constexpr int kTile = kSirThreads * kPerThread;    // 4096 agents per work item
 constexpr int kHeavyDeg = 32;
+constexpr int kChunk = 8;                          // row slots per scan pass
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kS = 0, kI = 1;
 
 static_assert(sizeof(abm_sir_instance) == 112, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
-// change-list workspace: header {count, overflow, pad, pad} then int2 entries
-struct ChangeHeader {
-  int32_t count;
+// Lists workspace: this header, then `capacity` change entries (int2 {inst, agent<<2 | new
+// compartment}), then `capacity` candidate entries (int4 {inst, agent, word, 0}).
+struct ListHeader {
+  int32_t changes;
   int32_t overflow;
-  int32_t pad[2];
+  int32_t candidates;
+  int32_t pad;
+};
+
+struct Lists {
+  ListHeader* hdr;
+  int2* changes;
+  int4* cands;
+  int capacity;
 };
 
 __device__ __forceinline__ uint2 coll_key_of(const abm_sir_instance* I, int t) {
@@ -63,89 +76,151 @@ __device__ __forceinline__ int live_count(const int32_t* live, int nwork) {
   return live != nullptr ? min(*live, nwork) : nwork;
 }
 
-// Decision for one agent slot of the warp; all 32 lanes call it together.  Returns the
-// CSR slots this lane's agent scanned.
-__device__ __forceinline__ int decide_one(const abm_sir_instance* I, int inst, int t,
-                                          const int32_t* __restrict__ word, int i, bool valid,
-                                          int32_t wi, uint2& coll, bool& have_coll, int lane,
-                                          ChangeHeader* __restrict__ hdr,
-                                          int2* __restrict__ changes, int capacity) {
-  const int s = wi & 3;
-  int cnt = wi >> 2;
-  int ns = s;
-  bool heavy = false;
-  int row0 = 0, deg = 0, scanned = 0;
-  const bool scan = valid && s == kS && cnt > 0;
-  const bool recover = valid && s == kI;
-  const bool any = __any_sync(kFull, scan || recover);
-  if (!any) return 0;  // warp-uniform: nothing to decide in this slot
-  if (!have_coll) {
-    coll = coll_key_of(I, t);
-    have_coll = true;
+// Warp-aggregated append: lanes with `want` get consecutive slots of *counter.
+__device__ __forceinline__ int warp_append(bool want, int32_t* counter, int lane) {
+  const unsigned m = __ballot_sync(kFull, want);
+  if (!m) return -1;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+__global__ void __launch_bounds__(kSirThreads)
+sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
+                 int nwork_max, const int32_t* __restrict__ live, Lists L) {
+  const int lane = threadIdx.x & 31;
+  const int nwork = live_count(live, nwork_max);
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int4 item = work[w];
+    const abm_sir_instance* I = insts + item.x;
+    if (I->t >= I->steps) continue;  // uniform over the CTA
+    const int32_t* __restrict__ word = I->state;
+    // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
+    // words are 16-byte aligned, scalar loads for a partial last vector
+    const bool vec_ok = ((reinterpret_cast<uintptr_t>(word) & 15) == 0) && ((item.y & 3) == 0);
+#pragma unroll
+    for (int v = 0; v < kVecsPerThread; ++v) {
+      const int base = item.y + v * (kSirThreads * kVec) + kVec * threadIdx.x;
+      int32_t wv[kVec];
+      if (vec_ok && base + kVec <= item.z) {
+        const int4 q = *reinterpret_cast<const int4*>(word + base);
+        wv[0] = q.x;
+        wv[1] = q.y;
+        wv[2] = q.z;
+        wv[3] = q.w;
+      } else {
+#pragma unroll
+        for (int c = 0; c < kVec; ++c) wv[c] = base + c < item.z ? word[base + c] : 2;
+      }
+#pragma unroll
+      for (int c = 0; c < kVec; ++c) {
+        const int s = wv[c] & 3;
+        const bool need = (s == kI) || (s == kS && (wv[c] >> 2) > 0);
+        const int pos = warp_append(need, &L.hdr->candidates, lane);
+        if (need) {
+          if (pos < L.capacity) L.cands[pos] = make_int4(item.x, base + c, wv[c], 0);
+          else L.hdr->overflow = 1;
+        }
+      }
+    }
   }
-  if (scan) {
-    const int32_t* __restrict__ rp = I->row_ptr;
-    row0 = rp[i];
-    deg = rp[i + 1] - row0;
-    if (deg > kHeavyDeg) {
-      heavy = true;
-    } else {
-      const int32_t* __restrict__ col = I->col;
-      const float beta = I->beta;
-      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-      // eight slots per pass: the eight column loads, then the eight neighbour-word loads,
-      // are issued together before any is used
-      constexpr int kChunk = 8;
-      scanned = deg;
-      bool done = false;
-      for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
-        int nb[kChunk];
-        int32_t wn[kChunk];
+}
+
+// Per-instance sum of `v` over the lanes of a warp (lanes grouped by instance), added to
+// *target of each group's instance by the group's lowest lane.
+__device__ __forceinline__ void add_by_instance(int inst, int v, abm_sir_instance* insts,
+                                                int lane) {
+  if (!__any_sync(kFull, v != 0)) return;
+  const unsigned group = __match_any_sync(kFull, inst);
+  const int sum = __reduce_add_sync(group, v);
+  if (lane == __ffs(group) - 1 && sum) atomicAdd(&insts[inst].edges_scanned, (unsigned long long)sum);
+}
+
+__global__ void __launch_bounds__(kSirThreads)
+sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
+  const int lane = threadIdx.x & 31;
+  const int ncand = min(L.hdr->candidates, L.capacity);
+  const int warps = gridDim.x * kWarpsPerCta;
+  for (int b = (blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5)) * 32; b < ncand; b += warps * 32) {
+    const int k = b + lane;
+    const bool valid = k < ncand;
+    const int4 e = valid ? L.cands[k] : make_int4(0, 0, 2, 0);
+    const int inst = e.x, i = e.y;
+    const abm_sir_instance* I = insts + inst;
+    const int s = e.z & 3;
+    int cnt = e.z >> 2;
+    int ns = s;
+    bool heavy = false;
+    int row0 = 0, deg = 0, scanned = 0;
+    uint2 coll = make_uint2(0, 0);
+    if (valid) coll = coll_key_of(I, I->t);
+    if (valid && s == kS) {
+      const int32_t* __restrict__ rp = I->row_ptr;
+      row0 = rp[i];
+      deg = rp[i + 1] - row0;
+      if (deg > kHeavyDeg) {
+        heavy = true;
+      } else {
+        const int32_t* __restrict__ col = I->col;
+        const int32_t* __restrict__ word = I->state;
+        const float beta = I->beta;
+        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
+        scanned = deg;
+        bool done = false;
+        for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
+          int nb[kChunk];
+          int32_t wn[kChunk];
 #pragma unroll
-        for (int q = 0; q < kChunk; ++q) nb[q] = k0 + q < deg ? col[row0 + k0 + q] : -1;
+          for (int q = 0; q < kChunk; ++q) nb[q] = k0 + q < deg ? col[row0 + k0 + q] : -1;
 #pragma unroll
-        for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? word[nb[q]] : 0;
+          for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? word[nb[q]] : 0;
 #pragma unroll
-        for (int q = 0; q < kChunk; ++q) {
-          if (!done && nb[q] >= 0 && (wn[q] & 3) == kI) {
-            const int k = k0 + q;
-            if (abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta) {
-              ns = kI;
-              done = true;
-              scanned = k + 1;
-            } else if (--cnt == 0) {
-              done = true;
-              scanned = k + 1;
+          for (int q = 0; q < kChunk; ++q) {
+            if (!done && nb[q] >= 0 && (wn[q] & 3) == kI) {
+              const int slot = k0 + q;
+              if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
+                ns = kI;
+                done = true;
+                scanned = slot + 1;
+              } else if (--cnt == 0) {
+                done = true;
+                scanned = slot + 1;
+              }
             }
           }
         }
       }
+    } else if (valid && s == kI) {
+      const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
+      if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
     }
-  } else if (recover) {
-    const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
-    if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
-  }
 
-  unsigned hmask = __ballot_sync(kFull, heavy);
-  if (hmask) {
-    const int32_t* __restrict__ col = I->col;
-    const float beta = I->beta;
+    // rows longer than kHeavyDeg: the whole warp scans them, one at a time
+    unsigned hmask = __ballot_sync(kFull, heavy);
     while (hmask) {
       const int src = __ffs(hmask) - 1;
       hmask &= hmask - 1;
+      const int hinst = __shfl_sync(kFull, inst, src);
       const int hi = __shfl_sync(kFull, i, src);
       const int hrow = __shfl_sync(kFull, row0, src);
       const int hdeg = __shfl_sync(kFull, deg, src);
       int remaining = __shfl_sync(kFull, cnt, src);
-      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
+      const uint2 hcoll = make_uint2(__shfl_sync(kFull, coll.x, src), __shfl_sync(kFull, coll.y, src));
+      const abm_sir_instance* H = insts + hinst;
+      const int32_t* __restrict__ col = H->col;
+      const int32_t* __restrict__ word = H->state;
+      const float beta = H->beta;
+      const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
       int c = 0;
       for (; c < hdeg && !fired && remaining > 0; c += 32) {
-        const int k = c + lane;
+        const int slot = c + lane;
         bool isI = false, f = false;
-        if (k < hdeg) {
-          isI = (word[col[hrow + k]] & 3) == kI;
-          if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)k)) < beta;
+        if (slot < hdeg) {
+          isI = (word[col[hrow + slot]] & 3) == kI;
+          if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
         }
         fired = __any_sync(kFull, f);
         remaining -= __popc(__ballot_sync(kFull, isI));
@@ -155,80 +230,25 @@ __device__ __forceinline__ int decide_one(const abm_sir_instance* I, int inst, i
         scanned = min(c, hdeg);
       }
     }
-  }
 
-  // warp-aggregated append of the agents whose compartment changes
-  const bool changed = valid && ns != s;
-  const unsigned cmask = __ballot_sync(kFull, changed);
-  if (cmask) {
-    const int leader = __ffs(cmask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&hdr->count, __popc(cmask));
-    base = __shfl_sync(kFull, base, leader);
+    const bool changed = valid && ns != s;
+    const int pos = warp_append(changed, &L.hdr->changes, lane);
     if (changed) {
-      const int pos = base + __popc(cmask & ((1u << lane) - 1u));
-      if (pos < capacity) changes[pos] = make_int2(inst, (i << 2) | ns);
-      else hdr->overflow = 1;
+      if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
+      else L.hdr->overflow = 1;
     }
-  }
-  return scanned;
-}
-
-__global__ void __launch_bounds__(kSirThreads)
-sir_decide_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
-                  int nwork_max, const int32_t* __restrict__ live, ChangeHeader* __restrict__ hdr,
-                  int2* __restrict__ changes, int capacity) {
-  const int lane = threadIdx.x & 31;
-  const int nwork = live_count(live, nwork_max);
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const int4 item = work[w];
-    abm_sir_instance* I = insts + item.x;
-    const int t = I->t;
-    if (t >= I->steps) continue;  // uniform over the CTA
-    const int32_t* __restrict__ word = I->state;
-    // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
-    // words are 16-byte aligned, scalar loads for a partial last vector
-    const bool vec_ok = ((reinterpret_cast<uintptr_t>(word) & 15) == 0) && ((item.y & 3) == 0);
-    int32_t wv[kPerThread];
-#pragma unroll
-    for (int v = 0; v < kVecsPerThread; ++v) {
-      const int base = item.y + v * (kSirThreads * kVec) + kVec * threadIdx.x;
-      if (vec_ok && base + kVec <= item.z) {
-        const int4 q = *reinterpret_cast<const int4*>(word + base);
-        wv[kVec * v] = q.x;
-        wv[kVec * v + 1] = q.y;
-        wv[kVec * v + 2] = q.z;
-        wv[kVec * v + 3] = q.w;
-      } else {
-#pragma unroll
-        for (int c = 0; c < kVec; ++c) wv[kVec * v + c] = base + c < item.z ? word[base + c] : 2;
-      }
-    }
-    uint2 coll = make_uint2(0, 0);
-    bool have_coll = false;
-    int tile_scanned = 0;
-#pragma unroll 1
-    for (int j = 0; j < kPerThread; ++j) {
-      const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
-      tile_scanned += decide_one(I, item.x, t, word, i, i < item.z, wv[j], coll, have_coll, lane,
-                                 hdr, changes, capacity);
-    }
-    if (__any_sync(kFull, tile_scanned != 0)) {
-      const int ws = abm::warp_sum(tile_scanned);
-      if (lane == 0) atomicAdd(&I->edges_scanned, (unsigned long long)ws);
-    }
+    add_by_instance(inst, scanned, insts, lane);
   }
 }
 
 // One warp per change: neighbours' infected counts +-1, own compartment +1.
 __global__ void __launch_bounds__(kSirThreads)
-sir_push_kernel(abm_sir_instance* __restrict__ insts, const ChangeHeader* __restrict__ hdr,
-                const int2* __restrict__ changes, int capacity) {
+sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   const int lane = threadIdx.x & 31;
-  const int warps = gridDim.x * (kSirThreads / 32);
-  const int count = min(hdr->count, capacity);
-  for (int e = blockIdx.x * (kSirThreads / 32) + (threadIdx.x >> 5); e < count; e += warps) {
-    const int2 ent = changes[e];
+  const int warps = gridDim.x * kWarpsPerCta;
+  const int count = min(L.hdr->changes, L.capacity);
+  for (int e = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); e < count; e += warps) {
+    const int2 ent = L.changes[e];
     abm_sir_instance* I = insts + ent.x;
     const int agent = ent.y >> 2;
     const int ns = ent.y & 3;
@@ -245,11 +265,14 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, const ChangeHeader* __rest
   }
 }
 
-// Counts after the step, key chain, step counter, done flag; clears the change list.
+// Counts after the step, key chain, step counter, done flag; clears the lists.
 __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
-                                    ChangeHeader* __restrict__ hdr) {
+                                    ListHeader* __restrict__ hdr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k == 0) hdr->count = 0;
+  if (k == 0) {
+    hdr->changes = 0;
+    hdr->candidates = 0;
+  }
   if (k >= ninst) return;
   abm_sir_instance* I = insts + k;
   const int t = I->t;
@@ -372,18 +395,29 @@ int default_grid(int nwork) {
   return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
 }
 
-// Persistent grid of the decide kernel: as many CTAs as can be resident at once.
-int decide_grid(int nwork) {
+// Persistent grid of a kernel: as many CTAs as can be resident at once.
+template <typename Kernel>
+int resident_grid(Kernel k, int fallback_per_sm) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sir_decide_kernel, kSirThreads, 0) !=
-          cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSirThreads, 0) != cudaSuccess ||
       per_sm <= 0)
-    per_sm = 4;
-  const int cap = abm_host::sm_count() * per_sm;
-  return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
+    per_sm = fallback_per_sm;
+  return abm_host::sm_count() * per_sm;
 }
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+Lists carve_lists(void* ws, size_t bytes) {
+  Lists L;
+  L.hdr = static_cast<ListHeader*>(ws);
+  size_t cap = (bytes - sizeof(ListHeader)) / (sizeof(int2) + sizeof(int4));
+  if (cap > 0x7FFFFFFE) cap = 0x7FFFFFFE;
+  cap &= ~(size_t)1;  // even: keeps the int4 candidate entries 16-byte aligned
+  L.capacity = (int)cap;
+  L.changes = reinterpret_cast<int2*>(L.hdr + 1);
+  L.cands = reinterpret_cast<int4*>(L.changes + L.capacity);
+  return L;
+}
 
 }  // namespace
 
@@ -395,7 +429,8 @@ int32_t abm_sir_tile_agents(void) { return kTile; }
 
 size_t abm_sir_changes_bytes(int64_t max_agents) {
   if (max_agents <= 0) return 0;
-  return sizeof(ChangeHeader) + (size_t)max_agents * sizeof(int2);
+  const size_t cap = ((size_t)max_agents + 1) & ~(size_t)1;
+  return sizeof(ListHeader) + cap * (sizeof(int2) + sizeof(int4));
 }
 
 int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
@@ -443,26 +478,28 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)) ||
       !abm_host::aligned(changes, 16) || (live_work && !abm_host::aligned(live_work, 4)))
     return ABM_ERR_BADARG;
-  if (changes_bytes < sizeof(ChangeHeader) + sizeof(int2)) return ABM_ERR_WORKSPACE;
-  const size_t cap_sz = (changes_bytes - sizeof(ChangeHeader)) / sizeof(int2);
-  const int capacity = cap_sz > 0x7FFFFFFF ? 0x7FFFFFFF : (int)cap_sz;
-  ChangeHeader* hdr = static_cast<ChangeHeader*>(changes);
-  int2* list = reinterpret_cast<int2*>(hdr + 1);
+  if (changes_bytes < abm_sir_changes_bytes(1)) return ABM_ERR_WORKSPACE;
+  const Lists L = carve_lists(changes, changes_bytes);
   cudaStream_t s = abm_host::as_stream(stream);
-  const int g = grid > 0 ? grid : decide_grid(nwork);
+  int g = grid > 0 ? grid : resident_grid(sir_sweep_kernel, 4);
+  if (nwork > 0 && g > nwork) g = nwork;
+  const int cand_grid = resident_grid(sir_candidates_kernel, 4);
   const int push_grid = abm_host::sm_count() * 8;
   const int fin_blocks = (ninst + 255) / 256;
   for (int32_t k = 0; k < nsteps; ++k) {
     if (nwork > 0) {
-      sir_decide_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work),
-                                                  nwork, live_work, hdr, list, capacity);
-      int st = abm_host::check_launch("abm_sir_steps/decide");
+      sir_sweep_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work), nwork,
+                                                 live_work, L);
+      int st = abm_host::check_launch("abm_sir_steps/sweep");
       if (st) return st;
-      sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, hdr, list, capacity);
+      sir_candidates_kernel<<<cand_grid, kSirThreads, 0, s>>>(insts, L);
+      st = abm_host::check_launch("abm_sir_steps/candidates");
+      if (st) return st;
+      sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, L);
       st = abm_host::check_launch("abm_sir_steps/push");
       if (st) return st;
     }
-    sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, hdr);
+    sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, L.hdr);
     int st = abm_host::check_launch("abm_sir_steps/finalize");
     if (st) return st;
   }
@@ -498,11 +535,11 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
   p += align256((size_t)n * sizeof(int32_t));
   int32_t* misc = reinterpret_cast<int32_t*>(p);  // sizes[3], status
   p += 256;
-  void* changes = p;
+  void* lists = p;
   int st = abm_sir_pack(state, row_ptr, col, n, words, misc, misc + 3, stream);
   if (st) return st;
-  st = abm_host::record_cuda_error(cudaMemsetAsync(changes, 0, sizeof(ChangeHeader), s),
-                                   "abm_sir_run/changes");
+  st = abm_host::record_cuda_error(cudaMemsetAsync(lists, 0, sizeof(ListHeader), s),
+                                   "abm_sir_run/lists");
   if (st) return st;
   sir_setup_single_kernel<<<(ntiles + 255) / 256, 256, 0, s>>>(
       d, work, ntiles, row_ptr, col, words, counts, coll_keys, (int32_t)n, steps, beta, gamma,
@@ -510,7 +547,7 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
   st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps, 0,
-                     changes, align256(abm_sir_changes_bytes(n)), stream);
+                     lists, align256(abm_sir_changes_bytes(n)), stream);
   if (st) return st;
   return abm_sir_unpack(words, n, state, stream);
 }

@@ -229,7 +229,7 @@ class SIRBatch:
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
     def launches_per_run(self):
-        return 3 * self.steps
+        return 4 * self.steps
 
     def edge_stats(self):
         """(CSR slots read by decide, CSR slots read by push, compartment changes) since
