@@ -90,7 +90,9 @@ __device__ __forceinline__ int warp_append(bool want, int32_t* counter, int lane
 __global__ void __launch_bounds__(kSirThreads)
 sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
                  int nwork_max, const int32_t* __restrict__ live, Lists L) {
-  const int lane = threadIdx.x & 31;
+  __shared__ int swarp[kWarpsPerCta];
+  __shared__ int sbase;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
@@ -100,28 +102,55 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
     // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
     // words are 16-byte aligned, scalar loads for a partial last vector
     const bool vec_ok = ((reinterpret_cast<uintptr_t>(word) & 15) == 0) && ((item.y & 3) == 0);
+    int32_t wv[kPerThread];
 #pragma unroll
     for (int v = 0; v < kVecsPerThread; ++v) {
       const int base = item.y + v * (kSirThreads * kVec) + kVec * threadIdx.x;
-      int32_t wv[kVec];
       if (vec_ok && base + kVec <= item.z) {
         const int4 q = *reinterpret_cast<const int4*>(word + base);
-        wv[0] = q.x;
-        wv[1] = q.y;
-        wv[2] = q.z;
-        wv[3] = q.w;
+        wv[kVec * v] = q.x;
+        wv[kVec * v + 1] = q.y;
+        wv[kVec * v + 2] = q.z;
+        wv[kVec * v + 3] = q.w;
       } else {
 #pragma unroll
-        for (int c = 0; c < kVec; ++c) wv[c] = base + c < item.z ? word[base + c] : 2;
+        for (int c = 0; c < kVec; ++c) wv[kVec * v + c] = base + c < item.z ? word[base + c] : 2;
       }
+    }
+    // agents needing a decision: susceptible with infected neighbours, or infected
+    unsigned need = 0;
 #pragma unroll
-      for (int c = 0; c < kVec; ++c) {
-        const int s = wv[c] & 3;
-        const bool need = (s == kI) || (s == kS && (wv[c] >> 2) > 0);
-        const int pos = warp_append(need, &L.hdr->candidates, lane);
-        if (need) {
-          if (pos < L.capacity) L.cands[pos] = make_int4(item.x, base + c, wv[c], 0);
+    for (int j = 0; j < kPerThread; ++j) {
+      const int s = wv[j] & 3;
+      if (s == kI || (s == kS && (wv[j] >> 2) > 0)) need |= 1u << j;
+    }
+    // one counter atomic per CTA and tile: thread offsets from a block-level scan
+    const int mine = __popc(need);
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) swarp[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int total = 0;
+      for (int q = 0; q < kWarpsPerCta; ++q) total += swarp[q];
+      sbase = total ? atomicAdd(&L.hdr->candidates, total) : 0;
+    }
+    __syncthreads();
+    int pos = sbase + incl - mine;
+    for (int q = 0; q < warp; ++q) pos += swarp[q];
+    __syncthreads();  // swarp/sbase are rewritten by the next tile
+    if (need) {
+#pragma unroll
+      for (int j = 0; j < kPerThread; ++j) {
+        if ((need >> j) & 1u) {
+          const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
+          if (pos < L.capacity) L.cands[pos] = make_int4(item.x, i, wv[j], 0);
           else L.hdr->overflow = 1;
+          ++pos;
         }
       }
     }
