@@ -138,7 +138,7 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
                                      int32_t* col, int64_t col_capacity);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (112 bytes, 8-byte aligned).
+/* Device-side descriptor of one SIR model instance (120 bytes, 8-byte aligned).
  * state holds one int32 word per agent, (infected neighbours << 2) | compartment
  * (0 S, 1 I, 2 R), built by abm_sir_pack and read back by abm_sir_unpack.
  * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
@@ -169,6 +169,7 @@ typedef struct abm_sir_instance {
   int32_t step_ir;
   unsigned long long edges_scanned;
   unsigned long long edges_pushed;
+  uint32_t coll[2]; /* collection key of the current step (written by abm_sir_steps) */
 } abm_sir_instance;
 
 /* A tile of agents [begin, end) of instance `inst` (end - begin <= abm_sir_tile_agents()). */

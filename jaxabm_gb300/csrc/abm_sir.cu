@@ -13,20 +13,22 @@
 //     word = (number of infected neighbours << 2) | compartment
 // and a step is four launches:
 //   sweep      over (instance, 4096-agent tile) work items, 16 agents per thread read with
-//              128-bit loads: the agents that need a decision -- susceptible with infected
-//              neighbours, and infected -- are appended to a candidate list (warp-aggregated
-//              atomics).  Everyone else (most agents) costs one 4-byte read.
+//              128-bit loads: agents that need a decision are appended to a candidate list
+//              -- susceptible ones with infected neighbours from its front, infected ones
+//              from its back -- with one counter atomic per CTA and tile (block scan for
+//              the offsets).  Everyone else (most agents) costs one 4-byte read.
 //   candidates one lane per candidate: a susceptible candidate scans its CSR row, eight
 //              column/neighbour loads in flight per pass, stopping at the first firing draw
 //              or once all its infected neighbours were seen (rows longer than 32 slots are
 //              scanned by the whole warp, 32 slots per pass, with warp votes); an infected
 //              candidate draws its recovery.  Changes go to a change list.  Nothing is
 //              written to the words, so every decision sees the pre-step states.
-//   push       one warp per change: adds +-4 to the word of every neighbour (infected-
-//              neighbour count) and +1 to the agent's own compartment; counts the
-//              instance's S->I and I->R transitions.
+//   push       one thread per change (one warp for rows longer than 32 slots): adds +-4 to
+//              the word of every neighbour (infected-neighbour count) and +1 to the agent's
+//              own compartment; counts the instance's S->I and I->R transitions.
 //   finalize   one thread per instance: S/I/R counts of the step from the transitions,
-//              rng = split(rng)[0], t += 1, done flag after the last step; clears the lists.
+//              rng = split(rng)[0], t += 1, the next step's collection key, done flag after
+//              the last step; clears the lists.
 // Integer atomics commute, so every result is exact and independent of scheduling.  No
 // kernel waits on anything.
 
@@ -45,16 +47,18 @@ constexpr int kChunk = 8;                          // row slots per scan pass
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kS = 0, kI = 1;
 
-static_assert(sizeof(abm_sir_instance) == 112, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 120, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
-// Lists workspace: this header, then `capacity` change entries (int2 {inst, agent<<2 | new
-// compartment}), then `capacity` candidate entries (int4 {inst, agent, word, 0}).
+// Lists workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
+// new compartment}), then `capacity` candidate entries (int4 {inst, agent, word, 0});
+// susceptible candidates fill the candidate array from the front, infected ones from the
+// back (an agent is at most one candidate, so the two never meet).
 struct ListHeader {
   int32_t changes;
   int32_t overflow;
-  int32_t candidates;
-  int32_t pad;
+  int32_t cand_s;
+  int32_t cand_i;
 };
 
 struct Lists {
@@ -64,12 +68,11 @@ struct Lists {
   int capacity;
 };
 
-__device__ __forceinline__ uint2 coll_key_of(const abm_sir_instance* I, int t) {
-  // coll_key of step t: given per step, or from the instance's own key chain
+__device__ __forceinline__ uint2 step_key_of(const abm_sir_instance* I, int t, uint2 rng) {
+  // collection key of step t: given per step, or from the instance's key chain
   // (step_key = split(rng)[1]; coll_key = split(step_key)[1], jaxabm/model.py:156,164)
-  return I->coll_keys != nullptr
-             ? abm::load_key(I->coll_keys + 2 * (size_t)t)
-             : abm::split_at(abm::split_at(make_uint2(I->rng[0], I->rng[1]), 1), 1);
+  return I->coll_keys != nullptr ? abm::load_key(I->coll_keys + 2 * (size_t)t)
+                                 : abm::split_at(abm::split_at(rng, 1), 1);
 }
 
 __device__ __forceinline__ int live_count(const int32_t* live, int nwork) {
@@ -87,11 +90,22 @@ __device__ __forceinline__ int warp_append(bool want, int32_t* counter, int lane
   return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
+// Collection key of each live instance's current step.
+__global__ void sir_prepare_kernel(abm_sir_instance* __restrict__ insts, int ninst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ninst) return;
+  abm_sir_instance* I = insts + k;
+  if (I->t >= I->steps) return;
+  const uint2 c = step_key_of(I, I->t, make_uint2(I->rng[0], I->rng[1]));
+  I->coll[0] = c.x;
+  I->coll[1] = c.y;
+}
+
 __global__ void __launch_bounds__(kSirThreads)
 sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
                  int nwork_max, const int32_t* __restrict__ live, Lists L) {
   __shared__ int swarp[kWarpsPerCta];
-  __shared__ int sbase;
+  __shared__ int sbase_s, sbase_i;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -117,15 +131,15 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
         for (int c = 0; c < kVec; ++c) wv[kVec * v + c] = base + c < item.z ? word[base + c] : 2;
       }
     }
-    // agents needing a decision: susceptible with infected neighbours, or infected
-    unsigned need = 0;
+    unsigned need_s = 0, need_i = 0;
 #pragma unroll
     for (int j = 0; j < kPerThread; ++j) {
       const int s = wv[j] & 3;
-      if (s == kI || (s == kS && (wv[j] >> 2) > 0)) need |= 1u << j;
+      if (s == kS && (wv[j] >> 2) > 0) need_s |= 1u << j;
+      if (s == kI) need_i |= 1u << j;
     }
-    // one counter atomic per CTA and tile: thread offsets from a block-level scan
-    const int mine = __popc(need);
+    // one counter atomic per list, CTA and tile: both counts scanned at once (16 bits each)
+    const int mine = __popc(need_s) | (__popc(need_i) << 16);
     int incl = mine;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -137,20 +151,28 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
     if (threadIdx.x == 0) {
       int total = 0;
       for (int q = 0; q < kWarpsPerCta; ++q) total += swarp[q];
-      sbase = total ? atomicAdd(&L.hdr->candidates, total) : 0;
+      const int ts = total & 0xFFFF, ti = total >> 16;
+      sbase_s = ts ? atomicAdd(&L.hdr->cand_s, ts) : 0;
+      sbase_i = ti ? atomicAdd(&L.hdr->cand_i, ti) : 0;
     }
     __syncthreads();
-    int pos = sbase + incl - mine;
-    for (int q = 0; q < warp; ++q) pos += swarp[q];
-    __syncthreads();  // swarp/sbase are rewritten by the next tile
-    if (need) {
+    int before = incl - mine;
+    for (int q = 0; q < warp; ++q) before += swarp[q];
+    int pos_s = sbase_s + (before & 0xFFFF);
+    int pos_i = sbase_i + (before >> 16);
+    __syncthreads();  // swarp/sbase_* are rewritten by the next tile
+    if (need_s | need_i) {
 #pragma unroll
       for (int j = 0; j < kPerThread; ++j) {
-        if ((need >> j) & 1u) {
-          const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
-          if (pos < L.capacity) L.cands[pos] = make_int4(item.x, i, wv[j], 0);
+        const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
+        if ((need_s >> j) & 1u) {
+          if (pos_s < L.capacity) L.cands[pos_s] = make_int4(item.x, i, wv[j], 0);
           else L.hdr->overflow = 1;
-          ++pos;
+          ++pos_s;
+        } else if ((need_i >> j) & 1u) {
+          if (pos_i < L.capacity) L.cands[L.capacity - 1 - pos_i] = make_int4(item.x, i, wv[j], 0);
+          else L.hdr->overflow = 1;
+          ++pos_i;
         }
       }
     }
@@ -158,34 +180,59 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
 }
 
 // Per-instance sum of `v` over the lanes of a warp (lanes grouped by instance), added to
-// *target of each group's instance by the group's lowest lane.
-__device__ __forceinline__ void add_by_instance(int inst, int v, abm_sir_instance* insts,
-                                                int lane) {
+// the group's instance by the group's lowest lane.
+__device__ __forceinline__ void add_scanned(int inst, int v, abm_sir_instance* insts, int lane) {
   if (!__any_sync(kFull, v != 0)) return;
   const unsigned group = __match_any_sync(kFull, inst);
   const int sum = __reduce_add_sync(group, v);
   if (lane == __ffs(group) - 1 && sum) atomicAdd(&insts[inst].edges_scanned, (unsigned long long)sum);
 }
 
+__device__ __forceinline__ void record_change(bool changed, int inst, int i, int ns, Lists& L,
+                                              int lane) {
+  const int pos = warp_append(changed, &L.hdr->changes, lane);
+  if (changed) {
+    if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
+    else L.hdr->overflow = 1;
+  }
+}
+
 __global__ void __launch_bounds__(kSirThreads)
 sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   const int lane = threadIdx.x & 31;
-  const int ncand = min(L.hdr->candidates, L.capacity);
   const int warps = gridDim.x * kWarpsPerCta;
-  for (int b = (blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5)) * 32; b < ncand; b += warps * 32) {
+  const int wid = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+
+  // infected candidates: recovery draws
+  const int ni = min(L.hdr->cand_i, L.capacity);
+  for (int b = wid * 32; b < ni; b += warps * 32) {
     const int k = b + lane;
-    const bool valid = k < ncand;
+    const bool valid = k < ni;
+    const int4 e = valid ? L.cands[L.capacity - 1 - k] : make_int4(0, 0, 2, 0);
+    bool changed = false;
+    if (valid) {
+      const abm_sir_instance* I = insts + e.x;
+      const uint2 coll = make_uint2(I->coll[0], I->coll[1]);
+      const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)e.y), 1);
+      changed = abm::unit_float(abm::bits_at(krec, 0)) < I->gamma;
+    }
+    record_change(changed, e.x, e.y, 2, L, lane);
+  }
+
+  // susceptible candidates with infected neighbours: row scans
+  const int ns_count = min(L.hdr->cand_s, L.capacity);
+  for (int b = wid * 32; b < ns_count; b += warps * 32) {
+    const int k = b + lane;
+    const bool valid = k < ns_count;
     const int4 e = valid ? L.cands[k] : make_int4(0, 0, 2, 0);
     const int inst = e.x, i = e.y;
     const abm_sir_instance* I = insts + inst;
-    const int s = e.z & 3;
     int cnt = e.z >> 2;
-    int ns = s;
-    bool heavy = false;
+    bool infected = false, heavy = false;
     int row0 = 0, deg = 0, scanned = 0;
     uint2 coll = make_uint2(0, 0);
-    if (valid) coll = coll_key_of(I, I->t);
-    if (valid && s == kS) {
+    if (valid) {
+      coll = make_uint2(I->coll[0], I->coll[1]);
       const int32_t* __restrict__ rp = I->row_ptr;
       row0 = rp[i];
       deg = rp[i + 1] - row0;
@@ -196,6 +243,8 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
         const int32_t* __restrict__ word = I->state;
         const float beta = I->beta;
         const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
+        // eight slots per pass: the eight column loads, then the eight neighbour-word
+        // loads, are issued together before any is used
         scanned = deg;
         bool done = false;
         for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
@@ -210,7 +259,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
             if (!done && nb[q] >= 0 && (wn[q] & 3) == kI) {
               const int slot = k0 + q;
               if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
-                ns = kI;
+                infected = true;
                 done = true;
                 scanned = slot + 1;
               } else if (--cnt == 0) {
@@ -221,9 +270,6 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           }
         }
       }
-    } else if (valid && s == kI) {
-      const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
-      if (abm::unit_float(abm::bits_at(krec, 0)) < I->gamma) ns = 2;
     }
 
     // rows longer than kHeavyDeg: the whole warp scans them, one at a time
@@ -236,8 +282,8 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const int hrow = __shfl_sync(kFull, row0, src);
       const int hdeg = __shfl_sync(kFull, deg, src);
       int remaining = __shfl_sync(kFull, cnt, src);
-      const uint2 hcoll = make_uint2(__shfl_sync(kFull, coll.x, src), __shfl_sync(kFull, coll.y, src));
       const abm_sir_instance* H = insts + hinst;
+      const uint2 hcoll = make_uint2(H->coll[0], H->coll[1]);
       const int32_t* __restrict__ col = H->col;
       const int32_t* __restrict__ word = H->state;
       const float beta = H->beta;
@@ -255,52 +301,78 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
         remaining -= __popc(__ballot_sync(kFull, isI));
       }
       if (lane == src) {
-        if (fired) ns = kI;
+        infected = fired;
         scanned = min(c, hdeg);
       }
     }
 
-    const bool changed = valid && ns != s;
-    const int pos = warp_append(changed, &L.hdr->changes, lane);
-    if (changed) {
-      if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
-      else L.hdr->overflow = 1;
-    }
-    add_by_instance(inst, scanned, insts, lane);
+    record_change(infected, inst, i, kI, L, lane);
+    add_scanned(inst, scanned, insts, lane);
   }
 }
 
-// One warp per change: neighbours' infected counts +-1, own compartment +1.
+// Neighbours' infected counts +-1 and own compartment +1 for every change: one thread per
+// change for rows up to kHeavyDeg slots (atomics issued without waiting for results), one
+// warp for longer rows.
 __global__ void __launch_bounds__(kSirThreads)
 sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   const int lane = threadIdx.x & 31;
-  const int warps = gridDim.x * kWarpsPerCta;
   const int count = min(L.hdr->changes, L.capacity);
-  for (int e = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); e < count; e += warps) {
-    const int2 ent = L.changes[e];
-    abm_sir_instance* I = insts + ent.x;
-    const int agent = ent.y >> 2;
-    const int ns = ent.y & 3;
-    int32_t* __restrict__ word = I->state;
-    const int32_t* __restrict__ col = I->col;
-    const int r0 = I->row_ptr[agent], r1 = I->row_ptr[agent + 1];
-    const int delta = ns == kI ? 4 : -4;
-    for (int k = r0 + lane; k < r1; k += 32) atomicAdd(&word[col[k]], delta);
-    if (lane == 0) {
-      atomicAdd(&word[agent], 1);  // S(0) -> I(1) and I(1) -> R(2) both add one
-      atomicAdd(ns == kI ? &I->step_si : &I->step_ir, 1);
+  const int threads = gridDim.x * kSirThreads;
+  for (int b = (blockIdx.x * kSirThreads + threadIdx.x) & ~31; b < count; b += threads) {
+    const int k = b + lane;
+    const bool valid = k < count;
+    int inst = 0, agent = 0, r0 = 0, r1 = 0, delta = 0;
+    abm_sir_instance* I = insts;
+    if (valid) {
+      const int2 ent = L.changes[k];
+      inst = ent.x;
+      agent = ent.y >> 2;
+      I = insts + inst;
+      delta = (ent.y & 3) == kI ? 4 : -4;
+      r0 = I->row_ptr[agent];
+      r1 = I->row_ptr[agent + 1];
+      atomicAdd(&I->state[agent], 1);  // S(0) -> I(1) and I(1) -> R(2) both add one
+      atomicAdd(delta > 0 ? &I->step_si : &I->step_ir, 1);
       atomicAdd(&I->edges_pushed, (unsigned long long)(r1 - r0));
+    }
+    const bool heavy = valid && r1 - r0 > kHeavyDeg;
+    if (valid && !heavy) {
+      int32_t* __restrict__ word = I->state;
+      const int32_t* __restrict__ col = I->col;
+      for (int e0 = r0; e0 < r1; e0 += kChunk) {
+        int nb[kChunk];
+#pragma unroll
+        for (int q = 0; q < kChunk; ++q) nb[q] = e0 + q < r1 ? col[e0 + q] : -1;
+#pragma unroll
+        for (int q = 0; q < kChunk; ++q)
+          if (nb[q] >= 0) atomicAdd(&word[nb[q]], delta);
+      }
+    }
+    unsigned hmask = __ballot_sync(kFull, heavy);
+    while (hmask) {
+      const int src = __ffs(hmask) - 1;
+      hmask &= hmask - 1;
+      const int hinst = __shfl_sync(kFull, inst, src);
+      const int hr0 = __shfl_sync(kFull, r0, src);
+      const int hr1 = __shfl_sync(kFull, r1, src);
+      const int hdelta = __shfl_sync(kFull, delta, src);
+      int32_t* __restrict__ word = insts[hinst].state;
+      const int32_t* __restrict__ col = insts[hinst].col;
+      for (int e = hr0 + lane; e < hr1; e += 32) atomicAdd(&word[col[e]], hdelta);
     }
   }
 }
 
-// Counts after the step, key chain, step counter, done flag; clears the lists.
+// Counts after the step, key chain, step counter, next step's key, done flag; clears the
+// lists.
 __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
                                     ListHeader* __restrict__ hdr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k == 0) {
     hdr->changes = 0;
-    hdr->candidates = 0;
+    hdr->cand_s = 0;
+    hdr->cand_i = 0;
   }
   if (k >= ninst) return;
   abm_sir_instance* I = insts + k;
@@ -319,6 +391,11 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   I->rng[0] = r.x;
   I->rng[1] = r.y;
   I->t = t + 1;
+  if (t + 1 < I->steps) {
+    const uint2 c = step_key_of(I, t + 1, r);
+    I->coll[0] = c.x;
+    I->coll[1] = c.y;
+  }
   if (t + 1 == I->steps && I->done_flag) {
     __threadfence_system();
     *reinterpret_cast<volatile int32_t*>(I->done_flag) = 1;
@@ -411,6 +488,8 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->step_ir = 0;
     d->edges_scanned = 0;
     d->edges_pushed = 0;
+    d->coll[0] = 0;
+    d->coll[1] = 0;
   }
   for (int b = g; b < ntiles; b += gridDim.x * blockDim.x) {
     const int begin = b * kTile;
@@ -508,29 +587,29 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
       !abm_host::aligned(changes, 16) || (live_work && !abm_host::aligned(live_work, 4)))
     return ABM_ERR_BADARG;
   if (changes_bytes < abm_sir_changes_bytes(1)) return ABM_ERR_WORKSPACE;
+  if (nsteps == 0) return ABM_OK;
   const Lists L = carve_lists(changes, changes_bytes);
   cudaStream_t s = abm_host::as_stream(stream);
   int g = grid > 0 ? grid : resident_grid(sir_sweep_kernel, 4);
   if (nwork > 0 && g > nwork) g = nwork;
   const int cand_grid = resident_grid(sir_candidates_kernel, 4);
-  const int push_grid = abm_host::sm_count() * 8;
+  const int push_grid = resident_grid(sir_push_kernel, 4);
   const int fin_blocks = (ninst + 255) / 256;
+  sir_prepare_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst);
+  int st = abm_host::check_launch("abm_sir_steps/prepare");
+  if (st) return st;
   for (int32_t k = 0; k < nsteps; ++k) {
     if (nwork > 0) {
       sir_sweep_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work), nwork,
                                                  live_work, L);
-      int st = abm_host::check_launch("abm_sir_steps/sweep");
-      if (st) return st;
+      if ((st = abm_host::check_launch("abm_sir_steps/sweep"))) return st;
       sir_candidates_kernel<<<cand_grid, kSirThreads, 0, s>>>(insts, L);
-      st = abm_host::check_launch("abm_sir_steps/candidates");
-      if (st) return st;
+      if ((st = abm_host::check_launch("abm_sir_steps/candidates"))) return st;
       sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, L);
-      st = abm_host::check_launch("abm_sir_steps/push");
-      if (st) return st;
+      if ((st = abm_host::check_launch("abm_sir_steps/push"))) return st;
     }
     sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, L.hdr);
-    int st = abm_host::check_launch("abm_sir_steps/finalize");
-    if (st) return st;
+    if ((st = abm_host::check_launch("abm_sir_steps/finalize"))) return st;
   }
   return ABM_OK;
 }

@@ -25,15 +25,15 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 4096  # agents per work item (abm_sir_tile_agents)
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 112 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 120 bytes
 INSTANCE_DTYPE = np.dtype([
     ("row_ptr", "<u8"), ("col", "<u8"), ("state", "<u8"), ("counts", "<u8"),
     ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)), ("n", "<i4"),
     ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("num_s", "<i4"),
     ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"), ("step_ir", "<i4"),
-    ("edges_scanned", "<u8"), ("edges_pushed", "<u8"),
+    ("edges_scanned", "<u8"), ("edges_pushed", "<u8"), ("coll", "<u4", (2,)),
 ])
-assert INSTANCE_DTYPE.itemsize == 112
+assert INSTANCE_DTYPE.itemsize == 120
 WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
