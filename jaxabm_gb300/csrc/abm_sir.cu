@@ -111,7 +111,9 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
     const abm_sir_instance* I = insts + item.x;
-    if (I->t >= I->steps) continue;  // uniform over the CTA
+    // finished instances, and instances without an infected agent (nothing can change in
+    // them any more: no infection source, no recovery), need no decisions
+    if (I->t >= I->steps || I->num_i == 0) continue;  // uniform over the CTA
     const int32_t* __restrict__ word = I->state;
     // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
     // words are 16-byte aligned, scalar loads for a partial last vector
