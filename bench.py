@@ -33,6 +33,19 @@ import torch  # noqa: E402
 L2_BYTES = 129 * 1024 * 1024
 
 
+def _profiled_traffic(instances):
+    """DRAM bytes of one full-ensemble replay from the committed ncu launch-list summary
+    (only for the full 4,096-instance workload it was captured on)."""
+    p = os.path.join(ROOT, "profiles", "sir_ensemble_4096_launch_list.md")
+    if instances != 4096 or not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_replay:"):
+                return int(line.split(":")[1]), "profiles/sir_ensemble_4096_launch_list.md"
+    return None, None
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -300,6 +313,7 @@ def run_ours(args):
     hbm_peak, peak_kind = _peaks()
     alg_bytes = wl.algorithmic_bytes()
     achieved = alg_bytes / (ms_local / 1e3) / 1e9
+    traffic, traffic_src = _profiled_traffic(wl.count)
     h2d, d2h = wl.e2e_bytes
     out = {
         "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world,
@@ -314,11 +328,12 @@ def run_ours(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": wl.launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": traffic_src,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback",
-                     "kernel": "sir_decide_kernel + sir_push_kernel + sir_finalize_kernel "
-                               "per step, all 365 steps in one graph replay",
+                     "kernel": "SIR step sequence (sweep + candidates + push + finalize per "
+                               "step; 365 steps in one CUDA-graph replay), timed as a unit",
                      "algorithmic_bytes_per_step": alg_bytes},
         "clocks": clk,
     }

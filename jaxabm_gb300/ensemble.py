@@ -239,13 +239,23 @@ class SIRBatch:
                       - 2 * (self.h_state0 == 2).sum())
         return int(d["edges_scanned"].sum()), int(d["edges_pushed"].sum()), changes
 
+    def live_agent_steps(self):
+        """Agent-steps the sweep reads: steps of an instance that start with at least one
+        infected agent (the others cannot change and are skipped)."""
+        counts = self.counts.reshape(self.k, self.steps, 3).cpu().numpy().astype(np.int64)
+        i0 = np.array([(self.h_state0[o:o + n] == 1).sum() for o, n in
+                       zip(self._offsets[2][:-1], self.n)], dtype=np.int64)
+        i_before = np.concatenate([i0[:, None], counts[:, :-1, 1]], axis=1)
+        return int(((i_before > 0).sum(axis=1) * self.n).sum())
+
     def algorithmic_bytes(self):
-        """Bytes the run must move (after it completed): per step and agent its 4-byte word;
-        per CSR slot read by decide 8 bytes (column index + neighbour word); per slot read
-        by push 12 bytes (column index + atomic read-modify-write); per compartment change
-        32 bytes (list entry write and read, row offsets, own word update)."""
+        """Bytes the run must move (after it completed), at 4-byte granularity: per live
+        agent-step its 4-byte word; per CSR slot read by the candidates kernel 8 bytes
+        (column index + neighbour word); per slot pushed 12 bytes (column index + atomic
+        read-modify-write); per compartment change 32 bytes (list entry write and read, row
+        offsets, own word update)."""
         scanned, pushed, changes = self.edge_stats()
-        return int(4 * self.n.sum() * self.steps + 8 * scanned + 12 * pushed + 32 * changes)
+        return int(4 * self.live_agent_steps() + 8 * scanned + 12 * pushed + 32 * changes)
 
 
 # ---- the batched-ensemble workload (4,096 SIR instances) -------------------------------
