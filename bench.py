@@ -147,6 +147,10 @@ class SIREnsembleBench:
         self.build_s = time.perf_counter() - t0
         self.batch = ensemble.SIRBatch(self.graphs, self.inits, spec["beta"], spec["gamma"],
                                        spec["seed"], steps)
+        from jaxabm_gb300 import autotune
+        t0 = time.perf_counter()
+        self.launch = autotune.tune_sir_batch(self.batch)
+        self.tune_s = time.perf_counter() - t0
         self.batch.capture(steps)
         self.units_per_step = self.batch.agent_steps
         self.launches_per_step = self.batch.launches_per_run()
@@ -344,7 +348,9 @@ def run_ours(args):
         out["served"]["served_over_plain"] = out["served"]["value"] / out["plain"]["value"]
     if rank == 0 and world == 1 and not args.quick:
         out["cpu_baseline"] = wl.cpu_baseline(os.cpu_count() or 1)
-    out["setup_s"] = {"graph_build": wl.build_s}
+    out["setup_s"] = {"graph_build": wl.build_s, "autotune": wl.tune_s}
+    out["config"]["launch_grids"] = {"sweep": wl.launch[0], "candidates": wl.launch[1],
+                                     "push": wl.launch[2], "picked_by": "jaxabm_gb300.autotune"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -209,8 +209,21 @@ ABM_API int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void*
  * agent: a change list and a candidate list). */
 ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
 
+/* Persistent-grid sizes (CTAs of 256 threads) of the three per-step SIR kernels; 0 picks
+ * the default (as many CTAs as are resident at once).  Any choice gives identical results;
+ * jaxabm_gb300.autotune picks them per GPU and workload. */
+typedef struct abm_sir_launch {
+  int32_t sweep_grid;
+  int32_t candidates_grid;
+  int32_t push_grid;
+  int32_t reserved;
+} abm_sir_launch;
+
+/* The default launch configuration on the current device. */
+ABM_API int abm_sir_default_launch(abm_sir_launch* out);
+
 /* nsteps synchronous SIR steps of every instance with t < steps, over the tiles `work`
- * (persistent grid of `grid` CTAs; 0 = 8 per SM).  When live_work (device int32) is not
+ * (launch: grid sizes in host memory, NULL for the defaults).  When live_work (device int32) is not
  * NULL, only the first min(*live_work, nwork) tiles are read, so a CUDA graph of this call
  * stays valid while the number of live tiles changes.  Per step and agent i of an instance:
  * agent_key = split(coll_key, n)[i], k_inf, k_rec = split(agent_key);
@@ -226,8 +239,9 @@ ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
  * and may be rewritten between calls (e.g. to admit instances) without re-capturing a
  * CUDA graph of this call. */
 ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                          int32_t nwork, const int32_t* live_work, int32_t nsteps, int32_t grid,
-                          void* changes, size_t changes_bytes, void* stream);
+                          int32_t nwork, const int32_t* live_work, int32_t nsteps,
+                          const abm_sir_launch* launch, void* changes, size_t changes_bytes,
+                          void* stream);
 
 ABM_API size_t abm_sir_run_workspace_bytes(int64_t n);
 

@@ -537,6 +537,15 @@ size_t abm_sir_instance_size(void) { return sizeof(abm_sir_instance); }
 
 int32_t abm_sir_tile_agents(void) { return kTile; }
 
+int abm_sir_default_launch(abm_sir_launch* out) {
+  if (!out) return ABM_ERR_BADARG;
+  out->sweep_grid = resident_grid(sir_sweep_kernel, 4);
+  out->candidates_grid = resident_grid(sir_candidates_kernel, 4);
+  out->push_grid = resident_grid(sir_push_kernel, 4);
+  out->reserved = 0;
+  return ABM_OK;
+}
+
 size_t abm_sir_changes_bytes(int64_t max_agents) {
   if (max_agents <= 0) return 0;
   const size_t cap = ((size_t)max_agents + 1) & ~(size_t)1;
@@ -581,7 +590,8 @@ int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream)
 }
 
 int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* work,
-                  int32_t nwork, const int32_t* live_work, int32_t nsteps, int32_t grid,
+                  int32_t nwork, const int32_t* live_work, int32_t nsteps,
+                  const abm_sir_launch* launch,
                   void* changes, size_t changes_bytes, void* stream) {
   if (!insts || ninst <= 0 || nwork < 0 || nsteps < 0 || (nwork > 0 && !work) || !changes)
     return ABM_ERR_BADARG;
@@ -592,10 +602,17 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   if (nsteps == 0) return ABM_OK;
   const Lists L = carve_lists(changes, changes_bytes);
   cudaStream_t s = abm_host::as_stream(stream);
-  int g = grid > 0 ? grid : resident_grid(sir_sweep_kernel, 4);
+  abm_sir_launch cfg;
+  abm_sir_default_launch(&cfg);
+  if (launch) {
+    if (launch->sweep_grid > 0) cfg.sweep_grid = launch->sweep_grid;
+    if (launch->candidates_grid > 0) cfg.candidates_grid = launch->candidates_grid;
+    if (launch->push_grid > 0) cfg.push_grid = launch->push_grid;
+  }
+  int g = cfg.sweep_grid;
   if (nwork > 0 && g > nwork) g = nwork;
-  const int cand_grid = resident_grid(sir_candidates_kernel, 4);
-  const int push_grid = resident_grid(sir_push_kernel, 4);
+  const int cand_grid = cfg.candidates_grid;
+  const int push_grid = cfg.push_grid;
   const int fin_blocks = (ninst + 255) / 256;
   sir_prepare_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst);
   int st = abm_host::check_launch("abm_sir_steps/prepare");
@@ -656,8 +673,8 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
       misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
-  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps, 0,
-                     lists, align256(abm_sir_changes_bytes(n)), stream);
+  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps,
+                     nullptr, lists, align256(abm_sir_changes_bytes(n)), stream);
   if (st) return st;
   return abm_sir_unpack(words, n, state, stream);
 }

@@ -73,6 +73,21 @@ def changes_workspace(max_agents, device=None):
     return torch.zeros(max(nbytes, 32), dtype=torch.uint8, device=device or _dev.device())
 
 
+def launch_struct(cfg):
+    """Host ``abm_sir_launch`` for (sweep, candidates, push) grid sizes (None: defaults)."""
+    if cfg is None:
+        return None
+    a = np.zeros(4, dtype=np.int32)
+    a[:3] = [int(v) for v in cfg]
+    return a
+
+
+def default_launch():
+    a = np.zeros(4, dtype=np.int32)
+    _lib.call("abm_sir_default_launch", a.ctypes.data)
+    return tuple(int(v) for v in a[:3])
+
+
 def changes_overflowed(ws):
     return int(ws[4:8].view(torch.int32).item()) != 0
 
@@ -156,7 +171,7 @@ class SIRBatch:
             raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
         self.words0 = self.words.clone()
         self.changes = changes_workspace(int(self.n.sum()))
-        self.grid = 0
+        self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_steps = None
 
@@ -187,8 +202,17 @@ class SIRBatch:
     def launch(self, nsteps, stream=None):
         """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps``)."""
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
-                  self.work.shape[0], None, int(nsteps), int(self.grid), _dev.ptr(self.changes),
+                  self.work.shape[0], None, int(nsteps), self._launch_ptr(), _dev.ptr(self.changes),
                   self.changes.numel(), _dev.stream_handle(stream))
+
+    def _launch_ptr(self):
+        self._launch_buf = launch_struct(self.launch_cfg)  # kept alive for the call
+        return None if self._launch_buf is None else self._launch_buf.ctypes.data
+
+    def set_launch(self, cfg):
+        """Use grid sizes ``cfg`` = (sweep, candidates, push); drops the captured graph."""
+        self.launch_cfg = None if cfg is None else tuple(int(v) for v in cfg)
+        self._graph = None
 
     def capture(self, nsteps):
         """Capture ``nsteps`` steps into a CUDA graph (replayed by :meth:`replay`)."""

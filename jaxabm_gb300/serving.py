@@ -28,7 +28,7 @@ import torch
 from . import _dev
 from . import _lib
 from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, changes_workspace,
-                       check_layout, model_rngs, pack_words, unpack_words)
+                       check_layout, launch_struct, model_rngs, pack_words, unpack_words)
 
 
 class Request:
@@ -72,18 +72,18 @@ class SIRServer:
         max_tiles: capacity of the work list (256-agent tiles of resident requests)
         steps_per_tick: steps every resident request advances per tick
         reserve_bytes: device memory kept free at admission
-        grid: persistent grid of the step kernel (0 = 8 CTAs per SM)
+        grid: (sweep, candidates, push) persistent grid sizes, or None for the defaults
     """
 
     def __init__(self, max_slots=512, max_tiles=65536, steps_per_tick=16,
-                 reserve_bytes=1 << 30, grid=0):
+                 reserve_bytes=1 << 30, grid=None):
         check_layout()
         dev = _dev.device()
         self.max_slots = int(max_slots)
         self.max_tiles = int(max_tiles)
         self.steps_per_tick = int(steps_per_tick)
         self.reserve = int(reserve_bytes)
-        self.grid = int(grid)
+        self.grid = None if grid is None else tuple(int(v) for v in grid)
         words = INSTANCE_DTYPE.itemsize // 4
         self.dummy = self.max_slots  # inactive descriptor row (t = steps = 0)
         self.desc = torch.zeros((self.max_slots + 1, words), dtype=torch.int32, device=dev)
@@ -115,9 +115,13 @@ class SIRServer:
     # -- graph ------------------------------------------------------------------------
     def _launch(self):
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.max_slots + 1, _dev.ptr(self.work),
-                  self.max_tiles, _dev.ptr(self.live), self.steps_per_tick, self.grid,
+                  self.max_tiles, _dev.ptr(self.live), self.steps_per_tick, self._launch_ptr(),
                   _dev.ptr(self.changes),
                   self.changes.numel(), self.stream.cuda_stream)
+
+    def _launch_ptr(self):
+        self._launch_buf = launch_struct(self.grid)  # kept alive for the call
+        return None if self._launch_buf is None else self._launch_buf.ctypes.data
 
     def _capture(self):
         torch.cuda.synchronize()
