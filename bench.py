@@ -138,9 +138,7 @@ class SIREnsembleBench:
         from jaxabm_gb300 import ensemble
         self.ensemble = ensemble
         self.count, self.T = count, steps
-        spec = ensemble.ensemble_spec(4096)
-        spec = {k: v[:count] for k, v in spec.items()}
-        spec["seed"] = spec["seed"] + rank * count  # each rank its own members
+        spec = ensemble.rank_spec(count, rank)  # each rank its own members
         self.spec = spec
         t0 = time.perf_counter()
         self.graphs, self.inits = ensemble.build_instances(spec)

@@ -307,6 +307,16 @@ def ensemble_spec(count=4096, n_lo=1_000, n_hi=100_000, seed=2, rate=200.0):
     return {"n": n, "beta": beta, "gamma": gamma, "arrival_s": arrivals, "seed": seeds}
 
 
+def rank_spec(count=4096, rank=0, full=4096):
+    """The first ``count`` members of the ensemble specification for one rank of a
+    multi-GPU run: every rank runs its own members (model, graph and infection seeds offset
+    by ``rank * full``), so ranks never share an instance and need no collective."""
+    spec = ensemble_spec(full)
+    spec = {k: v[:count].copy() for k, v in spec.items()}
+    spec["seed"] = spec["seed"] + int(rank) * int(full)
+    return spec
+
+
 def build_instances(spec, m=4, initial_infected=0.001, workers=None):
     """Host CSR graphs and initial compartments of every instance (native generator,
     threads across instances)."""
