@@ -261,6 +261,108 @@ class SIREnsembleBench:
                 "sample": f"first {k} of {self.count} instances, 365 steps each, C/OpenMP oracle"}
 
 
+def _time_ms(fn, reps=3, warmup=1):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def model_lines():
+    """Single-model throughput of the other workload models (device-resident inputs)."""
+    from jaxabm_gb300 import _dev, _lib, opinion, schelling, sir
+    import jaxabm_gb300.random as jr
+    L = _lib.load()
+    out = {}
+
+    # quick-start random walk: N = 10,000, 100 steps, PRNGKey(0)
+    n, T = 10_000, 100
+    x = torch.rand(n, device="cuda")
+    y = torch.rand(n, device="cuda")
+    rng = jr.split(jr.PRNGKey(0), 2)[0].contiguous()
+    ck = torch.empty((T, 1, 2), dtype=torch.int32, device="cuda")
+    means = torch.empty((T, 2), device="cuda")
+    ws = torch.empty(L.abm_randomwalk_workspace_bytes(n, T), dtype=torch.uint8, device="cuda")
+
+    def rw():
+        _lib.call("abm_keychain", _dev.ptr(rng), 1, 1, T, _dev.ptr(ck), None, None)
+        _lib.call("abm_randomwalk_run", _dev.ptr(x), _dev.ptr(y), n, _dev.ptr(ck), T, 0.01,
+                  _dev.ptr(means), _dev.ptr(ws), ws.numel(), None)
+    ms = _time_ms(rw, reps=20)
+    out["randomwalk_n10000_t100"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
+                                     "launches_per_run": 3}
+
+    # Schelling 256 x 256 torus, density 0.9, 200 steps, seed 1
+    W = H = 256
+    pos0, types = schelling.initial_layout(W, H, 0.9, 0.5, 1)
+    n = len(pos0)
+    T = 200
+    p = torch.from_numpy(pos0).cuda()
+    t8 = torch.from_numpy(types).cuda()
+    grid = torch.empty(W * H, dtype=torch.int8, device="cuda")
+    ca = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stats = torch.empty((T, 2), dtype=torch.int32, device="cuda")
+    ws = torch.empty(L.abm_schelling_workspace_bytes(n, W, H), dtype=torch.uint8, device="cuda")
+    rng = jr.split(jr.PRNGKey(1), 2)[0].contiguous()
+    ck = jr.keychain(rng.clone(), T, 1).reshape(T, 2).contiguous()
+    p0 = p.clone()
+
+    def sch():
+        p.copy_(p0)
+        _lib.call("abm_schelling_place", _dev.ptr(p), _dev.ptr(t8), n, W, H, _dev.ptr(grid),
+                  _dev.ptr(ca), _dev.ptr(status), None)
+        _lib.call("abm_schelling_run", _dev.ptr(p), _dev.ptr(t8), n, W, H, _dev.ptr(grid),
+                  _dev.ptr(ca), _dev.ptr(ck), T, _dev.ptr(stats), _dev.ptr(ws), ws.numel(), None)
+    ms = _time_ms(sch, reps=3)
+    out["schelling_256x256_t200"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
+                                     "launches_per_run": 4 * T + 4}
+
+    # SIR, one model: N = 2^20 Barabasi-Albert m=4, 365 steps (the plain engine)
+    n, T = 1 << 20, 365
+    rp, col = sir.barabasi_albert(n, 4, 0)
+    drp, dcol = torch.from_numpy(rp).cuda(), torch.from_numpy(col).cuda()
+    st0 = torch.from_numpy(sir.initial_states(n, 0.001, 0)).cuda()
+    st = st0.clone()
+    counts = torch.empty((T, 3), dtype=torch.int32, device="cuda")
+    ws = torch.empty(L.abm_sir_run_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    rng = jr.split(jr.PRNGKey(0), 2)[0].contiguous()
+    ck = jr.keychain(rng.clone(), T, 1).reshape(T, 2).contiguous()
+
+    def sir1():
+        st.copy_(st0)
+        _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(st), _dev.ptr(ck), T,
+                  0.05, 0.1, _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
+    ms = _time_ms(sir1, reps=3)
+    out["sir_ba_n1048576_t365"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
+                                   "launches_per_run": 4 * T + 5}
+
+    # opinion calibration: N = 2^18, 16-regular, 64 instances, 200 steps, checkpoints every 20
+    n, B, T = 1 << 18, 64, 200
+    rp, col = sir.random_regular(n, 16, 0)
+    o0 = opinion.initial_opinions(n, 0)
+    pr = opinion.calibration_params(B)
+    batch = opinion.OpinionBatch(rp, col, o0, pr[:, 0], pr[:, 1], pr[:, 2])
+    target = np.array([0.5, 0.3, 0.2, 0.15])
+    ms_f = _time_ms(lambda: batch.forward(T), reps=2)
+
+    def fwd_adj():
+        batch.forward(T, 20)
+        batch.backward(target)
+    ms_fa = _time_ms(fwd_adj, reps=1)
+    out["opinion_n262144_b64_t200"] = {
+        "instance_agent_steps_per_s_forward": n * B * T / (ms_f / 1e3), "ms_forward": ms_f,
+        "ms_forward_plus_adjoint": ms_fa,
+        "instance_agent_steps_per_s_forward_plus_adjoint": n * B * T / (ms_fa / 1e3)}
+    return out
+
+
 WORKLOADS = {"sir_ensemble": SIREnsembleBench}
 DEFAULT_WORKLOAD = "sir_ensemble"
 
@@ -346,6 +448,8 @@ def run_ours(args):
         out["served"]["served_over_plain"] = out["served"]["value"] / out["plain"]["value"]
     if rank == 0 and world == 1 and not args.quick:
         out["cpu_baseline"] = wl.cpu_baseline(os.cpu_count() or 1)
+    if not args.quick or args.models:
+        out["models"] = model_lines()
     out["setup_s"] = {"graph_build": wl.build_s, "autotune": wl.tune_s}
     out["config"]["launch_grids"] = {"sweep": wl.launch[0], "candidates": wl.launch[1],
                                      "push": wl.launch[2], "picked_by": "jaxabm_gb300.autotune"}
@@ -408,6 +512,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--quick", action="store_true",
                     help="only the batched value and e2e (no plain/served/cpu legs)")
+    ap.add_argument("--models", action="store_true",
+                    help="with --quick: also time the single-model workloads")
     ap.add_argument("--instances", type=int, default=4096,
                     help="ensemble members (the first K of the 4,096-member specification); "
                          "smaller values are for profiling captures")
