@@ -24,14 +24,13 @@ namespace {
 
 constexpr int kOpThreads = 256;
 
-__device__ __forceinline__ float comp(const float4& v, int c) {
-  return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
-}
-__device__ __forceinline__ void set_comp(float4& v, int c, float x) {
-  if (c == 0) v.x = x;
-  else if (c == 1) v.y = x;
-  else if (c == 2) v.z = x;
-  else v.w = x;
+// 16-byte load of the four floats of lane group `sub` of a row into registers.
+__device__ __forceinline__ void ld4(const float* __restrict__ row, int sub, float (&a)[4]) {
+  const float4 v = reinterpret_cast<const float4*>(row)[sub];
+  a[0] = v.x;
+  a[1] = v.y;
+  a[2] = v.z;
+  a[3] = v.w;
 }
 
 __device__ __forceinline__ float sigmoid_of(float eps, float itau, float d) {
@@ -49,31 +48,45 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
   const int node = (int)(g / LPN);
   const int sub = (int)(g % LPN);
   if (node >= n) return;
-  const float4 m4 = reinterpret_cast<const float4*>(mu)[sub];
-  const float4 e4 = reinterpret_cast<const float4*>(eps)[sub];
-  const float4 t4 = reinterpret_cast<const float4*>(tau)[sub];
-  const float4 it4 = make_float4(1.0f / t4.x, 1.0f / t4.y, 1.0f / t4.z, 1.0f / t4.w);
-  const float4 oi = reinterpret_cast<const float4*>(o + (size_t)node * B)[sub];
-  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  float m[4], ep[4], it[4], oi[4], acc[4] = {0.f, 0.f, 0.f, 0.f};
+  ld4(mu, sub, m);
+  ld4(eps, sub, ep);
+  ld4(tau, sub, it);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) it[c] = 1.0f / it[c];
+  ld4(o + (size_t)node * B, sub, oi);
   const int r0 = rp[node], r1 = rp[node + 1];
-  for (int e = r0; e < r1; ++e) {
-    const int j = col[e];
-    const float4 oj = reinterpret_cast<const float4*>(o + (size_t)j * B)[sub];
+  int e = r0;
+  // two neighbour rows in flight per iteration; accumulation stays in CSR order
+  for (; e + 1 < r1; e += 2) {
+    float oa[4], ob[4];
+    ld4(o + (size_t)col[e] * B, sub, oa);
+    ld4(o + (size_t)col[e + 1] * B, sub, ob);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const float d = comp(oj, c) - comp(oi, c);
-      const float s = sigmoid_of(comp(e4, c), comp(it4, c), d);
-      set_comp(acc, c, fmaf(s, d, comp(acc, c)));
+      const float da = oa[c] - oi[c];
+      acc[c] = fmaf(sigmoid_of(ep[c], it[c], da), da, acc[c]);
+      const float db = ob[c] - oi[c];
+      acc[c] = fmaf(sigmoid_of(ep[c], it[c], db), db, acc[c]);
     }
   }
-  float4 res = oi;
+  if (e < r1) {
+    float oa[4];
+    ld4(o + (size_t)col[e] * B, sub, oa);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float da = oa[c] - oi[c];
+      acc[c] = fmaf(sigmoid_of(ep[c], it[c], da), da, acc[c]);
+    }
+  }
+  float res[4] = {oi[0], oi[1], oi[2], oi[3]};
   const int deg = r1 - r0;
   if (deg > 0) {
     const float fdeg = (float)deg;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) set_comp(res, c, fmaf(comp(m4, c), comp(acc, c) / fdeg, comp(oi, c)));
+    for (int c = 0; c < 4; ++c) res[c] = fmaf(m[c], acc[c] / fdeg, oi[c]);
   }
-  reinterpret_cast<float4*>(out + (size_t)node * B)[sub] = res;
+  reinterpret_cast<float4*>(out + (size_t)node * B)[sub] = make_float4(res[0], res[1], res[2], res[3]);
 }
 
 // One adjoint step: lam_out from lam_in (= lambda^{t+1}) at the forward state o (= o^t);
@@ -91,52 +104,51 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
   const int sub = (int)(g % LPN);
   float gm[4] = {0.f, 0.f, 0.f, 0.f}, ge[4] = {0.f, 0.f, 0.f, 0.f}, gt[4] = {0.f, 0.f, 0.f, 0.f};
   if (node < n) {
-    const float4 m4 = reinterpret_cast<const float4*>(mu)[sub];
-    const float4 e4 = reinterpret_cast<const float4*>(eps)[sub];
-    const float4 t4 = reinterpret_cast<const float4*>(tau)[sub];
-    const float4 it4 = make_float4(1.0f / t4.x, 1.0f / t4.y, 1.0f / t4.z, 1.0f / t4.w);
-    const float4 oi = reinterpret_cast<const float4*>(o + (size_t)node * B)[sub];
-    const float4 li = reinterpret_cast<const float4*>(lam_in + (size_t)node * B)[sub];
+    float m[4], ep[4], it[4], oi[4], li[4], li_d[4];
+    ld4(mu, sub, m);
+    ld4(eps, sub, ep);
+    ld4(tau, sub, it);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) it[c] = 1.0f / it[c];
+    ld4(o + (size_t)node * B, sub, oi);
+    ld4(lam_in + (size_t)node * B, sub, li);
     const int r0 = rp[node], r1 = rp[node + 1];
     const float fdeg_i = (float)(r1 - r0);
-    float4 li_d = li;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) li_d[c] = r1 > r0 ? li[c] / fdeg_i : li[c];
     float sl[4] = {0.f, 0.f, 0.f, 0.f};  // sum_j g'(d) (lam_j/deg_j - lam_i/deg_i)
     float sgd[4] = {0.f, 0.f, 0.f, 0.f}, sse[4] = {0.f, 0.f, 0.f, 0.f}, sst[4] = {0.f, 0.f, 0.f, 0.f};
-    if (r1 > r0) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) set_comp(li_d, c, comp(li, c) / fdeg_i);
-    }
     for (int e = r0; e < r1; ++e) {
       const int j = col[e];
-      const float4 oj = reinterpret_cast<const float4*>(o + (size_t)j * B)[sub];
-      const float4 lj = reinterpret_cast<const float4*>(lam_in + (size_t)j * B)[sub];
+      float oj[4], lj[4];
+      ld4(o + (size_t)j * B, sub, oj);
+      ld4(lam_in + (size_t)j * B, sub, lj);
       const float fdeg_j = (float)(rp[j + 1] - rp[j]);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const float d = comp(oj, c) - comp(oi, c);
+        const float d = oj[c] - oi[c];
         const float a = fabsf(d);
-        const float itau = comp(it4, c);
-        const float z = (comp(e4, c) - a) * itau;
+        const float z = (ep[c] - a) * it[c];
         const float s = 1.0f / (1.0f + expf(-z));
         const float sp = s * (1.0f - s);
-        const float gprime = s - a * sp * itau;
-        sl[c] = fmaf(gprime, comp(lj, c) / fdeg_j - comp(li_d, c), sl[c]);
+        const float gprime = s - a * sp * it[c];
+        sl[c] = fmaf(gprime, lj[c] / fdeg_j - li_d[c], sl[c]);
         sgd[c] = fmaf(s, d, sgd[c]);
-        sse[c] = fmaf(sp * itau, d, sse[c]);
-        sst[c] = fmaf(-sp * z * itau, d, sst[c]);
+        sse[c] = fmaf(sp * it[c], d, sse[c]);
+        sst[c] = fmaf(-sp * z * it[c], d, sst[c]);
       }
     }
-    float4 lo;
+    float lo[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      set_comp(lo, c, fmaf(comp(m4, c), sl[c], comp(li, c)));
+      lo[c] = fmaf(m[c], sl[c], li[c]);
       if (r1 > r0) {
-        gm[c] = comp(li, c) * (sgd[c] / fdeg_i);
-        ge[c] = comp(li, c) * comp(m4, c) * (sse[c] / fdeg_i);
-        gt[c] = comp(li, c) * comp(m4, c) * (sst[c] / fdeg_i);
+        gm[c] = li[c] * (sgd[c] / fdeg_i);
+        ge[c] = li[c] * m[c] * (sse[c] / fdeg_i);
+        gt[c] = li[c] * m[c] * (sst[c] / fdeg_i);
       }
     }
-    reinterpret_cast<float4*>(lam_out + (size_t)node * B)[sub] = lo;
+    reinterpret_cast<float4*>(lam_out + (size_t)node * B)[sub] = make_float4(lo[0], lo[1], lo[2], lo[3]);
   }
   // per-CTA reduction of the parameter gradients per instance column (fixed order)
   constexpr int kNodes = kOpThreads / LPN;
