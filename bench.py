@@ -184,6 +184,10 @@ class SIREnsembleBench:
         self.batch.reset()
         self.batch.replay()
         torch.cuda.synchronize()
+        scanned, pushed, changes, cands = self.batch.edge_stats()
+        self.work_stats = {"live_agent_steps": self.batch.live_agent_steps(),
+                           "decision_candidates": cands, "csr_slots_scanned": scanned,
+                           "csr_slots_pushed": pushed, "compartment_changes": changes}
         return self.batch.algorithmic_bytes()
 
     def plain(self, sample=48):
@@ -200,12 +204,14 @@ class SIREnsembleBench:
             dcol = torch.from_numpy(col).cuda()
             buf = torch.from_numpy(self.inits[i]).cuda()
             counts = torch.empty((self.T, 3), dtype=torch.int32, device="cuda")
-            ws = torch.empty(L.abm_sir_run_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+            ws = torch.empty(L.abm_sir_run_workspace_bytes(n, len(col)), dtype=torch.uint8,
+                             device="cuda")
             rng = self.ensemble.model_rngs([int(self.spec["seed"][i])])[0].contiguous()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             ck = jr.keychain(rng, self.T, 1).reshape(self.T, 2).contiguous()
-            _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(buf), _dev.ptr(ck),
+            _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, len(col), _dev.ptr(buf),
+                      _dev.ptr(ck),
                       self.T, float(self.spec["beta"][i]), float(self.spec["gamma"][i]),
                       _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
             torch.cuda.synchronize()
@@ -215,8 +221,10 @@ class SIREnsembleBench:
                 "sample": f"first {min(sample, self.count)} instances, one simulation per "
                           f"launch sequence (keychain + 2 launches per step)"}
 
-    def served(self, rate_scale=1.0):
-        """Real-time replay of the Poisson request stream through the server."""
+    def served(self, burst=False):
+        """The request stream through the continuous-batching server: the Poisson arrivals
+        at 200 requests/s replayed in real time (latency under the stream's own load), or,
+        with ``burst``, every request submitted at once (the server's capacity)."""
         from jaxabm_gb300.serving import Request, SIRServer
         reqs = []
         for i in range(self.count):
@@ -226,9 +234,10 @@ class SIREnsembleBench:
                                 torch.from_numpy(self.inits[i]).pin_memory(),
                                 self.spec["beta"][i], self.spec["gamma"][i],
                                 int(self.spec["seed"][i]), self.T))
-        srv = SIRServer(max_slots=1024, max_tiles=1 << 17, steps_per_tick=32)
+        srv = SIRServer(max_slots=4096, max_tiles=1 << 17, steps_per_tick=32)
+        arrivals = np.zeros(self.count) if burst else self.spec["arrival_s"]
         torch.cuda.synchronize()
-        wall = srv.serve(reqs, self.spec["arrival_s"] / rate_scale)
+        wall = srv.serve(reqs, arrivals)
         lat = srv.latencies()
         units = sum(r.n for r in reqs) * self.T
         # spot-check a few results against the batched run (bit-identical by design)
@@ -240,8 +249,9 @@ class SIREnsembleBench:
         return {"value": units / wall, "unit": "agent-steps/s",
                 "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "requests": len(lat), "rate_per_s": 200.0 * rate_scale, "wall_s": wall,
-                "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
+                "requests": len(lat),
+                "arrivals": "all at t=0" if burst else "Poisson, 200 requests/s, real time",
+                "wall_s": wall, "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
                 "results_match_batched": bool(same)}
 
     def cpu_baseline(self, threads, budget_s=12.0):
@@ -331,13 +341,15 @@ def model_lines():
     st0 = torch.from_numpy(sir.initial_states(n, 0.001, 0)).cuda()
     st = st0.clone()
     counts = torch.empty((T, 3), dtype=torch.int32, device="cuda")
-    ws = torch.empty(L.abm_sir_run_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+    ws = torch.empty(L.abm_sir_run_workspace_bytes(n, len(col)), dtype=torch.uint8,
+                     device="cuda")
     rng = jr.split(jr.PRNGKey(0), 2)[0].contiguous()
     ck = jr.keychain(rng.clone(), T, 1).reshape(T, 2).contiguous()
 
     def sir1():
         st.copy_(st0)
-        _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(st), _dev.ptr(ck), T,
+        _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, len(col), _dev.ptr(st),
+                  _dev.ptr(ck), T,
                   0.05, 0.1, _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
     ms = _time_ms(sir1, reps=3)
     out["sir_ba_n1048576_t365"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
@@ -438,7 +450,8 @@ def run_ours(args):
                      if peak_kind == "measured" else "fallback",
                      "kernel": "SIR step sequence (sweep + candidates + push + finalize per "
                                "step; 365 steps in one CUDA-graph replay), timed as a unit",
-                     "algorithmic_bytes_per_step": alg_bytes},
+                     "algorithmic_bytes_per_step": alg_bytes,
+                     "work_per_step": wl.work_stats},
         "clocks": clk,
     }
     if not args.quick:
@@ -446,6 +459,9 @@ def run_ours(args):
         out["plain"]["batched_over_plain"] = value / out["plain"]["value"]
         out["served"] = wl.served()
         out["served"]["served_over_plain"] = out["served"]["value"] / out["plain"]["value"]
+        out["served_burst"] = wl.served(burst=True)
+        out["served_burst"]["served_over_plain"] = (out["served_burst"]["value"]
+                                                    / out["plain"]["value"])
     if rank == 0 and world == 1 and not args.quick:
         out["cpu_baseline"] = wl.cpu_baseline(os.cpu_count() or 1)
     if not args.quick or args.models:

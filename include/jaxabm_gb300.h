@@ -138,9 +138,13 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
                                      int32_t* col, int64_t col_capacity);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (120 bytes, 8-byte aligned).
- * state holds one int32 word per agent, (infected neighbours << 2) | compartment
- * (0 S, 1 I, 2 R), built by abm_sir_pack and read back by abm_sir_unpack.
+/* Device-side descriptor of one SIR model instance (136 bytes, 8-byte aligned).
+ * words holds one byte per agent, (infected neighbours << 2) | compartment (0 S, 1 I,
+ * 2 R); an agent of degree >= abm_sir_hub_degree() (a hub) has 63 in the count field and
+ * its count in hub_counts[i] (int32[n]).  words is 16-byte aligned and round_up(n, 16)
+ * bytes long (padding bytes read as R).  adj is the instance's CSR column array with
+ * bit 31 set on entries whose neighbour is a hub.  All three are written by
+ * abm_sir_pack / abm_sir_pack_batch; abm_sir_unpack reads the compartments back.
  * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
  * NULL, else it is derived from rng, the instance's Model.step key-chain state
  * (jaxabm/model.py:156,164), which is advanced once per step either way.  num_s/num_i/num_r
@@ -148,11 +152,13 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
  * S, I, R after each step (int32[steps][3]); step_si/step_ir are the transitions of the
  * step in flight (zero before step 0); done_flag (nullable, may be host-mapped) is set to
  * 1 after the last step; edges_scanned / edges_pushed accumulate the CSR slots read by
- * the decide and push phases (zero before step 0). */
+ * the decide and push phases and candidates the agents that needed a decision (all zero
+ * before step 0). */
 typedef struct abm_sir_instance {
   const int32_t* row_ptr;
-  const int32_t* col;
-  int32_t* state;
+  int32_t* adj;
+  uint8_t* words;
+  int32_t* hub_counts;
   int32_t* counts;
   int32_t* done_flag;
   const uint32_t* coll_keys;
@@ -169,6 +175,7 @@ typedef struct abm_sir_instance {
   int32_t step_ir;
   unsigned long long edges_scanned;
   unsigned long long edges_pushed;
+  unsigned long long candidates;
   uint32_t coll[2]; /* collection key of the current step (written by abm_sir_steps) */
 } abm_sir_instance;
 
@@ -183,26 +190,34 @@ typedef struct abm_work_item {
 ABM_API size_t abm_sir_instance_size(void);
 
 /* Largest tile (agents per work item) of the SIR kernels: 4096.  Words are read with
- * 128-bit loads when an instance's word array is 16-byte aligned and tiles start at
- * multiples of 4 agents (scalar loads otherwise). */
+ * 128-bit loads (16 agents) where a tile's bytes are 16-byte aligned, byte loads
+ * otherwise. */
 ABM_API int32_t abm_sir_tile_agents(void);
 
-/* Per-agent words of one instance from int8 compartments state[n] (n < 2^29): the number
- * of infected neighbours over the CSR is counted; sizes (device int32[3]) receives the
- * S, I, R totals; *status (device int32) becomes 1 on a compartment outside 0..2. */
-ABM_API int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col,
-                         int64_t n, int32_t* words, int32_t* sizes, int32_t* status,
-                         void* stream);
+/* Degree from which an agent's infected-neighbour count lives in hub_counts: 63. */
+ABM_API int32_t abm_sir_hub_degree(void);
 
-/* abm_sir_pack for every tile of `work` at once: the int8 compartments of an instance are
- * read from states8 at the same element offset as its words (insts[i].state) from
- * words_base.  Descriptors must already point at their CSR and words. */
+/* Words of one instance from int8 compartments state[n] (n < 2^29): compartments, hub
+ * marks, infected-neighbour counts over the CSR (row_ptr[n+1], col[row_ptr[n]]); adj
+ * (row_ptr[n] entries, may be col itself) receives the columns with hub tags; words
+ * (16-byte aligned, round_up(n,16) bytes) and hub_counts (int32[n]) as described at
+ * abm_sir_instance; sizes (device int32[3]) receives the S, I, R totals; *status (device
+ * int32) becomes 1 on a compartment outside 0..2 (stored as R) or a column outside 0..n-1
+ * (replaced by a self-loop). */
+ABM_API int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col,
+                         int64_t n, int32_t* adj, uint8_t* words, int32_t* hub_counts,
+                         int32_t* sizes, int32_t* status, void* stream);
+
+/* abm_sir_pack for every tile of `work` at once, in place on each descriptor's adj: the
+ * int8 compartments of an instance are read from states8 at the same byte offset as its
+ * words from words_base.  Descriptors must already point at their CSR, words and hub
+ * counts. */
 ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
-                               int32_t nwork, const int8_t* states8, const int32_t* words_base,
+                               int32_t nwork, const int8_t* states8, const uint8_t* words_base,
                                int32_t* status, void* stream);
 
 /* int8 compartments of n packed words. */
-ABM_API int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream);
+ABM_API int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream);
 
 /* Bytes of the list workspace of abm_sir_steps for up to max_agents live agents (16-byte
  * header {changes, overflow, candidates, 0}, zeroed once by the caller, then 24 bytes per
@@ -243,15 +258,17 @@ ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work
                           const abm_sir_launch* launch, void* changes, size_t changes_bytes,
                           void* stream);
 
-ABM_API size_t abm_sir_run_workspace_bytes(int64_t n);
+/* Workspace of abm_sir_run for n agents and num_edges = row_ptr[n] CSR entries. */
+ABM_API size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges);
 
 /* One SIR model for `steps` steps (the plain engine: one simulation per launch sequence)
  * with the per-step collection keys coll_keys uint32[steps][2] (abm_keychain, ncoll = 1).
- * state int8[n] holds the compartments before the run and receives them after it;
- * counts int32[steps][3]. */
-ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* state,
-                        const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
-                        int32_t* counts, void* workspace, size_t workspace_bytes, void* stream);
+ * The CSR (row_ptr[n+1], col[num_edges]) is only read.  state int8[n] holds the
+ * compartments before the run and receives them after it; counts int32[steps][3]. */
+ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t num_edges,
+                        int8_t* state, const uint32_t* coll_keys, int32_t steps, float beta,
+                        float gamma, int32_t* counts, void* workspace, size_t workspace_bytes,
+                        void* stream);
 
 /* ---- K3/K4: Schelling segregation on a torus Grid ----------------------------------- */
 /* Cell (x, y) of a W x H grid has index x*H + y; grid int8[W*H] holds -1 (empty) or the

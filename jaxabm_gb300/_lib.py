@@ -50,15 +50,16 @@ SIGNATURES = {
     "abm_graph_barabasi_albert": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_graph_random_regular": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_sir_instance_size": (_sz, []),
-    "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p]),
+    "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p, _p, _p]),
     "abm_sir_pack_batch": (_int, [_p, _p, _i32, _p, _p, _p, _p]),
     "abm_sir_unpack": (_int, [_p, _i64, _p, _p]),
     "abm_sir_changes_bytes": (_sz, [_i64]),
     "abm_sir_steps": (_int, [_p, _i32, _p, _i32, _p, _i32, _p, _p, _sz, _p]),
     "abm_sir_default_launch": (_int, [_p]),
     "abm_sir_tile_agents": (_i32, []),
-    "abm_sir_run_workspace_bytes": (_sz, [_i64]),
-    "abm_sir_run": (_int, [_p, _p, _i64, _p, _p, _i32, _f32, _f32, _p, _p, _sz, _p]),
+    "abm_sir_hub_degree": (_i32, []),
+    "abm_sir_run_workspace_bytes": (_sz, [_i64, _i64]),
+    "abm_sir_run": (_int, [_p, _p, _i64, _i64, _p, _p, _i32, _f32, _f32, _p, _p, _sz, _p]),
     "abm_schelling_workspace_bytes": (_sz, [_i64, _i32, _i32]),
     "abm_schelling_place": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _p]),
     "abm_schelling_run": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _i32, _p, _p, _sz, _p]),

@@ -9,23 +9,34 @@
 // All agents read the pre-step states (synchronous update, jaxabm/agent.py:168-177); the
 // S/I/R counts after each step are the metrics (jaxabm/model.py:193-200).
 //
-// Work-efficient ("frontier") formulation.  Each agent has one int32 word
-//     word = (number of infected neighbours << 2) | compartment
-// and a step is four launches:
+// Work-efficient ("frontier") formulation over one byte per agent:
+//     word = (number of infected neighbours << 2) | compartment      (degree < 63)
+//     word = (63 << 2) | compartment, count in hub_counts[i]          (hubs: degree >= 63)
+// One byte per agent keeps the words of a whole 4,096-instance ensemble (~87 MB) inside
+// the 129 MB L2, so the random neighbour reads and count updates of a step are L2 traffic;
+// CSR columns and list entries are read with the streaming (evict-first) policy so that
+// they do not displace the words.  Column entries that point at a hub carry bit 31 (set
+// by abm_sir_pack), so a count update knows where its target's count lives without a
+// further read.  A count update is a 32-bit atomic add on the aligned word holding the
+// target byte: the byte never borrows or carries into its neighbours, because a count
+// never drops below the number of its pre-step infected neighbours that are still to
+// recover, and never exceeds the degree (< 63).
+//
+// A step is four launches:
 //   sweep      over (instance, 4096-agent tile) work items, 16 agents per thread read with
-//              128-bit loads: agents that need a decision are appended to a candidate list
-//              -- susceptible ones with infected neighbours from its front, infected ones
-//              from its back -- with one counter atomic per CTA and tile (block scan for
-//              the offsets).  Everyone else (most agents) costs one 4-byte read.
+//              one 128-bit load: agents that need a decision are appended to a candidate
+//              list -- susceptible ones with infected neighbours from its front, infected
+//              ones from its back -- with one counter atomic per CTA and tile (block scan
+//              for the offsets).  Everyone else (most agents) costs one byte.
 //   candidates one lane per candidate: a susceptible candidate scans its CSR row, eight
 //              column/neighbour loads in flight per pass, stopping at the first firing draw
 //              or once all its infected neighbours were seen (rows longer than 32 slots are
 //              scanned by the whole warp, 32 slots per pass, with warp votes); an infected
 //              candidate draws its recovery.  Changes go to a change list.  Nothing is
 //              written to the words, so every decision sees the pre-step states.
-//   push       one thread per change (one warp for rows longer than 32 slots): adds +-4 to
-//              the word of every neighbour (infected-neighbour count) and +1 to the agent's
-//              own compartment; counts the instance's S->I and I->R transitions.
+//   push       one thread per change (one warp for rows longer than 32 slots): adds +-1 to
+//              the infected-neighbour count of every neighbour and +1 to the agent's own
+//              compartment; counts the instance's S->I and I->R transitions.
 //   finalize   one thread per instance: S/I/R counts of the step from the transitions,
 //              rng = split(rng)[0], t += 1, the next step's collection key, done flag after
 //              the last step; clears the lists.
@@ -38,20 +49,22 @@ namespace {
 
 constexpr int kSirThreads = 256;
 constexpr int kWarpsPerCta = kSirThreads / 32;
-constexpr int kVec = 4;                            // words per 128-bit load
-constexpr int kVecsPerThread = 4;
-constexpr int kPerThread = kVec * kVecsPerThread;  // 16 agents per thread
+constexpr int kPerThread = 16;                     // agents (bytes) per thread: one 128-bit load
 constexpr int kTile = kSirThreads * kPerThread;    // 4096 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr int kChunk = 8;                          // row slots per scan pass
+constexpr int kHubDeg = 63;                        // degree from which a count is a hub count
+constexpr uint32_t kHubMark = 63;                  // count field of a hub's word
+constexpr uint32_t kTag = 0x80000000u;             // column entry of a hub neighbour
+constexpr uint32_t kIdx = 0x7FFFFFFFu;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kS = 0, kI = 1;
+constexpr uint32_t kS = 0, kI = 1;
 
-static_assert(sizeof(abm_sir_instance) == 120, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 136, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
 // Lists workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
-// new compartment}), then `capacity` candidate entries (int4 {inst, agent, word, 0});
+// new compartment}), then `capacity` candidate entries (int4 {inst, agent, count, 0});
 // susceptible candidates fill the candidate array from the front, infected ones from the
 // back (an agent is at most one candidate, so the two never meet).
 struct ListHeader {
@@ -79,6 +92,23 @@ __device__ __forceinline__ int live_count(const int32_t* live, int nwork) {
   return live != nullptr ? min(*live, nwork) : nwork;
 }
 
+// Column entry k of a row, read once (streaming policy: evict first from L1 and L2).
+__device__ __forceinline__ uint32_t ld_col(const int32_t* __restrict__ adj, int k) {
+  return static_cast<uint32_t>(__ldcs(adj + k));
+}
+
+// Adds d to the infected-neighbour count of the agent that column entry v points at.
+__device__ __forceinline__ void add_count(uint8_t* words, int32_t* hubs, uint32_t v, int d) {
+  const uint32_t t = v & kIdx;
+  if (v & kTag) {
+    atomicAdd(hubs + t, d);
+  } else {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(words + t);
+    atomicAdd(reinterpret_cast<unsigned*>(a & ~static_cast<uintptr_t>(3)),
+              static_cast<unsigned>(4 * d) << (8u * static_cast<unsigned>(a & 3)));
+  }
+}
+
 // Warp-aggregated append: lanes with `want` get consecutive slots of *counter.
 __device__ __forceinline__ int warp_append(bool want, int32_t* counter, int lane) {
   const unsigned m = __ballot_sync(kFull, want);
@@ -101,8 +131,12 @@ __global__ void sir_prepare_kernel(abm_sir_instance* __restrict__ insts, int nin
   I->coll[1] = c.y;
 }
 
+__device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4], int j) {
+  return (q[j >> 2] >> (8 * (j & 3))) & 0xFFu;
+}
+
 __global__ void __launch_bounds__(kSirThreads)
-sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
+sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
                  int nwork_max, const int32_t* __restrict__ live, Lists L) {
   __shared__ int swarp[kWarpsPerCta];
   __shared__ int sbase_s, sbase_i;
@@ -110,34 +144,40 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
   const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
-    const abm_sir_instance* I = insts + item.x;
+    abm_sir_instance* I = insts + item.x;
     // finished instances, and instances without an infected agent (nothing can change in
     // them any more: no infection source, no recovery), need no decisions
     if (I->t >= I->steps || I->num_i == 0) continue;  // uniform over the CTA
-    const int32_t* __restrict__ word = I->state;
-    // thread t owns agents begin + v*1024 + 4t + c (v, c < 4): four 128-bit loads when the
-    // words are 16-byte aligned, scalar loads for a partial last vector
-    const bool vec_ok = ((reinterpret_cast<uintptr_t>(word) & 15) == 0) && ((item.y & 3) == 0);
-    int32_t wv[kPerThread];
+    const uint8_t* __restrict__ words = I->words;
+    const int32_t* __restrict__ hubs = I->hub_counts;
+    // thread t owns agents base .. base + 15: one 128-bit load when the bytes are 16-byte
+    // aligned and inside the tile, byte loads otherwise (bytes past the tile read as R)
+    const int base = item.y + kPerThread * threadIdx.x;
+    uint32_t q[4];
+    if (((reinterpret_cast<uintptr_t>(words + base) & 15) == 0) && base + kPerThread <= item.z) {
+      const uint4 v = *reinterpret_cast<const uint4*>(words + base);
+      q[0] = v.x;
+      q[1] = v.y;
+      q[2] = v.z;
+      q[3] = v.w;
+    } else {
 #pragma unroll
-    for (int v = 0; v < kVecsPerThread; ++v) {
-      const int base = item.y + v * (kSirThreads * kVec) + kVec * threadIdx.x;
-      if (vec_ok && base + kVec <= item.z) {
-        const int4 q = *reinterpret_cast<const int4*>(word + base);
-        wv[kVec * v] = q.x;
-        wv[kVec * v + 1] = q.y;
-        wv[kVec * v + 2] = q.z;
-        wv[kVec * v + 3] = q.w;
-      } else {
+      for (int c = 0; c < 4; ++c) {
+        uint32_t r = 0;
 #pragma unroll
-        for (int c = 0; c < kVec; ++c) wv[kVec * v + c] = base + c < item.z ? word[base + c] : 2;
+        for (int b = 0; b < 4; ++b) {
+          const int i = base + 4 * c + b;
+          r |= (i < item.z ? static_cast<uint32_t>(words[i]) : 2u) << (8 * b);
+        }
+        q[c] = r;
       }
     }
     unsigned need_s = 0, need_i = 0;
 #pragma unroll
     for (int j = 0; j < kPerThread; ++j) {
-      const int s = wv[j] & 3;
-      if (s == kS && (wv[j] >> 2) > 0) need_s |= 1u << j;
+      const uint32_t b = byte_of(q, j);
+      const uint32_t s = b & 3u, c = b >> 2;
+      if (s == kS && c != 0 && (c != kHubMark || hubs[base + j] > 0)) need_s |= 1u << j;
       if (s == kI) need_i |= 1u << j;
     }
     // one counter atomic per list, CTA and tile: both counts scanned at once (16 bits each)
@@ -152,27 +192,30 @@ sir_sweep_kernel(const abm_sir_instance* __restrict__ insts, const int4* __restr
     __syncthreads();
     if (threadIdx.x == 0) {
       int total = 0;
-      for (int q = 0; q < kWarpsPerCta; ++q) total += swarp[q];
+      for (int x = 0; x < kWarpsPerCta; ++x) total += swarp[x];
       const int ts = total & 0xFFFF, ti = total >> 16;
       sbase_s = ts ? atomicAdd(&L.hdr->cand_s, ts) : 0;
       sbase_i = ti ? atomicAdd(&L.hdr->cand_i, ti) : 0;
+      if (ts + ti) atomicAdd(&I->candidates, static_cast<unsigned long long>(ts + ti));
     }
     __syncthreads();
     int before = incl - mine;
-    for (int q = 0; q < warp; ++q) before += swarp[q];
+    for (int x = 0; x < warp; ++x) before += swarp[x];
     int pos_s = sbase_s + (before & 0xFFFF);
     int pos_i = sbase_i + (before >> 16);
     __syncthreads();  // swarp/sbase_* are rewritten by the next tile
     if (need_s | need_i) {
 #pragma unroll
       for (int j = 0; j < kPerThread; ++j) {
-        const int i = item.y + (j / kVec) * (kSirThreads * kVec) + kVec * threadIdx.x + (j % kVec);
+        const int i = base + j;
         if ((need_s >> j) & 1u) {
-          if (pos_s < L.capacity) L.cands[pos_s] = make_int4(item.x, i, wv[j], 0);
+          uint32_t c = byte_of(q, j) >> 2;
+          if (c == kHubMark) c = static_cast<uint32_t>(hubs[i]);
+          if (pos_s < L.capacity) L.cands[pos_s] = make_int4(item.x, i, static_cast<int>(c), 0);
           else L.hdr->overflow = 1;
           ++pos_s;
         } else if ((need_i >> j) & 1u) {
-          if (pos_i < L.capacity) L.cands[L.capacity - 1 - pos_i] = make_int4(item.x, i, wv[j], 0);
+          if (pos_i < L.capacity) L.cands[L.capacity - 1 - pos_i] = make_int4(item.x, i, 0, 0);
           else L.hdr->overflow = 1;
           ++pos_i;
         }
@@ -210,7 +253,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   for (int b = wid * 32; b < ni; b += warps * 32) {
     const int k = b + lane;
     const bool valid = k < ni;
-    const int4 e = valid ? L.cands[L.capacity - 1 - k] : make_int4(0, 0, 2, 0);
+    const int4 e = valid ? __ldcs(&L.cands[L.capacity - 1 - k]) : make_int4(0, 0, 0, 0);
     bool changed = false;
     if (valid) {
       const abm_sir_instance* I = insts + e.x;
@@ -226,23 +269,22 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   for (int b = wid * 32; b < ns_count; b += warps * 32) {
     const int k = b + lane;
     const bool valid = k < ns_count;
-    const int4 e = valid ? L.cands[k] : make_int4(0, 0, 2, 0);
+    const int4 e = valid ? __ldcs(&L.cands[k]) : make_int4(0, 0, 0, 0);
     const int inst = e.x, i = e.y;
     const abm_sir_instance* I = insts + inst;
-    int cnt = e.z >> 2;
+    int cnt = e.z;
     bool infected = false, heavy = false;
     int row0 = 0, deg = 0, scanned = 0;
-    uint2 coll = make_uint2(0, 0);
     if (valid) {
-      coll = make_uint2(I->coll[0], I->coll[1]);
       const int32_t* __restrict__ rp = I->row_ptr;
       row0 = rp[i];
       deg = rp[i + 1] - row0;
       if (deg > kHeavyDeg) {
         heavy = true;
       } else {
-        const int32_t* __restrict__ col = I->col;
-        const int32_t* __restrict__ word = I->state;
+        const uint2 coll = make_uint2(I->coll[0], I->coll[1]);
+        const int32_t* __restrict__ adj = I->adj;
+        const uint8_t* __restrict__ words = I->words;
         const float beta = I->beta;
         const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
         // eight slots per pass: the eight column loads, then the eight neighbour-word
@@ -251,14 +293,15 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
         bool done = false;
         for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
           int nb[kChunk];
-          int32_t wn[kChunk];
+          uint32_t wn[kChunk];
 #pragma unroll
-          for (int q = 0; q < kChunk; ++q) nb[q] = k0 + q < deg ? col[row0 + k0 + q] : -1;
+          for (int q = 0; q < kChunk; ++q)
+            nb[q] = k0 + q < deg ? static_cast<int>(ld_col(adj, row0 + k0 + q) & kIdx) : -1;
 #pragma unroll
-          for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? word[nb[q]] : 0;
+          for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? words[nb[q]] : 0u;
 #pragma unroll
           for (int q = 0; q < kChunk; ++q) {
-            if (!done && nb[q] >= 0 && (wn[q] & 3) == kI) {
+            if (!done && nb[q] >= 0 && (wn[q] & 3u) == kI) {
               const int slot = k0 + q;
               if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
                 infected = true;
@@ -286,8 +329,8 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       int remaining = __shfl_sync(kFull, cnt, src);
       const abm_sir_instance* H = insts + hinst;
       const uint2 hcoll = make_uint2(H->coll[0], H->coll[1]);
-      const int32_t* __restrict__ col = H->col;
-      const int32_t* __restrict__ word = H->state;
+      const int32_t* __restrict__ adj = H->adj;
+      const uint8_t* __restrict__ words = H->words;
       const float beta = H->beta;
       const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
@@ -296,7 +339,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
         const int slot = c + lane;
         bool isI = false, f = false;
         if (slot < hdeg) {
-          isI = (word[col[hrow + slot]] & 3) == kI;
+          isI = (words[ld_col(adj, hrow + slot) & kIdx] & 3u) == kI;
           if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
         }
         fired = __any_sync(kFull, f);
@@ -327,28 +370,32 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     int inst = 0, agent = 0, r0 = 0, r1 = 0, delta = 0;
     abm_sir_instance* I = insts;
     if (valid) {
-      const int2 ent = L.changes[k];
+      const int2 ent = __ldcs(&L.changes[k]);
       inst = ent.x;
       agent = ent.y >> 2;
       I = insts + inst;
-      delta = (ent.y & 3) == kI ? 4 : -4;
+      delta = (ent.y & 3) == static_cast<int>(kI) ? 1 : -1;
       r0 = I->row_ptr[agent];
       r1 = I->row_ptr[agent + 1];
-      atomicAdd(&I->state[agent], 1);  // S(0) -> I(1) and I(1) -> R(2) both add one
+      // S(0) -> I(1) and I(1) -> R(2) both add one to the agent's own compartment field
+      const uintptr_t a = reinterpret_cast<uintptr_t>(I->words + agent);
+      atomicAdd(reinterpret_cast<unsigned*>(a & ~static_cast<uintptr_t>(3)),
+                1u << (8u * static_cast<unsigned>(a & 3)));
       atomicAdd(delta > 0 ? &I->step_si : &I->step_ir, 1);
       atomicAdd(&I->edges_pushed, (unsigned long long)(r1 - r0));
     }
     const bool heavy = valid && r1 - r0 > kHeavyDeg;
     if (valid && !heavy) {
-      int32_t* __restrict__ word = I->state;
-      const int32_t* __restrict__ col = I->col;
+      uint8_t* words = I->words;
+      int32_t* hubs = I->hub_counts;
+      const int32_t* __restrict__ adj = I->adj;
       for (int e0 = r0; e0 < r1; e0 += kChunk) {
-        int nb[kChunk];
+        uint32_t nb[kChunk];
 #pragma unroll
-        for (int q = 0; q < kChunk; ++q) nb[q] = e0 + q < r1 ? col[e0 + q] : -1;
+        for (int q = 0; q < kChunk; ++q) nb[q] = e0 + q < r1 ? ld_col(adj, e0 + q) : 0u;
 #pragma unroll
         for (int q = 0; q < kChunk; ++q)
-          if (nb[q] >= 0) atomicAdd(&word[nb[q]], delta);
+          if (e0 + q < r1) add_count(words, hubs, nb[q], delta);
       }
     }
     unsigned hmask = __ballot_sync(kFull, heavy);
@@ -359,9 +406,10 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const int hr0 = __shfl_sync(kFull, r0, src);
       const int hr1 = __shfl_sync(kFull, r1, src);
       const int hdelta = __shfl_sync(kFull, delta, src);
-      int32_t* __restrict__ word = insts[hinst].state;
-      const int32_t* __restrict__ col = insts[hinst].col;
-      for (int e = hr0 + lane; e < hr1; e += 32) atomicAdd(&word[col[e]], hdelta);
+      uint8_t* words = insts[hinst].words;
+      int32_t* hubs = insts[hinst].hub_counts;
+      const int32_t* __restrict__ adj = insts[hinst].adj;
+      for (int e = hr0 + lane; e < hr1; e += 32) add_count(words, hubs, ld_col(adj, e), hdelta);
     }
   }
 }
@@ -404,75 +452,132 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   }
 }
 
-__device__ __forceinline__ int32_t pack_word(const int8_t* __restrict__ st,
-                                             const int32_t* __restrict__ rp,
-                                             const int32_t* __restrict__ col, int i, int s) {
-  int c = 0;
-  for (int k = rp[i]; k < rp[i + 1]; ++k) c += st[col[k]] == kI;
-  return (c << 2) | s;
+// ---- packing: int8 compartments -> words ---------------------------------------------
+
+__host__ __device__ constexpr int64_t round16(int64_t n) { return (n + 15) & ~static_cast<int64_t>(15); }
+
+// Pass 1, agent (or padding byte) i: compartment and hub mark; padding bytes read as R.
+__device__ __forceinline__ int pack_mark(const int8_t* __restrict__ st,
+                                         const int32_t* __restrict__ rp, int n,
+                                         uint8_t* __restrict__ words, int i,
+                                         int32_t* __restrict__ bad) {
+  if (i >= n) {
+    words[i] = 2;
+    return -1;
+  }
+  const int s = st[i];
+  if (s < 0 || s > 2) {
+    atomicExch(bad, 1);
+    words[i] = 2;
+    return -1;
+  }
+  const int deg = rp[i + 1] - rp[i];
+  words[i] = static_cast<uint8_t>((deg >= kHubDeg ? (kHubMark << 2) : 0u) | static_cast<uint32_t>(s));
+  return s;
 }
 
-// word[i] = (infected neighbours << 2) | state[i]; compartment sizes into *sizes.
-__global__ void sir_pack_kernel(const int8_t* __restrict__ state, const int32_t* __restrict__ rp,
-                                const int32_t* __restrict__ col, int n, int32_t* __restrict__ word,
-                                int32_t* __restrict__ sizes, int32_t* __restrict__ bad) {
+// Pass 2, agent i: counts its infected neighbours and writes its column entries with the
+// hub tag of their target (adj may be col itself; col entries may already carry tags).
+// Other threads read this agent's byte meanwhile: only its count bits change, never its
+// compartment or hub mark, so every reader sees the same compartment and mark.
+__device__ __forceinline__ void pack_count(const int32_t* __restrict__ rp, const int32_t* col,
+                                           int32_t* adj, int n, uint8_t* words,
+                                           int32_t* __restrict__ hubs, int i,
+                                           int32_t* __restrict__ bad) {
+  int c = 0;
+  for (int k = rp[i]; k < rp[i + 1]; ++k) {
+    const uint32_t v = static_cast<uint32_t>(col[k]);
+    const uint32_t t = v & kIdx;
+    if (t >= static_cast<uint32_t>(n)) {
+      // out-of-range column: flagged, and replaced by a self-loop so that no step kernel
+      // reads outside the instance
+      atomicExch(bad, 1);
+      adj[k] = static_cast<int32_t>((words[i] >> 2) == kHubMark ? (static_cast<uint32_t>(i) | kTag)
+                                                                : static_cast<uint32_t>(i));
+      continue;
+    }
+    const uint32_t w = words[t];
+    const uint32_t tagged = (w >> 2) == kHubMark ? (t | kTag) : t;
+    if (tagged != v || adj != col) adj[k] = static_cast<int32_t>(tagged);
+    c += (w & 3u) == kI;
+  }
+  const uint32_t own = words[i];
+  if ((own >> 2) == kHubMark) hubs[i] = c;
+  else words[i] = static_cast<uint8_t>(own | (static_cast<uint32_t>(c) << 2));
+}
+
+__global__ void sir_pack_mark_kernel(const int8_t* __restrict__ state,
+                                     const int32_t* __restrict__ rp, int n, int npad,
+                                     uint8_t* __restrict__ words, int32_t* __restrict__ sizes,
+                                     int32_t* __restrict__ bad) {
   __shared__ int sc[3];
   if (threadIdx.x < 3) sc[threadIdx.x] = 0;
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    const int s = state[i];
-    if (s < 0 || s > 2) {
-      atomicExch(bad, 1);
-    } else {
-      word[i] = pack_word(state, rp, col, i, s);
-      atomicAdd(&sc[s], 1);
-    }
+  if (i < npad) {
+    const int s = pack_mark(state, rp, n, words, i, bad);
+    if (s >= 0) atomicAdd(&sc[s], 1);
   }
   __syncthreads();
   if (threadIdx.x < 3 && sc[threadIdx.x]) atomicAdd(&sizes[threadIdx.x], sc[threadIdx.x]);
 }
 
-// The same over the tiles of many instances: the int8 compartments of an instance sit in
-// states8 at the same element offset as its words from words_base.
-__global__ void sir_pack_tiles_kernel(const abm_sir_instance* __restrict__ insts,
-                                      const int4* __restrict__ work, int nwork,
-                                      const int8_t* __restrict__ states8,
-                                      const int32_t* __restrict__ words_base,
-                                      int32_t* __restrict__ bad) {
+__global__ void sir_pack_count_kernel(const int32_t* __restrict__ rp, const int32_t* col,
+                                      int32_t* adj, int n, uint8_t* words,
+                                      int32_t* __restrict__ hubs, int32_t* __restrict__ bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pack_count(rp, col, adj, n, words, hubs, i, bad);
+}
+
+// The same over the tiles of many instances (in place: each descriptor's adj holds its
+// columns).  The int8 compartments of an instance sit in states8 at the same byte offset
+// as its words from words_base.
+__global__ void sir_pack_mark_tiles_kernel(const abm_sir_instance* __restrict__ insts,
+                                           const int4* __restrict__ work, int nwork,
+                                           const int8_t* __restrict__ states8,
+                                           const uint8_t* __restrict__ words_base,
+                                           int32_t* __restrict__ bad) {
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
     const abm_sir_instance* I = insts + item.x;
-    int32_t* word = I->state;
-    const int8_t* st = states8 + (word - words_base);
-    for (int i = item.y + threadIdx.x; i < item.z; i += blockDim.x) {
-      const int s = st[i];
-      if (s < 0 || s > 2) {
-        atomicExch(bad, 1);
-        continue;
-      }
-      word[i] = pack_word(st, I->row_ptr, I->col, i, s);
-    }
+    uint8_t* words = I->words;
+    const int8_t* st = states8 + (words - words_base);
+    const int end = item.z == I->n ? static_cast<int>(round16(I->n)) : item.z;
+    for (int i = item.y + threadIdx.x; i < end; i += blockDim.x)
+      pack_mark(st, I->row_ptr, I->n, words, i, bad);
   }
 }
 
-__global__ void sir_unpack_kernel(const int32_t* __restrict__ word, int n, int8_t* __restrict__ out) {
+__global__ void sir_pack_count_tiles_kernel(const abm_sir_instance* __restrict__ insts,
+                                            const int4* __restrict__ work, int nwork,
+                                            int32_t* __restrict__ bad) {
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int4 item = work[w];
+    const abm_sir_instance* I = insts + item.x;
+    for (int i = item.y + threadIdx.x; i < item.z; i += blockDim.x)
+      pack_count(I->row_ptr, I->adj, I->adj, I->n, I->words, I->hub_counts, i, bad);
+  }
+}
+
+__global__ void sir_unpack_kernel(const uint8_t* __restrict__ words, int n,
+                                  int8_t* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (int8_t)(word[i] & 3);
+  if (i < n) out[i] = static_cast<int8_t>(words[i] & 3u);
 }
 
 // Single-instance descriptor and tile list written on the device, so abm_sir_run makes
 // no host-to-device copy and can be captured in a CUDA graph.
 __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int ntiles,
-                                       const int32_t* row_ptr, const int32_t* col, int32_t* words,
-                                       int32_t* counts, const uint32_t* coll_keys, int32_t n,
-                                       int32_t steps, float beta, float gamma,
-                                       const int32_t* sizes) {
+                                        const int32_t* row_ptr, int32_t* adj, uint8_t* words,
+                                        int32_t* hubs, int32_t* counts,
+                                        const uint32_t* coll_keys, int32_t n, int32_t steps,
+                                        float beta, float gamma, const int32_t* sizes) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g == 0) {
     d->row_ptr = row_ptr;
-    d->col = col;
-    d->state = words;
+    d->adj = adj;
+    d->words = words;
+    d->hub_counts = hubs;
     d->counts = counts;
     d->done_flag = nullptr;
     d->coll_keys = coll_keys;
@@ -490,6 +595,7 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->step_ir = 0;
     d->edges_scanned = 0;
     d->edges_pushed = 0;
+    d->candidates = 0;
     d->coll[0] = 0;
     d->coll[1] = 0;
   }
@@ -537,6 +643,8 @@ size_t abm_sir_instance_size(void) { return sizeof(abm_sir_instance); }
 
 int32_t abm_sir_tile_agents(void) { return kTile; }
 
+int32_t abm_sir_hub_degree(void) { return kHubDeg; }
+
 int abm_sir_default_launch(abm_sir_launch* out) {
   if (!out) return ABM_ERR_BADARG;
   out->sweep_grid = resident_grid(sir_sweep_kernel, 4);
@@ -553,9 +661,12 @@ size_t abm_sir_changes_bytes(int64_t max_agents) {
 }
 
 int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
-                 int32_t* words, int32_t* sizes, int32_t* status, void* stream) {
-  if (!state || !row_ptr || !col || !words || !sizes || !status || n <= 0 || n >= (1ll << 29))
+                 int32_t* adj, uint8_t* words, int32_t* hub_counts, int32_t* sizes,
+                 int32_t* status, void* stream) {
+  if (!state || !row_ptr || !col || !adj || !words || !hub_counts || !sizes || !status ||
+      n <= 0 || n >= (1ll << 29))
     return ABM_ERR_BADARG;
+  if (!abm_host::aligned(words, 16)) return ABM_ERR_BADARG;
   cudaStream_t s = abm_host::as_stream(stream);
   int st = abm_host::record_cuda_error(cudaMemsetAsync(sizes, 0, 3 * sizeof(int32_t), s),
                                        "abm_sir_pack/sizes");
@@ -563,13 +674,17 @@ int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col
   st = abm_host::record_cuda_error(cudaMemsetAsync(status, 0, sizeof(int32_t), s),
                                    "abm_sir_pack/status");
   if (st) return st;
-  sir_pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(state, row_ptr, col, (int)n, words,
-                                                             sizes, status);
-  return abm_host::check_launch("abm_sir_pack");
+  const int64_t npad = round16(n);
+  sir_pack_mark_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(
+      state, row_ptr, (int)n, (int)npad, words, sizes, status);
+  if ((st = abm_host::check_launch("abm_sir_pack/mark"))) return st;
+  sir_pack_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(row_ptr, col, adj, (int)n,
+                                                                   words, hub_counts, status);
+  return abm_host::check_launch("abm_sir_pack/count");
 }
 
 int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work, int32_t nwork,
-                       const int8_t* states8, const int32_t* words_base, int32_t* status,
+                       const int8_t* states8, const uint8_t* words_base, int32_t* status,
                        void* stream) {
   if (!insts || !work || nwork <= 0 || !states8 || !words_base || !status) return ABM_ERR_BADARG;
   if (!abm_host::aligned(insts, 8) || !abm_host::aligned(work, 16)) return ABM_ERR_BADARG;
@@ -577,12 +692,17 @@ int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
   int st = abm_host::record_cuda_error(cudaMemsetAsync(status, 0, sizeof(int32_t), s),
                                        "abm_sir_pack_batch/status");
   if (st) return st;
-  sir_pack_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(
-      insts, reinterpret_cast<const int4*>(work), nwork, states8, words_base, status);
-  return abm_host::check_launch("abm_sir_pack_batch");
+  const int4* w4 = reinterpret_cast<const int4*>(work);
+  sir_pack_mark_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(insts, w4, nwork,
+                                                                         states8, words_base,
+                                                                         status);
+  if ((st = abm_host::check_launch("abm_sir_pack_batch/mark"))) return st;
+  sir_pack_count_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(insts, w4, nwork,
+                                                                          status);
+  return abm_host::check_launch("abm_sir_pack_batch/count");
 }
 
-int abm_sir_unpack(const int32_t* words, int64_t n, int8_t* state, void* stream) {
+int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream) {
   if (!words || !state || n <= 0 || n >= (1ll << 29)) return ABM_ERR_BADARG;
   sir_unpack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, abm_host::as_stream(stream)>>>(
       words, (int)n, state);
@@ -633,21 +753,22 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   return ABM_OK;
 }
 
-size_t abm_sir_run_workspace_bytes(int64_t n) {
-  if (n <= 0) return 0;
+size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges) {
+  if (n <= 0 || num_edges < 0) return 0;
   const int64_t tiles = (n + kTile - 1) / kTile;
   return align256(sizeof(abm_sir_instance)) + align256((size_t)tiles * sizeof(int4)) +
-         align256((size_t)n * sizeof(int32_t)) + 256 + align256(abm_sir_changes_bytes(n));
+         align256((size_t)round16(n)) + align256((size_t)n * sizeof(int32_t)) + 256 +
+         align256((size_t)num_edges * sizeof(int32_t)) + align256(abm_sir_changes_bytes(n));
 }
 
-int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* state,
-                const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
+int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t num_edges,
+                int8_t* state, const uint32_t* coll_keys, int32_t steps, float beta, float gamma,
                 int32_t* counts, void* workspace, size_t workspace_bytes, void* stream) {
   if (!row_ptr || !col || !state || !coll_keys || !counts || n <= 0 || n >= (1ll << 29) ||
-      steps < 0)
+      num_edges < 0 || num_edges >= (1ll << 31) || steps < 0)
     return ABM_ERR_BADARG;
   if (!abm_host::aligned(coll_keys, 8)) return ABM_ERR_BADARG;
-  const size_t need = abm_sir_run_workspace_bytes(n);
+  const size_t need = abm_sir_run_workspace_bytes(n, num_edges);
   if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 256))
     return ABM_ERR_WORKSPACE;
   if (steps == 0) return ABM_OK;
@@ -658,19 +779,23 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int8_t* s
   const int ntiles = (int)((n + kTile - 1) / kTile);
   int4* work = reinterpret_cast<int4*>(p);
   p += align256((size_t)ntiles * sizeof(int4));
-  int32_t* words = reinterpret_cast<int32_t*>(p);
+  uint8_t* words = reinterpret_cast<uint8_t*>(p);
+  p += align256((size_t)round16(n));
+  int32_t* hubs = reinterpret_cast<int32_t*>(p);
   p += align256((size_t)n * sizeof(int32_t));
   int32_t* misc = reinterpret_cast<int32_t*>(p);  // sizes[3], status
   p += 256;
+  int32_t* adj = reinterpret_cast<int32_t*>(p);
+  p += align256((size_t)num_edges * sizeof(int32_t));
   void* lists = p;
-  int st = abm_sir_pack(state, row_ptr, col, n, words, misc, misc + 3, stream);
+  int st = abm_sir_pack(state, row_ptr, col, n, adj, words, hubs, misc, misc + 3, stream);
   if (st) return st;
   st = abm_host::record_cuda_error(cudaMemsetAsync(lists, 0, sizeof(ListHeader), s),
                                    "abm_sir_run/lists");
   if (st) return st;
   sir_setup_single_kernel<<<(ntiles + 255) / 256, 256, 0, s>>>(
-      d, work, ntiles, row_ptr, col, words, counts, coll_keys, (int32_t)n, steps, beta, gamma,
-      misc);
+      d, work, ntiles, row_ptr, adj, words, hubs, counts, coll_keys, (int32_t)n, steps, beta,
+      gamma, misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
   st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps,

@@ -25,15 +25,16 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 4096  # agents per work item (abm_sir_tile_agents)
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 120 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 136 bytes
 INSTANCE_DTYPE = np.dtype([
-    ("row_ptr", "<u8"), ("col", "<u8"), ("state", "<u8"), ("counts", "<u8"),
-    ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)), ("n", "<i4"),
-    ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"), ("num_s", "<i4"),
-    ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"), ("step_ir", "<i4"),
-    ("edges_scanned", "<u8"), ("edges_pushed", "<u8"), ("coll", "<u4", (2,)),
+    ("row_ptr", "<u8"), ("adj", "<u8"), ("words", "<u8"), ("hub_counts", "<u8"),
+    ("counts", "<u8"), ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)),
+    ("n", "<i4"), ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"),
+    ("num_s", "<i4"), ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"),
+    ("step_ir", "<i4"), ("edges_scanned", "<u8"), ("edges_pushed", "<u8"),
+    ("candidates", "<u8"), ("coll", "<u4", (2,)),
 ])
-assert INSTANCE_DTYPE.itemsize == 120
+assert INSTANCE_DTYPE.itemsize == 136
 WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
@@ -92,19 +93,26 @@ def changes_overflowed(ws):
     return int(ws[4:8].view(torch.int32).item()) != 0
 
 
-def pack_words(state_i8, row_ptr, col, words, stream=None):
-    """Per-agent words (infected-neighbour count << 2 | compartment) of one instance."""
+def word_bytes(n):
+    """Bytes of an instance's word array: one per agent, padded to a multiple of 16."""
+    return (int(n) + 15) // 16 * 16
+
+
+def pack_words(state_i8, row_ptr, col, adj, words, hub_counts, stream=None):
+    """Per-agent words of one instance (compartment, hub mark, infected-neighbour count),
+    the hub counts and the hub-tagged columns ``adj`` (may be ``col`` itself)."""
     n = state_i8.numel()
     scratch = torch.zeros(4, dtype=torch.int32, device=words.device)
     _lib.call("abm_sir_pack", _dev.ptr(state_i8), _dev.ptr(row_ptr), _dev.ptr(col), n,
-              _dev.ptr(words), _dev.ptr(scratch), _dev.ptr(scratch[3:]), _dev.stream_handle(stream))
+              _dev.ptr(adj), _dev.ptr(words), _dev.ptr(hub_counts), _dev.ptr(scratch),
+              _dev.ptr(scratch[3:]), _dev.stream_handle(stream))
     return scratch
 
 
-def unpack_words(words, stream=None):
-    out = torch.empty(words.numel(), dtype=torch.int8, device=words.device)
-    _lib.call("abm_sir_unpack", _dev.ptr(words), words.numel(), _dev.ptr(out),
-              _dev.stream_handle(stream))
+def unpack_words(words, n=None, stream=None):
+    n = words.numel() if n is None else int(n)
+    out = torch.empty(n, dtype=torch.int8, device=words.device)
+    _lib.call("abm_sir_unpack", _dev.ptr(words), n, _dev.ptr(out), _dev.stream_handle(stream))
     return out
 
 
@@ -129,8 +137,8 @@ class SIRBatch:
         self.e = np.array([len(c) for _, c in graphs], dtype=np.int64)
         rp_off = np.concatenate([[0], np.cumsum(self.n + 1)])
         col_off = np.concatenate([[0], np.cumsum(self.e)])
-        # word arrays start 16-byte aligned (128-bit loads): pad each to a multiple of 4
-        w_off = np.concatenate([[0], np.cumsum((self.n + 3) // 4 * 4)])
+        # word arrays (one byte per agent) start 16-byte aligned and are padded to 16 bytes
+        w_off = np.concatenate([[0], np.cumsum((self.n + 15) // 16 * 16)])
         cnt_off = np.arange(k + 1, dtype=np.int64) * self.steps * 3
         h_rp = np.empty(rp_off[-1], dtype=np.int32)
         h_col = np.empty(col_off[-1], dtype=np.int32)
@@ -143,7 +151,8 @@ class SIRBatch:
         self.row_ptr = torch.from_numpy(h_rp).to(dev)
         self.col = torch.from_numpy(h_col).to(dev)
         self.state8 = torch.from_numpy(h_st).to(dev)
-        self.words = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
+        self.words = torch.empty(int(w_off[-1]), dtype=torch.uint8, device=dev)
+        self.hub_counts = torch.zeros(int(w_off[-1]), dtype=torch.int32, device=dev)
         self.counts = torch.zeros(int(cnt_off[-1]), dtype=torch.int32, device=dev)
         self._offsets = (rp_off, col_off, w_off, cnt_off)
         sizes = np.array([[int((st == c).sum()) for c in (0, 1, 2)] for st in init_states],
@@ -151,8 +160,9 @@ class SIRBatch:
         self.s0 = sizes[:, 0].astype(np.int64)
         desc = np.zeros(k, dtype=INSTANCE_DTYPE)
         desc["row_ptr"] = self.row_ptr.data_ptr() + 4 * rp_off[:-1]
-        desc["col"] = self.col.data_ptr() + 4 * col_off[:-1]
-        desc["state"] = self.words.data_ptr() + 4 * w_off[:-1]
+        desc["adj"] = self.col.data_ptr() + 4 * col_off[:-1]
+        desc["words"] = self.words.data_ptr() + w_off[:-1]
+        desc["hub_counts"] = self.hub_counts.data_ptr() + 4 * w_off[:-1]
         desc["counts"] = self.counts.data_ptr() + 4 * cnt_off[:-1]
         desc["n"] = self.n
         desc["steps"] = self.steps
@@ -170,20 +180,23 @@ class SIRBatch:
         if int(self._status.item()) != 0:
             raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
         self.words0 = self.words.clone()
+        self.hub_counts0 = self.hub_counts.clone()
         self.changes = changes_workspace(int(self.n.sum()))
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_steps = None
 
     def pack(self, stream=None):
-        """Words of every instance from the int8 compartments in ``state8`` (one launch)."""
+        """Words and hub counts of every instance from the int8 compartments in ``state8``;
+        tags the hub entries of ``col`` in place (two launches)."""
         _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(self.work),
                   self.work.shape[0], _dev.ptr(self.state8), _dev.ptr(self.words),
                   _dev.ptr(self._status), _dev.stream_handle(stream))
 
     def load_host(self, h_row_ptr, h_col, h_state8, stream=None):
         """Inputs from (pinned) host buffers laid out like ``row_ptr``/``col``/``state8``:
-        copy them in, rebuild the words and rewind every instance to step 0."""
+        copy them in, rebuild the words, hub counts and column tags, and rewind every
+        instance to step 0."""
         self.row_ptr.copy_(h_row_ptr, non_blocking=True)
         self.col.copy_(h_col, non_blocking=True)
         self.state8.copy_(h_state8, non_blocking=True)
@@ -197,6 +210,7 @@ class SIRBatch:
     def reset(self):
         """Back to step 0 (words, counters, key chains) without reallocating."""
         self.words.copy_(self.words0)
+        self.hub_counts.copy_(self.hub_counts0)
         self.desc.copy_(self.desc0)
 
     def launch(self, nsteps, stream=None):
@@ -256,12 +270,13 @@ class SIRBatch:
         return 4 * self.steps
 
     def edge_stats(self):
-        """(CSR slots read by decide, CSR slots read by push, compartment changes) since
-        the last reset, summed over instances."""
+        """(CSR slots read by decide, CSR slots read by push, compartment changes,
+        decision candidates) since the last reset, summed over instances."""
         d = self.desc.cpu().numpy().view(INSTANCE_DTYPE).reshape(-1)
         changes = int((d["num_i"] + 2 * d["num_r"]).sum() - (self.h_state0 == 1).sum()
                       - 2 * (self.h_state0 == 2).sum())
-        return int(d["edges_scanned"].sum()), int(d["edges_pushed"].sum()), changes
+        return (int(d["edges_scanned"].sum()), int(d["edges_pushed"].sum()), changes,
+                int(d["candidates"].sum()))
 
     def live_agent_steps(self):
         """Agent-steps the sweep reads: steps of an instance that start with at least one
@@ -273,13 +288,14 @@ class SIRBatch:
         return int(((i_before > 0).sum(axis=1) * self.n).sum())
 
     def algorithmic_bytes(self):
-        """Bytes the run must move (after it completed), at 4-byte granularity: per live
-        agent-step its 4-byte word; per CSR slot read by the candidates kernel 8 bytes
-        (column index + neighbour word); per slot pushed 12 bytes (column index + atomic
-        read-modify-write); per compartment change 32 bytes (list entry write and read, row
-        offsets, own word update)."""
-        scanned, pushed, changes = self.edge_stats()
-        return int(4 * self.live_agent_steps() + 8 * scanned + 12 * pushed + 32 * changes)
+        """Bytes the run must move (after it completed), each datum at its own size: per
+        live agent-step its 1-byte word; per decision candidate its 8-byte list entry; per
+        CSR slot read by the candidates kernel 5 bytes (4-byte column + neighbour word);
+        per slot pushed 6 bytes (column + count read and write); per compartment change 18
+        bytes (8-byte list entry, 8-byte row offsets, own word read and write)."""
+        scanned, pushed, changes, cands = self.edge_stats()
+        return int(self.live_agent_steps() + 8 * cands + 5 * scanned + 6 * pushed
+                   + 18 * changes)
 
 
 # ---- the batched-ensemble workload (4,096 SIR instances) -------------------------------

@@ -28,7 +28,8 @@ import torch
 from . import _dev
 from . import _lib
 from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, changes_workspace,
-                       check_layout, launch_struct, model_rngs, pack_words, unpack_words)
+                       check_layout, launch_struct, model_rngs, pack_words, unpack_words,
+                       word_bytes)
 
 
 class Request:
@@ -57,7 +58,8 @@ class Request:
 
     def device_bytes(self):
         n, e = self.n, len(self.col)
-        return 4 * (n + 1) + 4 * e + 5 * n + 12 * self.steps
+        # CSR, int8 compartments, word bytes (padded to 16), hub counts, per-step counts
+        return 4 * (n + 1) + 4 * e + n + (n + 15) // 16 * 16 + 4 * n + 12 * self.steps
 
     @property
     def latency(self):
@@ -164,15 +166,17 @@ class SIRServer:
             rp = torch.as_tensor(req.row_ptr).to(dev, non_blocking=True)
             col = torch.as_tensor(req.col).to(dev, non_blocking=True)
             st8 = torch.as_tensor(req.state).to(dev, non_blocking=True)
-            st = torch.empty(req.n, dtype=torch.int32, device=dev)
-            pack_words(st8, rp, col, st, s)
+            st = torch.empty(word_bytes(req.n), dtype=torch.uint8, device=dev)
+            hubs = torch.empty(req.n, dtype=torch.int32, device=dev)
+            pack_words(st8, rp, col, col, st, hubs, s)
             counts = torch.zeros(req.steps * 3, dtype=torch.int32, device=dev)
             rng = model_rngs([req.seed])
         host_state = np.asarray(req.state)
         row = np.zeros(1, dtype=INSTANCE_DTYPE)
         row["row_ptr"] = rp.data_ptr()
-        row["col"] = col.data_ptr()
-        row["state"] = st.data_ptr()
+        row["adj"] = col.data_ptr()
+        row["words"] = st.data_ptr()
+        row["hub_counts"] = hubs.data_ptr()
         row["counts"] = counts.data_ptr()
         row["done_flag"] = self.done.data_ptr() + 4 * slot
         row["n"] = req.n
@@ -189,7 +193,7 @@ class SIRServer:
             self.desc[slot].copy_(self.h_desc[slot], non_blocking=True)
             self.desc[slot, RNG_WORD:RNG_WORD + 2] = rng[0]
         req._slot = slot
-        req._bufs = (rp, col, st, counts)
+        req._bufs = (rp, col, st, hubs, counts)
         req.admitted = time.perf_counter()
         self.active[slot] = req
         self._tiles_used += self._tiles(req)
@@ -224,13 +228,13 @@ class SIRServer:
         finished = [slot for slot in self.active if int(self.done[slot]) == 1]
         for slot in finished:
             req = self.active.pop(slot)
-            rp, col, st, counts = req._bufs
+            rp, col, st, hubs, counts = req._bufs
             with torch.cuda.stream(self.stream):
                 req.counts = torch.empty((req.steps, 3), dtype=torch.int32).pin_memory()
                 req.counts.copy_(counts.view(req.steps, 3), non_blocking=True)
                 if req.keep_state:
                     req.final_state = torch.empty(req.n, dtype=torch.int8).pin_memory()
-                    req.final_state.copy_(unpack_words(st, self.stream), non_blocking=True)
+                    req.final_state.copy_(unpack_words(st, req.n, self.stream), non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
             req._event = ev

@@ -10,8 +10,10 @@ Agent semantics (partitionable ``jax.random``; agent ``i`` holds
     R: stays R
 
 with the compartments' counts ``S``, ``I``, ``R`` recorded after every step.  The step runs
-in ``abm_sir_run``/``abm_sir_steps`` (one thread per agent, warp-cooperative scans of rows
-longer than 32 slots).
+in ``abm_sir_run``/``abm_sir_steps``: one byte per agent holds its compartment and its
+number of infected neighbours, so only agents that can change (susceptible agents with an
+infected neighbour, infected agents) read their CSR row or draw, and each change updates
+its neighbours' counts.
 """
 
 import ctypes
@@ -91,8 +93,9 @@ class SIRKernel(StepKernel):
         n = st.numel()
         rp, col = env["network_row_ptr"], env["network_col"]
         counts = torch.empty((steps, 3), dtype=torch.int32, device=st.device)
-        ws = _dev.workspace(_lib.load().abm_sir_run_workspace_bytes(n))
-        _lib.call("abm_sir_run", _dev.ptr(rp), _dev.ptr(col), n, _dev.ptr(st),
+        e = col.numel()
+        ws = _dev.workspace(_lib.load().abm_sir_run_workspace_bytes(n, e))
+        _lib.call("abm_sir_run", _dev.ptr(rp), _dev.ptr(col), n, e, _dev.ptr(st),
                   _dev.ptr(coll_keys), steps, float(params["beta"]), float(params["gamma"]),
                   _dev.ptr(counts), _dev.ptr(ws), ws.numel(), _dev.stream_handle())
         return {"state": st}, counts

@@ -24,7 +24,8 @@ def _graph(kind, n, seed=0):
         return rp, col
     if kind == "rr":
         return sir.random_regular(n, 16, seed)
-    if kind == "clique":  # every row 63 long: every S agent takes the warp path
+    if kind == "clique":  # n = 64: every row 63 long, every agent a hub (count in hub_counts)
+        # n = 63: every row 62 long, the longest row whose count lives in the agent's byte
         rp = (np.arange(n + 1) * (n - 1)).astype(np.int32)
         col = np.concatenate([np.delete(np.arange(n), i) for i in range(n)]).astype(np.int32)
         return rp, col
@@ -41,26 +42,30 @@ def _run_abi(rp, col, st0, seed, steps, beta, gamma):
     drp = torch.from_numpy(rp).cuda()
     dcol = torch.from_numpy(col).cuda()
     counts = torch.empty((steps, 3), dtype=torch.int32, device="cuda")
-    wsb = _lib.load().abm_sir_run_workspace_bytes(n)
+    wsb = _lib.load().abm_sir_run_workspace_bytes(n, len(col))
     ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
-    _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, _dev.ptr(buf), _dev.ptr(ck), steps,
+    _lib.call("abm_sir_run", _dev.ptr(drp), _dev.ptr(dcol), n, len(col), _dev.ptr(buf),
+              _dev.ptr(ck), steps,
               beta, gamma, _dev.ptr(counts), _dev.ptr(ws), wsb, None)
     torch.cuda.synchronize()
     fin = buf.cpu().numpy()
     return fin, counts.cpu().numpy()
 
 
-@pytest.mark.parametrize("kind,n,steps,beta,gamma", [
-    ("ba2", 200, 30, 0.3, 0.1),
-    ("ba", 5000, 60, 0.05, 0.1),
-    ("star", 3000, 25, 0.02, 0.05),
-    ("clique", 64, 20, 0.01, 0.2),
-    ("rr", 4096, 40, 0.1, 0.2),
+@pytest.mark.parametrize("kind,n,steps,beta,gamma,frac", [
+    ("ba2", 200, 30, 0.3, 0.1, 0.01),
+    ("ba", 5000, 60, 0.05, 0.1, 0.01),
+    ("ba", 30000, 40, 0.02, 0.05, 0.3),   # many hubs with many infected neighbours
+    ("star", 3000, 25, 0.02, 0.05, 0.01),
+    ("clique", 64, 20, 0.01, 0.2, 0.01),
+    ("clique", 64, 12, 0.002, 0.02, 0.6),
+    ("clique", 63, 12, 0.002, 0.02, 0.6),  # byte counts near their 62 limit
+    ("rr", 4096, 40, 0.1, 0.2, 0.01),
 ])
-def test_sir_abi_bit_exact(cuda, kind, n, steps, beta, gamma):
+def test_sir_abi_bit_exact(cuda, kind, n, steps, beta, gamma, frac):
     from jaxabm_gb300 import sir
     rp, col = _graph(kind, n)
-    st0 = sir.initial_states(n, 0.01, 1)
+    st0 = sir.initial_states(n, frac, 1)
     fin, counts = _run_abi(rp, col, st0, 7, steps, beta, gamma)
     rng, _ = models.model_keys(7, 1)
     ref_st, ref_counts, _ = coracle.sir_run(rp, col, st0, rng, steps, beta, gamma)
@@ -135,5 +140,5 @@ def test_sir_bad_args(cuda):
     from jaxabm_gb300 import _lib
     L = _lib.load()
     assert L.abm_sir_steps(None, 1, None, 0, None, 1, 0, None, 0, None) == _lib.ABM_ERR_BADARG
-    assert L.abm_sir_run(None, None, 10, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
+    assert L.abm_sir_run(None, None, 10, 0, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
         _lib.ABM_ERR_BADARG
