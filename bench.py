@@ -134,7 +134,7 @@ def _reduce(v, world, op):
 class SIREnsembleBench:
     name = "sir_ensemble_4096_ba_m4_n1e3_1e5_t365"
 
-    def __init__(self, rank, count=4096, steps=365):
+    def __init__(self, rank, count=4096, steps=365, grids=None):
         from jaxabm_gb300 import ensemble
         self.ensemble = ensemble
         self.count, self.T = count, steps
@@ -147,7 +147,13 @@ class SIREnsembleBench:
                                        spec["seed"], steps)
         from jaxabm_gb300 import autotune
         t0 = time.perf_counter()
-        self.launch = autotune.tune_sir_batch(self.batch)
+        if grids is None:
+            self.launch = autotune.tune_sir_batch(self.batch)
+            self.picked_by = "jaxabm_gb300.autotune"
+        else:
+            self.batch.set_launch(grids)
+            self.launch = tuple(grids)
+            self.picked_by = "--grids"
         self.tune_s = time.perf_counter() - t0
         self.batch.capture(steps)
         self.units_per_step = self.batch.agent_steps
@@ -387,7 +393,8 @@ def run_ours(args):
     import jaxabm_gb300 as jx
     jx.set_verbose(False)
     jx.build()
-    wl = WORKLOADS[args.workload](rank, count=args.instances)
+    grids = None if not args.grids else tuple(int(v) for v in args.grids.split(","))
+    wl = WORKLOADS[args.workload](rank, count=args.instances, grids=grids)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         wl.reset()
@@ -468,7 +475,7 @@ def run_ours(args):
         out["models"] = model_lines()
     out["setup_s"] = {"graph_build": wl.build_s, "autotune": wl.tune_s}
     out["config"]["launch_grids"] = {"sweep": wl.launch[0], "candidates": wl.launch[1],
-                                     "push": wl.launch[2], "picked_by": "jaxabm_gb300.autotune"}
+                                     "push": wl.launch[2], "picked_by": wl.picked_by}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -533,6 +540,9 @@ def main():
     ap.add_argument("--instances", type=int, default=4096,
                     help="ensemble members (the first K of the 4,096-member specification); "
                          "smaller values are for profiling captures")
+    ap.add_argument("--grids", default=None,
+                    help="fixed sweep,candidates,push grid sizes instead of the autotuner "
+                         "(profiling captures: keeps the launch sequence short)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

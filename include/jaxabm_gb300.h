@@ -220,7 +220,7 @@ ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_ite
 ABM_API int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream);
 
 /* Bytes of the list workspace of abm_sir_steps for up to max_agents live agents (16-byte
- * header {changes, overflow, candidates, 0}, zeroed once by the caller, then 24 bytes per
+ * header {changes, overflow, candidates, 0}, zeroed once by the caller, then 16 bytes per
  * agent: a change list and a candidate list). */
 ABM_API size_t abm_sir_changes_bytes(int64_t max_agents);
 
@@ -246,7 +246,7 @@ ABM_API int abm_sir_default_launch(abm_sir_launch* out);
  *   I -> R if uniform(k_rec) < gamma.
  * A susceptible agent whose word says it has no infected neighbour reads nothing else;
  * changes are pushed to the neighbours' words after all decisions (four launches per
- * step: sweep, candidates, push, finalize).  `changes` must hold abm_sir_changes_bytes(total agents
+ * step: sweep, candidates, push, finalize).  At most 2^26 instances.  `changes` must hold abm_sir_changes_bytes(total agents
  * of all live instances); its overflow flag is set (and changes dropped) if it is smaller.
  * Replaces Model.step's AgentCollection.update (jaxabm/model.py:163-171,
  * jaxabm/agent.py:132-179) for the SIR agent, batched over instances (the serial loops of

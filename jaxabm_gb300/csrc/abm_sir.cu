@@ -14,8 +14,8 @@
 //     word = (63 << 2) | compartment, count in hub_counts[i]          (hubs: degree >= 63)
 // One byte per agent keeps the words of a whole 4,096-instance ensemble (~87 MB) inside
 // the 129 MB L2, so the random neighbour reads and count updates of a step are L2 traffic;
-// CSR columns and list entries are read with the streaming (evict-first) policy so that
-// they do not displace the words.  Column entries that point at a hub carry bit 31 (set
+// CSR columns, row offsets and change entries are read with the streaming (evict-first)
+// policy so that they do not displace the words.  Column entries that point at a hub carry bit 31 (set
 // by abm_sir_pack), so a count update knows where its target's count lives without a
 // further read.  A count update is a 32-bit atomic add on the aligned word holding the
 // target byte: the byte never borrows or carries into its neighbours, because a count
@@ -23,20 +23,21 @@
 // recover, and never exceeds the degree (< 63).
 //
 // A step is four launches:
-//   sweep      over (instance, 4096-agent tile) work items, 16 agents per thread read with
-//              one 128-bit load: agents that need a decision are appended to a candidate
-//              list -- susceptible ones with infected neighbours from its front, infected
-//              ones from its back -- with one counter atomic per CTA and tile (block scan
-//              for the offsets).  Everyone else (most agents) costs one byte.
-//   candidates one lane per candidate: a susceptible candidate scans its CSR row, eight
-//              column/neighbour loads in flight per pass, stopping at the first firing draw
-//              or once all its infected neighbours were seen (rows longer than 32 slots are
-//              scanned by the whole warp, 32 slots per pass, with warp votes); an infected
-//              candidate draws its recovery.  Changes go to a change list.  Nothing is
-//              written to the words, so every decision sees the pre-step states.
+//   sweep      over (instance, 4096-agent tile) work items, 16 agents per lane read with
+//              one 128-bit load.  Infected agents draw their recovery right there (each
+//              warp queues its infected agents in shared memory and draws them one lane
+//              each); susceptible agents with infected neighbours are appended to a
+//              candidate list in agent order (8-byte entries; one counter atomic per CTA
+//              and tile).  Everyone else (most agents) costs one byte.
+//   candidates one lane per candidate: it scans its CSR row, eight column/neighbour loads
+//              in flight per pass, stopping at the first firing draw or once all its
+//              infected neighbours were seen (rows longer than 32 slots are scanned by the
+//              whole warp, 128 slots per pass, with warp votes).  Changes of both kernels
+//              go to a change list; no word is written, so every decision sees the
+//              pre-step states.
 //   push       one thread per change (one warp for rows longer than 32 slots): adds +-1 to
 //              the infected-neighbour count of every neighbour and +1 to the agent's own
-//              compartment; counts the instance's S->I and I->R transitions.
+//              compartment.
 //   finalize   one thread per instance: S/I/R counts of the step from the transitions,
 //              rng = split(rng)[0], t += 1, the next step's collection key, done flag after
 //              the last step; clears the lists.
@@ -49,35 +50,37 @@ namespace {
 
 constexpr int kSirThreads = 256;
 constexpr int kWarpsPerCta = kSirThreads / 32;
-constexpr int kPerThread = 16;                     // agents (bytes) per thread: one 128-bit load
+constexpr int kPerThread = 16;                     // agents (bytes) per lane: one 128-bit load
+constexpr int kSub = 32 * kPerThread;              // 512 agents per warp and tile
 constexpr int kTile = kSirThreads * kPerThread;    // 4096 agents per work item
 constexpr int kHeavyDeg = 32;
+constexpr int kHeavyUnroll = 4;                    // slots per lane per pass of a warp row scan
 constexpr int kChunk = 8;                          // row slots per scan pass
 constexpr int kHubDeg = 63;                        // degree from which a count is a hub count
 constexpr uint32_t kHubMark = 63;                  // count field of a hub's word
 constexpr uint32_t kTag = 0x80000000u;             // column entry of a hub neighbour
 constexpr uint32_t kIdx = 0x7FFFFFFFu;
+constexpr int kInstBits = 26;                      // instance bits of a candidate entry
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kS = 0, kI = 1;
 
 static_assert(sizeof(abm_sir_instance) == 136, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
-// Lists workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
-// new compartment}), then `capacity` candidate entries (int4 {inst, agent, count, 0});
-// susceptible candidates fill the candidate array from the front, infected ones from the
-// back (an agent is at most one candidate, so the two never meet).
+// List workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
+// new compartment}), then `capacity` candidate entries of susceptible agents (int2
+// {inst | min(count, 63) << kInstBits, agent}).
 struct ListHeader {
   int32_t changes;
   int32_t overflow;
   int32_t cand_s;
-  int32_t cand_i;
+  int32_t reserved;
 };
 
 struct Lists {
   ListHeader* hdr;
   int2* changes;
-  int4* cands;
+  int2* cands;
   int capacity;
 };
 
@@ -135,12 +138,45 @@ __device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4], int j) {
   return (q[j >> 2] >> (8 * (j & 3))) & 0xFFu;
 }
 
+__device__ __forceinline__ void record_change(bool changed, int inst, int i, int ns, Lists& L,
+                                              int lane) {
+  const int pos = warp_append(changed, &L.hdr->changes, lane);
+  if (changed) {
+    if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
+    else L.hdr->overflow = 1;
+  }
+}
+
+// Per-instance sums over the lanes of a warp (lanes grouped by instance), added to the
+// group's instance by the group's lowest lane: CSR slots scanned and infections.
+__device__ __forceinline__ void add_decided(bool valid, int inst, int scanned, int infected,
+                                            abm_sir_instance* insts, int lane) {
+  if (!__any_sync(kFull, scanned != 0 || infected != 0)) return;
+  const unsigned group = __match_any_sync(kFull, valid ? inst : -1);
+  const int s = __reduce_add_sync(group, scanned);
+  const int f = __reduce_add_sync(group, infected);
+  if (valid && lane == __ffs(group) - 1) {
+    if (s) atomicAdd(&insts[inst].edges_scanned, static_cast<unsigned long long>(s));
+    if (f) atomicAdd(&insts[inst].step_si, f);
+  }
+}
+
+// One step's sweep over (instance, 4096-agent tile) work items: lane l of warp w reads
+// agents 512w + 16l .. 512w + 16l + 15 of the tile with one 128-bit load.
+//  * Infected agents draw their recovery here: each warp queues its infected agents in
+//    shared memory and draws them 32 at a time, one lane each (no list entry).
+//  * Susceptible agents with infected neighbours are appended to the candidate list in
+//    agent order (block scan; one counter atomic per CTA and tile), so that consecutive
+//    entries read nearby row offsets and CSR rows.
+// Everyone else (most agents) costs one byte.
 __global__ void __launch_bounds__(kSirThreads)
 sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ work,
                  int nwork_max, const int32_t* __restrict__ live, Lists L) {
   __shared__ int swarp[kWarpsPerCta];
-  __shared__ int sbase_s, sbase_i;
+  __shared__ int sbase;
+  __shared__ uint16_t squeue[kWarpsPerCta][kSub];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint16_t* __restrict__ queue = squeue[warp];
   const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
@@ -150,9 +186,8 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
     if (I->t >= I->steps || I->num_i == 0) continue;  // uniform over the CTA
     const uint8_t* __restrict__ words = I->words;
     const int32_t* __restrict__ hubs = I->hub_counts;
-    // thread t owns agents base .. base + 15: one 128-bit load when the bytes are 16-byte
-    // aligned and inside the tile, byte loads otherwise (bytes past the tile read as R)
-    const int base = item.y + kPerThread * threadIdx.x;
+    const int off = kSub * warp + kPerThread * lane;  // offset in the tile
+    const int base = item.y + off;
     uint32_t q[4];
     if (((reinterpret_cast<uintptr_t>(words + base) & 15) == 0) && base + kPerThread <= item.z) {
       const uint4 v = *reinterpret_cast<const uint4*>(words + base);
@@ -180,7 +215,7 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
       if (s == kS && c != 0 && (c != kHubMark || hubs[base + j] > 0)) need_s |= 1u << j;
       if (s == kI) need_i |= 1u << j;
     }
-    // one counter atomic per list, CTA and tile: both counts scanned at once (16 bits each)
+    // both counts scanned at once (16 bits each): warp scan, then block totals
     const int mine = __popc(need_s) | (__popc(need_i) << 16);
     int incl = mine;
 #pragma unroll
@@ -188,121 +223,112 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
       const int u = __shfl_up_sync(kFull, incl, o);
       if (lane >= o) incl += u;
     }
+    const int wtotal = __shfl_sync(kFull, incl, 31);
     if (lane == 31) swarp[warp] = incl;
     __syncthreads();
     if (threadIdx.x == 0) {
       int total = 0;
       for (int x = 0; x < kWarpsPerCta; ++x) total += swarp[x];
       const int ts = total & 0xFFFF, ti = total >> 16;
-      sbase_s = ts ? atomicAdd(&L.hdr->cand_s, ts) : 0;
-      sbase_i = ti ? atomicAdd(&L.hdr->cand_i, ti) : 0;
+      sbase = ts ? atomicAdd(&L.hdr->cand_s, ts) : 0;
       if (ts + ti) atomicAdd(&I->candidates, static_cast<unsigned long long>(ts + ti));
     }
     __syncthreads();
-    int before = incl - mine;
-    for (int x = 0; x < warp; ++x) before += swarp[x];
-    int pos_s = sbase_s + (before & 0xFFFF);
-    int pos_i = sbase_i + (before >> 16);
-    __syncthreads();  // swarp/sbase_* are rewritten by the next tile
+    int pos_s = (incl - mine) & 0xFFFF;
+    for (int x = 0; x < warp; ++x) pos_s += swarp[x] & 0xFFFF;
+    pos_s += sbase;
+    int pos_i = (incl - mine) >> 16;  // within the warp's queue
     if (need_s | need_i) {
 #pragma unroll
       for (int j = 0; j < kPerThread; ++j) {
-        const int i = base + j;
         if ((need_s >> j) & 1u) {
-          uint32_t c = byte_of(q, j) >> 2;
-          if (c == kHubMark) c = static_cast<uint32_t>(hubs[i]);
-          if (pos_s < L.capacity) L.cands[pos_s] = make_int4(item.x, i, static_cast<int>(c), 0);
+          // {inst | min(count, 63) << 26, agent}: 63 is a hub's mark (count in hub_counts)
+          const int c = static_cast<int>(byte_of(q, j) >> 2);
+          if (pos_s < L.capacity) L.cands[pos_s] = make_int2(item.x | (c << kInstBits), base + j);
           else L.hdr->overflow = 1;
           ++pos_s;
         } else if ((need_i >> j) & 1u) {
-          if (pos_i < L.capacity) L.cands[L.capacity - 1 - pos_i] = make_int4(item.x, i, 0, 0);
-          else L.hdr->overflow = 1;
-          ++pos_i;
+          queue[pos_i++] = static_cast<uint16_t>(off + j);
         }
       }
     }
+    __syncwarp();
+    // recovery draws of the warp's infected agents
+    const int ni = wtotal >> 16;
+    if (ni) {
+      const uint2 coll = make_uint2(I->coll[0], I->coll[1]);
+      const float gamma = I->gamma;
+      int ir = 0;
+      for (int k0 = 0; k0 < ni; k0 += 32) {
+        const int k = k0 + lane;
+        const bool valid = k < ni;
+        const int i = item.y + (valid ? queue[k] : 0);
+        bool changed = false;
+        if (valid) {
+          const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
+          changed = abm::unit_float(abm::bits_at(krec, 0)) < gamma;
+        }
+        ir += changed;
+        record_change(changed, item.x, i, 2, L, lane);
+      }
+      ir = __reduce_add_sync(kFull, ir);
+      if (lane == 0 && ir) atomicAdd(&I->step_ir, ir);
+    }
+    __syncthreads();  // swarp, sbase and the queues are rewritten by the next tile
   }
 }
 
-// Per-instance sum of `v` over the lanes of a warp (lanes grouped by instance), added to
-// the group's instance by the group's lowest lane.
-__device__ __forceinline__ void add_scanned(int inst, int v, abm_sir_instance* insts, int lane) {
-  if (!__any_sync(kFull, v != 0)) return;
-  const unsigned group = __match_any_sync(kFull, inst);
-  const int sum = __reduce_add_sync(group, v);
-  if (lane == __ffs(group) - 1 && sum) atomicAdd(&insts[inst].edges_scanned, (unsigned long long)sum);
-}
-
-__device__ __forceinline__ void record_change(bool changed, int inst, int i, int ns, Lists& L,
-                                              int lane) {
-  const int pos = warp_append(changed, &L.hdr->changes, lane);
-  if (changed) {
-    if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
-    else L.hdr->overflow = 1;
-  }
-}
-
-__global__ void __launch_bounds__(kSirThreads)
+// Susceptible candidates: one lane each scans its CSR row, eight slots per pass (the eight
+// column loads, then the eight neighbour-word loads, issued together), stopping at the
+// first firing draw or once all its infected neighbours were seen; rows longer than 32
+// slots are scanned by the whole warp, 128 slots per pass, with warp votes.  Changes go to
+// the change list; no word is written, so every decision sees the pre-step states.
+__global__ void __launch_bounds__(kSirThreads, 5)
 sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * kWarpsPerCta;
   const int wid = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
-
-  // infected candidates: recovery draws
-  const int ni = min(L.hdr->cand_i, L.capacity);
-  for (int b = wid * 32; b < ni; b += warps * 32) {
-    const int k = b + lane;
-    const bool valid = k < ni;
-    const int4 e = valid ? __ldcs(&L.cands[L.capacity - 1 - k]) : make_int4(0, 0, 0, 0);
-    bool changed = false;
-    if (valid) {
-      const abm_sir_instance* I = insts + e.x;
-      const uint2 coll = make_uint2(I->coll[0], I->coll[1]);
-      const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)e.y), 1);
-      changed = abm::unit_float(abm::bits_at(krec, 0)) < I->gamma;
-    }
-    record_change(changed, e.x, e.y, 2, L, lane);
-  }
-
-  // susceptible candidates with infected neighbours: row scans
   const int ns_count = min(L.hdr->cand_s, L.capacity);
   for (int b = wid * 32; b < ns_count; b += warps * 32) {
     const int k = b + lane;
     const bool valid = k < ns_count;
-    const int4 e = valid ? __ldcs(&L.cands[k]) : make_int4(0, 0, 0, 0);
-    const int inst = e.x, i = e.y;
+    const int2 e = valid ? __ldcs(&L.cands[k]) : make_int2(0, 0);
+    const int inst = e.x & ((1 << kInstBits) - 1), i = e.y;
     const abm_sir_instance* I = insts + inst;
-    int cnt = e.z;
+    int cnt = static_cast<int>(static_cast<uint32_t>(e.x) >> kInstBits);
     bool infected = false, heavy = false;
     int row0 = 0, deg = 0, scanned = 0;
+    uint2 coll = make_uint2(0, 0);
+    const int32_t* __restrict__ adj = nullptr;
+    const uint8_t* __restrict__ words = nullptr;
+    float beta = 0.f;
     if (valid) {
+      if (cnt == static_cast<int>(kHubMark)) cnt = I->hub_counts[i];
+      coll = make_uint2(I->coll[0], I->coll[1]);
+      adj = I->adj;
+      words = I->words;
+      beta = I->beta;
       const int32_t* __restrict__ rp = I->row_ptr;
-      row0 = rp[i];
-      deg = rp[i + 1] - row0;
+      row0 = __ldcs(rp + i);
+      deg = __ldcs(rp + i + 1) - row0;
       if (deg > kHeavyDeg) {
         heavy = true;
       } else {
-        const uint2 coll = make_uint2(I->coll[0], I->coll[1]);
-        const int32_t* __restrict__ adj = I->adj;
-        const uint8_t* __restrict__ words = I->words;
-        const float beta = I->beta;
         const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-        // eight slots per pass: the eight column loads, then the eight neighbour-word
-        // loads, are issued together before any is used
         scanned = deg;
         bool done = false;
-        for (int k0 = 0; k0 < deg && !done; k0 += kChunk) {
+        for (int k1 = 0; k1 < deg && !done; k1 += kChunk) {
           int nb[kChunk];
           uint32_t wn[kChunk];
 #pragma unroll
-          for (int q = 0; q < kChunk; ++q)
-            nb[q] = k0 + q < deg ? static_cast<int>(ld_col(adj, row0 + k0 + q) & kIdx) : -1;
+          for (int c = 0; c < kChunk; ++c)
+            nb[c] = k1 + c < deg ? static_cast<int>(ld_col(adj, row0 + k1 + c) & kIdx) : -1;
 #pragma unroll
-          for (int q = 0; q < kChunk; ++q) wn[q] = nb[q] >= 0 ? words[nb[q]] : 0u;
+          for (int c = 0; c < kChunk; ++c) wn[c] = nb[c] >= 0 ? words[nb[c]] : 0u;
 #pragma unroll
-          for (int q = 0; q < kChunk; ++q) {
-            if (!done && nb[q] >= 0 && (wn[q] & 3u) == kI) {
-              const int slot = k0 + q;
+          for (int c = 0; c < kChunk; ++c) {
+            if (!done && nb[c] >= 0 && (wn[c] & 3u) == kI) {
+              const int slot = k1 + c;
               if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
                 infected = true;
                 done = true;
@@ -322,28 +348,43 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     while (hmask) {
       const int src = __ffs(hmask) - 1;
       hmask &= hmask - 1;
-      const int hinst = __shfl_sync(kFull, inst, src);
       const int hi = __shfl_sync(kFull, i, src);
       const int hrow = __shfl_sync(kFull, row0, src);
       const int hdeg = __shfl_sync(kFull, deg, src);
       int remaining = __shfl_sync(kFull, cnt, src);
-      const abm_sir_instance* H = insts + hinst;
-      const uint2 hcoll = make_uint2(H->coll[0], H->coll[1]);
-      const int32_t* __restrict__ adj = H->adj;
-      const uint8_t* __restrict__ words = H->words;
-      const float beta = H->beta;
+      const uint2 hcoll = make_uint2(__shfl_sync(kFull, coll.x, src), __shfl_sync(kFull, coll.y, src));
+      const float hbeta = __shfl_sync(kFull, beta, src);
+      const int32_t* __restrict__ hadj = reinterpret_cast<const int32_t*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(adj), src));
+      const uint8_t* __restrict__ hwords = reinterpret_cast<const uint8_t*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(words), src));
       const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
       int c = 0;
-      for (; c < hdeg && !fired && remaining > 0; c += 32) {
-        const int slot = c + lane;
-        bool isI = false, f = false;
-        if (slot < hdeg) {
-          isI = (words[ld_col(adj, hrow + slot) & kIdx] & 3u) == kI;
-          if (isI) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
+      for (; c < hdeg && !fired && remaining > 0; c += 32 * kHeavyUnroll) {
+        uint32_t wv[kHeavyUnroll];
+#pragma unroll
+        for (int u = 0; u < kHeavyUnroll; ++u) {
+          const int slot = c + 32 * u + lane;
+          wv[u] = slot < hdeg ? ld_col(hadj, hrow + slot) : kTag;
+        }
+#pragma unroll
+        for (int u = 0; u < kHeavyUnroll; ++u) {
+          const int slot = c + 32 * u + lane;
+          wv[u] = slot < hdeg ? static_cast<uint32_t>(hwords[wv[u] & kIdx]) : 0u;
+        }
+        bool f = false;
+        int seen = 0;
+#pragma unroll
+        for (int u = 0; u < kHeavyUnroll; ++u) {
+          const int slot = c + 32 * u + lane;
+          if (slot < hdeg && (wv[u] & 3u) == kI) {
+            ++seen;
+            if (!f) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < hbeta;
+          }
         }
         fired = __any_sync(kFull, f);
-        remaining -= __popc(__ballot_sync(kFull, isI));
+        remaining -= __reduce_add_sync(kFull, seen);
       }
       if (lane == src) {
         infected = fired;
@@ -351,14 +392,14 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       }
     }
 
-    record_change(infected, inst, i, kI, L, lane);
-    add_scanned(inst, scanned, insts, lane);
+    record_change(infected, inst, i, static_cast<int>(kI), L, lane);
+    add_decided(valid, inst, scanned, infected ? 1 : 0, insts, lane);
   }
 }
 
 // Neighbours' infected counts +-1 and own compartment +1 for every change: one thread per
 // change for rows up to kHeavyDeg slots (atomics issued without waiting for results), one
-// warp for longer rows.
+// warp for longer rows (kHeavyUnroll column loads per lane in flight).
 __global__ void __launch_bounds__(kSirThreads)
 sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   const int lane = threadIdx.x & 31;
@@ -367,7 +408,7 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   for (int b = (blockIdx.x * kSirThreads + threadIdx.x) & ~31; b < count; b += threads) {
     const int k = b + lane;
     const bool valid = k < count;
-    int inst = 0, agent = 0, r0 = 0, r1 = 0, delta = 0;
+    int inst = -1, agent = 0, r0 = 0, r1 = 0, delta = 0;
     abm_sir_instance* I = insts;
     if (valid) {
       const int2 ent = __ldcs(&L.changes[k]);
@@ -375,14 +416,19 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       agent = ent.y >> 2;
       I = insts + inst;
       delta = (ent.y & 3) == static_cast<int>(kI) ? 1 : -1;
-      r0 = I->row_ptr[agent];
-      r1 = I->row_ptr[agent + 1];
+      r0 = __ldcs(I->row_ptr + agent);
+      r1 = __ldcs(I->row_ptr + agent + 1);
       // S(0) -> I(1) and I(1) -> R(2) both add one to the agent's own compartment field
       const uintptr_t a = reinterpret_cast<uintptr_t>(I->words + agent);
       atomicAdd(reinterpret_cast<unsigned*>(a & ~static_cast<uintptr_t>(3)),
                 1u << (8u * static_cast<unsigned>(a & 3)));
-      atomicAdd(delta > 0 ? &I->step_si : &I->step_ir, 1);
-      atomicAdd(&I->edges_pushed, (unsigned long long)(r1 - r0));
+    }
+    // slots pushed, summed per instance over the warp's lanes
+    {
+      const unsigned group = __match_any_sync(kFull, inst);
+      const int sum = __reduce_add_sync(group, r1 - r0);
+      if (valid && lane == __ffs(group) - 1 && sum)
+        atomicAdd(&I->edges_pushed, static_cast<unsigned long long>(sum));
     }
     const bool heavy = valid && r1 - r0 > kHeavyDeg;
     if (valid && !heavy) {
@@ -409,7 +455,17 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       uint8_t* words = insts[hinst].words;
       int32_t* hubs = insts[hinst].hub_counts;
       const int32_t* __restrict__ adj = insts[hinst].adj;
-      for (int e = hr0 + lane; e < hr1; e += 32) add_count(words, hubs, ld_col(adj, e), hdelta);
+      for (int e0 = hr0; e0 < hr1; e0 += 32 * kHeavyUnroll) {
+        uint32_t nb[kHeavyUnroll];
+#pragma unroll
+        for (int u = 0; u < kHeavyUnroll; ++u) {
+          const int e = e0 + 32 * u + lane;
+          nb[u] = e < hr1 ? ld_col(adj, e) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kHeavyUnroll; ++u)
+          if (e0 + 32 * u + lane < hr1) add_count(words, hubs, nb[u], hdelta);
+      }
     }
   }
 }
@@ -422,7 +478,6 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   if (k == 0) {
     hdr->changes = 0;
     hdr->cand_s = 0;
-    hdr->cand_i = 0;
   }
   if (k >= ninst) return;
   abm_sir_instance* I = insts + k;
@@ -626,12 +681,11 @@ size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 Lists carve_lists(void* ws, size_t bytes) {
   Lists L;
   L.hdr = static_cast<ListHeader*>(ws);
-  size_t cap = (bytes - sizeof(ListHeader)) / (sizeof(int2) + sizeof(int4));
+  size_t cap = (bytes - sizeof(ListHeader)) / (2 * sizeof(int2));
   if (cap > 0x7FFFFFFE) cap = 0x7FFFFFFE;
-  cap &= ~(size_t)1;  // even: keeps the int4 candidate entries 16-byte aligned
   L.capacity = (int)cap;
   L.changes = reinterpret_cast<int2*>(L.hdr + 1);
-  L.cands = reinterpret_cast<int4*>(L.changes + L.capacity);
+  L.cands = L.changes + L.capacity;
   return L;
 }
 
@@ -656,8 +710,7 @@ int abm_sir_default_launch(abm_sir_launch* out) {
 
 size_t abm_sir_changes_bytes(int64_t max_agents) {
   if (max_agents <= 0) return 0;
-  const size_t cap = ((size_t)max_agents + 1) & ~(size_t)1;
-  return sizeof(ListHeader) + cap * (sizeof(int2) + sizeof(int4));
+  return sizeof(ListHeader) + (size_t)max_agents * 2 * sizeof(int2);
 }
 
 int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
@@ -713,7 +766,8 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
                   int32_t nwork, const int32_t* live_work, int32_t nsteps,
                   const abm_sir_launch* launch,
                   void* changes, size_t changes_bytes, void* stream) {
-  if (!insts || ninst <= 0 || nwork < 0 || nsteps < 0 || (nwork > 0 && !work) || !changes)
+  if (!insts || ninst <= 0 || ninst > (1 << kInstBits) || nwork < 0 || nsteps < 0 ||
+      (nwork > 0 && !work) || !changes)
     return ABM_ERR_BADARG;
   if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)) ||
       !abm_host::aligned(changes, 16) || (live_work && !abm_host::aligned(live_work, 4)))

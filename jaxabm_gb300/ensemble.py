@@ -267,7 +267,7 @@ class SIRBatch:
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
     def launches_per_run(self):
-        return 4 * self.steps
+        return 4 * self.steps + 1
 
     def edge_stats(self):
         """(CSR slots read by decide, CSR slots read by push, compartment changes,
@@ -279,8 +279,8 @@ class SIRBatch:
                 int(d["candidates"].sum()))
 
     def live_agent_steps(self):
-        """Agent-steps the sweep reads: steps of an instance that start with at least one
-        infected agent (the others cannot change and are skipped)."""
+        """Agent-steps whose words the sweep reads: steps of an instance that start with at
+        least one infected agent (the others cannot change and are skipped)."""
         counts = self.counts.reshape(self.k, self.steps, 3).cpu().numpy().astype(np.int64)
         i0 = np.array([(self.h_state0[o:o + n] == 1).sum() for o, n in
                        zip(self._offsets[2][:-1], self.n)], dtype=np.int64)
@@ -289,13 +289,15 @@ class SIRBatch:
 
     def algorithmic_bytes(self):
         """Bytes the run must move (after it completed), each datum at its own size: per
-        live agent-step its 1-byte word; per decision candidate its 8-byte list entry; per
-        CSR slot read by the candidates kernel 5 bytes (4-byte column + neighbour word);
-        per slot pushed 6 bytes (column + count read and write); per compartment change 18
-        bytes (8-byte list entry, 8-byte row offsets, own word read and write)."""
+        live agent-step its 1-byte word; per decision candidate 8 bytes (a susceptible
+        candidate's row offsets; an infected one reads nothing more, so this over-counts);
+        per CSR slot read by a decision 5 bytes (4-byte column + neighbour word); per slot
+        pushed 6 bytes (column + count read and write); per compartment change 26 bytes
+        (8-byte list entry written and read, 8-byte row offsets, own word read and
+        write)."""
         scanned, pushed, changes, cands = self.edge_stats()
         return int(self.live_agent_steps() + 8 * cands + 5 * scanned + 6 * pushed
-                   + 18 * changes)
+                   + 26 * changes)
 
 
 # ---- the batched-ensemble workload (4,096 SIR instances) -------------------------------

@@ -271,7 +271,7 @@ class SIRServer:
             while len(self._in_flight) > self.max_ticks_in_flight:
                 self._in_flight.popleft().synchronize()
             self.ticks += 1
-            self.launches += 4 * self.steps_per_tick
+            self.launches += 4 * self.steps_per_tick + 1
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)
