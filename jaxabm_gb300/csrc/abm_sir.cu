@@ -207,13 +207,20 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
         q[c] = r;
       }
     }
-    unsigned need_s = 0, need_i = 0;
+    unsigned need_s = 0, need_i = 0, hub_s = 0;
 #pragma unroll
     for (int j = 0; j < kPerThread; ++j) {
       const uint32_t b = byte_of(q, j);
-      const uint32_t s = b & 3u, c = b >> 2;
-      if (s == kS && c != 0 && (c != kHubMark || hubs[base + j] > 0)) need_s |= 1u << j;
-      if (s == kI) need_i |= 1u << j;
+      const uint32_t s = b & 3u;
+      need_s |= static_cast<unsigned>(s == kS && b >= 4u) << j;
+      need_i |= static_cast<unsigned>(s == kI) << j;
+      hub_s |= static_cast<unsigned>(b == (kHubMark << 2)) << j;
+    }
+    // susceptible hubs need a decision only with infected neighbours (count in hub_counts)
+    while (hub_s) {
+      const int j = __ffs(hub_s) - 1;
+      hub_s &= hub_s - 1;
+      if (hubs[base + j] <= 0) need_s &= ~(1u << j);
     }
     // both counts scanned at once (16 bits each): warp scan, then block totals
     const int mine = __popc(need_s) | (__popc(need_i) << 16);
@@ -238,19 +245,18 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
     for (int x = 0; x < warp; ++x) pos_s += swarp[x] & 0xFFFF;
     pos_s += sbase;
     int pos_i = (incl - mine) >> 16;  // within the warp's queue
-    if (need_s | need_i) {
-#pragma unroll
-      for (int j = 0; j < kPerThread; ++j) {
-        if ((need_s >> j) & 1u) {
-          // {inst | min(count, 63) << 26, agent}: 63 is a hub's mark (count in hub_counts)
-          const int c = static_cast<int>(byte_of(q, j) >> 2);
-          if (pos_s < L.capacity) L.cands[pos_s] = make_int2(item.x | (c << kInstBits), base + j);
-          else L.hdr->overflow = 1;
-          ++pos_s;
-        } else if ((need_i >> j) & 1u) {
-          queue[pos_i++] = static_cast<uint16_t>(off + j);
-        }
+    {
+      const uint64_t lo = q[0] | (static_cast<uint64_t>(q[1]) << 32);
+      const uint64_t hi = q[2] | (static_cast<uint64_t>(q[3]) << 32);
+      for (unsigned m = need_s; m; m &= m - 1) {
+        const int j = __ffs(m) - 1;
+        // {inst | min(count, 63) << 26, agent}: 63 is a hub's mark (count in hub_counts)
+        const int c = static_cast<int>(((j < 8 ? lo >> (8 * j) : hi >> (8 * (j - 8))) & 0xFFu) >> 2);
+        if (pos_s < L.capacity) L.cands[pos_s] = make_int2(item.x | (c << kInstBits), base + j);
+        else L.hdr->overflow = 1;
+        ++pos_s;
       }
+      for (unsigned m = need_i; m; m &= m - 1) queue[pos_i++] = static_cast<uint16_t>(off + __ffs(m) - 1);
     }
     __syncwarp();
     // recovery draws of the warp's infected agents
@@ -298,6 +304,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     int cnt = static_cast<int>(static_cast<uint32_t>(e.x) >> kInstBits);
     bool infected = false, heavy = false;
     int row0 = 0, deg = 0, scanned = 0;
+    unsigned imask = 0;
     uint2 coll = make_uint2(0, 0);
     const int32_t* __restrict__ adj = nullptr;
     const uint8_t* __restrict__ words = nullptr;
@@ -311,13 +318,12 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const int32_t* __restrict__ rp = I->row_ptr;
       row0 = __ldcs(rp + i);
       deg = __ldcs(rp + i + 1) - row0;
-      if (deg > kHeavyDeg) {
-        heavy = true;
-      } else {
-        const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-        scanned = deg;
-        bool done = false;
-        for (int k1 = 0; k1 < deg && !done; k1 += kChunk) {
+      heavy = deg > kHeavyDeg;
+      if (!heavy) {
+        // slots of infected neighbours (bit k: slot k), read until all `cnt` were seen;
+        // eight column loads, then eight neighbour loads, in flight per pass
+        int seen = 0, k1 = 0;
+        for (; k1 < deg && seen < cnt; k1 += kChunk) {
           int nb[kChunk];
           uint32_t wn[kChunk];
 #pragma unroll
@@ -327,17 +333,25 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           for (int c = 0; c < kChunk; ++c) wn[c] = nb[c] >= 0 ? words[nb[c]] : 0u;
 #pragma unroll
           for (int c = 0; c < kChunk; ++c) {
-            if (!done && nb[c] >= 0 && (wn[c] & 3u) == kI) {
-              const int slot = k1 + c;
-              if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
-                infected = true;
-                done = true;
-                scanned = slot + 1;
-              } else if (--cnt == 0) {
-                done = true;
-                scanned = slot + 1;
-              }
-            }
+            const bool inf = nb[c] >= 0 && (wn[c] & 3u) == kI;
+            imask |= static_cast<unsigned>(inf) << (k1 + c);
+            seen += inf;
+          }
+        }
+        scanned = min(k1, deg);
+      }
+    }
+    // infection draws in slot order, one per lane and pass, so that the lanes of the warp
+    // draw together: a susceptible agent is infected iff some infected slot fires
+    if (__any_sync(kFull, imask != 0)) {
+      const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
+      while (__any_sync(kFull, imask != 0)) {
+        if (imask) {
+          const int slot = __ffs(imask) - 1;
+          imask &= imask - 1;
+          if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
+            infected = true;
+            imask = 0;
           }
         }
       }
