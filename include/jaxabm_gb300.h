@@ -189,7 +189,7 @@ typedef struct abm_work_item {
 
 ABM_API size_t abm_sir_instance_size(void);
 
-/* Largest tile (agents per work item) of the SIR kernels: 4096.  Words are read with
+/* Largest tile (agents per work item) of the SIR kernels: 8192.  Words are read with
  * 128-bit loads (16 agents) where a tile's bytes are 16-byte aligned, byte loads
  * otherwise. */
 ABM_API int32_t abm_sir_tile_agents(void);

@@ -23,8 +23,8 @@
 // recover, and never exceeds the degree (< 63).
 //
 // A step is four launches:
-//   sweep      over (instance, 4096-agent tile) work items, 16 agents per lane read with
-//              one 128-bit load.  Infected agents draw their recovery right there (each
+//   sweep      over (instance, 8192-agent tile) work items, 32 agents per lane read with
+//              two 128-bit loads.  Infected agents draw their recovery right there (each
 //              warp queues its infected agents in shared memory and draws them one lane
 //              each); susceptible agents with infected neighbours are appended to a
 //              candidate list in agent order (8-byte entries; one counter atomic per CTA
@@ -50,9 +50,10 @@ namespace {
 
 constexpr int kSirThreads = 256;
 constexpr int kWarpsPerCta = kSirThreads / 32;
-constexpr int kPerThread = 16;                     // agents (bytes) per lane: one 128-bit load
-constexpr int kSub = 32 * kPerThread;              // 512 agents per warp and tile
-constexpr int kTile = kSirThreads * kPerThread;    // 4096 agents per work item
+constexpr int kVecs = 2;                           // 128-bit loads per lane and tile
+constexpr int kPerThread = 16 * kVecs;             // agents (bytes) per lane: 32
+constexpr int kSub = 32 * kPerThread;              // 1024 agents per warp and tile
+constexpr int kTile = kSirThreads * kPerThread;    // 8192 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr int kHeavyUnroll = 4;                    // slots per lane per pass of a warp row scan
 constexpr int kChunk = 8;                          // row slots per scan pass
@@ -134,7 +135,7 @@ __global__ void sir_prepare_kernel(abm_sir_instance* __restrict__ insts, int nin
   I->coll[1] = c.y;
 }
 
-__device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4], int j) {
+__device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4 * kVecs], int j) {
   return (q[j >> 2] >> (8 * (j & 3))) & 0xFFu;
 }
 
@@ -161,8 +162,8 @@ __device__ __forceinline__ void add_decided(bool valid, int inst, int scanned, i
   }
 }
 
-// One step's sweep over (instance, 4096-agent tile) work items: lane l of warp w reads
-// agents 512w + 16l .. 512w + 16l + 15 of the tile with one 128-bit load.
+// One step's sweep over (instance, 8192-agent tile) work items: lane l of warp w reads
+// agents 1024w + 32l .. 1024w + 32l + 31 of the tile with two 128-bit loads.
 //  * Infected agents draw their recovery here: each warp queues its infected agents in
 //    shared memory and draws them 32 at a time, one lane each (no list entry).
 //  * Susceptible agents with infected neighbours are appended to the candidate list in
@@ -188,23 +189,28 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
     const int32_t* __restrict__ hubs = I->hub_counts;
     const int off = kSub * warp + kPerThread * lane;  // offset in the tile
     const int base = item.y + off;
-    uint32_t q[4];
-    if (((reinterpret_cast<uintptr_t>(words + base) & 15) == 0) && base + kPerThread <= item.z) {
-      const uint4 v = *reinterpret_cast<const uint4*>(words + base);
-      q[0] = v.x;
-      q[1] = v.y;
-      q[2] = v.z;
-      q[3] = v.w;
-    } else {
+    uint32_t q[4 * kVecs];
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(words + base) & 15) == 0;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        uint32_t r = 0;
+    for (int v = 0; v < kVecs; ++v) {
+      const int b16 = base + 16 * v;
+      if (vec_ok && b16 + 16 <= item.z) {
+        const uint4 x = *reinterpret_cast<const uint4*>(words + b16);
+        q[4 * v] = x.x;
+        q[4 * v + 1] = x.y;
+        q[4 * v + 2] = x.z;
+        q[4 * v + 3] = x.w;
+      } else {
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const int i = base + 4 * c + b;
-          r |= (i < item.z ? static_cast<uint32_t>(words[i]) : 2u) << (8 * b);
+        for (int c = 0; c < 4; ++c) {
+          uint32_t r = 0;
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int i = b16 + 4 * c + b;
+            r |= (i < item.z ? static_cast<uint32_t>(words[i]) : 2u) << (8 * b);
+          }
+          q[4 * v + c] = r;
         }
-        q[c] = r;
       }
     }
     unsigned need_s = 0, need_i = 0, hub_s = 0;
@@ -245,19 +251,15 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
     for (int x = 0; x < warp; ++x) pos_s += swarp[x] & 0xFFFF;
     pos_s += sbase;
     int pos_i = (incl - mine) >> 16;  // within the warp's queue
-    {
-      const uint64_t lo = q[0] | (static_cast<uint64_t>(q[1]) << 32);
-      const uint64_t hi = q[2] | (static_cast<uint64_t>(q[3]) << 32);
-      for (unsigned m = need_s; m; m &= m - 1) {
-        const int j = __ffs(m) - 1;
-        // {inst | min(count, 63) << 26, agent}: 63 is a hub's mark (count in hub_counts)
-        const int c = static_cast<int>(((j < 8 ? lo >> (8 * j) : hi >> (8 * (j - 8))) & 0xFFu) >> 2);
-        if (pos_s < L.capacity) L.cands[pos_s] = make_int2(item.x | (c << kInstBits), base + j);
-        else L.hdr->overflow = 1;
-        ++pos_s;
-      }
-      for (unsigned m = need_i; m; m &= m - 1) queue[pos_i++] = static_cast<uint16_t>(off + __ffs(m) - 1);
+    for (unsigned m = need_s; m; m &= m - 1) {
+      const int j = __ffs(m) - 1;
+      // {inst | min(count, 63) << 26, agent}: 63 is a hub's mark (count in hub_counts)
+      const int c = static_cast<int>(words[base + j] >> 2);  // just loaded: an L1 hit
+      if (pos_s < L.capacity) L.cands[pos_s] = make_int2(item.x | (c << kInstBits), base + j);
+      else L.hdr->overflow = 1;
+      ++pos_s;
     }
+    for (unsigned m = need_i; m; m &= m - 1) queue[pos_i++] = static_cast<uint16_t>(off + __ffs(m) - 1);
     __syncwarp();
     // recovery draws of the warp's infected agents
     const int ni = wtotal >> 16;

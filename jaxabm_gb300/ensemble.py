@@ -5,7 +5,7 @@ The reference runs ensembles as serial Python loops of ``model.run()``
 jaxabm/analysis.py:97-165).  Here every member is an *instance*: its CSR, per-agent words
 and per-step counts live in packed device buffers, a device descriptor
 (``abm_sir_instance``) points into them, and ``abm_sir_steps`` advances all live instances
-over a persistent grid of (instance, 256-agent tile) work items.  The whole multi-step
+over a persistent grid of (instance, 8192-agent tile) work items.  The whole multi-step
 launch sequence is captured once in a CUDA graph and replayed.
 
 Each instance follows exactly the single-model key chain (``PRNGKey(seed)`` ->
@@ -23,7 +23,7 @@ from . import _lib
 from . import random as jrandom
 from .sir import barabasi_albert, initial_states
 
-TILE = 4096  # agents per work item (abm_sir_tile_agents)
+TILE = 8192  # agents per work item (abm_sir_tile_agents)
 
 # numpy view of abm_sir_instance (include/jaxabm_gb300.h), 136 bytes
 INSTANCE_DTYPE = np.dtype([

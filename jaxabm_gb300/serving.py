@@ -71,7 +71,7 @@ class SIRServer:
 
     Args:
         max_slots: concurrently resident requests
-        max_tiles: capacity of the work list (256-agent tiles of resident requests)
+        max_tiles: capacity of the work list (8192-agent tiles of resident requests)
         steps_per_tick: steps every resident request advances per tick
         reserve_bytes: device memory kept free at admission
         grid: (sweep, candidates, push) persistent grid sizes, or None for the defaults

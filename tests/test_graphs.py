@@ -56,9 +56,9 @@ def test_instance_layout(lib):
 
 def test_tiles_cover_instance(lib):
     assert ensemble.TILE == lib.abm_sir_tile_agents()
-    t = ensemble.tiles_for(3, 9000)
-    assert t[0].tolist() == [3, 0, 4096, 0] and t[-1].tolist() == [3, 8192, 9000, 0]
-    assert (t[:, 2] - t[:, 1]).sum() == 9000
+    t = ensemble.tiles_for(3, 20000)
+    assert t[0].tolist() == [3, 0, 8192, 0] and t[-1].tolist() == [3, 16384, 20000, 0]
+    assert (t[:, 2] - t[:, 1]).sum() == 20000
     assert ensemble.tiles_for(0, 1000).tolist() == [[0, 0, 1000, 0]]
 
 
