@@ -359,7 +359,7 @@ def model_lines():
                   0.05, 0.1, _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
     ms = _time_ms(sir1, reps=3)
     out["sir_ba_n1048576_t365"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
-                                   "launches_per_run": 4 * T + 5}
+                                   "launches_per_run": 4 * T + 5 + (T + 7) // 8}
 
     # opinion calibration: N = 2^18, 16-regular, 64 instances, 200 steps, checkpoints every 20
     n, B, T = 1 << 18, 64, 200

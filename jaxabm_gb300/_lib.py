@@ -53,7 +53,7 @@ SIGNATURES = {
     "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p, _p, _p]),
     "abm_sir_pack_batch": (_int, [_p, _p, _i32, _p, _p, _p, _p]),
     "abm_sir_unpack": (_int, [_p, _i64, _p, _p]),
-    "abm_sir_changes_bytes": (_sz, [_i64]),
+    "abm_sir_changes_bytes": (_sz, [_i64, _i64]),
     "abm_sir_steps": (_int, [_p, _i32, _p, _i32, _p, _i32, _p, _p, _sz, _p]),
     "abm_sir_default_launch": (_int, [_p]),
     "abm_sir_tile_agents": (_i32, []),

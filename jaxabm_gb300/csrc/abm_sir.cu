@@ -62,6 +62,7 @@ constexpr uint32_t kHubMark = 63;                  // count field of a hub's wor
 constexpr uint32_t kTag = 0x80000000u;             // column entry of a hub neighbour
 constexpr uint32_t kIdx = 0x7FFFFFFFu;
 constexpr int kInstBits = 26;                      // instance bits of a candidate entry
+constexpr int kCompactEvery = 8;                   // steps between work-list compactions
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kS = 0, kI = 1;
 
@@ -70,18 +71,21 @@ static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
 // List workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
 // new compartment}), then `capacity` candidate entries of susceptible agents (int2
-// {inst | min(count, 63) << kInstBits, agent}).
+// {inst | min(count, 63) << kInstBits, agent}), then the compacted work list.
 struct ListHeader {
   int32_t changes;
   int32_t overflow;
   int32_t cand_s;
-  int32_t reserved;
+  int32_t live_tiles;  // length of the compacted work list
 };
 
+// The compacted work list (tiles of live instances, `max_tiles` int4 entries) sits at the
+// end of the workspace.
 struct Lists {
   ListHeader* hdr;
   int2* changes;
   int2* cands;
+  int4* live_work;
   int capacity;
 };
 
@@ -486,6 +490,29 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   }
 }
 
+// Work items of instances that can still change (t < steps and an infected agent) into the
+// compacted work list; instances never come back once they stop, so the list may be
+// rebuilt every few steps.  The count is zeroed by the caller.
+__global__ void sir_compact_kernel(const abm_sir_instance* __restrict__ insts,
+                                   const int4* __restrict__ work, int nwork_max,
+                                   const int32_t* __restrict__ live, Lists L) {
+  const int lane = threadIdx.x & 31;
+  const int nwork = live_count(live, nwork_max);
+  const int stride = gridDim.x * blockDim.x;
+  for (int b = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; b < nwork; b += stride) {
+    const int k = b + lane;
+    int4 item = make_int4(0, 0, 0, 0);
+    bool keep = false;
+    if (k < nwork) {
+      item = work[k];
+      const abm_sir_instance* I = insts + item.x;
+      keep = I->t < I->steps && I->num_i > 0 && item.y < item.z;
+    }
+    const int pos = warp_append(keep, &L.hdr->live_tiles, lane);
+    if (keep) L.live_work[pos] = item;
+  }
+}
+
 // Counts after the step, key chain, step counter, next step's key, done flag; clears the
 // lists.
 __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
@@ -694,14 +721,19 @@ int resident_grid(Kernel k, int fallback_per_sm) {
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-Lists carve_lists(void* ws, size_t bytes) {
+size_t work_list_bytes(int64_t max_tiles) { return align256((size_t)max_tiles * sizeof(int4)); }
+
+Lists carve_lists(void* ws, size_t bytes, int64_t max_tiles) {
   Lists L;
   L.hdr = static_cast<ListHeader*>(ws);
-  size_t cap = (bytes - sizeof(ListHeader)) / (2 * sizeof(int2));
+  const size_t wl = work_list_bytes(max_tiles);
+  const size_t end = (bytes / 256) * 256;  // the work list ends here
+  size_t cap = (end - wl - sizeof(ListHeader)) / (2 * sizeof(int2));
   if (cap > 0x7FFFFFFE) cap = 0x7FFFFFFE;
   L.capacity = (int)cap;
   L.changes = reinterpret_cast<int2*>(L.hdr + 1);
   L.cands = L.changes + L.capacity;
+  L.live_work = reinterpret_cast<int4*>(static_cast<char*>(ws) + end - wl);
   return L;
 }
 
@@ -724,9 +756,10 @@ int abm_sir_default_launch(abm_sir_launch* out) {
   return ABM_OK;
 }
 
-size_t abm_sir_changes_bytes(int64_t max_agents) {
-  if (max_agents <= 0) return 0;
-  return sizeof(ListHeader) + (size_t)max_agents * 2 * sizeof(int2);
+size_t abm_sir_changes_bytes(int64_t max_agents, int64_t max_tiles) {
+  if (max_agents <= 0 || max_tiles < 0) return 0;
+  return align256(sizeof(ListHeader) + (size_t)max_agents * 2 * sizeof(int2)) +
+         work_list_bytes(max_tiles);
 }
 
 int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
@@ -788,9 +821,9 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   if (!abm_host::aligned(insts, 8) || (work && !abm_host::aligned(work, 16)) ||
       !abm_host::aligned(changes, 16) || (live_work && !abm_host::aligned(live_work, 4)))
     return ABM_ERR_BADARG;
-  if (changes_bytes < abm_sir_changes_bytes(1)) return ABM_ERR_WORKSPACE;
+  if (changes_bytes < abm_sir_changes_bytes(1, nwork)) return ABM_ERR_WORKSPACE;
   if (nsteps == 0) return ABM_OK;
-  const Lists L = carve_lists(changes, changes_bytes);
+  const Lists L = carve_lists(changes, changes_bytes, nwork);
   cudaStream_t s = abm_host::as_stream(stream);
   abm_sir_launch cfg;
   abm_sir_default_launch(&cfg);
@@ -804,13 +837,21 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   const int cand_grid = cfg.candidates_grid;
   const int push_grid = cfg.push_grid;
   const int fin_blocks = (ninst + 255) / 256;
+  const int compact_blocks = nwork > 0 ? min((nwork + 255) / 256, abm_host::sm_count() * 4) : 1;
   sir_prepare_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst);
   int st = abm_host::check_launch("abm_sir_steps/prepare");
   if (st) return st;
   for (int32_t k = 0; k < nsteps; ++k) {
     if (nwork > 0) {
-      sir_sweep_kernel<<<g, kSirThreads, 0, s>>>(insts, reinterpret_cast<const int4*>(work), nwork,
-                                                 live_work, L);
+      if (k % kCompactEvery == 0) {
+        st = abm_host::record_cuda_error(
+            cudaMemsetAsync(&L.hdr->live_tiles, 0, sizeof(int32_t), s), "abm_sir_steps/compact");
+        if (st) return st;
+        sir_compact_kernel<<<compact_blocks, 256, 0, s>>>(
+            insts, reinterpret_cast<const int4*>(work), nwork, live_work, L);
+        if ((st = abm_host::check_launch("abm_sir_steps/compact"))) return st;
+      }
+      sir_sweep_kernel<<<g, kSirThreads, 0, s>>>(insts, L.live_work, nwork, &L.hdr->live_tiles, L);
       if ((st = abm_host::check_launch("abm_sir_steps/sweep"))) return st;
       sir_candidates_kernel<<<cand_grid, kSirThreads, 0, s>>>(insts, L);
       if ((st = abm_host::check_launch("abm_sir_steps/candidates"))) return st;
@@ -828,7 +869,7 @@ size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges) {
   const int64_t tiles = (n + kTile - 1) / kTile;
   return align256(sizeof(abm_sir_instance)) + align256((size_t)tiles * sizeof(int4)) +
          align256((size_t)round16(n)) + align256((size_t)n * sizeof(int32_t)) + 256 +
-         align256((size_t)num_edges * sizeof(int32_t)) + align256(abm_sir_changes_bytes(n));
+         align256((size_t)num_edges * sizeof(int32_t)) + align256(abm_sir_changes_bytes(n, tiles));
 }
 
 int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t num_edges,
@@ -869,7 +910,7 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t n
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
   st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps,
-                     nullptr, lists, align256(abm_sir_changes_bytes(n)), stream);
+                     nullptr, lists, align256(abm_sir_changes_bytes(n, ntiles)), stream);
   if (st) return st;
   return abm_sir_unpack(words, n, state, stream);
 }

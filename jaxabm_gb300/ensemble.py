@@ -68,9 +68,10 @@ def model_rngs(seeds):
     return jrandom.split(dk, 2)[:, 0].contiguous()
 
 
-def changes_workspace(max_agents, device=None):
-    """Zeroed change-list workspace of ``abm_sir_steps`` for ``max_agents`` live agents."""
-    nbytes = _lib.load().abm_sir_changes_bytes(int(max_agents))
+def changes_workspace(max_agents, max_tiles, device=None):
+    """Zeroed list workspace of ``abm_sir_steps`` for ``max_agents`` live agents in at most
+    ``max_tiles`` work items."""
+    nbytes = _lib.load().abm_sir_changes_bytes(int(max_agents), int(max_tiles))
     return torch.zeros(max(nbytes, 32), dtype=torch.uint8, device=device or _dev.device())
 
 
@@ -181,7 +182,7 @@ class SIRBatch:
             raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
         self.words0 = self.words.clone()
         self.hub_counts0 = self.hub_counts.clone()
-        self.changes = changes_workspace(int(self.n.sum()))
+        self.changes = changes_workspace(int(self.n.sum()), self.work.shape[0])
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_steps = None
@@ -267,7 +268,9 @@ class SIRBatch:
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
     def launches_per_run(self):
-        return 4 * self.steps + 1
+        # prepare, then per step sweep, candidates, push, finalize, and a work-list
+        # compaction every 8 steps
+        return 4 * self.steps + 1 + (self.steps + 7) // 8
 
     def edge_stats(self):
         """(CSR slots read by decide, CSR slots read by push, compartment changes,

@@ -94,7 +94,7 @@ class SIRServer:
         self.h_work[:, 0] = self.dummy
         self.work = torch.zeros((self.max_tiles, 4), dtype=torch.int32, device=dev)
         self.work.copy_(self.h_work)
-        self.changes = changes_workspace(self.max_tiles * TILE)
+        self.changes = changes_workspace(self.max_tiles * TILE, self.max_tiles)
         # number of live work items, read by the kernels on every replay
         self.live = torch.zeros(1, dtype=torch.int32, device=dev)
         self.h_live = torch.zeros(1, dtype=torch.int32).pin_memory()
@@ -271,7 +271,7 @@ class SIRServer:
             while len(self._in_flight) > self.max_ticks_in_flight:
                 self._in_flight.popleft().synchronize()
             self.ticks += 1
-            self.launches += 4 * self.steps_per_tick + 1
+            self.launches += 4 * self.steps_per_tick + 1 + (self.steps_per_tick + 7) // 8
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)
