@@ -105,15 +105,21 @@ __device__ __forceinline__ uint32_t ld_col(const int32_t* __restrict__ adj, int 
   return static_cast<uint32_t>(__ldcs(adj + k));
 }
 
+// Fire-and-forget global reduction (no value returned, so the issuing warp never waits
+// for it).
+__device__ __forceinline__ void red_add(uint32_t* p, uint32_t v) {
+  asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Adds d to the infected-neighbour count of the agent that column entry v points at.
 __device__ __forceinline__ void add_count(uint8_t* words, int32_t* hubs, uint32_t v, int d) {
   const uint32_t t = v & kIdx;
   if (v & kTag) {
-    atomicAdd(hubs + t, d);
+    red_add(reinterpret_cast<uint32_t*>(hubs + t), static_cast<uint32_t>(d));
   } else {
     const uintptr_t a = reinterpret_cast<uintptr_t>(words + t);
-    atomicAdd(reinterpret_cast<unsigned*>(a & ~static_cast<uintptr_t>(3)),
-              static_cast<unsigned>(4 * d) << (8u * static_cast<unsigned>(a & 3)));
+    red_add(reinterpret_cast<uint32_t*>(a & ~static_cast<uintptr_t>(3)),
+            static_cast<uint32_t>(4 * d) << (8u * static_cast<uint32_t>(a & 3)));
   }
 }
 
@@ -440,8 +446,8 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       r1 = __ldcs(I->row_ptr + agent + 1);
       // S(0) -> I(1) and I(1) -> R(2) both add one to the agent's own compartment field
       const uintptr_t a = reinterpret_cast<uintptr_t>(I->words + agent);
-      atomicAdd(reinterpret_cast<unsigned*>(a & ~static_cast<uintptr_t>(3)),
-                1u << (8u * static_cast<unsigned>(a & 3)));
+      red_add(reinterpret_cast<uint32_t*>(a & ~static_cast<uintptr_t>(3)),
+              1u << (8u * static_cast<uint32_t>(a & 3)));
     }
     // slots pushed, summed per instance over the warp's lanes
     {

@@ -7,7 +7,9 @@ steps per tick:
 
 * admission: a request is admitted when a descriptor slot is free, its tiles fit the work
   list, and its buffers fit the free device memory (``torch.cuda.mem_get_info``) minus a
-  reserve; otherwise it waits in the queue (first come, first served);
+  reserve; otherwise it waits in the queue (first come, first served).  Everything that
+  fits at a tick is admitted as one group (one allocation per buffer kind, one pack
+  launch);
 * every tick replays ONE captured CUDA graph over a fixed-capacity work list; admitting or
   retiring requests only rewrites device tables (descriptor rows, work items), so the graph
   is never re-captured;
@@ -28,8 +30,17 @@ import torch
 from . import _dev
 from . import _lib
 from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, changes_workspace,
-                       check_layout, launch_struct, model_rngs, pack_words, unpack_words,
+                       check_layout, launch_struct, model_rngs, tiles_for, unpack_words,
                        word_bytes)
+
+
+class _Group:
+    """Device buffers shared by the requests admitted together; every request of the group
+    holds it, so the buffers are freed once the last of them has retired."""
+    __slots__ = ("bufs",)
+
+    def __init__(self, bufs):
+        self.bufs = bufs
 
 
 class Request:
@@ -58,8 +69,9 @@ class Request:
 
     def device_bytes(self):
         n, e = self.n, len(self.col)
-        # CSR, int8 compartments, word bytes (padded to 16), hub counts, per-step counts
-        return 4 * (n + 1) + 4 * e + n + (n + 15) // 16 * 16 + 4 * n + 12 * self.steps
+        # CSR; int8 compartments, word bytes and hub counts (each padded to 16 agents);
+        # per-step counts
+        return 4 * (n + 1) + 4 * e + 6 * word_bytes(n) + 12 * self.steps
 
     @property
     def latency(self):
@@ -154,51 +166,92 @@ class SIRServer:
         if changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed")
 
-    def _try_admit(self, req) -> bool:
-        if not self.free_slots or self._tiles_used + self._tiles(req) > self.max_tiles:
-            return False
-        if self.free_bytes() - self.reserve < req.device_bytes():
-            return False
-        slot = self.free_slots.pop()
-        dev = self.desc.device
-        s = self.stream
+    def _admit(self):
+        """Admit the longest prefix of the queue that fits (free slots, work-list tiles,
+        free device memory minus the reserve) as one group: one allocation per buffer kind,
+        one host-to-device copy per input array, one descriptor scatter, one key-split
+        launch and one pack launch for the whole group."""
+        if not self.queue or not self.free_slots:
+            return 0
+        room = self.free_bytes() - self.reserve
+        tiles_left = self.max_tiles - self._tiles_used
+        picked, need = [], 0
+        for req in self.queue:
+            t, b = self._tiles(req), req.device_bytes()
+            if len(picked) == len(self.free_slots) or t > tiles_left or need + b > room:
+                break
+            picked.append(req)
+            tiles_left -= t
+            need += b
+        if not picked:
+            return 0
+        for _ in picked:
+            self.queue.popleft()
+        g = len(picked)
+        dev, s = self.desc.device, self.stream
+        n = np.array([r.n for r in picked], dtype=np.int64)
+        e = np.array([len(r.col) for r in picked], dtype=np.int64)
+        steps = np.array([r.steps for r in picked], dtype=np.int64)
+        wb = (n + 15) // 16 * 16
+        rp_off = np.concatenate([[0], np.cumsum(n + 1)])
+        col_off = np.concatenate([[0], np.cumsum(e)])
+        w_off = np.concatenate([[0], np.cumsum(wb)])
+        c_off = np.concatenate([[0], np.cumsum(3 * steps)])
+        slots = [self.free_slots.pop() for _ in range(g)]
         with torch.cuda.stream(s):
-            rp = torch.as_tensor(req.row_ptr).to(dev, non_blocking=True)
-            col = torch.as_tensor(req.col).to(dev, non_blocking=True)
-            st8 = torch.as_tensor(req.state).to(dev, non_blocking=True)
-            st = torch.empty(word_bytes(req.n), dtype=torch.uint8, device=dev)
-            hubs = torch.empty(req.n, dtype=torch.int32, device=dev)
-            pack_words(st8, rp, col, col, st, hubs, s)
-            counts = torch.zeros(req.steps * 3, dtype=torch.int32, device=dev)
-            rng = model_rngs([req.seed])
-        host_state = np.asarray(req.state)
-        row = np.zeros(1, dtype=INSTANCE_DTYPE)
-        row["row_ptr"] = rp.data_ptr()
-        row["adj"] = col.data_ptr()
-        row["words"] = st.data_ptr()
-        row["hub_counts"] = hubs.data_ptr()
-        row["counts"] = counts.data_ptr()
-        row["done_flag"] = self.done.data_ptr() + 4 * slot
-        row["n"] = req.n
-        row["t"] = 0
-        row["steps"] = req.steps
-        row["beta"] = req.beta
-        row["gamma"] = req.gamma
-        row["num_s"] = int((host_state == 0).sum())
-        row["num_i"] = int((host_state == 1).sum())
-        row["num_r"] = int((host_state == 2).sum())
-        self.done[slot] = 0
-        self.h_desc[slot] = torch.from_numpy(row.view(np.int32).copy())
+            rp = torch.empty(int(rp_off[-1]), dtype=torch.int32, device=dev)
+            col = torch.empty(int(col_off[-1]), dtype=torch.int32, device=dev)
+            st8 = torch.empty(int(w_off[-1]), dtype=torch.int8, device=dev)
+            words = torch.empty(int(w_off[-1]), dtype=torch.uint8, device=dev)
+            hubs = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
+            counts = torch.zeros(int(c_off[-1]), dtype=torch.int32, device=dev)
+            for k, r in enumerate(picked):
+                rp[rp_off[k]:rp_off[k + 1]].copy_(torch.as_tensor(r.row_ptr), non_blocking=True)
+                col[col_off[k]:col_off[k + 1]].copy_(torch.as_tensor(r.col), non_blocking=True)
+                st8[w_off[k]:w_off[k] + n[k]].copy_(torch.as_tensor(r.state), non_blocking=True)
+            rngs = model_rngs([r.seed for r in picked])
+        sizes = np.array([np.bincount(np.asarray(r.state, dtype=np.int8).astype(np.int64),
+                                      minlength=3)[:3] for r in picked], dtype=np.int32)
+        rows = np.zeros(g, dtype=INSTANCE_DTYPE)
+        rows["row_ptr"] = rp.data_ptr() + 4 * rp_off[:-1]
+        rows["adj"] = col.data_ptr() + 4 * col_off[:-1]
+        rows["words"] = words.data_ptr() + w_off[:-1]
+        rows["hub_counts"] = hubs.data_ptr() + 4 * w_off[:-1]
+        rows["counts"] = counts.data_ptr() + 4 * c_off[:-1]
+        rows["done_flag"] = self.done.data_ptr() + 4 * np.asarray(slots, dtype=np.int64)
+        rows["n"] = n
+        rows["steps"] = steps
+        rows["beta"] = [r.beta for r in picked]
+        rows["gamma"] = [r.gamma for r in picked]
+        rows["num_s"], rows["num_i"], rows["num_r"] = sizes[:, 0], sizes[:, 1], sizes[:, 2]
+        work = np.concatenate([tiles_for(slot, int(nk)) for slot, nk in zip(slots, n)])
+        for slot in slots:
+            self.done[slot] = 0
+        h_rows = torch.from_numpy(rows.view(np.int32).reshape(g, -1).copy()).pin_memory()
+        h_work = torch.from_numpy(work).pin_memory()
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
         with torch.cuda.stream(s):
-            self.desc[slot].copy_(self.h_desc[slot], non_blocking=True)
-            self.desc[slot, RNG_WORD:RNG_WORD + 2] = rng[0]
-        req._slot = slot
-        req._bufs = (rp, col, st, hubs, counts)
-        req.admitted = time.perf_counter()
-        self.active[slot] = req
-        self._tiles_used += self._tiles(req)
+            d_rows = h_rows.to(dev, non_blocking=True)
+            d_rows[:, RNG_WORD:RNG_WORD + 2] = rngs
+            self.desc.index_copy_(0, torch.as_tensor(slots, device=dev), d_rows)
+            d_work = h_work.to(dev, non_blocking=True)
+            _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(d_work), work.shape[0],
+                      _dev.ptr(st8), _dev.ptr(words), _dev.ptr(status), s.cuda_stream)
+            # staging buffers stay alive until the copies and the pack have run
+            done_ev = torch.cuda.Event()
+            done_ev.record(s)
+        group = _Group((rp, col, st8, words, hubs, counts, h_rows, h_work, d_work, status,
+                        done_ev))
+        now = time.perf_counter()
+        for k, (req, slot) in enumerate(zip(picked, slots)):
+            req._slot = slot
+            req._bufs = (group, words[w_off[k]:w_off[k] + n[k]],
+                         counts[c_off[k]:c_off[k + 1]])
+            req.admitted = now
+            self.active[slot] = req
+            self._tiles_used += self._tiles(req)
         self._work_dirty = True
-        return True
+        return g
 
     def _rebuild_work(self):
         # the pinned staging buffers may still feed the previous rebuild's copies
@@ -228,7 +281,7 @@ class SIRServer:
         finished = [slot for slot in self.active if int(self.done[slot]) == 1]
         for slot in finished:
             req = self.active.pop(slot)
-            rp, col, st, hubs, counts = req._bufs
+            group, st, counts = req._bufs
             with torch.cuda.stream(self.stream):
                 req.counts = torch.empty((req.steps, 3), dtype=torch.int32).pin_memory()
                 req.counts.copy_(counts.view(req.steps, 3), non_blocking=True)
@@ -256,8 +309,7 @@ class SIRServer:
         """Admit what fits, advance every resident request by steps_per_tick steps, and
         harvest completions."""
         self._harvest()
-        while self.queue and self._try_admit(self.queue[0]):
-            self.queue.popleft()
+        self._admit()
         if self._work_dirty:
             self._rebuild_work()
         if self.active:
