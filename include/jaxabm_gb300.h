@@ -138,13 +138,15 @@ ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_
                                      int32_t* col, int64_t col_capacity);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (136 bytes, 8-byte aligned).
+/* Device-side descriptor of one SIR model instance (144 bytes, 8-byte aligned).
  * words holds one byte per agent, (infected neighbours << 2) | compartment (0 S, 1 I,
  * 2 R); an agent of degree >= abm_sir_hub_degree() (a hub) has 63 in the count field and
  * its count in hub_counts[i] (int32[n]).  words is 16-byte aligned and round_up(n, 16)
- * bytes long (padding bytes read as R).  adj is the instance's CSR column array with
- * bit 31 set on entries whose neighbour is a hub.  All three are written by
- * abm_sir_pack / abm_sir_pack_batch; abm_sir_unpack reads the compartments back.
+ * bytes long (padding bytes read as R).  comp holds the compartments again, 2 bits per
+ * agent (agent i in bits 2(i%16)..2(i%16)+1 of comp[i/16]; round_up(n,16)/16 words).
+ * adj is the instance's CSR column array with bit 31 set on entries whose neighbour is a
+ * hub.  All four are written by abm_sir_pack / abm_sir_pack_batch; abm_sir_unpack reads
+ * the compartments back.
  * The collection key of step t is coll_keys[t] (uint32[steps][2]) when coll_keys is not
  * NULL, else it is derived from rng, the instance's Model.step key-chain state
  * (jaxabm/model.py:156,164), which is advanced once per step either way.  num_s/num_i/num_r
@@ -159,6 +161,7 @@ typedef struct abm_sir_instance {
   int32_t* adj;
   uint8_t* words;
   int32_t* hub_counts;
+  uint32_t* comp;
   int32_t* counts;
   int32_t* done_flag;
   const uint32_t* coll_keys;
@@ -200,18 +203,18 @@ ABM_API int32_t abm_sir_hub_degree(void);
 /* Words of one instance from int8 compartments state[n] (n < 2^29): compartments, hub
  * marks, infected-neighbour counts over the CSR (row_ptr[n+1], col[row_ptr[n]]); adj
  * (row_ptr[n] entries, may be col itself) receives the columns with hub tags; words
- * (16-byte aligned, round_up(n,16) bytes) and hub_counts (int32[n]) as described at
- * abm_sir_instance; sizes (device int32[3]) receives the S, I, R totals; *status (device
- * int32) becomes 1 on a compartment outside 0..2 (stored as R) or a column outside 0..n-1
- * (replaced by a self-loop). */
+ * (16-byte aligned, round_up(n,16) bytes), hub_counts (int32[n]) and comp
+ * (round_up(n,16)/16 words) as described at abm_sir_instance; sizes (device int32[3])
+ * receives the S, I, R totals; *status (device int32) becomes 1 on a compartment outside
+ * 0..2 (stored as R) or a column outside 0..n-1 (replaced by a self-loop). */
 ABM_API int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col,
                          int64_t n, int32_t* adj, uint8_t* words, int32_t* hub_counts,
-                         int32_t* sizes, int32_t* status, void* stream);
+                         uint32_t* comp, int32_t* sizes, int32_t* status, void* stream);
 
 /* abm_sir_pack for every tile of `work` at once, in place on each descriptor's adj: the
  * int8 compartments of an instance are read from states8 at the same byte offset as its
- * words from words_base.  Descriptors must already point at their CSR, words and hub
- * counts. */
+ * words from words_base.  Descriptors must already point at their CSR, words, hub counts
+ * and comp; tiles start at multiples of 16 agents. */
 ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
                                int32_t nwork, const int8_t* states8, const uint8_t* words_base,
                                int32_t* status, void* stream);

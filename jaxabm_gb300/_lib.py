@@ -50,7 +50,7 @@ SIGNATURES = {
     "abm_graph_barabasi_albert": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_graph_random_regular": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_sir_instance_size": (_sz, []),
-    "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p, _p, _p]),
+    "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p, _p, _p, _p]),
     "abm_sir_pack_batch": (_int, [_p, _p, _i32, _p, _p, _p, _p]),
     "abm_sir_unpack": (_int, [_p, _i64, _p, _p]),
     "abm_sir_changes_bytes": (_sz, [_i64, _i64]),

@@ -12,8 +12,9 @@
 // Work-efficient ("frontier") formulation over one byte per agent:
 //     word = (number of infected neighbours << 2) | compartment      (degree < 63)
 //     word = (63 << 2) | compartment, count in hub_counts[i]          (hubs: degree >= 63)
-// One byte per agent keeps the words of a whole 4,096-instance ensemble (~87 MB) inside
-// the 129 MB L2, so the random neighbour reads and count updates of a step are L2 traffic;
+// A second copy of the compartments, 2 bits per agent (16 agents per 32-bit word of
+// `comp`, ~22 MB for a 4,096-instance ensemble), serves the random neighbour reads of the
+// decisions from L2; the bytes (~87 MB) serve the sweep and the count updates;
 // CSR columns, row offsets and change entries are read with the streaming (evict-first)
 // policy so that they do not displace the words.  Column entries that point at a hub carry bit 31 (set
 // by abm_sir_pack), so a count update knows where its target's count lives without a
@@ -66,7 +67,7 @@ constexpr int kCompactEvery = 8;                   // steps between work-list co
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kS = 0, kI = 1;
 
-static_assert(sizeof(abm_sir_instance) == 136, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 144, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
 // List workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
@@ -103,6 +104,11 @@ __device__ __forceinline__ int live_count(const int32_t* live, int nwork) {
 // Column entry k of a row, read once (streaming policy: evict first from L1 and L2).
 __device__ __forceinline__ uint32_t ld_col(const int32_t* __restrict__ adj, int k) {
   return static_cast<uint32_t>(__ldcs(adj + k));
+}
+
+// Compartment of agent t from the 2-bit compartment array (16 agents per 32-bit word).
+__device__ __forceinline__ uint32_t comp_of(const uint32_t* __restrict__ comp, uint32_t t) {
+  return (comp[t >> 4] >> (2u * (t & 15u))) & 3u;
 }
 
 // Fire-and-forget global reduction (no value returned, so the issuing warp never waits
@@ -149,12 +155,38 @@ __device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4 * kVecs], int 
   return (q[j >> 2] >> (8 * (j & 3))) & 0xFFu;
 }
 
-__device__ __forceinline__ void record_change(bool changed, int inst, int i, int ns, Lists& L,
-                                              int lane) {
-  const int pos = warp_append(changed, &L.hdr->changes, lane);
-  if (changed) {
-    if (pos < L.capacity) L.changes[pos] = make_int2(inst, (i << 2) | ns);
+// Changes buffered per warp in shared memory and appended to the change list 32 at a time
+// (one counter atomic per 32 changes instead of one per pass).
+constexpr int kBuf = 64;
+
+__device__ __forceinline__ void flush_changes(int2* buf, int k, Lists& L, int lane) {
+  if (k == 0) return;  // uniform over the warp
+  int base = 0;
+  if (lane == 0) base = atomicAdd(&L.hdr->changes, k);
+  base = __shfl_sync(kFull, base, 0);
+  if (lane < k) {
+    const int pos = base + lane;
+    if (pos < L.capacity) L.changes[pos] = buf[lane];
     else L.hdr->overflow = 1;
+  }
+}
+
+__device__ __forceinline__ void buffer_change(bool changed, int2 entry, int2* buf, int& count,
+                                              Lists& L, int lane) {
+  const unsigned m = __ballot_sync(kFull, changed);
+  if (!m) return;
+  if (changed) buf[count + __popc(m & ((1u << lane) - 1u))] = entry;
+  count += __popc(m);
+  __syncwarp();
+  if (count >= 32) {
+    flush_changes(buf, 32, L, lane);
+    const int rest = count - 32;
+    int2 v = make_int2(0, 0);
+    if (lane < rest) v = buf[32 + lane];
+    __syncwarp();
+    if (lane < rest) buf[lane] = v;
+    __syncwarp();
+    count = rest;
   }
 }
 
@@ -186,8 +218,11 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
   __shared__ int swarp[kWarpsPerCta];
   __shared__ int sbase;
   __shared__ uint16_t squeue[kWarpsPerCta][kSub];
+  __shared__ int2 sbuf[kWarpsPerCta][kBuf];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint16_t* __restrict__ queue = squeue[warp];
+  int2* buf = sbuf[warp];
+  int nbuf = 0;
   const int nwork = live_count(live, nwork_max);
   for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
     const int4 item = work[w];
@@ -287,13 +322,14 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
           changed = abm::unit_float(abm::bits_at(krec, 0)) < gamma;
         }
         ir += changed;
-        record_change(changed, item.x, i, 2, L, lane);
+        buffer_change(changed, make_int2(item.x, (i << 2) | 2), buf, nbuf, L, lane);
       }
       ir = __reduce_add_sync(kFull, ir);
       if (lane == 0 && ir) atomicAdd(&I->step_ir, ir);
     }
     __syncthreads();  // swarp, sbase and the queues are rewritten by the next tile
   }
+  flush_changes(buf, nbuf, L, lane);
 }
 
 // Susceptible candidates: one lane each scans its CSR row, eight slots per pass (the eight
@@ -303,14 +339,22 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
 // the change list; no word is written, so every decision sees the pre-step states.
 __global__ void __launch_bounds__(kSirThreads, 5)
 sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
+  __shared__ int2 sbuf[kWarpsPerCta][kBuf];
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * kWarpsPerCta;
   const int wid = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  int2* buf = sbuf[threadIdx.x >> 5];
+  int nbuf = 0;
   const int ns_count = min(L.hdr->cand_s, L.capacity);
-  for (int b = wid * 32; b < ns_count; b += warps * 32) {
+  const int stride = warps * 32;
+  // the lane's entry for the next pass is loaded one pass ahead
+  int2 e_next = make_int2(0, 0);
+  if (wid * 32 + lane < ns_count) e_next = __ldcs(&L.cands[wid * 32 + lane]);
+  for (int b = wid * 32; b < ns_count; b += stride) {
     const int k = b + lane;
     const bool valid = k < ns_count;
-    const int2 e = valid ? __ldcs(&L.cands[k]) : make_int2(0, 0);
+    const int2 e = e_next;
+    if (k + stride < ns_count) e_next = __ldcs(&L.cands[k + stride]);
     const int inst = e.x & ((1 << kInstBits) - 1), i = e.y;
     const abm_sir_instance* I = insts + inst;
     int cnt = static_cast<int>(static_cast<uint32_t>(e.x) >> kInstBits);
@@ -319,13 +363,13 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     unsigned imask = 0;
     uint2 coll = make_uint2(0, 0);
     const int32_t* __restrict__ adj = nullptr;
-    const uint8_t* __restrict__ words = nullptr;
+    const uint32_t* __restrict__ comp = nullptr;
     float beta = 0.f;
     if (valid) {
       if (cnt == static_cast<int>(kHubMark)) cnt = I->hub_counts[i];
       coll = make_uint2(I->coll[0], I->coll[1]);
       adj = I->adj;
-      words = I->words;
+      comp = I->comp;
       beta = I->beta;
       const int32_t* __restrict__ rp = I->row_ptr;
       row0 = __ldcs(rp + i);
@@ -342,7 +386,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           for (int c = 0; c < kChunk; ++c)
             nb[c] = k1 + c < deg ? static_cast<int>(ld_col(adj, row0 + k1 + c) & kIdx) : -1;
 #pragma unroll
-          for (int c = 0; c < kChunk; ++c) wn[c] = nb[c] >= 0 ? words[nb[c]] : 0u;
+          for (int c = 0; c < kChunk; ++c) wn[c] = nb[c] >= 0 ? comp_of(comp, nb[c]) : 0u;
 #pragma unroll
           for (int c = 0; c < kChunk; ++c) {
             const bool inf = nb[c] >= 0 && (wn[c] & 3u) == kI;
@@ -382,8 +426,8 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const float hbeta = __shfl_sync(kFull, beta, src);
       const int32_t* __restrict__ hadj = reinterpret_cast<const int32_t*>(
           __shfl_sync(kFull, reinterpret_cast<unsigned long long>(adj), src));
-      const uint8_t* __restrict__ hwords = reinterpret_cast<const uint8_t*>(
-          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(words), src));
+      const uint32_t* __restrict__ hcomp = reinterpret_cast<const uint32_t*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(comp), src));
       const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
       int c = 0;
@@ -397,7 +441,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
 #pragma unroll
         for (int u = 0; u < kHeavyUnroll; ++u) {
           const int slot = c + 32 * u + lane;
-          wv[u] = slot < hdeg ? static_cast<uint32_t>(hwords[wv[u] & kIdx]) : 0u;
+          wv[u] = slot < hdeg ? comp_of(hcomp, wv[u] & kIdx) : 0u;
         }
         bool f = false;
         int seen = 0;
@@ -418,9 +462,10 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       }
     }
 
-    record_change(infected, inst, i, static_cast<int>(kI), L, lane);
+    buffer_change(infected, make_int2(inst, (i << 2) | static_cast<int>(kI)), buf, nbuf, L, lane);
     add_decided(valid, inst, scanned, infected ? 1 : 0, insts, lane);
   }
+  flush_changes(buf, nbuf, L, lane);
 }
 
 // Neighbours' infected counts +-1 and own compartment +1 for every change: one thread per
@@ -448,6 +493,7 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const uintptr_t a = reinterpret_cast<uintptr_t>(I->words + agent);
       red_add(reinterpret_cast<uint32_t*>(a & ~static_cast<uintptr_t>(3)),
               1u << (8u * static_cast<uint32_t>(a & 3)));
+      red_add(I->comp + (agent >> 4), 1u << (2u * static_cast<uint32_t>(agent & 15)));
     }
     // slots pushed, summed per instance over the warp's lanes
     {
@@ -663,6 +709,35 @@ __global__ void sir_pack_count_tiles_kernel(const abm_sir_instance* __restrict__
   }
 }
 
+// Pass 1b, group g of 16 agents: their compartments as 2-bit fields of comp[g] (from the
+// bytes of pass 1; padding bytes read as R).
+__device__ __forceinline__ void pack_comp_group(const uint8_t* __restrict__ words,
+                                                uint32_t* __restrict__ comp, int g) {
+  const uint4 v = *reinterpret_cast<const uint4*>(words + 16 * g);
+  const uint32_t q[4] = {v.x, v.y, v.z, v.w};
+  uint32_t w = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) w |= ((q[j >> 2] >> (8 * (j & 3))) & 3u) << (2 * j);
+  comp[g] = w;
+}
+
+__global__ void sir_pack_comp_kernel(const uint8_t* __restrict__ words, int ngroups,
+                                     uint32_t* __restrict__ comp) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < ngroups) pack_comp_group(words, comp, g);
+}
+
+__global__ void sir_pack_comp_tiles_kernel(const abm_sir_instance* __restrict__ insts,
+                                           const int4* __restrict__ work, int nwork) {
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    const int4 item = work[w];
+    const abm_sir_instance* I = insts + item.x;
+    const int end = item.z == I->n ? static_cast<int>(round16(I->n)) : item.z;
+    for (int g = item.y / 16 + threadIdx.x; g < (end + 15) / 16; g += blockDim.x)
+      pack_comp_group(I->words, I->comp, g);
+  }
+}
+
 __global__ void sir_unpack_kernel(const uint8_t* __restrict__ words, int n,
                                   int8_t* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -673,7 +748,7 @@ __global__ void sir_unpack_kernel(const uint8_t* __restrict__ words, int n,
 // no host-to-device copy and can be captured in a CUDA graph.
 __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int ntiles,
                                         const int32_t* row_ptr, int32_t* adj, uint8_t* words,
-                                        int32_t* hubs, int32_t* counts,
+                                        int32_t* hubs, uint32_t* comp, int32_t* counts,
                                         const uint32_t* coll_keys, int32_t n, int32_t steps,
                                         float beta, float gamma, const int32_t* sizes) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -682,6 +757,7 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
     d->adj = adj;
     d->words = words;
     d->hub_counts = hubs;
+    d->comp = comp;
     d->counts = counts;
     d->done_flag = nullptr;
     d->coll_keys = coll_keys;
@@ -769,12 +845,12 @@ size_t abm_sir_changes_bytes(int64_t max_agents, int64_t max_tiles) {
 }
 
 int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col, int64_t n,
-                 int32_t* adj, uint8_t* words, int32_t* hub_counts, int32_t* sizes,
-                 int32_t* status, void* stream) {
-  if (!state || !row_ptr || !col || !adj || !words || !hub_counts || !sizes || !status ||
-      n <= 0 || n >= (1ll << 29))
+                 int32_t* adj, uint8_t* words, int32_t* hub_counts, uint32_t* comp,
+                 int32_t* sizes, int32_t* status, void* stream) {
+  if (!state || !row_ptr || !col || !adj || !words || !hub_counts || !comp || !sizes ||
+      !status || n <= 0 || n >= (1ll << 29))
     return ABM_ERR_BADARG;
-  if (!abm_host::aligned(words, 16)) return ABM_ERR_BADARG;
+  if (!abm_host::aligned(words, 16) || !abm_host::aligned(comp, 4)) return ABM_ERR_BADARG;
   cudaStream_t s = abm_host::as_stream(stream);
   int st = abm_host::record_cuda_error(cudaMemsetAsync(sizes, 0, 3 * sizeof(int32_t), s),
                                        "abm_sir_pack/sizes");
@@ -786,6 +862,9 @@ int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col
   sir_pack_mark_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(
       state, row_ptr, (int)n, (int)npad, words, sizes, status);
   if ((st = abm_host::check_launch("abm_sir_pack/mark"))) return st;
+  const int ngroups = (int)(npad / 16);
+  sir_pack_comp_kernel<<<(ngroups + 255) / 256, 256, 0, s>>>(words, ngroups, comp);
+  if ((st = abm_host::check_launch("abm_sir_pack/comp"))) return st;
   sir_pack_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(row_ptr, col, adj, (int)n,
                                                                    words, hub_counts, status);
   return abm_host::check_launch("abm_sir_pack/count");
@@ -805,6 +884,8 @@ int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
                                                                          states8, words_base,
                                                                          status);
   if ((st = abm_host::check_launch("abm_sir_pack_batch/mark"))) return st;
+  sir_pack_comp_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(insts, w4, nwork);
+  if ((st = abm_host::check_launch("abm_sir_pack_batch/comp"))) return st;
   sir_pack_count_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(insts, w4, nwork,
                                                                           status);
   return abm_host::check_launch("abm_sir_pack_batch/count");
@@ -874,7 +955,8 @@ size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges) {
   if (n <= 0 || num_edges < 0) return 0;
   const int64_t tiles = (n + kTile - 1) / kTile;
   return align256(sizeof(abm_sir_instance)) + align256((size_t)tiles * sizeof(int4)) +
-         align256((size_t)round16(n)) + align256((size_t)n * sizeof(int32_t)) + 256 +
+         align256((size_t)round16(n)) + align256((size_t)n * sizeof(int32_t)) +
+         align256((size_t)round16(n) / 4) + 256 +
          align256((size_t)num_edges * sizeof(int32_t)) + align256(abm_sir_changes_bytes(n, tiles));
 }
 
@@ -900,19 +982,21 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t n
   p += align256((size_t)round16(n));
   int32_t* hubs = reinterpret_cast<int32_t*>(p);
   p += align256((size_t)n * sizeof(int32_t));
+  uint32_t* comp = reinterpret_cast<uint32_t*>(p);
+  p += align256((size_t)round16(n) / 4);
   int32_t* misc = reinterpret_cast<int32_t*>(p);  // sizes[3], status
   p += 256;
   int32_t* adj = reinterpret_cast<int32_t*>(p);
   p += align256((size_t)num_edges * sizeof(int32_t));
   void* lists = p;
-  int st = abm_sir_pack(state, row_ptr, col, n, adj, words, hubs, misc, misc + 3, stream);
+  int st = abm_sir_pack(state, row_ptr, col, n, adj, words, hubs, comp, misc, misc + 3, stream);
   if (st) return st;
   st = abm_host::record_cuda_error(cudaMemsetAsync(lists, 0, sizeof(ListHeader), s),
                                    "abm_sir_run/lists");
   if (st) return st;
   sir_setup_single_kernel<<<(ntiles + 255) / 256, 256, 0, s>>>(
-      d, work, ntiles, row_ptr, adj, words, hubs, counts, coll_keys, (int32_t)n, steps, beta,
-      gamma, misc);
+      d, work, ntiles, row_ptr, adj, words, hubs, comp, counts, coll_keys, (int32_t)n, steps,
+      beta, gamma, misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
   st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps,

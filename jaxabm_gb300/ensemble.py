@@ -25,16 +25,17 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 8192  # agents per work item (abm_sir_tile_agents)
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 136 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 144 bytes
 INSTANCE_DTYPE = np.dtype([
     ("row_ptr", "<u8"), ("adj", "<u8"), ("words", "<u8"), ("hub_counts", "<u8"),
-    ("counts", "<u8"), ("done_flag", "<u8"), ("coll_keys", "<u8"), ("rng", "<u4", (2,)),
+    ("comp", "<u8"), ("counts", "<u8"), ("done_flag", "<u8"), ("coll_keys", "<u8"),
+    ("rng", "<u4", (2,)),
     ("n", "<i4"), ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"),
     ("num_s", "<i4"), ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"),
     ("step_ir", "<i4"), ("edges_scanned", "<u8"), ("edges_pushed", "<u8"),
     ("candidates", "<u8"), ("coll", "<u4", (2,)),
 ])
-assert INSTANCE_DTYPE.itemsize == 136
+assert INSTANCE_DTYPE.itemsize == 144
 WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
@@ -99,14 +100,15 @@ def word_bytes(n):
     return (int(n) + 15) // 16 * 16
 
 
-def pack_words(state_i8, row_ptr, col, adj, words, hub_counts, stream=None):
+def pack_words(state_i8, row_ptr, col, adj, words, hub_counts, comp, stream=None):
     """Per-agent words of one instance (compartment, hub mark, infected-neighbour count),
-    the hub counts and the hub-tagged columns ``adj`` (may be ``col`` itself)."""
+    the hub counts, the 2-bit compartments and the hub-tagged columns ``adj`` (may be
+    ``col`` itself)."""
     n = state_i8.numel()
     scratch = torch.zeros(4, dtype=torch.int32, device=words.device)
     _lib.call("abm_sir_pack", _dev.ptr(state_i8), _dev.ptr(row_ptr), _dev.ptr(col), n,
-              _dev.ptr(adj), _dev.ptr(words), _dev.ptr(hub_counts), _dev.ptr(scratch),
-              _dev.ptr(scratch[3:]), _dev.stream_handle(stream))
+              _dev.ptr(adj), _dev.ptr(words), _dev.ptr(hub_counts), _dev.ptr(comp),
+              _dev.ptr(scratch), _dev.ptr(scratch[3:]), _dev.stream_handle(stream))
     return scratch
 
 
@@ -154,6 +156,7 @@ class SIRBatch:
         self.state8 = torch.from_numpy(h_st).to(dev)
         self.words = torch.empty(int(w_off[-1]), dtype=torch.uint8, device=dev)
         self.hub_counts = torch.zeros(int(w_off[-1]), dtype=torch.int32, device=dev)
+        self.comp = torch.zeros(int(w_off[-1]) // 16, dtype=torch.int32, device=dev)
         self.counts = torch.zeros(int(cnt_off[-1]), dtype=torch.int32, device=dev)
         self._offsets = (rp_off, col_off, w_off, cnt_off)
         sizes = np.array([[int((st == c).sum()) for c in (0, 1, 2)] for st in init_states],
@@ -164,6 +167,7 @@ class SIRBatch:
         desc["adj"] = self.col.data_ptr() + 4 * col_off[:-1]
         desc["words"] = self.words.data_ptr() + w_off[:-1]
         desc["hub_counts"] = self.hub_counts.data_ptr() + 4 * w_off[:-1]
+        desc["comp"] = self.comp.data_ptr() + w_off[:-1] // 4
         desc["counts"] = self.counts.data_ptr() + 4 * cnt_off[:-1]
         desc["n"] = self.n
         desc["steps"] = self.steps
@@ -182,14 +186,16 @@ class SIRBatch:
             raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
         self.words0 = self.words.clone()
         self.hub_counts0 = self.hub_counts.clone()
+        self.comp0 = self.comp.clone()
         self.changes = changes_workspace(int(self.n.sum()), self.work.shape[0])
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_steps = None
 
     def pack(self, stream=None):
-        """Words and hub counts of every instance from the int8 compartments in ``state8``;
-        tags the hub entries of ``col`` in place (two launches)."""
+        """Words, hub counts and 2-bit compartments of every instance from the int8
+        compartments in ``state8``; tags the hub entries of ``col`` in place (three
+        launches)."""
         _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(self.work),
                   self.work.shape[0], _dev.ptr(self.state8), _dev.ptr(self.words),
                   _dev.ptr(self._status), _dev.stream_handle(stream))
@@ -212,6 +218,7 @@ class SIRBatch:
         """Back to step 0 (words, counters, key chains) without reallocating."""
         self.words.copy_(self.words0)
         self.hub_counts.copy_(self.hub_counts0)
+        self.comp.copy_(self.comp0)
         self.desc.copy_(self.desc0)
 
     def launch(self, nsteps, stream=None):

@@ -69,9 +69,9 @@ class Request:
 
     def device_bytes(self):
         n, e = self.n, len(self.col)
-        # CSR; int8 compartments, word bytes and hub counts (each padded to 16 agents);
-        # per-step counts
-        return 4 * (n + 1) + 4 * e + 6 * word_bytes(n) + 12 * self.steps
+        # CSR; int8 compartments, word bytes, hub counts and 2-bit compartments (each padded
+        # to 16 agents); per-step counts
+        return 4 * (n + 1) + 4 * e + 6 * word_bytes(n) + word_bytes(n) // 4 + 12 * self.steps
 
     @property
     def latency(self):
@@ -204,6 +204,7 @@ class SIRServer:
             st8 = torch.empty(int(w_off[-1]), dtype=torch.int8, device=dev)
             words = torch.empty(int(w_off[-1]), dtype=torch.uint8, device=dev)
             hubs = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
+            comp = torch.empty(int(w_off[-1]) // 16, dtype=torch.int32, device=dev)
             counts = torch.zeros(int(c_off[-1]), dtype=torch.int32, device=dev)
             for k, r in enumerate(picked):
                 rp[rp_off[k]:rp_off[k + 1]].copy_(torch.as_tensor(r.row_ptr), non_blocking=True)
@@ -217,6 +218,7 @@ class SIRServer:
         rows["adj"] = col.data_ptr() + 4 * col_off[:-1]
         rows["words"] = words.data_ptr() + w_off[:-1]
         rows["hub_counts"] = hubs.data_ptr() + 4 * w_off[:-1]
+        rows["comp"] = comp.data_ptr() + w_off[:-1] // 4
         rows["counts"] = counts.data_ptr() + 4 * c_off[:-1]
         rows["done_flag"] = self.done.data_ptr() + 4 * np.asarray(slots, dtype=np.int64)
         rows["n"] = n
@@ -240,8 +242,8 @@ class SIRServer:
             # staging buffers stay alive until the copies and the pack have run
             done_ev = torch.cuda.Event()
             done_ev.record(s)
-        group = _Group((rp, col, st8, words, hubs, counts, h_rows, h_work, d_work, status,
-                        done_ev))
+        group = _Group((rp, col, st8, words, hubs, comp, counts, h_rows, h_work, d_work,
+                        status, done_ev))
         now = time.perf_counter()
         for k, (req, slot) in enumerate(zip(picked, slots)):
             req._slot = slot
