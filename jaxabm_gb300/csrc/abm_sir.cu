@@ -117,6 +117,13 @@ __device__ __forceinline__ void red_add(uint32_t* p, uint32_t v) {
   asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ void red_add(int32_t* p, int32_t v) {
+  asm volatile("red.relaxed.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_add(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // Adds d to the infected-neighbour count of the agent that column entry v points at.
 __device__ __forceinline__ void add_count(uint8_t* words, int32_t* hubs, uint32_t v, int d) {
   const uint32_t t = v & kIdx;
@@ -199,8 +206,8 @@ __device__ __forceinline__ void add_decided(bool valid, int inst, int scanned, i
   const int s = __reduce_add_sync(group, scanned);
   const int f = __reduce_add_sync(group, infected);
   if (valid && lane == __ffs(group) - 1) {
-    if (s) atomicAdd(&insts[inst].edges_scanned, static_cast<unsigned long long>(s));
-    if (f) atomicAdd(&insts[inst].step_si, f);
+    if (s) red_add(&insts[inst].edges_scanned, static_cast<unsigned long long>(s));
+    if (f) red_add(&insts[inst].step_si, f);
   }
 }
 
@@ -289,7 +296,7 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
       for (int x = 0; x < kWarpsPerCta; ++x) total += swarp[x];
       const int ts = total & 0xFFFF, ti = total >> 16;
       sbase = ts ? atomicAdd(&L.hdr->cand_s, ts) : 0;
-      if (ts + ti) atomicAdd(&I->candidates, static_cast<unsigned long long>(ts + ti));
+      if (ts + ti) red_add(&I->candidates, static_cast<unsigned long long>(ts + ti));
     }
     __syncthreads();
     int pos_s = (incl - mine) & 0xFFFF;
@@ -325,7 +332,7 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
         buffer_change(changed, make_int2(item.x, (i << 2) | 2), buf, nbuf, L, lane);
       }
       ir = __reduce_add_sync(kFull, ir);
-      if (lane == 0 && ir) atomicAdd(&I->step_ir, ir);
+      if (lane == 0 && ir) red_add(&I->step_ir, ir);
     }
     __syncthreads();  // swarp, sbase and the queues are rewritten by the next tile
   }
@@ -347,14 +354,32 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   int nbuf = 0;
   const int ns_count = min(L.hdr->cand_s, L.capacity);
   const int stride = warps * 32;
-  // the lane's entry for the next pass is loaded one pass ahead
-  int2 e_next = make_int2(0, 0);
-  if (wid * 32 + lane < ns_count) e_next = __ldcs(&L.cands[wid * 32 + lane]);
+  // a lane's list entries are loaded two passes ahead and their row offsets one pass
+  // ahead, so a pass starts with both in registers
+  int2 e_next = make_int2(0, 0), e_next2 = make_int2(0, 0);
+  int r0_next = 0, r1_next = 0;
+  {
+    const int k = wid * 32 + lane;
+    if (k < ns_count) {
+      e_next = __ldcs(&L.cands[k]);
+      const int32_t* rp = insts[e_next.x & ((1 << kInstBits) - 1)].row_ptr;
+      r0_next = __ldcs(rp + e_next.y);
+      r1_next = __ldcs(rp + e_next.y + 1);
+    }
+    if (k + stride < ns_count) e_next2 = __ldcs(&L.cands[k + stride]);
+  }
   for (int b = wid * 32; b < ns_count; b += stride) {
     const int k = b + lane;
     const bool valid = k < ns_count;
     const int2 e = e_next;
-    if (k + stride < ns_count) e_next = __ldcs(&L.cands[k + stride]);
+    const int r0_cur = r0_next, r1_cur = r1_next;
+    e_next = e_next2;
+    if (k + stride < ns_count) {
+      const int32_t* rp = insts[e_next.x & ((1 << kInstBits) - 1)].row_ptr;
+      r0_next = __ldcs(rp + e_next.y);
+      r1_next = __ldcs(rp + e_next.y + 1);
+    }
+    if (k + 2 * stride < ns_count) e_next2 = __ldcs(&L.cands[k + 2 * stride]);
     const int inst = e.x & ((1 << kInstBits) - 1), i = e.y;
     const abm_sir_instance* I = insts + inst;
     int cnt = static_cast<int>(static_cast<uint32_t>(e.x) >> kInstBits);
@@ -371,9 +396,8 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       adj = I->adj;
       comp = I->comp;
       beta = I->beta;
-      const int32_t* __restrict__ rp = I->row_ptr;
-      row0 = __ldcs(rp + i);
-      deg = __ldcs(rp + i + 1) - row0;
+      row0 = r0_cur;
+      deg = r1_cur - r0_cur;
       heavy = deg > kHeavyDeg;
       if (!heavy) {
         // slots of infected neighbours (bit k: slot k), read until all `cnt` were seen;
@@ -500,7 +524,7 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const unsigned group = __match_any_sync(kFull, inst);
       const int sum = __reduce_add_sync(group, r1 - r0);
       if (valid && lane == __ffs(group) - 1 && sum)
-        atomicAdd(&I->edges_pushed, static_cast<unsigned long long>(sum));
+        red_add(&I->edges_pushed, static_cast<unsigned long long>(sum));
     }
     const bool heavy = valid && r1 - r0 > kHeavyDeg;
     if (valid && !heavy) {
