@@ -374,11 +374,60 @@ def model_lines():
         batch.forward(T, 20)
         batch.backward(target)
     ms_fa = _time_ms(fwd_adj, reps=1)
+    # two special-function ops (exponential, reciprocal) per edge, instance and step
+    mufu = 2.0 * len(col) * B * T
     out["opinion_n262144_b64_t200"] = {
         "instance_agent_steps_per_s_forward": n * B * T / (ms_f / 1e3), "ms_forward": ms_f,
         "ms_forward_plus_adjoint": ms_fa,
-        "instance_agent_steps_per_s_forward_plus_adjoint": n * B * T / (ms_fa / 1e3)}
+        "instance_agent_steps_per_s_forward_plus_adjoint": n * B * T / (ms_fa / 1e3),
+        "roofline_forward": {"bound": "sfu", "achieved": mufu / (ms_f / 1e3) / 1e12,
+                             "peak": SFU_TOPS, "unit": "T special-function ops/s",
+                             "frac": mufu / (ms_f / 1e3) / 1e12 / SFU_TOPS,
+                             "peak_kind": "nominal (152 SMs x 16 per clock x 2.07 GHz)"}}
+
+    hbm, _ = _peaks()
+    # K6 compaction of a 2^28-entry mask (half set, larger than L2) into int32 indices
+    n = 1 << 28
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    mask = (torch.rand(n, device="cuda", generator=g) < 0.5).view(torch.uint8)
+    idx = torch.empty(n, dtype=torch.int32, device="cuda")
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    ws = torch.empty(L.abm_select_workspace_bytes(n), dtype=torch.uint8, device="cuda")
+
+    def sel():
+        _lib.call("abm_select_indices", _dev.ptr(mask), n, _dev.ptr(idx), _dev.ptr(count),
+                  _dev.ptr(ws), ws.numel(), None)
+    ms = _time_ms(sel, reps=5)
+    k = int(count.item())
+    alg = n + 4 * k  # mask read once, indices written once
+    out["select_mask_268435456"] = {
+        "entries_per_s": n / (ms / 1e3), "ms": ms, "selected": k, "launches_per_call": 3,
+        "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": hbm,
+                     "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / hbm,
+                     "algorithmic_bytes": alg,
+                     "note": "1 B mask read + 4 B per selected index written; the kernels "
+                             "read the mask twice (count pass, scatter pass)"}}
+    del mask, idx, ws
+
+    # K1 sampler: jax.random.uniform(PRNGKey(0), (2^28,)) -- one threefry per element
+    out_u = torch.empty(n, dtype=torch.float32, device="cuda")
+    key = jr.PRNGKey(0)
+
+    def uni():
+        _lib.call("abm_rng_uniform", _dev.ptr(key), 1, n, 0.0, 1.0, _dev.ptr(out_u), 1, None)
+    ms = _time_ms(uni, reps=5)
+    out["rng_uniform_268435456"] = {
+        "samples_per_s": n / (ms / 1e3), "ms": ms,
+        "roofline": {"bound": "alu", "achieved": 4 * n / (ms / 1e3) / 1e9, "peak": hbm,
+                     "unit": "GB/s written", "frac": 4 * n / (ms / 1e3) / 1e9 / hbm,
+                     "note": "one threefry2x32-20 block per sample; HBM fraction of the "
+                             "4-byte writes"}}
     return out
+
+
+# nominal special-function (exponential / reciprocal) throughput: 152 SMs x 16 per clock
+SFU_TOPS = 152 * 16 * 2.07e9 / 1e12
 
 
 WORKLOADS = {"sir_ensemble": SIREnsembleBench}
