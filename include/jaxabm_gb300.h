@@ -318,6 +318,16 @@ ABM_API int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, cons
                             const float* tau, int32_t steps, int32_t ckpt_every,
                             float* checkpoints, void* stream);
 
+/* One forward step from o_in to o_out (distinct buffers); the reverse pass recomputes a
+ * segment's states from its checkpoint with it. */
+ABM_API int abm_opinion_step(const float* o_in, float* o_out, const int32_t* row_ptr,
+                             const int32_t* col, int64_t n, int32_t B, const float* mu,
+                             const float* eps, const float* tau, void* stream);
+
+/* inv_deg float32[n] = 1 / deg_i (0 for isolated nodes), read by abm_opinion_adjoint_step. */
+ABM_API int abm_opinion_inv_degree(const int32_t* row_ptr, int64_t n, float* inv_deg,
+                                   void* stream);
+
 ABM_API size_t abm_opinion_moments_workspace_bytes(int64_t n, int32_t B);
 
 /* Raw moments m_k = mean_i o_i^k, k = 1..4, per instance -> moments float64[B][4]. */
@@ -335,9 +345,9 @@ ABM_API size_t abm_opinion_grad_workspace_bytes(int64_t n, int32_t B);
 /* One reverse step at forward state o (= o^t): lam_out = lambda^t from lam_in =
  * lambda^{t+1}, and grad_partials += lambda^{t+1} . dF/d(mu, eps, tau). */
 ABM_API int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out,
-                                     const int32_t* row_ptr, const int32_t* col, int64_t n,
-                                     int32_t B, const float* mu, const float* eps,
-                                     const float* tau, double* grad_partials,
+                                     const int32_t* row_ptr, const int32_t* col,
+                                     const float* inv_deg, int64_t n, int32_t B, const float* mu,
+                                     const float* eps, const float* tau, double* grad_partials,
                                      size_t grad_partials_bytes, void* stream);
 
 /* grads float64[B][3] (d/dmu, d/deps, d/dtau) from the accumulated partials. */

@@ -96,13 +96,13 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
 // One adjoint step: lam_out from lam_in (= lambda^{t+1}) at the forward state o (= o^t);
 // gpart[cta][b][3] += this CTA's lambda * dF/d(mu, eps, tau).
 template <int LPN>
-__global__ void __launch_bounds__(kOpThreads)
+__global__ void __launch_bounds__(kOpThreads, 4)
 opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ lam_in,
                        float* __restrict__ lam_out, const int32_t* __restrict__ rp,
-                       const int32_t* __restrict__ col, int n, int B, const float* __restrict__ mu,
-                       const float* __restrict__ eps, const float* __restrict__ tau,
-                       double* __restrict__ gpart) {
-  extern __shared__ double sg[];  // [kOpThreads / LPN][B/4 groups -> per thread 12 values]
+                       const int32_t* __restrict__ col, const float* __restrict__ inv_deg, int n,
+                       int B, const float* __restrict__ mu, const float* __restrict__ eps,
+                       const float* __restrict__ tau, double* __restrict__ gpart) {
+  extern __shared__ float sg[];  // [kOpThreads][12]: this thread's 4 instances x 3 params
   const long long g = (long long)blockIdx.x * kOpThreads + threadIdx.x;
   const int node = (int)(g / LPN);
   const int sub = (int)(g % LPN);
@@ -117,9 +117,9 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     ld4(o + (size_t)node * B, sub, oi);
     ld4(lam_in + (size_t)node * B, sub, li);
     const int r0 = rp[node], r1 = rp[node + 1];
-    const float fdeg_i = (float)(r1 - r0);
+    const float inv_deg_i = inv_deg[node];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) li_d[c] = r1 > r0 ? li[c] / fdeg_i : li[c];
+    for (int c = 0; c < 4; ++c) li_d[c] = r1 > r0 ? li[c] * inv_deg_i : li[c];
     float sl[4] = {0.f, 0.f, 0.f, 0.f};  // sum_j g'(d) (lam_j/deg_j - lam_i/deg_i)
     float sgd[4] = {0.f, 0.f, 0.f, 0.f}, sse[4] = {0.f, 0.f, 0.f, 0.f}, sst[4] = {0.f, 0.f, 0.f, 0.f};
     for (int e = r0; e < r1; ++e) {
@@ -127,7 +127,7 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
       float oj[4], lj[4];
       ld4(o + (size_t)j * B, sub, oj);
       ld4(lam_in + (size_t)j * B, sub, lj);
-      const float inv_deg_j = 1.0f / (float)(rp[j + 1] - rp[j]);
+      const float inv_deg_j = inv_deg[j];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const float d = oj[c] - oi[c];
@@ -147,16 +147,17 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     for (int c = 0; c < 4; ++c) {
       lo[c] = fmaf(m[c], sl[c], li[c]);
       if (r1 > r0) {
-        gm[c] = li[c] * (sgd[c] / fdeg_i);
-        ge[c] = li[c] * m[c] * (sse[c] / fdeg_i);
-        gt[c] = li[c] * m[c] * (sst[c] / fdeg_i);
+        gm[c] = li[c] * (sgd[c] * inv_deg_i);
+        ge[c] = li[c] * m[c] * (sse[c] * inv_deg_i);
+        gt[c] = li[c] * m[c] * (sst[c] * inv_deg_i);
       }
     }
     reinterpret_cast<float4*>(lam_out + (size_t)node * B)[sub] = make_float4(lo[0], lo[1], lo[2], lo[3]);
   }
-  // per-CTA reduction of the parameter gradients per instance column (fixed order)
+  // per-CTA reduction of the parameter gradients per instance column (fixed order; float
+  // over the CTA's kNodes nodes, double across CTAs and steps)
   constexpr int kNodes = kOpThreads / LPN;
-  double* mine = sg + (size_t)threadIdx.x * 12;
+  float* mine = sg + (size_t)threadIdx.x * 12;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     mine[c] = gm[c];
@@ -166,12 +167,12 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
   __syncthreads();
   for (int q = threadIdx.x; q < LPN * 12; q += kOpThreads) {
     const int s_ = q / 12, v = q % 12;
-    double acc = 0.0;
+    float acc = 0.0f;
     for (int k = 0; k < kNodes; ++k) acc += sg[(size_t)(k * LPN + s_) * 12 + v];
     // v: param*4 + component; instance b = 4*s_ + component
     const int param = v / 4, c = v % 4;
     const int b = 4 * s_ + c;
-    gpart[((size_t)blockIdx.x * B + b) * 3 + param] += acc;
+    gpart[((size_t)blockIdx.x * B + b) * 3 + param] += (double)acc;
   }
 }
 
@@ -229,6 +230,14 @@ __global__ void sum_partials_kernel(const double* __restrict__ part, int nparts,
   double s = 0.0;
   for (int p = 0; p < nparts; ++p) s += part[(size_t)p * width + k];
   out[k] = s * scale;
+}
+
+__global__ void inv_degree_kernel(const int32_t* __restrict__ rp, int n, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const int d = rp[i + 1] - rp[i];
+    out[i] = d > 0 ? 1.0f / (float)d : 0.0f;
+  }
 }
 
 bool valid_batch(int B) { return B >= 4 && B <= 128 && (B & (B - 1)) == 0; }
@@ -291,6 +300,28 @@ int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, const int32_
   return ABM_OK;
 }
 
+int abm_opinion_step(const float* o_in, float* o_out, const int32_t* row_ptr, const int32_t* col,
+                     int64_t n, int32_t B, const float* mu, const float* eps, const float* tau,
+                     void* stream) {
+  if (!o_in || !o_out || o_in == o_out || !row_ptr || !col || !mu || !eps || !tau || n <= 0 ||
+      n > 0x7FFFFFFFll || !valid_batch(B))
+    return ABM_ERR_BADARG;
+  if (!abm_host::aligned(o_in, 16) || !abm_host::aligned(o_out, 16) || !abm_host::aligned(mu, 16) ||
+      !abm_host::aligned(eps, 16) || !abm_host::aligned(tau, 16))
+    return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  ABM_OP_DISPATCH(opinion_step_kernel, B / 4, step_blocks(n, B), 0, s, o_in, o_out, row_ptr, col,
+                  (int)n, B, mu, eps, tau);
+  return abm_host::check_launch("abm_opinion_step");
+}
+
+int abm_opinion_inv_degree(const int32_t* row_ptr, int64_t n, float* inv_deg, void* stream) {
+  if (!row_ptr || !inv_deg || n <= 0 || n > 0x7FFFFFFFll) return ABM_ERR_BADARG;
+  inv_degree_kernel<<<(unsigned)((n + 255) / 256), 256, 0, abm_host::as_stream(stream)>>>(
+      row_ptr, (int)n, inv_deg);
+  return abm_host::check_launch("abm_opinion_inv_degree");
+}
+
 size_t abm_opinion_moments_workspace_bytes(int64_t n, int32_t B) {
   if (n <= 0 || !valid_batch(B)) return 0;
   const int rows_per_cta = 1024;
@@ -336,10 +367,11 @@ size_t abm_opinion_grad_workspace_bytes(int64_t n, int32_t B) {
 }
 
 int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out,
-                             const int32_t* row_ptr, const int32_t* col, int64_t n, int32_t B,
-                             const float* mu, const float* eps, const float* tau,
-                             double* grad_partials, size_t grad_partials_bytes, void* stream) {
-  if (!o || !lam_in || !lam_out || !row_ptr || !col || !mu || !eps || !tau || n <= 0 ||
+                             const int32_t* row_ptr, const int32_t* col, const float* inv_deg,
+                             int64_t n, int32_t B, const float* mu, const float* eps,
+                             const float* tau, double* grad_partials, size_t grad_partials_bytes,
+                             void* stream) {
+  if (!o || !lam_in || !lam_out || !row_ptr || !col || !inv_deg || !mu || !eps || !tau || n <= 0 ||
       n > 0x7FFFFFFFll || !valid_batch(B) || lam_in == lam_out)
     return ABM_ERR_BADARG;
   if (!abm_host::aligned(o, 16) || !abm_host::aligned(lam_in, 16) ||
@@ -352,9 +384,9 @@ int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out
   cudaStream_t s = abm_host::as_stream(stream);
   const int lpn = B / 4;
   const int blocks = step_blocks(n, B);
-  const size_t smem = (size_t)kOpThreads * 12 * sizeof(double);
+  const size_t smem = (size_t)kOpThreads * 12 * sizeof(float);
   ABM_OP_DISPATCH(opinion_adjoint_kernel, lpn, blocks, smem, s, o, lam_in, lam_out, row_ptr, col,
-                  (int)n, B, mu, eps, tau, grad_partials);
+                  inv_deg, (int)n, B, mu, eps, tau, grad_partials);
   return abm_host::check_launch("abm_opinion_adjoint_step");
 }
 

@@ -54,50 +54,56 @@ select_count_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
 }
 
 // Single block: exclusive scan of tile_counts into tile_offsets (int64), total -> *count.
+// Thread t owns the contiguous chunk [t*per, (t+1)*per) of the tile counts: it sums the
+// chunk, the block scans the 1024 chunk sums, and the thread writes its chunk's offsets.
 __global__ void __launch_bounds__(1024)
 select_scan_kernel(const int32_t* __restrict__ tile_counts, int64_t ntiles,
                    int64_t* __restrict__ tile_offsets, int64_t* __restrict__ count) {
   __shared__ int64_t swarp[32];
-  __shared__ int64_t carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t b0 = 0; b0 < ntiles; b0 += 1024) {
-    const int64_t b = b0 + threadIdx.x;
-    const int64_t v = b < ntiles ? tile_counts[b] : 0;
-    int64_t incl = v;
+  const int64_t per = (ntiles + 1023) / 1024;
+  const int64_t c0 = (int64_t)threadIdx.x * per;
+  const int64_t c1 = c0 + per < ntiles ? c0 + per : ntiles;
+  int64_t sum = 0;
+#pragma unroll 8
+  for (int64_t b = c0; b < c1; ++b) sum += tile_counts[b];
+  int64_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) swarp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = swarp[lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int64_t u = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += u;
+      const int64_t u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
     }
-    if (lane == 31) swarp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-      int64_t w = swarp[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int64_t u = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += u;
-      }
-      swarp[lane] = w;  // inclusive over warps
-    }
-    __syncthreads();
-    const int64_t warp_excl = warp > 0 ? swarp[warp - 1] : 0;
-    if (b < ntiles) tile_offsets[b] = carry + warp_excl + incl - v;
-    __syncthreads();
-    if (threadIdx.x == 0) carry += swarp[31];
-    __syncthreads();
+    swarp[lane] = w;  // inclusive over warps
   }
-  if (threadIdx.x == 0) *count = carry;
+  __syncthreads();
+  int64_t run = (warp > 0 ? swarp[warp - 1] : 0) + incl - sum;
+#pragma unroll 8
+  for (int64_t b = c0; b < c1; ++b) {
+    tile_offsets[b] = run;
+    run += tile_counts[b];
+  }
+  if (threadIdx.x == 1023) *count = run;
 }
 
+// Each tile's selected indices, in ascending order, are staged in shared memory at their
+// rank within the tile and then written out by the whole block with coalesced stores.
 __global__ void __launch_bounds__(kSelThreads)
 select_scatter_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
                       const int64_t* __restrict__ tile_offsets, int32_t* __restrict__ out_idx) {
   __shared__ int swarp[kSelThreads / 32];
+  __shared__ int32_t sidx[kTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kSelPerThread;
+  const int64_t tile0 = (int64_t)blockIdx.x * kTile;
+  const int64_t base = tile0 + (int64_t)threadIdx.x * kSelPerThread;
   const uint32_t bits = load_flags(mask, n, base, vec_ok);
   const int c = __popc(bits);
   int incl = c;
@@ -108,15 +114,18 @@ select_scatter_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
   }
   if (lane == 31) swarp[warp] = incl;
   __syncthreads();
-  int warp_excl = 0;
-  for (int w = 0; w < warp; ++w) warp_excl += swarp[w];
-  int64_t pos = tile_offsets[blockIdx.x] + warp_excl + (incl - c);
-  uint32_t rest = bits;
-  while (rest) {
-    const int j = __ffs(rest) - 1;
-    rest &= rest - 1;
-    out_idx[pos++] = (int32_t)(base + j);
+  int warp_excl = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kSelThreads / 32; ++w) {
+    warp_excl += w < warp ? swarp[w] : 0;
+    total += swarp[w];
   }
+  int pos = warp_excl + (incl - c);
+  for (uint32_t rest = bits; rest; rest &= rest - 1)
+    sidx[pos++] = (int32_t)(base + __ffs(rest) - 1);
+  __syncthreads();
+  int32_t* __restrict__ dst = out_idx + tile_offsets[blockIdx.x];
+  for (int k = threadIdx.x; k < total; k += kSelThreads) dst[k] = sidx[k];
 }
 
 // out[r] = src[idx[r]] for rows of `row_bytes` bytes, copied in 4-byte words when possible.

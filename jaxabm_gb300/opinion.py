@@ -69,6 +69,7 @@ class OpinionBatch:
         self.o = self.o0.clone()
         self.tmp = torch.empty_like(self.o)
         self.ckpts = None
+        self.inv_deg = None  # 1 / degree per node, built by the first backward
         self.ckpt_every = None
         self.steps_done = 0
 
@@ -136,24 +137,28 @@ class OpinionBatch:
                   _dev.ptr(lam), _dev.stream_handle())
         gws = torch.zeros(_lib.load().abm_opinion_grad_workspace_bytes(self.n, self.B) // 8,
                           dtype=torch.float64, device=dev)
-        seg = torch.empty((k, self.n, self.B), dtype=torch.float32, device=dev)
-        scratch = torch.empty_like(self.o)
+        seg = torch.empty((k - 1, self.n, self.B), dtype=torch.float32, device=dev)
+        if self.inv_deg is None:
+            self.inv_deg = torch.empty(self.n, dtype=torch.float32, device=dev)
+            _lib.call("abm_opinion_inv_degree", _dev.ptr(self.rp), self.n, _dev.ptr(self.inv_deg),
+                      _dev.stream_handle())
         nseg = self.ckpts.shape[0]
         for s in range(nseg - 1, -1, -1):
             t0 = s * k
             length = min(k, T - t0)
-            # recompute o^{t0} .. o^{t0+length-1} from the checkpoint
-            seg[0].copy_(self.ckpts[s])
+            # recompute o^{t0+1} .. o^{t0+length-1} from the checkpoint o^{t0}
+            states = [self.ckpts[s]] + [seg[q] for q in range(length - 1)]
             for q in range(1, length):
-                seg[q].copy_(seg[q - 1])
-                _lib.call("abm_opinion_run", _dev.ptr(seg[q]), _dev.ptr(scratch), _dev.ptr(self.rp),
-                          _dev.ptr(self.col), self.n, self.B, _dev.ptr(self.mu), _dev.ptr(self.eps),
-                          _dev.ptr(self.tau), 1, 0, None, _dev.stream_handle())
-            for q in range(length - 1, -1, -1):
-                _lib.call("abm_opinion_adjoint_step", _dev.ptr(seg[q]), _dev.ptr(lam),
-                          _dev.ptr(lam2), _dev.ptr(self.rp), _dev.ptr(self.col), self.n, self.B,
+                _lib.call("abm_opinion_step", _dev.ptr(states[q - 1]), _dev.ptr(states[q]),
+                          _dev.ptr(self.rp), _dev.ptr(self.col), self.n, self.B,
                           _dev.ptr(self.mu), _dev.ptr(self.eps), _dev.ptr(self.tau),
-                          _dev.ptr(gws), gws.numel() * 8, _dev.stream_handle())
+                          _dev.stream_handle())
+            for q in range(length - 1, -1, -1):
+                _lib.call("abm_opinion_adjoint_step", _dev.ptr(states[q]), _dev.ptr(lam),
+                          _dev.ptr(lam2), _dev.ptr(self.rp), _dev.ptr(self.col),
+                          _dev.ptr(self.inv_deg), self.n, self.B, _dev.ptr(self.mu),
+                          _dev.ptr(self.eps), _dev.ptr(self.tau), _dev.ptr(gws), gws.numel() * 8,
+                          _dev.stream_handle())
                 lam, lam2 = lam2, lam
         grads = torch.empty((self.B, 3), dtype=torch.float64, device=dev)
         _lib.call("abm_opinion_grad_reduce", _dev.ptr(gws), self.n, self.B, _dev.ptr(grads),
