@@ -14,16 +14,17 @@ thread_local char g_last_cuda_error[256] = "";
 
 constexpr int kThreads = 256;
 
+// Grids are 2-D: keys along y, a key's elements along x (no per-element division).
 __global__ void split_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t num,
                              uint32_t* __restrict__ out, int mode) {
-  const int64_t total = nkeys * num;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = g / num, i = g - k * num;
+  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
     const uint2 key = abm::load_key(keys + 2 * k);
-    const uint2 r = mode == ABM_RNG_PARTITIONABLE ? abm::split_at(key, (uint64_t)i)
-                                                  : abm::legacy_split_at(key, num, i);
-    reinterpret_cast<uint2*>(out)[g] = r;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < num;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const uint2 r = mode == ABM_RNG_PARTITIONABLE ? abm::split_at(key, (uint64_t)i)
+                                                    : abm::legacy_split_at(key, num, i);
+      reinterpret_cast<uint2*>(out)[k * num + i] = r;
+    }
   }
 }
 
@@ -31,21 +32,22 @@ __global__ void split_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, i
 template <int kKind>
 __global__ void sample_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t count,
                               float a, float b, void* __restrict__ out, int mode) {
-  const int64_t total = nkeys * count;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = g / count, i = g - k * count;
+  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
     const uint2 key = abm::load_key(keys + 2 * k);
-    const uint32_t w = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(key, (uint64_t)i)
-                                                     : abm::legacy_bits_at(key, count, i);
-    if (kKind == 0) {
-      static_cast<uint32_t*>(out)[g] = w;
-    } else if (kKind == 1) {
-      static_cast<float*>(out)[g] = abm::uniform_from_bits(w, a, b);
-    } else if (kKind == 2) {
-      static_cast<float*>(out)[g] = abm::normal_from_bits(w);
-    } else {
-      static_cast<uint8_t*>(out)[g] = abm::unit_float(w) < a ? 1 : 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t g = k * count + i;
+      const uint32_t w = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(key, (uint64_t)i)
+                                                       : abm::legacy_bits_at(key, count, i);
+      if (kKind == 0) {
+        static_cast<uint32_t*>(out)[g] = w;
+      } else if (kKind == 1) {
+        static_cast<float*>(out)[g] = abm::uniform_from_bits(w, a, b);
+      } else if (kKind == 2) {
+        static_cast<float*>(out)[g] = abm::normal_from_bits(w);
+      } else {
+        static_cast<uint8_t*>(out)[g] = abm::unit_float(w) < a ? 1 : 0;
+      }
     }
   }
 }
@@ -57,13 +59,10 @@ __global__ void sample_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, 
 __global__ void randint_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t count,
                                int32_t minval, int32_t maxval, int32_t* __restrict__ out,
                                int mode) {
-  const int64_t total = nkeys * count;
   const uint32_t span = maxval <= minval ? 1u : (uint32_t)((int64_t)maxval - (int64_t)minval);
   uint32_t mult = 65536u % span;
   mult = (mult * mult) % span;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = g / count, i = g - k * count;
+  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
     const uint2 key = abm::load_key(keys + 2 * k);
     uint2 k1, k2;
     if (mode == ABM_RNG_PARTITIONABLE) {
@@ -73,13 +72,16 @@ __global__ void randint_kernel(const uint32_t* __restrict__ keys, int64_t nkeys,
       k1 = abm::legacy_split_at(key, 2, 0);
       k2 = abm::legacy_split_at(key, 2, 1);
     }
-    const uint32_t hi = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k1, (uint64_t)i)
-                                                      : abm::legacy_bits_at(k1, count, i);
-    const uint32_t lo = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k2, (uint64_t)i)
-                                                      : abm::legacy_bits_at(k2, count, i);
-    uint32_t r = (hi % span) * mult + (lo % span);
-    r %= span;
-    out[g] = (int32_t)((uint32_t)minval + r);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const uint32_t hi = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k1, (uint64_t)i)
+                                                        : abm::legacy_bits_at(k1, count, i);
+      const uint32_t lo = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k2, (uint64_t)i)
+                                                        : abm::legacy_bits_at(k2, count, i);
+      uint32_t r = (hi % span) * mult + (lo % span);
+      r %= span;
+      out[k * count + i] = (int32_t)((uint32_t)minval + r);
+    }
   }
 }
 
@@ -107,12 +109,18 @@ __global__ void keychain_kernel(uint32_t* __restrict__ rng, int64_t ninst, int32
   rng[2 * inst + 1] = r.y;
 }
 
-int grid_for(int64_t total) {
-  int64_t blocks = (total + kThreads - 1) / kThreads;
+// 2-D grid for nkeys x count elements: x covers a key's elements, y the keys; at most
+// 16 CTAs per SM in total.
+dim3 grid_for(int64_t nkeys, int64_t count) {
   const int64_t cap = (int64_t)abm_host::sm_count() * 16;
-  if (blocks > cap) blocks = cap;
-  if (blocks < 1) blocks = 1;
-  return (int)blocks;
+  int64_t x = (count + kThreads - 1) / kThreads;
+  if (x > cap) x = cap;
+  if (x < 1) x = 1;
+  int64_t y = cap / x;
+  if (y > nkeys) y = nkeys;
+  if (y > 65535) y = 65535;
+  if (y < 1) y = 1;
+  return dim3((unsigned)x, (unsigned)y);
 }
 
 bool bad_mode(int mode) { return mode != ABM_RNG_LEGACY && mode != ABM_RNG_PARTITIONABLE; }
@@ -123,8 +131,7 @@ int launch_sample(const uint32_t* keys, int64_t nkeys, int64_t count, float a, f
   if (!keys || !out || nkeys < 0 || count < 0 || bad_mode(mode)) return ABM_ERR_BADARG;
   if (nkeys == 0 || count == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && count > 0xFFFFFFFFll) return ABM_ERR_BADARG;
-  const int64_t total = nkeys * count;
-  sample_kernel<kKind><<<grid_for(total), kThreads, 0, abm_host::as_stream(stream)>>>(
+  sample_kernel<kKind><<<grid_for(nkeys, count), kThreads, 0, abm_host::as_stream(stream)>>>(
       keys, nkeys, count, a, b, out, mode);
   return abm_host::check_launch("abm_rng_sample");
 }
@@ -191,8 +198,7 @@ int abm_rng_split(const uint32_t* keys, int64_t nkeys, int64_t num, uint32_t* ou
   if (!keys || !out || nkeys < 0 || num < 0 || bad_mode(mode)) return ABM_ERR_BADARG;
   if (nkeys == 0 || num == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && 2 * num > 0xFFFFFFFFll) return ABM_ERR_BADARG;
-  const int64_t total = nkeys * num;
-  split_kernel<<<grid_for(total), kThreads, 0, abm_host::as_stream(stream)>>>(keys, nkeys, num,
+  split_kernel<<<grid_for(nkeys, num), kThreads, 0, abm_host::as_stream(stream)>>>(keys, nkeys, num,
                                                                                out, mode);
   return abm_host::check_launch("abm_rng_split");
 }
@@ -222,8 +228,7 @@ int abm_rng_randint(const uint32_t* keys, int64_t nkeys, int64_t count, int32_t 
   if (!keys || !out || nkeys < 0 || count < 0 || bad_mode(mode)) return ABM_ERR_BADARG;
   if (nkeys == 0 || count == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && count > 0xFFFFFFFFll) return ABM_ERR_BADARG;
-  const int64_t total = nkeys * count;
-  randint_kernel<<<grid_for(total), kThreads, 0, abm_host::as_stream(stream)>>>(
+  randint_kernel<<<grid_for(nkeys, count), kThreads, 0, abm_host::as_stream(stream)>>>(
       keys, nkeys, count, minval, maxval, out, mode);
   return abm_host::check_launch("abm_rng_randint");
 }
