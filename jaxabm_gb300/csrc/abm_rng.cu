@@ -14,42 +14,67 @@ thread_local char g_last_cuda_error[256] = "";
 
 constexpr int kThreads = 256;
 
-// Grids are 2-D: keys along y, a key's elements along x (no per-element division).
-__global__ void split_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t num,
-                             uint32_t* __restrict__ out, int mode) {
-  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
-    const uint2 key = abm::load_key(keys + 2 * k);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < num;
-         i += (int64_t)gridDim.x * blockDim.x) {
-      const uint2 r = mode == ABM_RNG_PARTITIONABLE ? abm::split_at(key, (uint64_t)i)
-                                                    : abm::legacy_split_at(key, num, i);
-      reinterpret_cast<uint2*>(out)[k * num + i] = r;
+// Element (key k, index i) of a launch over nkeys x count elements.  Keys with many
+// elements use a 2-D grid (keys along y, a key's elements along x: no per-element division);
+// keys with few elements (count < kThreads, e.g. one draw per agent key) use a flat 1-D
+// grid, with a 32-bit division when the element count allows it.
+template <typename F>
+__device__ __forceinline__ void for_each_element(int64_t nkeys, int64_t count, bool flat, F&& f) {
+  if (flat) {
+    const int64_t total = nkeys * count;
+    const bool small = total <= 0xFFFFFFFFll;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
+         g += (int64_t)gridDim.x * blockDim.x) {
+      int64_t k, i;
+      if (count == 1) {
+        k = g;
+        i = 0;
+      } else if (small) {
+        k = (uint32_t)g / (uint32_t)count;
+        i = g - k * count;
+      } else {
+        k = g / count;
+        i = g - k * count;
+      }
+      f(k, i);
     }
+  } else {
+    for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y)
+      for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+           i += (int64_t)gridDim.x * blockDim.x)
+        f(k, i);
   }
+}
+
+__global__ void split_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t num,
+                             uint32_t* __restrict__ out, int mode, bool flat) {
+  for_each_element(nkeys, num, flat, [&](int64_t k, int64_t i) {
+    const uint2 key = abm::load_key(keys + 2 * k);
+    const uint2 r = mode == ABM_RNG_PARTITIONABLE ? abm::split_at(key, (uint64_t)i)
+                                                  : abm::legacy_split_at(key, num, i);
+    reinterpret_cast<uint2*>(out)[k * num + i] = r;
+  });
 }
 
 // kind: 0 bits, 1 uniform, 2 normal, 3 bernoulli
 template <int kKind>
 __global__ void sample_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t count,
-                              float a, float b, void* __restrict__ out, int mode) {
-  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
+                              float a, float b, void* __restrict__ out, int mode, bool flat) {
+  for_each_element(nkeys, count, flat, [&](int64_t k, int64_t i) {
     const uint2 key = abm::load_key(keys + 2 * k);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
-         i += (int64_t)gridDim.x * blockDim.x) {
-      const int64_t g = k * count + i;
-      const uint32_t w = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(key, (uint64_t)i)
-                                                       : abm::legacy_bits_at(key, count, i);
-      if (kKind == 0) {
-        static_cast<uint32_t*>(out)[g] = w;
-      } else if (kKind == 1) {
-        static_cast<float*>(out)[g] = abm::uniform_from_bits(w, a, b);
-      } else if (kKind == 2) {
-        static_cast<float*>(out)[g] = abm::normal_from_bits(w);
-      } else {
-        static_cast<uint8_t*>(out)[g] = abm::unit_float(w) < a ? 1 : 0;
-      }
+    const int64_t g = k * count + i;
+    const uint32_t w = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(key, (uint64_t)i)
+                                                     : abm::legacy_bits_at(key, count, i);
+    if (kKind == 0) {
+      static_cast<uint32_t*>(out)[g] = w;
+    } else if (kKind == 1) {
+      static_cast<float*>(out)[g] = abm::uniform_from_bits(w, a, b);
+    } else if (kKind == 2) {
+      static_cast<float*>(out)[g] = abm::normal_from_bits(w);
+    } else {
+      static_cast<uint8_t*>(out)[g] = abm::unit_float(w) < a ? 1 : 0;
     }
-  }
+  });
 }
 
 // jax.random.randint(key, (count,), minval, maxval, int32): k1, k2 = split(key);
@@ -58,11 +83,11 @@ __global__ void sample_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, 
 // in wrapping uint32 arithmetic; out = minval + r.
 __global__ void randint_kernel(const uint32_t* __restrict__ keys, int64_t nkeys, int64_t count,
                                int32_t minval, int32_t maxval, int32_t* __restrict__ out,
-                               int mode) {
+                               int mode, bool flat) {
   const uint32_t span = maxval <= minval ? 1u : (uint32_t)((int64_t)maxval - (int64_t)minval);
   uint32_t mult = 65536u % span;
   mult = (mult * mult) % span;
-  for (int64_t k = blockIdx.y; k < nkeys; k += gridDim.y) {
+  for_each_element(nkeys, count, flat, [&](int64_t k, int64_t i) {
     const uint2 key = abm::load_key(keys + 2 * k);
     uint2 k1, k2;
     if (mode == ABM_RNG_PARTITIONABLE) {
@@ -72,17 +97,14 @@ __global__ void randint_kernel(const uint32_t* __restrict__ keys, int64_t nkeys,
       k1 = abm::legacy_split_at(key, 2, 0);
       k2 = abm::legacy_split_at(key, 2, 1);
     }
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
-         i += (int64_t)gridDim.x * blockDim.x) {
-      const uint32_t hi = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k1, (uint64_t)i)
-                                                        : abm::legacy_bits_at(k1, count, i);
-      const uint32_t lo = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k2, (uint64_t)i)
-                                                        : abm::legacy_bits_at(k2, count, i);
-      uint32_t r = (hi % span) * mult + (lo % span);
-      r %= span;
-      out[k * count + i] = (int32_t)((uint32_t)minval + r);
-    }
-  }
+    const uint32_t hi = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k1, (uint64_t)i)
+                                                      : abm::legacy_bits_at(k1, count, i);
+    const uint32_t lo = mode == ABM_RNG_PARTITIONABLE ? abm::bits_at(k2, (uint64_t)i)
+                                                      : abm::legacy_bits_at(k2, count, i);
+    uint32_t r = (hi % span) * mult + (lo % span);
+    r %= span;
+    out[k * count + i] = (int32_t)((uint32_t)minval + r);
+  });
 }
 
 // One thread per model instance walks the sequential chain of Model.step
@@ -109,10 +131,17 @@ __global__ void keychain_kernel(uint32_t* __restrict__ rng, int64_t ninst, int32
   rng[2 * inst + 1] = r.y;
 }
 
-// 2-D grid for nkeys x count elements: x covers a key's elements, y the keys; at most
-// 16 CTAs per SM in total.
+bool flat_launch(int64_t count) { return count < kThreads; }
+
+// Grid for nkeys x count elements (at most 16 CTAs per SM): flat for few elements per key,
+// else x covers a key's elements and y the keys.
 dim3 grid_for(int64_t nkeys, int64_t count) {
   const int64_t cap = (int64_t)abm_host::sm_count() * 16;
+  if (flat_launch(count)) {
+    int64_t blocks = (nkeys * count + kThreads - 1) / kThreads;
+    if (blocks > cap) blocks = cap;
+    return dim3((unsigned)(blocks < 1 ? 1 : blocks));
+  }
   int64_t x = (count + kThreads - 1) / kThreads;
   if (x > cap) x = cap;
   if (x < 1) x = 1;
@@ -132,7 +161,7 @@ int launch_sample(const uint32_t* keys, int64_t nkeys, int64_t count, float a, f
   if (nkeys == 0 || count == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && count > 0xFFFFFFFFll) return ABM_ERR_BADARG;
   sample_kernel<kKind><<<grid_for(nkeys, count), kThreads, 0, abm_host::as_stream(stream)>>>(
-      keys, nkeys, count, a, b, out, mode);
+      keys, nkeys, count, a, b, out, mode, flat_launch(count));
   return abm_host::check_launch("abm_rng_sample");
 }
 
@@ -198,8 +227,8 @@ int abm_rng_split(const uint32_t* keys, int64_t nkeys, int64_t num, uint32_t* ou
   if (!keys || !out || nkeys < 0 || num < 0 || bad_mode(mode)) return ABM_ERR_BADARG;
   if (nkeys == 0 || num == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && 2 * num > 0xFFFFFFFFll) return ABM_ERR_BADARG;
-  split_kernel<<<grid_for(nkeys, num), kThreads, 0, abm_host::as_stream(stream)>>>(keys, nkeys, num,
-                                                                               out, mode);
+  split_kernel<<<grid_for(nkeys, num), kThreads, 0, abm_host::as_stream(stream)>>>(
+      keys, nkeys, num, out, mode, flat_launch(num));
   return abm_host::check_launch("abm_rng_split");
 }
 
@@ -229,7 +258,7 @@ int abm_rng_randint(const uint32_t* keys, int64_t nkeys, int64_t count, int32_t 
   if (nkeys == 0 || count == 0) return ABM_OK;
   if (mode == ABM_RNG_LEGACY && count > 0xFFFFFFFFll) return ABM_ERR_BADARG;
   randint_kernel<<<grid_for(nkeys, count), kThreads, 0, abm_host::as_stream(stream)>>>(
-      keys, nkeys, count, minval, maxval, out, mode);
+      keys, nkeys, count, minval, maxval, out, mode, flat_launch(count));
   return abm_host::check_launch("abm_rng_randint");
 }
 

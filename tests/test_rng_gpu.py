@@ -122,3 +122,19 @@ def test_bad_mode_rejected():
     out = torch.empty((1, 2, 2), dtype=torch.int32, device="cuda")
     st = _lib.load().abm_rng_split(_dev.ptr(keys), 1, 2, _dev.ptr(out), 7, None)
     assert st == _lib.ABM_ERR_BADARG
+
+
+@pytest.mark.parametrize("nkeys,count", [(3000, 1), (1500, 3), (40, 700)])
+def test_many_keys(nkeys, count):
+    """Per-agent draws (many keys, few elements each: the flat launch) and many keys with
+    many elements each (the 2-D launch) match the oracle."""
+    import jaxabm_gb300.random as jr
+    jr.set_partitionable(True)
+    keys = _keys(nkeys, count + 11)
+    dk = _dev_keys(keys)
+    b = _u32(jr.bits(dk, (count,)))
+    rb = np.stack([t.bits(k, (count,), t.PARTITIONABLE) for k in keys])
+    assert np.array_equal(b, rb)
+    s = _u32(jr.split(dk, count))
+    rs = np.stack([t.split(k, count, t.PARTITIONABLE) for k in keys])
+    assert np.array_equal(s, rs)
