@@ -54,26 +54,34 @@ select_count_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
 }
 
 // Single block: exclusive scan of tile_counts into tile_offsets (int64), total -> *count.
-// Thread t owns the contiguous chunk [t*per, (t+1)*per) of the tile counts: it sums the
-// chunk, the block scans the 1024 chunk sums, and the thread writes its chunk's offsets.
+// Warp w owns the contiguous chunk [w*per, (w+1)*per) (per a multiple of 128) and reads it
+// 128 counts at a time, four per lane (coalesced): pass 1 sums the chunk, the block scans
+// the 32 chunk sums, pass 2 writes the chunk's offsets from warp scans.
 __global__ void __launch_bounds__(1024)
 select_scan_kernel(const int32_t* __restrict__ tile_counts, int64_t ntiles,
                    int64_t* __restrict__ tile_offsets, int64_t* __restrict__ count) {
   __shared__ int64_t swarp[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t per = (ntiles + 1023) / 1024;
-  const int64_t c0 = (int64_t)threadIdx.x * per;
+  const int64_t per = ((ntiles + 31) / 32 + 127) / 128 * 128;
+  const int64_t c0 = (int64_t)warp * per;
   const int64_t c1 = c0 + per < ntiles ? c0 + per : ntiles;
-  int64_t sum = 0;
-#pragma unroll 8
-  for (int64_t b = c0; b < c1; ++b) sum += tile_counts[b];
-  int64_t incl = sum;
+  // the four counts of lane `lane` in the group starting at b
+  auto load4 = [&](int64_t b, int (&v)[4]) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int64_t u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
+    for (int q = 0; q < 4; ++q) {
+      const int64_t t = b + 4 * lane + q;
+      v[q] = t < c1 ? tile_counts[t] : 0;
+    }
+  };
+  int64_t sum = 0;
+  for (int64_t b = c0; b < c1; b += 128) {
+    int v[4];
+    load4(b, v);
+    sum += v[0] + v[1] + v[2] + v[3];
   }
-  if (lane == 31) swarp[warp] = incl;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) swarp[warp] = sum;
   __syncthreads();
   if (warp == 0) {
     int64_t w = swarp[lane];
@@ -85,13 +93,27 @@ select_scan_kernel(const int32_t* __restrict__ tile_counts, int64_t ntiles,
     swarp[lane] = w;  // inclusive over warps
   }
   __syncthreads();
-  int64_t run = (warp > 0 ? swarp[warp - 1] : 0) + incl - sum;
-#pragma unroll 8
-  for (int64_t b = c0; b < c1; ++b) {
-    tile_offsets[b] = run;
-    run += tile_counts[b];
+  int64_t run = warp > 0 ? swarp[warp - 1] : 0;
+  for (int64_t b = c0; b < c1; b += 128) {
+    int v[4];
+    load4(b, v);
+    const int mine = v[0] + v[1] + v[2] + v[3];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    int64_t off = run + (incl - mine);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t t = b + 4 * lane + q;
+      if (t < c1) tile_offsets[t] = off;
+      off += v[q];
+    }
+    run += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (threadIdx.x == 1023) *count = run;
+  if (threadIdx.x == 0) *count = swarp[31];
 }
 
 // Each tile's selected indices, in ascending order, are staged in shared memory at their

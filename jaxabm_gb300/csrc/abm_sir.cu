@@ -15,13 +15,13 @@
 // A second copy of the compartments, 2 bits per agent (16 agents per 32-bit word of
 // `comp`, ~22 MB for a 4,096-instance ensemble), serves the random neighbour reads of the
 // decisions from L2; the bytes (~87 MB) serve the sweep and the count updates;
-// CSR columns, row offsets and change entries are read with the streaming (evict-first)
-// policy so that they do not displace the words.  Column entries that point at a hub carry bit 31 (set
-// by abm_sir_pack), so a count update knows where its target's count lives without a
-// further read.  A count update is a 32-bit atomic add on the aligned word holding the
-// target byte: the byte never borrows or carries into its neighbours, because a count
-// never drops below the number of its pre-step infected neighbours that are still to
-// recover, and never exceeds the degree (< 63).
+// CSR columns, row offsets and list entries are read with the streaming (evict-first)
+// policy so that they do not displace the words.  Column entries that point at a hub carry
+// bit 31 (set by abm_sir_pack), so a count update knows where its target's count lives
+// without a further read.  A count update is a 32-bit reduction (red.global.add) on the
+// aligned word holding the target byte: the byte never borrows or carries into its
+// neighbours, because a count never drops below the number of its pre-step infected
+// neighbours that are still to recover, and never exceeds the degree (< 63).
 //
 // A step is four launches:
 //   sweep      over (instance, 8192-agent tile) work items, 32 agents per lane read with
@@ -30,12 +30,14 @@
 //              each); susceptible agents with infected neighbours are appended to a
 //              candidate list in agent order (8-byte entries; one counter atomic per CTA
 //              and tile).  Everyone else (most agents) costs one byte.
-//   candidates one lane per candidate: it scans its CSR row, eight column/neighbour loads
-//              in flight per pass, stopping at the first firing draw or once all its
-//              infected neighbours were seen (rows longer than 32 slots are scanned by the
-//              whole warp, 128 slots per pass, with warp votes).  Changes of both kernels
-//              go to a change list; no word is written, so every decision sees the
-//              pre-step states.
+//   candidates one lane per candidate (entries and row offsets loaded a pass ahead): it
+//              reads its CSR row, eight column/compartment loads in flight per pass, until
+//              all its infected neighbours were seen, then draws for those slots in order
+//              with the lanes of the warp drawing together, stopping at the first firing
+//              draw (rows longer than 32 slots are scanned by the whole warp, 128 slots per
+//              pass, with warp votes).  Changes of both kernels are buffered per warp in
+//              shared memory and appended to the change list 32 at a time; no word is
+//              written, so every decision sees the pre-step states.
 //   push       one thread per change (one warp for rows longer than 32 slots): adds +-1 to
 //              the infected-neighbour count of every neighbour and +1 to the agent's own
 //              compartment.
