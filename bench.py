@@ -359,7 +359,23 @@ def model_lines():
                   0.05, 0.1, _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
     ms = _time_ms(sir1, reps=3)
     out["sir_ba_n1048576_t365"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
-                                   "launches_per_run": 4 * T + 5 + (T + 7) // 8}
+                                   "launches_per_run": 4 * T + 5 + (T + 7) // 8,
+                                   "path": "abm_sir_run, kernels launched one by one"}
+    # the same model as a one-instance batch, its 365 steps replayed from one CUDA graph
+    from jaxabm_gb300 import ensemble
+    b1 = ensemble.SIRBatch([(rp, col)], [sir.initial_states(n, 0.001, 0)], [0.05], [0.1], [0],
+                           T)
+    b1.capture(T)
+
+    def sir_graph():
+        b1.reset()
+        b1.replay()
+    ms = _time_ms(sir_graph, reps=3)
+    out["sir_ba_n1048576_t365_graph"] = {
+        "agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
+        "launches_per_run": b1.launches_per_run(),
+        "path": "SIRBatch of one instance, CUDA-graph replay (reset included)"}
+    del b1
 
     # opinion calibration: N = 2^18, 16-regular, 64 instances, 200 steps, checkpoints every 20
     n, B, T = 1 << 18, 64, 200

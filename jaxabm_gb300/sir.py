@@ -135,3 +135,60 @@ class SIRModel(Model):
                                       gamma=float(self.p.get("gamma", 0.1)),
                                       initial_infected=float(self.p.get("initial_infected", 0.001)),
                                       infection_seed=int(self.p.get("infection_seed", self.seed)))
+
+    def batch_run(self, parameter_ranges, repetitions=1):
+        """Every parameter combination, ``repetitions`` runs each, as ONE batched launch
+        sequence of the ensemble engine (the reference runs them one after another,
+        jaxabm/agentpy.py:1116-1152).  Run r of a combination uses seed ``self.seed + r``,
+        as the serial loop does, so each result equals that run done alone.  Subclasses
+        with Python hooks (``step``, ``update_state``, ``compute_metrics``) take the serial
+        path."""
+        import itertools
+
+        from .agentpy import Results
+        from .ensemble import SIRBatch
+        if self._hooks() != (None, None):
+            return super().batch_run(parameter_ranges, repetitions)
+        names = list(parameter_ranges.keys())
+        combos = list(itertools.product(*parameter_ranges.values()))
+        specs = []
+        for values in combos:
+            for r in range(repetitions):
+                p = dict(self.p)
+                p.update(zip(names, values))
+                specs.append((tuple(values), p, self.seed + r))
+        if not specs:
+            return {}
+        steps = {int(p.get("steps", self.steps)) for _, p, _ in specs}
+        if len(steps) != 1:
+            return super().batch_run(parameter_ranges, repetitions)
+        steps = steps.pop()
+        graphs, inits, betas, gammas, seeds = [], [], [], [], []
+        cache = {}
+        for _, p, seed in specs:
+            n = int(p.get("n", 1 << 20))
+            if "row_ptr" in p:
+                g = (np.asarray(p["row_ptr"], np.int32), np.asarray(p["col"], np.int32))
+            else:
+                key = (n, int(p.get("m", 4)), int(p.get("graph_seed", seed)))
+                if key not in cache:
+                    cache[key] = barabasi_albert(*key)
+                g = cache[key]
+            graphs.append(g)
+            inits.append(initial_states(n, float(p.get("initial_infected", 0.001)),
+                                        int(p.get("infection_seed", seed))))
+            betas.append(float(p.get("beta", 0.05)))
+            gammas.append(float(p.get("gamma", 0.1)))
+            seeds.append(seed)
+        batch = SIRBatch(graphs, inits, betas, gammas, seeds, steps)
+        batch.run()
+        batch.check()
+        counts = batch.counts.reshape(len(specs), steps, 3).cpu().numpy()
+        results = {}
+        for k, (values, _, _) in enumerate(specs):
+            data = {"step": list(range(1, steps + 1)),
+                    "S": counts[k, :, 0].tolist(), "I": counts[k, :, 1].tolist(),
+                    "R": counts[k, :, 2].tolist(),
+                    "agents.people.state": batch.final_state(k).cpu().numpy()}
+            results.setdefault(values, []).append(Results(data))
+        return results

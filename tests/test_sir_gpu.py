@@ -142,3 +142,20 @@ def test_sir_bad_args(cuda):
     assert L.abm_sir_steps(None, 1, None, 0, None, 1, 0, None, 0, None) == _lib.ABM_ERR_BADARG
     assert L.abm_sir_run(None, None, 10, 0, None, None, 1, 0.1, 0.1, None, None, 0, None) == \
         _lib.ABM_ERR_BADARG
+
+
+def test_sir_batch_run_matches_serial(cuda):
+    """SIRModel.batch_run runs every combination and repetition in one batched launch
+    sequence; each result equals the same model run alone (the reference's serial loop)."""
+    import jaxabm_gb300 as jx
+    base = {"n": 3000, "steps": 30, "m": 3}
+    model = jx.SIRModel(dict(base), seed=5)
+    res = model.batch_run({"beta": [0.05, 0.2], "gamma": [0.1, 0.3]}, repetitions=2)
+    assert len(res) == 4 and all(len(v) == 2 for v in res.values())
+    for (beta, gamma), runs in res.items():
+        for r, got in enumerate(runs):
+            p = dict(base, beta=beta, gamma=gamma)
+            ref = jx.SIRModel(p, seed=5 + r).run()
+            for key in ("S", "I", "R"):
+                assert list(got[key]) == list(ref[key]), (beta, gamma, r, key)
+            assert np.array_equal(got["agents.people.state"], ref["agents.people.state"])
