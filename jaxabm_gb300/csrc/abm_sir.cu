@@ -59,6 +59,7 @@ constexpr int kSub = 32 * kPerThread;              // 1024 agents per warp and t
 constexpr int kTile = kSirThreads * kPerThread;    // 8192 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr int kHeavyUnroll = 4;                    // slots per lane per pass of a warp row scan
+constexpr int kDrawFirstDeg = 96;                  // rows longer than this draw before reading
 constexpr int kChunk = 8;                          // row slots per scan pass
 constexpr int kHubDeg = 63;                        // degree from which a count is a hub count
 constexpr uint32_t kHubMark = 63;                  // count field of a hub's word
@@ -457,6 +458,37 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
       int c = 0;
+      if (hdeg > kDrawFirstDeg) {
+        // long rows: the draws first (ALU only), the neighbour's compartment read only
+        // where a draw fires -- a fraction beta of the slots -- in slot order, so the
+        // first firing slot with an infected neighbour decides as in the scan below
+        int loaded = 0;
+        for (; c < hdeg && !fired; c += 32 * kHeavyUnroll) {
+          unsigned fire = 0;
+#pragma unroll
+          for (int u = 0; u < kHeavyUnroll; ++u) {
+            const int slot = c + 32 * u + lane;
+            if (slot < hdeg && abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < hbeta)
+              fire |= 1u << u;
+          }
+          uint32_t wv[kHeavyUnroll];
+#pragma unroll
+          for (int u = 0; u < kHeavyUnroll; ++u)
+            wv[u] = (fire >> u) & 1u ? ld_col(hadj, hrow + c + 32 * u + lane) : 0u;
+          bool f = false;
+#pragma unroll
+          for (int u = 0; u < kHeavyUnroll; ++u)
+            if ((fire >> u) & 1u) f |= comp_of(hcomp, wv[u] & kIdx) == kI;
+          loaded += __popc(fire);
+          fired = __any_sync(kFull, f);
+        }
+        loaded = __reduce_add_sync(kFull, loaded);
+        if (lane == src) {
+          infected = fired;
+          scanned = loaded;
+        }
+        continue;
+      }
       for (; c < hdeg && !fired && remaining > 0; c += 32 * kHeavyUnroll) {
         uint32_t wv[kHeavyUnroll];
 #pragma unroll
