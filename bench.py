@@ -402,6 +402,27 @@ def model_lines():
                              "peak_kind": "nominal (152 SMs x 16 per clock x 2.07 GHz)"}}
 
     hbm, _ = _peaks()
+    # Network CSR on the device: the 8,388,576 directed edges of BA(2^20, m=4) in shuffled
+    # order -> row_ptr/col (stable radix sort by source)
+    rp, col = sir.barabasi_albert(1 << 20, 4, 0)
+    nn = len(rp) - 1
+    perm = np.random.RandomState(0).permutation(len(col))
+    esrc = torch.from_numpy(np.repeat(np.arange(nn), np.diff(rp)).astype(np.int32)[perm]).cuda()
+    edst = torch.from_numpy(col[perm]).cuda()
+    E = len(col)
+    crp = torch.empty(nn + 1, dtype=torch.int32, device="cuda")
+    ccol = torch.empty(E, dtype=torch.int32, device="cuda")
+    cst = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ws = torch.empty(L.abm_csr_workspace_bytes(E, nn), dtype=torch.uint8, device="cuda")
+
+    def csr():
+        _lib.call("abm_csr_from_edges", _dev.ptr(esrc), _dev.ptr(edst), E, nn, _dev.ptr(crp),
+                  _dev.ptr(ccol), _dev.ptr(cst), _dev.ptr(ws), ws.numel(), None)
+    ms = _time_ms(csr, reps=5)
+    out["csr_from_edges_ba_n1048576"] = {"edges_per_s": E / (ms / 1e3), "ms": ms,
+                                         "launches_per_call": 3 * 3 + 2}
+    del esrc, edst, ccol, ws
+
     # K6 compaction of a 2^28-entry mask (half set, larger than L2) into int32 indices
     n = 1 << 28
     g = torch.Generator(device="cuda")

@@ -137,6 +137,21 @@ ABM_API int abm_graph_barabasi_albert(int64_t n, int32_t m, uint64_t seed, int32
 ABM_API int abm_graph_random_regular(int64_t n, int32_t d, uint64_t seed, int32_t* row_ptr,
                                      int32_t* col, int64_t col_capacity);
 
+/* ---- Network CSR construction on the device ------------------------------------------ */
+/* Workspace of abm_csr_from_edges for num_edges edges over n nodes (four edge-sized
+ * buffers and the per-tile digit histograms). */
+ABM_API size_t abm_csr_workspace_bytes(int64_t num_edges, int64_t n);
+
+/* CSR of a directed edge list on the device: row i of (row_ptr int32[n+1], col int32[E])
+ * holds dst[e] of the edges with src[e] == i in ascending e (a stable radix sort by
+ * source).  Edges whose source is outside 0..n-1 are left out of every row (they follow
+ * row_ptr[n] in col) and set *status to 1, as does a destination outside 0..n-1.  col must
+ * not alias src or dst.  Replaces building a Network edge by edge (Network.add_edge,
+ * jaxabm/agentpy.py:559-582) and the host-side sort of its edge list. */
+ABM_API int abm_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t num_edges,
+                               int64_t n, int32_t* row_ptr, int32_t* col, int32_t* status,
+                               void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
 /* Device-side descriptor of one SIR model instance (144 bytes, 8-byte aligned).
  * words holds one byte per agent, (infected neighbours << 2) | compartment (0 S, 1 I,

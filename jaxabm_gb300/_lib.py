@@ -49,6 +49,8 @@ SIGNATURES = {
     "abm_graph_ba_num_edges": (_i64, [_i64, _i32]),
     "abm_graph_barabasi_albert": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_graph_random_regular": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
+    "abm_csr_workspace_bytes": (_sz, [_i64, _i64]),
+    "abm_csr_from_edges": (_int, [_p, _p, _i64, _i64, _p, _p, _p, _p, _sz, _p]),
     "abm_sir_instance_size": (_sz, []),
     "abm_sir_pack": (_int, [_p, _p, _p, _i64, _p, _p, _p, _p, _p, _p, _p]),
     "abm_sir_pack_batch": (_int, [_p, _p, _i32, _p, _p, _p, _p]),

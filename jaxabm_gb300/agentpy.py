@@ -288,6 +288,31 @@ class Grid:
         coll._states["position"] = positions
 
 
+def csr_from_edges(edges, n):
+    """Device CSR (row_ptr int32[n+1], col int32[E]) of an (E, 2) edge array over nodes
+    0..n-1, stable by source (``abm_csr_from_edges``: a radix sort on the device)."""
+    from . import _lib
+    e = np.ascontiguousarray(np.asarray(edges, dtype=np.int32).reshape(-1, 2))
+    dev = _dev.device()
+    E = e.shape[0]
+    if n <= 0:
+        if E:
+            raise ValueError("edges given for a network without nodes")
+        return (torch.zeros(1, dtype=torch.int32, device=dev),
+                torch.zeros(0, dtype=torch.int32, device=dev))
+    src = torch.from_numpy(np.ascontiguousarray(e[:, 0])).to(dev)
+    dst = torch.from_numpy(np.ascontiguousarray(e[:, 1])).to(dev)
+    rp = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    col = torch.empty(max(E, 1), dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = _dev.workspace(_lib.load().abm_csr_workspace_bytes(E, n))
+    _lib.call("abm_csr_from_edges", _dev.ptr(src), _dev.ptr(dst), E, n, _dev.ptr(rp),
+              _dev.ptr(col), _dev.ptr(status), _dev.ptr(ws), ws.numel(), _dev.stream_handle())
+    if int(status.item()) != 0:
+        raise ValueError(f"an edge endpoint lies outside 0..{n - 1}")
+    return rp, col[:E]
+
+
 class Network:
     """Agent network (jaxabm/agentpy.py:530-615), held as an int32 edge list in the
     environment plus CSR adjacency (``network_row_ptr``/``network_col``) for kernels."""
@@ -330,17 +355,16 @@ class Network:
         self.model.env.add_state("network_col", cl)
 
     def csr(self):
-        """(row_ptr, col) device tensors; built from the edge list (stable by source) when
-        the network was given as edges."""
+        """(row_ptr, col) device tensors; built on the device from the edge list (stable by
+        source: a row keeps its edges in the order they were added) when the network was
+        given as edges."""
         if getattr(self, "_csr", None) is None:
             e = self._edges
             n = int(e.max()) + 1 if e.size else 0
-            order = np.argsort(e[:, 0], kind="stable")
-            col = e[order, 1]
-            counts = np.bincount(e[:, 0], minlength=n)
-            rp = np.zeros(n + 1, dtype=np.int64)
-            np.cumsum(counts, out=rp[1:])
-            self.from_csr(rp.astype(np.int32), col.astype(np.int32))
+            rp, col = csr_from_edges(e, n)
+            self._csr = (rp, col)
+            self.model.env.add_state("network_row_ptr", rp)
+            self.model.env.add_state("network_col", col)
         return self._csr
 
     def get_neighbors(self, agent: Union[Agent, int]):
