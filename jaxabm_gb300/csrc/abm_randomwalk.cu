@@ -77,6 +77,56 @@ __global__ void __launch_bounds__(kBlock) rw_run_kernel(float* __restrict__ x,
   }
 }
 
+// Few agents (n below kWideAgents): one agent per thread would leave most of the GPU idle,
+// so each CTA takes kWideAgents-per-block = 32 agents and, for each chunk of kChunk steps,
+// first computes their noise draws with all 256 threads (the draws do not depend on the
+// state), then warp 0 applies the steps to (x, y) in order -- the same arithmetic per agent
+// as rw_run_kernel -- and writes the per-step warp sums.
+constexpr int kWideThreads = 256;
+constexpr int kWideAgents = 32;
+constexpr int64_t kWideBelow = 1 << 17;  // agent count below which the wide kernel is used
+
+__global__ void __launch_bounds__(kWideThreads)
+rw_run_wide_kernel(float* __restrict__ x, float* __restrict__ y, int64_t n,
+                   const uint32_t* __restrict__ coll_keys, int32_t steps, float sigma,
+                   float2* __restrict__ partial) {
+  __shared__ float2 snoise[kChunk][kWideAgents];
+  const int64_t a0 = (int64_t)blockIdx.x * kWideAgents;
+  const int lane = threadIdx.x & 31;
+  const bool owner = threadIdx.x < kWideAgents;  // warp 0 keeps the agents' state
+  const int64_t i = a0 + lane;
+  const bool active = owner && i < n;
+  float xi = active ? x[i] : 0.f;
+  float yi = active ? y[i] : 0.f;
+  for (int32_t t0 = 0; t0 < steps; t0 += kChunk) {
+    const int nt = min(kChunk, steps - t0);
+    for (int p = threadIdx.x; p < nt * kWideAgents; p += kWideThreads) {
+      const int k = p / kWideAgents, a = p % kWideAgents;
+      const uint2 ak = abm::split_at(abm::load_key(coll_keys + 2 * (int64_t)(t0 + k)),
+                                     (uint64_t)(a0 + a));
+      const uint2 kx = abm::split_at(ak, 0), ky = abm::split_at(ak, 1);
+      snoise[k][a] = make_float2(abm::normal_from_bits(abm::bits_at(kx, 0)),
+                                 abm::normal_from_bits(abm::bits_at(ky, 0)));
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      for (int k = 0; k < nt; ++k) {
+        const float2 nz = snoise[k][lane];
+        xi = abm::mod1(__fadd_rn(xi, __fmul_rn(sigma, nz.x)));
+        yi = abm::mod1(__fadd_rn(yi, __fmul_rn(sigma, nz.y)));
+        const float sx = abm::warp_sum(active ? xi : 0.f);
+        const float sy = abm::warp_sum(active ? yi : 0.f);
+        if (lane == 0) partial[(int64_t)(t0 + k) * gridDim.x + blockIdx.x] = make_float2(sx, sy);
+      }
+    }
+    __syncthreads();
+  }
+  if (active) {
+    x[i] = xi;
+    y[i] = yi;
+  }
+}
+
 // means[t] = (sum_b partial[t][b]) / n, one block per step, fixed reduction tree.
 __global__ void rw_means_kernel(const float2* __restrict__ partial, int nblocks, int64_t n,
                                 float2* __restrict__ means) {
@@ -103,7 +153,9 @@ __global__ void rw_means_kernel(const float2* __restrict__ partial, int nblocks,
   }
 }
 
-int64_t rw_blocks(int64_t n) { return (n + kBlock - 1) / kBlock; }
+int64_t rw_blocks(int64_t n) {
+  return n < kWideBelow ? (n + kWideAgents - 1) / kWideAgents : (n + kBlock - 1) / kBlock;
+}
 
 }  // namespace
 
@@ -136,7 +188,11 @@ int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* coll_keys,
     return ABM_ERR_WORKSPACE;
   cudaStream_t s = abm_host::as_stream(stream);
   float2* partial = static_cast<float2*>(workspace);
-  rw_run_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(x, y, n, coll_keys, steps, sigma, partial);
+  if (n < kWideBelow)
+    rw_run_wide_kernel<<<(unsigned)blocks, kWideThreads, 0, s>>>(x, y, n, coll_keys, steps, sigma,
+                                                                partial);
+  else
+    rw_run_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(x, y, n, coll_keys, steps, sigma, partial);
   int st = abm_host::check_launch("abm_randomwalk_run");
   if (st) return st;
   rw_means_kernel<<<(unsigned)steps, kBlock, 0, s>>>(partial, (int)blocks, n,

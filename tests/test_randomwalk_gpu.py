@@ -41,7 +41,8 @@ def _run_abi(seed, n, steps, sigma=0.01):
     return init, x.cpu().numpy(), y.cpu().numpy(), means.cpu().numpy()
 
 
-@pytest.mark.parametrize("n,steps", [(1, 3), (31, 5), (1000, 20), (10_000, 100), (4099, 130)])
+@pytest.mark.parametrize("n,steps", [(1, 3), (31, 5), (1000, 20), (10_000, 100), (4099, 130),
+                                     (140_000, 7)])  # the last: one agent per thread
 def test_randomwalk_abi_vs_oracle(cuda, n, steps):
     init, x, y, means = _run_abi(0, n, steps)
     rng, (ik,) = models.model_keys(0, 1)
