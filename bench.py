@@ -338,7 +338,7 @@ def model_lines():
                   _dev.ptr(ca), _dev.ptr(ck), T, _dev.ptr(stats), _dev.ptr(ws), ws.numel(), None)
     ms = _time_ms(sch, reps=3)
     out["schelling_256x256_t200"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
-                                     "launches_per_run": 4 * T + 4}
+                                     "launches_per_run": 3}
 
     # SIR, one model: N = 2^20 Barabasi-Albert m=4, 365 steps (the plain engine)
     n, T = 1 << 20, 365

@@ -12,7 +12,8 @@
 //   others stay.  Everyone reads the pre-step grid (synchronous update).
 // Metrics per step: number of unhappy agents, number of agents that moved.
 //
-// One step = four launches (no device-side waits anywhere):
+// Grids of up to 2^18 cells run every step in one thread-block cluster (below); larger
+// grids take one step = four launches (no device-side waits anywhere):
 //   scan    one CTA per grid row: rows x-1, x, x+1 staged in shared memory (torus halo),
 //           unhappiness of every occupant, empty-cell count of the row
 //   empties one CTA per row: exclusive prefix over the row counts, ordered warp-ballot
@@ -20,7 +21,11 @@
 //   claim   one thread per agent: draw, target, atomicMin claim on the target cell
 //   resolve one thread per agent: the claim owner moves; claims are reset for next step
 
+#include <cooperative_groups.h>
+
 #include "abm_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -172,6 +177,184 @@ schelling_resolve_kernel(int32_t n, int8_t* __restrict__ grid, int32_t* __restri
   }
 }
 
+// ---- small grids: every step of the run in one thread-block cluster ----------------------
+// A grid of up to kClusterMaxCells cells is handled by one cluster of kClusterCtas CTAs of
+// 1024 threads for the whole run; the four phases of a step (scan, ordered empty list,
+// claim, resolve) are separated by the hardware cluster barrier (release/acquire at cluster
+// scope), which makes each phase's global writes visible to the next, so a step costs four
+// barriers instead of four launches.  Thread g of the cluster owns the contiguous cells
+// [g*chunk, (g+1)*chunk), read from the CTA's rows staged in shared memory with a halo row
+// on each side; the empty list stays in ascending cell order (a block scan of the
+// per-thread counts plus the lower-ranked CTAs' totals, read through distributed shared
+// memory); unhappy agents go to a list (order free: claims are atomicMin), so the claim and
+// resolve phases touch only them.  The arithmetic per agent is that of the four-kernel path.
+// Cross-CTA data is read with L2-only loads.
+constexpr int kClusterCtas = 8;
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterWarps = kClusterThreads / 32;
+constexpr int64_t kClusterMaxCells = int64_t(1) << 18;
+constexpr size_t kClusterMaxRowBytes = 96 * 1024;  // staged rows per CTA (wide grids: launches)
+
+__device__ __forceinline__ int block_sum(int v, int* sred) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = abm::warp_sum(v);
+  if (lane == 0) sred[warp] = v;
+  __syncthreads();
+  int total = 0;
+  if (warp == 0) {
+    total = abm::warp_sum(lane < kClusterWarps ? sred[lane] : 0);
+  }
+  __syncthreads();
+  return total;  // valid in thread 0
+}
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+schelling_cluster_kernel(int32_t* __restrict__ pos, const int8_t* __restrict__ type, int32_t n,
+                         int32_t W, int32_t H, int8_t* grid, int32_t* cell_agent,
+                         const uint32_t* __restrict__ coll_keys, int32_t steps,
+                         int32_t* __restrict__ stats, int32_t* target, int32_t* claim,
+                         int32_t* empty_list, int32_t* unhappy_list, int32_t* unhappy_count) {
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ int8_t srows[];  // this CTA's grid rows with one halo row on each side
+  __shared__ int swarp[kClusterWarps];
+  __shared__ int sred[kClusterWarps];
+  __shared__ int s_cta_total;  // empties in this CTA's cells, read by the other CTAs
+  const unsigned rank = cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nthreads = kClusterCtas * kClusterThreads;
+  const int g = (int)rank * kClusterThreads + tid;
+  const int C = W * H;
+  const int chunk = (C + nthreads - 1) / nthreads;
+  const int c0 = min(g * chunk, C), c1 = min(c0 + chunk, C);
+  // rows staged by this CTA: x_lo - 1 .. x_hi + 1 (torus), x_lo/x_hi the rows of its cells
+  const int cta_c0 = min((int)rank * kClusterThreads * chunk, C);
+  const int cta_c1 = min(cta_c0 + kClusterThreads * chunk, C);
+  const int x_lo = cta_c0 / H;
+  const int x_hi = cta_c1 > cta_c0 ? (cta_c1 - 1) / H : x_lo;
+  const int nrows = x_hi - x_lo + 3;
+  for (int t = 0; t < steps; ++t) {
+    const int32_t* ucount = unhappy_count + (t & 1);
+    if (g == 0) unhappy_count[(t + 1) & 1] = 0;  // the counter of the next step
+    for (int k = tid; k < nrows * H; k += kClusterThreads) {
+      const int r = k / H, y = k - r * H;
+      int x = x_lo - 1 + r;
+      x = x < 0 ? x + W : (x >= W ? x - W : x);
+      srows[k] = __ldcg(grid + x * H + y);
+    }
+    __syncthreads();
+    // scan: unhappiness of the occupants of my cells (neighbours from the staged rows),
+    // unhappy agents to the cluster's list, and my empty cells
+    int empties = 0, unhappy = 0;
+    for (int c = c0; c < c1; ++c) {
+      const int x = c / H, y = c - x * H;
+      const int r = x - x_lo + 1;
+      const int8_t gv = srows[r * H + y];
+      if (gv < 0) {
+        ++empties;
+        continue;
+      }
+      const int ym = y == 0 ? H - 1 : y - 1, yp = y == H - 1 ? 0 : y + 1;
+      const int8_t* up = srows + (r - 1) * H;
+      const int8_t* mid = srows + r * H;
+      const int8_t* dn = srows + (r + 1) * H;
+      const int8_t nb[8] = {up[ym], up[y], up[yp], mid[ym], mid[yp], dn[ym], dn[y], dn[yp]};
+      int occ = 0, same = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        occ += nb[k] >= 0;
+        same += nb[k] == gv;
+      }
+      if (8 * same < 3 * occ) {
+        ++unhappy;
+        const int i = __ldcg(cell_agent + c);
+        unhappy_list[atomicAdd(const_cast<int32_t*>(ucount), 1)] = i;
+      }
+    }
+    // ordered position of my empties: block scan, then the lower-ranked CTAs' totals
+    int incl = empties;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) swarp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      int w = swarp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += u;
+      }
+      swarp[lane] = w;
+    }
+    __syncthreads();
+    const int excl = (warp > 0 ? swarp[warp - 1] : 0) + incl - empties;
+    if (tid == kClusterThreads - 1) s_cta_total = excl + empties;
+    const int u_cta = block_sum(unhappy, sred);
+    if (tid == 0 && u_cta) atomicAdd(&stats[2 * t], u_cta);
+    cluster.sync();  // (1) every CTA's total and every unhappy agent are in
+    int base = 0, e_total = 0;
+#pragma unroll
+    for (int r = 0; r < kClusterCtas; ++r) {
+      const int v = *cluster.map_shared_rank(&s_cta_total, r);
+      base += r < (int)rank ? v : 0;
+      e_total += v;
+    }
+    int pe = base + excl;
+    for (int c = c0; c < c1; ++c) {
+      const int x = c / H;
+      if (srows[(x - x_lo + 1) * H + (c - x * H)] < 0) empty_list[pe++] = c;
+    }
+    cluster.sync();  // (2) the empty list is complete
+    // claim: an unhappy agent draws an empty cell; the lowest id wins it
+    const int nu = __ldcg(ucount);
+    const uint2 ck = abm::load_key(coll_keys + 2 * (size_t)t);
+    if (e_total > 0) {
+      for (int k = g; k < nu; k += nthreads) {
+        const int i = __ldcg(unhappy_list + k);
+        const uint2 ak = abm::split_at(ck, (uint64_t)i);
+        const float u = abm::unit_float(abm::bits_at(ak, 0));
+        int idx = (int)floorf(__fmul_rn(u, (float)e_total));
+        if (idx > e_total - 1) idx = e_total - 1;
+        const int tgt = __ldcg(empty_list + idx);
+        target[i] = tgt;
+        atomicMin(&claim[tgt], i);
+      }
+    }
+    cluster.sync();  // (3) every claim is in
+    // resolve: the claim owner moves
+    int moved = 0;
+    if (e_total > 0) {
+      for (int k = g; k < nu; k += nthreads) {
+        const int i = __ldcg(unhappy_list + k);
+        const int tgt = __ldcg(target + i);
+        if (__ldcg(claim + tgt) == i) {
+          const int old = pos[i];
+          grid[old] = -1;
+          cell_agent[old] = -1;
+          grid[tgt] = type[i];
+          cell_agent[tgt] = i;
+          pos[i] = tgt;
+          claim[tgt] = kNoClaim;
+          ++moved;
+        }
+      }
+    }
+    const int m_cta = block_sum(moved, sred);
+    if (tid == 0 && m_cta) atomicAdd(&stats[2 * t + 1], m_cta);
+    cluster.sync();  // (4) the grid of the next step is complete; totals may be rewritten
+  }
+}
+
+// Bytes of the staged rows of one CTA of schelling_cluster_kernel.
+size_t cluster_smem_bytes(int32_t W, int32_t H) {
+  const int64_t C = (int64_t)W * H;
+  const int64_t chunk = (C + kClusterCtas * kClusterThreads - 1) / (kClusterCtas * kClusterThreads);
+  const int64_t cells = chunk * kClusterThreads;          // cells per CTA
+  return (size_t)((cells + H - 1) / H + 3) * (size_t)H;   // rows spanned + halo rows
+}
+
 // Grid and occupancy map from the agents' positions and types: clear, then place.
 __global__ void schelling_clear_kernel(int32_t C, int8_t* __restrict__ grid,
                                        int32_t* __restrict__ cell_agent) {
@@ -205,8 +388,10 @@ struct Workspace {
   int32_t* target;
   int32_t* row_empty;
   int32_t* empty_list;
+  int32_t* unhappy_list;
   int32_t* e_total;
   int32_t* bad;
+  int32_t* unhappy_count;  // two counters, one per step parity
 };
 
 Workspace carve(void* ws, int64_t n, int32_t W, int32_t H) {
@@ -221,8 +406,11 @@ Workspace carve(void* ws, int64_t n, int32_t W, int32_t H) {
   p += align256((size_t)W * 4);
   w.empty_list = reinterpret_cast<int32_t*>(p);
   p += align256(C * 4);
+  w.unhappy_list = reinterpret_cast<int32_t*>(p);
+  p += align256((size_t)n * 4);
   w.e_total = reinterpret_cast<int32_t*>(p);
   w.bad = w.e_total + 1;
+  w.unhappy_count = w.e_total + 2;
   return w;
 }
 
@@ -234,7 +422,7 @@ size_t abm_schelling_workspace_bytes(int64_t n, int32_t W, int32_t H) {
   if (n <= 0 || W <= 0 || H <= 0) return 0;
   const size_t C = (size_t)W * H;
   return align256(C * 4) + align256((size_t)n * 4) + align256((size_t)W * 4) + align256(C * 4) +
-         256;
+         align256((size_t)n * 4) + 256;
 }
 
 int abm_schelling_place(const int32_t* pos, const int8_t* type, int64_t n, int32_t W, int32_t H,
@@ -274,6 +462,21 @@ int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, in
   st = abm_host::record_cuda_error(
       cudaMemsetAsync(w.claim, 0x7F, sizeof(int32_t) * (size_t)W * H, s), "abm_schelling_run/claims");
   if (st) return st;
+  if ((int64_t)W * H <= kClusterMaxCells && cluster_smem_bytes(W, H) <= kClusterMaxRowBytes) {
+    // one cluster launch for the whole run
+    st = abm_host::record_cuda_error(
+        cudaMemsetAsync(w.unhappy_count, 0, 2 * sizeof(int32_t), s), "abm_schelling_run/counters");
+    if (st) return st;
+    const size_t rows_bytes = cluster_smem_bytes(W, H);  // <= kClusterMaxRowBytes
+    cudaError_t e = cudaFuncSetAttribute(schelling_cluster_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rows_bytes);
+    if (e != cudaSuccess) return abm_host::record_cuda_error(e, "abm_schelling_run/cluster smem");
+    schelling_cluster_kernel<<<kClusterCtas, kClusterThreads, rows_bytes, s>>>(
+        pos, type, (int32_t)n, W, H, grid, cell_agent, coll_keys, steps, stats, w.target, w.claim,
+        w.empty_list, w.unhappy_list, w.unhappy_count);
+    return abm_host::check_launch("abm_schelling_run/cluster");
+  }
   const unsigned agent_blocks = (unsigned)((n + kAgentThreads - 1) / kAgentThreads);
   const size_t smem = 3 * (size_t)H;
   for (int32_t t = 0; t < steps; ++t) {

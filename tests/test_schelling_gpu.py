@@ -42,6 +42,7 @@ def _run_abi(pos, types, W, H, ck):
 @pytest.mark.parametrize("W,H,density,steps,seed", [
     (8, 8, 0.5, 10, 0), (16, 16, 0.9, 30, 3), (3, 5, 0.6, 12, 2), (64, 32, 0.75, 40, 5),
     (300, 17, 0.9, 15, 7), (256, 256, 0.97, 10, 4),
+    (600, 500, 0.9, 6, 8),  # above 2^18 cells: four launches per step instead of one cluster
 ])
 def test_schelling_small_bit_exact(cuda, W, H, density, steps, seed):
     from jaxabm_gb300.schelling import initial_layout
