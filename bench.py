@@ -359,7 +359,7 @@ def model_lines():
                   0.05, 0.1, _dev.ptr(counts), _dev.ptr(ws), ws.numel(), None)
     ms = _time_ms(sir1, reps=3)
     out["sir_ba_n1048576_t365"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
-                                   "launches_per_run": 4 * T + 5 + (T + 7) // 8,
+                                   "launches_per_run": 3 * T + 6 + (T + 7) // 8,
                                    "path": "abm_sir_run, kernels launched one by one"}
     # the same model as a one-instance batch, its 365 steps replayed from one CUDA graph
     from jaxabm_gb300 import ensemble

@@ -238,8 +238,9 @@ ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_ite
 ABM_API int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream);
 
 /* Bytes of the list workspace of abm_sir_steps for up to max_agents live agents in up to
- * max_tiles work items: a 16-byte header {changes, overflow, candidates, live tiles},
- * zeroed once by the caller, then 16 bytes per agent (a change list and a candidate list),
+ * max_tiles work items: a 32-byte header {changes, overflow, candidates, live tiles, push
+ * ticket, 0, 0, 0}, zeroed once by the caller, then 16 bytes per agent (a change list and
+ * a candidate list),
  * then a compacted copy of the work list (16 bytes per tile, rebuilt every 8 steps from
  * the tiles of instances that can still change). */
 ABM_API size_t abm_sir_changes_bytes(int64_t max_agents, int64_t max_tiles);
@@ -266,7 +267,8 @@ ABM_API int abm_sir_default_launch(abm_sir_launch* out);
  *   I -> R if uniform(k_rec) < gamma.
  * A susceptible agent whose word says it has no infected neighbour reads nothing else;
  * changes are pushed to the neighbours' words after all decisions (four launches per
- * step: sweep, candidates, push, finalize).  At most 2^26 instances.  `changes` (16-byte
+ * step: sweep, candidates, push, finalize; with at most 256 instances the push kernel's last
+ * CTA finalizes, three launches).  At most 2^26 instances.  `changes` (16-byte
  * aligned) must hold abm_sir_changes_bytes(total agents of all live instances, nwork); its
  * overflow flag is set (and changes dropped) if it is smaller.
  * Replaces Model.step's AgentCollection.update (jaxabm/model.py:163-171,

@@ -122,12 +122,8 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     for (int c = 0; c < 4; ++c) li_d[c] = r1 > r0 ? li[c] * inv_deg_i : li[c];
     float sl[4] = {0.f, 0.f, 0.f, 0.f};  // sum_j g'(d) (lam_j/deg_j - lam_i/deg_i)
     float sgd[4] = {0.f, 0.f, 0.f, 0.f}, sse[4] = {0.f, 0.f, 0.f, 0.f}, sst[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int e = r0; e < r1; ++e) {
-      const int j = col[e];
-      float oj[4], lj[4];
-      ld4(o + (size_t)j * B, sub, oj);
-      ld4(lam_in + (size_t)j * B, sub, lj);
-      const float inv_deg_j = inv_deg[j];
+    // one neighbour's contribution, accumulated in CSR order
+    auto edge = [&](const float (&oj)[4], const float (&lj)[4], float inv_deg_j) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const float d = oj[c] - oi[c];
@@ -141,6 +137,26 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
         sse[c] = fmaf(sp * it[c], d, sse[c]);
         sst[c] = fmaf(-sp * z * it[c], d, sst[c]);
       }
+    };
+    int e = r0;
+    // two neighbours' opinion and adjoint rows in flight per iteration
+    for (; e + 1 < r1; e += 2) {
+      const int ja = col[e], jb = col[e + 1];
+      float oa[4], la[4], ob[4], lb[4];
+      ld4(o + (size_t)ja * B, sub, oa);
+      ld4(lam_in + (size_t)ja * B, sub, la);
+      ld4(o + (size_t)jb * B, sub, ob);
+      ld4(lam_in + (size_t)jb * B, sub, lb);
+      const float da = inv_deg[ja], db = inv_deg[jb];
+      edge(oa, la, da);
+      edge(ob, lb, db);
+    }
+    if (e < r1) {
+      const int j = col[e];
+      float oj[4], lj[4];
+      ld4(o + (size_t)j * B, sub, oj);
+      ld4(lam_in + (size_t)j * B, sub, lj);
+      edge(oj, lj, inv_deg[j]);
     }
     float lo[4];
 #pragma unroll

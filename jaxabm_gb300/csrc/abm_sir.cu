@@ -67,6 +67,7 @@ constexpr uint32_t kTag = 0x80000000u;             // column entry of a hub neig
 constexpr uint32_t kIdx = 0x7FFFFFFFu;
 constexpr int kInstBits = 26;                      // instance bits of a candidate entry
 constexpr int kCompactEvery = 8;                   // steps between work-list compactions
+constexpr int kFusedFinalizeMax = 256;             // instances finalized by the last push CTA
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kS = 0, kI = 1;
 
@@ -80,8 +81,11 @@ struct ListHeader {
   int32_t changes;
   int32_t overflow;
   int32_t cand_s;
-  int32_t live_tiles;  // length of the compacted work list
+  int32_t live_tiles;   // length of the compacted work list
+  uint32_t push_done;   // CTAs of the push kernel that finished (fused finalize)
+  int32_t reserved[3];
 };
+static_assert(sizeof(ListHeader) == 32, "list header layout");
 
 // The compacted work list (tiles of live instances, `max_tiles` int4 entries) sits at the
 // end of the workspace.
@@ -526,11 +530,54 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   flush_changes(buf, nbuf, L, lane);
 }
 
+// Counts after the step, key chain, step counter, next step's key, done flag of one
+// instance.
+__device__ __forceinline__ void finalize_one(abm_sir_instance* __restrict__ I) {
+  const int t = I->t;
+  if (t >= I->steps) return;
+  const int si = I->step_si, ir = I->step_ir;
+  I->num_s -= si;
+  I->num_i += si - ir;
+  I->num_r += ir;
+  I->step_si = 0;
+  I->step_ir = 0;
+  I->counts[3 * t] = I->num_s;
+  I->counts[3 * t + 1] = I->num_i;
+  I->counts[3 * t + 2] = I->num_r;
+  const uint2 r = abm::split_at(make_uint2(I->rng[0], I->rng[1]), 0);
+  I->rng[0] = r.x;
+  I->rng[1] = r.y;
+  I->t = t + 1;
+  if (t + 1 < I->steps) {
+    const uint2 c = step_key_of(I, t + 1, r);
+    I->coll[0] = c.x;
+    I->coll[1] = c.y;
+  }
+  if (t + 1 == I->steps && I->done_flag) {
+    __threadfence_system();
+    *reinterpret_cast<volatile int32_t*>(I->done_flag) = 1;
+  }
+}
+
+// The step's finalization of every instance; clears the lists.
+__global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
+                                    ListHeader* __restrict__ hdr) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0) {
+    hdr->changes = 0;
+    hdr->cand_s = 0;
+  }
+  if (k < ninst) finalize_one(insts + k);
+}
+
 // Neighbours' infected counts +-1 and own compartment +1 for every change: one thread per
 // change for rows up to kHeavyDeg slots (atomics issued without waiting for results), one
 // warp for longer rows (kHeavyUnroll column loads per lane in flight).
+// With few instances (ninst_fused > 0) the last push CTA to finish also finalizes the
+// step: each CTA takes a ticket when done, and the CTA holding the last one runs after
+// every change was pushed.
 __global__ void __launch_bounds__(kSirThreads)
-sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
+sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L, int ninst_fused) {
   const int lane = threadIdx.x & 31;
   const int count = min(L.hdr->changes, L.capacity);
   const int threads = gridDim.x * kSirThreads;
@@ -598,6 +645,22 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       }
     }
   }
+  if (ninst_fused <= 0) return;
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&L.hdr->push_done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int k = threadIdx.x; k < ninst_fused; k += blockDim.x) finalize_one(insts + k);
+  if (threadIdx.x == 0) {
+    L.hdr->push_done = 0;
+    L.hdr->changes = 0;
+    L.hdr->cand_s = 0;
+  }
 }
 
 // Work items of instances that can still change (t < steps and an infected agent) into the
@@ -620,43 +683,6 @@ __global__ void sir_compact_kernel(const abm_sir_instance* __restrict__ insts,
     }
     const int pos = warp_append(keep, &L.hdr->live_tiles, lane);
     if (keep) L.live_work[pos] = item;
-  }
-}
-
-// Counts after the step, key chain, step counter, next step's key, done flag; clears the
-// lists.
-__global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ninst,
-                                    ListHeader* __restrict__ hdr) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k == 0) {
-    hdr->changes = 0;
-    hdr->cand_s = 0;
-  }
-  if (k >= ninst) return;
-  abm_sir_instance* I = insts + k;
-  const int t = I->t;
-  if (t >= I->steps) return;
-  const int si = I->step_si, ir = I->step_ir;
-  I->num_s -= si;
-  I->num_i += si - ir;
-  I->num_r += ir;
-  I->step_si = 0;
-  I->step_ir = 0;
-  I->counts[3 * t] = I->num_s;
-  I->counts[3 * t + 1] = I->num_i;
-  I->counts[3 * t + 2] = I->num_r;
-  const uint2 r = abm::split_at(make_uint2(I->rng[0], I->rng[1]), 0);
-  I->rng[0] = r.x;
-  I->rng[1] = r.y;
-  I->t = t + 1;
-  if (t + 1 < I->steps) {
-    const uint2 c = step_key_of(I, t + 1, r);
-    I->coll[0] = c.x;
-    I->coll[1] = c.y;
-  }
-  if (t + 1 == I->steps && I->done_flag) {
-    __threadfence_system();
-    *reinterpret_cast<volatile int32_t*>(I->done_flag) = 1;
   }
 }
 
@@ -982,6 +1008,8 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
   const int cand_grid = cfg.candidates_grid;
   const int push_grid = cfg.push_grid;
   const int fin_blocks = (ninst + 255) / 256;
+  // few instances: the push kernel's last CTA finalizes the step (one launch less per step)
+  const bool fuse = ninst <= kFusedFinalizeMax;
   const int compact_blocks = nwork > 0 ? min((nwork + 255) / 256, abm_host::sm_count() * 4) : 1;
   sir_prepare_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst);
   int st = abm_host::check_launch("abm_sir_steps/prepare");
@@ -1000,11 +1028,13 @@ int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work_item* w
       if ((st = abm_host::check_launch("abm_sir_steps/sweep"))) return st;
       sir_candidates_kernel<<<cand_grid, kSirThreads, 0, s>>>(insts, L);
       if ((st = abm_host::check_launch("abm_sir_steps/candidates"))) return st;
-      sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, L);
+      sir_push_kernel<<<push_grid, kSirThreads, 0, s>>>(insts, L, fuse ? ninst : 0);
       if ((st = abm_host::check_launch("abm_sir_steps/push"))) return st;
     }
-    sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, L.hdr);
-    if ((st = abm_host::check_launch("abm_sir_steps/finalize"))) return st;
+    if (!fuse || nwork == 0) {
+      sir_finalize_kernel<<<fin_blocks, 256, 0, s>>>(insts, ninst, L.hdr);
+      if ((st = abm_host::check_launch("abm_sir_steps/finalize"))) return st;
+    }
   }
   return ABM_OK;
 }

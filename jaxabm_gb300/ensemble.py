@@ -275,9 +275,10 @@ class SIRBatch:
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
     def launches_per_run(self):
-        # prepare, then per step sweep, candidates, push, finalize, and a work-list
-        # compaction every 8 steps
-        return 4 * self.steps + 1 + (self.steps + 7) // 8
+        # prepare, then per step sweep, candidates, push and (more than 256 instances)
+        # finalize, and a work-list compaction every 8 steps
+        per_step = 3 if self.k <= 256 else 4
+        return per_step * self.steps + 1 + (self.steps + 7) // 8
 
     def edge_stats(self):
         """(CSR slots read by decide, CSR slots read by push, compartment changes,

@@ -325,7 +325,8 @@ class SIRServer:
             while len(self._in_flight) > self.max_ticks_in_flight:
                 self._in_flight.popleft().synchronize()
             self.ticks += 1
-            self.launches += 4 * self.steps_per_tick + 1 + (self.steps_per_tick + 7) // 8
+            per_step = 3 if self.max_slots + 1 <= 256 else 4
+            self.launches += per_step * self.steps_per_tick + 1 + (self.steps_per_tick + 7) // 8
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)
