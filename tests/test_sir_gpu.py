@@ -159,3 +159,28 @@ def test_sir_batch_run_matches_serial(cuda):
             for key in ("S", "I", "R"):
                 assert list(got[key]) == list(ref[key]), (beta, gamma, r, key)
             assert np.array_equal(got["agents.people.state"], ref["agents.people.state"])
+
+
+def test_sir_repack_is_idempotent(cuda):
+    """Packing a batch again (its columns already carry hub tags) gives the same words,
+    hub counts and results; a graph with hubs (BA m=8, n=3000) exercises the tags."""
+    from jaxabm_gb300 import ensemble, sir
+    sizes, seeds = [3000, 1500], [21, 22]
+    graphs = [sir.barabasi_albert(n, 8, s) for n, s in zip(sizes, seeds)]
+    inits = [sir.initial_states(n, 0.01, s) for n, s in zip(sizes, seeds)]
+    b = ensemble.SIRBatch(graphs, inits, [0.08, 0.15], [0.1, 0.2], seeds, 25)
+    w0, h0, c0 = b.words.clone(), b.hub_counts.clone(), b.col.clone()
+    assert (c0 < 0).any()  # some columns point at hubs (bit 31 set)
+    b.pack()
+    torch.cuda.synchronize()
+    assert torch.equal(b.words, w0) and torch.equal(b.col, c0)
+    hubs = (w0 >> 2) == 63
+    assert torch.equal(b.hub_counts[hubs.nonzero()], h0[hubs.nonzero()])
+    b.run()
+    torch.cuda.synchronize()
+    for i in range(2):
+        rng, _ = models.model_keys(seeds[i], 1)
+        ref_st, ref_counts, _ = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng, 25,
+                                                [0.08, 0.15][i], [0.1, 0.2][i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts)
+        assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st)
