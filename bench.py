@@ -446,6 +446,39 @@ def model_lines():
                              "frac": mufu / (ms_f / 1e3) / 1e12 / SFU_TOPS,
                              "peak_kind": "nominal (152 SMs x 16 per clock x 2.07 GHz)"}}
 
+    # sensitivity analysis: 256 Latin-hypercube samples of (beta, gamma) for an SIR model of
+    # 10,000 agents (BA m=4, its own graph per sample seed), 365 steps; host wall time of the
+    # whole analysis (graphs, packing, one batched replay, results) against the same
+    # models run one by one (8 of them timed, scaled to 256)
+    import time
+
+    import jaxabm_gb300 as jx
+
+    def sa_factory(params=None, config=None):
+        p = {"n": 10_000, "m": 4, "steps": 365}
+        p.update(params or {})
+        return jx.SIRModel(p, seed=config.seed)
+    ranges = {"beta": (0.01, 0.2), "gamma": (0.05, 0.3)}
+    sa = jx.SensitivityAnalysis(sa_factory, ranges, ["I", "R"], num_samples=256, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sa.run(verbose=False)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    host = sa.samples.cpu().numpy()
+    t0 = time.perf_counter()
+    for i in range(8):
+        sa_factory(params={"beta": float(host[i, 0]), "gamma": float(host[i, 1])},
+                   config=jx.ModelConfig(seed=1000 + i)).run()
+    torch.cuda.synchronize()
+    serial = (time.perf_counter() - t0) / 8 * 256
+    out["sensitivity_sir_256_samples_n10000_t365"] = {
+        "wall_s": wall, "batched": sa.batched, "serial_wall_s_estimate": serial,
+        "speedup": serial / wall, "agent_steps_per_s": 256 * 10_000 * 365 / wall,
+        "note": "host clock around SensitivityAnalysis.run (graph generation and packing "
+                "included); serial = each sample's model.run() alone, 8 timed"}
+    del sa
+
     hbm, _ = _peaks()
     # Network CSR on the device: the 8,388,576 directed edges of BA(2^20, m=4) in shuffled
     # order -> row_ptr/col (stable radix sort by source)

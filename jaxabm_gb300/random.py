@@ -115,6 +115,27 @@ def randint(key: torch.Tensor, shape, minval, maxval) -> torch.Tensor:
     return out.reshape(lead + shape)
 
 
+def permutation(key: torch.Tensor, x) -> torch.Tensor:
+    """``jax.random.permutation(key, x)`` for an int ``x`` (a shuffle of ``arange(x)``) or a
+    1-D tensor (its entries shuffled, on the device).  JAX's shuffle: ``ceil(3 ln n /
+    ln(2**32 - 1))`` rounds, each splitting the key into (key, subkey) and stably sorting
+    the entries by ``bits(subkey, (n,))`` read as unsigned words."""
+    if isinstance(x, int):
+        arr = torch.arange(int(x), device=_dev.device())
+    else:
+        arr = torch.as_tensor(x).to(_dev.device())
+        if arr.dim() != 1:
+            raise ValueError("permutation takes an int or a 1-D tensor")
+    n = arr.shape[0]
+    rounds = int(math.ceil(3 * math.log(max(1, n)) / math.log(2.0**32 - 1)))
+    for _ in range(rounds):
+        pair = split(key, 2)
+        key, sub = pair[0], pair[1]
+        words = bits(sub, (n,)).to(torch.int64) & 0xFFFFFFFF
+        arr = arr[torch.sort(words, stable=True).indices]
+    return arr
+
+
 def keychain(rng: torch.Tensor, steps: int, ncoll: int = 1, update_keys: bool = False):
     """Advance ``rng`` (int32[..., 2], in place) through ``steps`` calls of Model.step and
     return the per-step collection keys int32[..., steps, ncoll, 2]

@@ -136,6 +136,29 @@ class SIRModel(Model):
                                       initial_infected=float(self.p.get("initial_infected", 0.001)),
                                       infection_seed=int(self.p.get("infection_seed", self.seed)))
 
+    def ensemble_member(self, graph_cache=None):
+        """This model as one member of an SIR ensemble: ``(row_ptr, col, initial states,
+        beta, gamma, seed, steps)`` built from its parameters exactly as ``setup`` and
+        ``run`` would, or None when it cannot run batched (a subclass with Python hooks or
+        its own ``setup``).  ``graph_cache`` shares generated graphs between members."""
+        if self._hooks() != (None, None) or type(self).setup is not SIRModel.setup:
+            return None
+        p, seed = self.p, int(self.seed)
+        n = int(p.get("n", 1 << 20))
+        if "row_ptr" in p:
+            g = (np.asarray(p["row_ptr"], np.int32), np.asarray(p["col"], np.int32))
+        else:
+            key = (n, int(p.get("m", 4)), int(p.get("graph_seed", seed)))
+            if graph_cache is None:
+                graph_cache = {}
+            if key not in graph_cache:
+                graph_cache[key] = barabasi_albert(*key)
+            g = graph_cache[key]
+        init = initial_states(n, float(p.get("initial_infected", 0.001)),
+                              int(p.get("infection_seed", seed)))
+        return (g[0], g[1], init, float(p.get("beta", 0.05)), float(p.get("gamma", 0.1)),
+                seed, int(self.steps))
+
     def batch_run(self, parameter_ranges, repetitions=1):
         """Every parameter combination, ``repetitions`` runs each, as ONE batched launch
         sequence of the ensemble engine (the reference runs them one after another,
@@ -145,50 +168,58 @@ class SIRModel(Model):
         path."""
         import itertools
 
-        from .agentpy import Results
-        from .ensemble import SIRBatch
         if self._hooks() != (None, None):
             return super().batch_run(parameter_ranges, repetitions)
         names = list(parameter_ranges.keys())
-        combos = list(itertools.product(*parameter_ranges.values()))
-        specs = []
-        for values in combos:
+        keys, models = [], []
+        for values in itertools.product(*parameter_ranges.values()):
             for r in range(repetitions):
                 p = dict(self.p)
                 p.update(zip(names, values))
-                specs.append((tuple(values), p, self.seed + r))
-        if not specs:
+                keys.append(tuple(values))
+                models.append(self.__class__(p, seed=self.seed + r))
+        if not models:
             return {}
-        steps = {int(p.get("steps", self.steps)) for _, p, _ in specs}
-        if len(steps) != 1:
+        runs = run_ensemble(models)
+        if runs is None:
             return super().batch_run(parameter_ranges, repetitions)
-        steps = steps.pop()
-        graphs, inits, betas, gammas, seeds = [], [], [], [], []
-        cache = {}
-        for _, p, seed in specs:
-            n = int(p.get("n", 1 << 20))
-            if "row_ptr" in p:
-                g = (np.asarray(p["row_ptr"], np.int32), np.asarray(p["col"], np.int32))
-            else:
-                key = (n, int(p.get("m", 4)), int(p.get("graph_seed", seed)))
-                if key not in cache:
-                    cache[key] = barabasi_albert(*key)
-                g = cache[key]
-            graphs.append(g)
-            inits.append(initial_states(n, float(p.get("initial_infected", 0.001)),
-                                        int(p.get("infection_seed", seed))))
-            betas.append(float(p.get("beta", 0.05)))
-            gammas.append(float(p.get("gamma", 0.1)))
-            seeds.append(seed)
-        batch = SIRBatch(graphs, inits, betas, gammas, seeds, steps)
-        batch.run()
-        batch.check()
-        counts = batch.counts.reshape(len(specs), steps, 3).cpu().numpy()
         results = {}
-        for k, (values, _, _) in enumerate(specs):
-            data = {"step": list(range(1, steps + 1)),
-                    "S": counts[k, :, 0].tolist(), "I": counts[k, :, 1].tolist(),
-                    "R": counts[k, :, 2].tolist(),
-                    "agents.people.state": batch.final_state(k).cpu().numpy()}
-            results.setdefault(values, []).append(Results(data))
+        for values, res in zip(keys, runs):
+            results.setdefault(values, []).append(res)
         return results
+
+
+def run_ensemble(models):
+    """Run SIR models as one batched launch sequence (``ensemble.SIRBatch``: every member and
+    step in one CUDA-graph replay) and return one ``Results`` per model, each equal to that
+    model's own ``run()`` (keys ``step``, ``S``, ``I``, ``R``, ``agents.people.state``).
+    Returns None unless every model is a batchable ``SIRModel`` (``ensemble_member``) and all
+    run the same number of steps."""
+    from .agentpy import Results
+    from .ensemble import SIRBatch
+    cache, members = {}, []
+    for m in models:
+        spec = m.ensemble_member(cache) if isinstance(m, SIRModel) else None
+        if spec is None:
+            return None
+        members.append(spec)
+    if not members:
+        return []
+    steps = {spec[6] for spec in members}
+    if len(steps) != 1:
+        return None
+    steps = steps.pop()
+    batch = SIRBatch([(s[0], s[1]) for s in members], [s[2] for s in members],
+                     [s[3] for s in members], [s[4] for s in members],
+                     [s[5] for s in members], steps)
+    batch.run()
+    batch.check()
+    counts = batch.counts.reshape(len(members), steps, 3).cpu().numpy()
+    out = []
+    for k in range(len(members)):
+        data = {"step": list(range(1, steps + 1)),
+                "S": counts[k, :, 0].tolist(), "I": counts[k, :, 1].tolist(),
+                "R": counts[k, :, 2].tolist(),
+                "agents.people.state": batch.final_state(k).cpu().numpy()}
+        out.append(Results(data))
+    return out

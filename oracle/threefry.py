@@ -230,3 +230,19 @@ def randint(key, shape, minval, maxval, mode=PARTITIONABLE):
     r = (((hi % span) * np.uint64(mult)) & np.uint64(0xFFFFFFFF)) + (lo % span)
     r = (r & np.uint64(0xFFFFFFFF)) % np.uint64(span)
     return ((np.int64(minval) + r.astype(np.int64)) & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
+
+
+def permutation(key, x, mode=PARTITIONABLE):
+    """``jax.random.permutation(key, x)`` for an int ``x`` (a shuffle of ``arange(x)``) or a
+    1-D array (its entries shuffled).  Published JAX shuffle (``jax/_src/random.py``,
+    ``_shuffle``): ``ceil(3 ln n / ln(2**32 - 1))`` rounds; each round splits the key into
+    (key, subkey) and stably sorts the entries by ``bits(subkey, (n,))``."""
+    arr = np.arange(int(x)) if np.ndim(x) == 0 else np.asarray(x).copy()
+    n = arr.shape[0]
+    rounds = int(np.ceil(3 * np.log(max(1, n)) / np.log(np.iinfo(np.uint32).max)))
+    key = np.asarray(key, dtype=np.uint32)
+    for _ in range(rounds):
+        key, sub = split(key, 2, mode)
+        order = np.argsort(bits(sub, (n,), mode), kind="stable")
+        arr = arr[order]
+    return arr
