@@ -28,7 +28,7 @@ from . import schelling  # noqa: E402  registers SchellingAgent
 from .schelling import SchellingAgent, SchellingModel  # noqa: E402
 from . import opinion  # noqa: E402  registers OpinionAgent
 from .opinion import OpinionAgent, OpinionModel  # noqa: E402
-from .analysis import SensitivityAnalysis  # noqa: E402
+from .analysis import ModelCalibrator, SensitivityAnalysis  # noqa: E402
 
 
 def build(force: bool = False) -> str:
@@ -54,5 +54,5 @@ __all__ = [
     "AgentType", "AgentCollection", "JaxModel", "ModelConfig",
     "StepKernel", "UnregisteredAgentError", "register_step", "unregister_step", "lookup",
     "convert_to_numpy", "format_time", "random", "build", "show_info", "set_verbose",
-    "RandomWalker", "RandomWalkModel", "AbmError", "SensitivityAnalysis",
+    "RandomWalker", "RandomWalkModel", "AbmError", "SensitivityAnalysis", "ModelCalibrator",
 ]

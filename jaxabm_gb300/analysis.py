@@ -1,4 +1,4 @@
-"""Sensitivity analysis over model parameters, run on the ensemble engine.
+"""Sensitivity analysis and population-based calibration, run on the ensemble engine.
 
 ``SensitivityAnalysis`` keeps the reference's interface and sampling
 (jaxabm/analysis.py:23-203): Latin-hypercube samples drawn with ``jax.random`` semantics,
@@ -8,6 +8,8 @@ sensitivity indices.  The reference runs the samples one after another; here, wh
 sample's model is a batchable SIR model, all of them run as one ensemble (one CUDA-graph
 replay for every member and step, ``sir.run_ensemble``) and each member's result equals
 that model's own ``run()``.  Other models run one by one, as in the reference.
+``ModelCalibrator`` evaluates each iteration's population (every candidate times every
+evaluation run) the same way.
 """
 
 from typing import Any, Callable, Dict, List, Tuple
@@ -15,6 +17,7 @@ from typing import Any, Callable, Dict, List, Tuple
 import numpy as np
 import torch
 
+from . import _dev
 from . import random as jr
 from .core import ModelConfig
 
@@ -135,3 +138,303 @@ class SensitivityAnalysis:
                 per_param[name] = float(np.mean(s_norm * v_norm) ** 2)
             indices[metric] = per_param
         return indices
+
+
+def _evaluate_models(models, steps):
+    """Run ``models`` for ``steps`` steps each: batchable SIR models as one ensemble
+    (``sir.run_ensemble``), anything else one by one.  Returns (results, batched)."""
+    from .sir import run_ensemble
+    for m in models:
+        if hasattr(m, "steps"):
+            m.steps = steps
+    runs = run_ensemble(models) if models else []
+    if runs is not None:
+        return runs, bool(models)
+    return [m.run(steps=steps) for m in models], False
+
+
+class ModelCalibrator:
+    """Population-based calibration of model parameters (jaxabm/analysis.py:290-1580,
+    methods ``"es"``, ``"pso"`` and ``"cem"``).
+
+    The constructor, ``calibrate``, the loss functions, the robust evaluation (mean metrics
+    over ``num_evaluation_runs`` runs with seeds ``randint(subkey, (), 0, 1_000_000)``,
+    normalised loss, 95 % intervals) and the update rules follow the reference.  What
+    changes is how a population is evaluated: the reference runs its ``population x runs``
+    models one after another; here every candidate of an iteration is drawn first (the key
+    chain advances in the reference's order) and, for SIR models, all of them run as one
+    ensemble.  ``batched_evaluations`` counts the iterations that did.
+
+    Gradient methods (``"adam"``, ``"sgd"``: ``jit(grad)`` through ``model.run``) and the
+    reinforcement-learning methods are not provided: the differentiable model of this
+    engine calibrates through ``opinion.OpinionLoss`` (a ``torch.autograd.Function`` with the
+    hand-written adjoint), and the RL policies are not agent-step work.
+    """
+
+    POPULATION_METHODS = ("es", "pso", "cem")
+
+    def __init__(self, model_factory, initial_params: Dict[str, float],
+                 target_metrics: Dict[str, float], param_bounds=None, metrics_weights=None,
+                 learning_rate: float = 0.01, max_iterations: int = 100, method: str = "adam",
+                 loss_type: str = "mse", evaluation_steps: int = 50,
+                 num_evaluation_runs: int = 3, tolerance: float = 1e-6, patience: int = 10,
+                 seed: int = 0):
+        self.model_factory = model_factory
+        self.params = dict(initial_params)
+        self.target_metrics = target_metrics
+        self.param_bounds = param_bounds or {k: (0.01, 10.0) for k in initial_params}
+        self.metrics_weights = metrics_weights or {k: 1.0 for k in target_metrics}
+        self.learning_rate = learning_rate
+        self.max_iterations = max_iterations
+        self.method = method
+        self.loss_type = loss_type
+        self.evaluation_steps = evaluation_steps
+        self.num_evaluation_runs = num_evaluation_runs
+        self.tolerance = tolerance
+        self.patience = patience
+        self._check_method()
+        self.key = jr.PRNGKey(seed)
+        self.loss_history: List[float] = []
+        self.param_history: List[Dict[str, float]] = []
+        self.confidence_intervals: List[Dict[str, Tuple[float, float]]] = []
+        self.best_params = dict(initial_params)
+        self.best_loss = float("inf")
+        self.batched_evaluations = 0
+        self._setup_optimization_method()
+
+    # -- key chain ------------------------------------------------------------------------
+
+    def _split(self, num=2):
+        keys = jr.split(self.key, num)
+        self.key = keys[0].contiguous()
+        return [keys[i].contiguous() for i in range(1, num)]
+
+    def _names(self):
+        return list(self.params.keys())
+
+    def _clip(self, pop):
+        """Clip column i to the i-th entry of ``param_bounds`` (the reference pairs the
+        columns with the bounds in insertion order)."""
+        for i, (lo, hi) in enumerate(self.param_bounds.values()):
+            pop[..., i] = torch.clamp(pop[..., i], float(lo), float(hi))
+        return pop
+
+    # -- setup (jaxabm/analysis.py:376-399, 533-597) --------------------------------------
+
+    def _check_method(self):
+        if self.method not in self.POPULATION_METHODS:
+            known = ("adam", "sgd", "bayesian", "q_learning", "policy_gradient",
+                     "actor_critic", "multi_agent_rl", "dqn")
+            if self.method in known:
+                raise NotImplementedError(
+                    f"calibration method {self.method!r} is not provided by this engine; "
+                    f"population methods: {', '.join(self.POPULATION_METHODS)} (gradients of "
+                    "the opinion model: opinion.OpinionLoss)")
+            raise ValueError(f"Unknown calibration method: {self.method}")
+
+    def _setup_optimization_method(self):
+        self._check_method()
+        n = len(self.params)
+        init = torch.tensor([float(self.params[k]) for k in self._names()],
+                            dtype=torch.float32)
+        if self.method == "es":
+            self.es_population_size, self.es_sigma, self.es_elite_ratio = 20, 0.1, 0.2
+            (sub,) = self._split()
+            pop = jr.normal(sub, (self.es_population_size, n)) * self.es_sigma
+            self.es_population = self._clip(pop + init.to(pop.device)[None, :])
+        elif self.method == "pso":
+            self.pso_population_size, self.pso_w, self.pso_c1, self.pso_c2 = 20, 0.7, 1.5, 1.5
+            (sub,) = self._split()
+            pos = jr.uniform(sub, (self.pso_population_size, n))
+            for i, (lo, hi) in enumerate(self.param_bounds.values()):
+                pos[:, i] *= np.float32(hi - lo)
+                pos[:, i] += np.float32(lo)
+            self.pso_positions = pos
+            (sub,) = self._split()
+            self.pso_velocities = jr.normal(sub, (self.pso_population_size, n)) * 0.1
+            self.pso_personal_best = pos.clone()
+            self.pso_personal_best_scores = torch.full((self.pso_population_size,),
+                                                       float("inf"), device=pos.device)
+            self.pso_global_best = pos[0].clone()
+            self.pso_global_best_score = float("inf")
+        else:
+            self.cem_population_size, self.cem_elite_ratio, self.cem_noise_decay = 50, 0.2, 0.99
+            self.cem_mean = init.to(_dev.device())
+            self.cem_std = torch.ones(n, dtype=torch.float32, device=self.cem_mean.device) * 0.5
+
+    # -- losses (jaxabm/analysis.py:401-487) ----------------------------------------------
+
+    def _compute_loss(self, metrics: Dict[str, float]) -> float:
+        loss = 0.0
+        for metric, target in self.target_metrics.items():
+            if metric not in metrics:
+                continue
+            value, weight = metrics[metric], self.metrics_weights[metric]
+            if self.loss_type == "mse":
+                metric_loss = (value - target) ** 2
+            elif self.loss_type == "mae":
+                metric_loss = abs(value - target)
+            elif self.loss_type == "huber":
+                residual = abs(value - target)
+                metric_loss = 0.5 * residual ** 2 if residual <= 1.0 else residual - 0.5
+            elif self.loss_type == "relative":
+                metric_loss = abs(value - target) / (abs(target) + 1e-8)
+            else:
+                raise ValueError(f"Unknown loss type: {self.loss_type}")
+            loss += weight * metric_loss
+        return loss
+
+    def _compute_normalized_loss(self, metrics: Dict[str, float]) -> float:
+        total = 0.0
+        for metric, target in self.target_metrics.items():
+            if metric in metrics:
+                total += (abs(metrics[metric] - target) / (abs(target) + 1e-8)) ** 2
+        return float(total)
+
+    # -- evaluation (jaxabm/analysis.py:434-476) ------------------------------------------
+
+    def _metric_values(self, results):
+        data = _as_dict(results)
+        out = {}
+        for metric in self.target_metrics:
+            v = data[metric] if metric in data else None
+            if v is not None and hasattr(v, "__len__") and len(v) > 0:
+                out[metric] = float(v[-1])
+            else:
+                out[metric] = 0.0
+        return out
+
+    def _summarise(self, runs):
+        """Normalised loss and 95 % intervals of one candidate's runs."""
+        means, cis = {}, {}
+        for metric in self.target_metrics:
+            vals = np.array([r[metric] for r in runs], dtype=np.float32)
+            mean, std = float(vals.mean()), float(vals.std())
+            half = 1.96 * std / float(np.sqrt(np.float32(len(vals))))
+            means[metric] = mean
+            cis[metric] = (mean - half, mean + half)
+        return self._compute_normalized_loss(means), cis
+
+    def _evaluate_population(self, candidates: List[Dict[str, float]]):
+        """(loss, intervals) per candidate.  Seeds are drawn candidate by candidate, run by
+        run, as the reference's serial loop draws them; then every model runs."""
+        models = []
+        for params in candidates:
+            for _ in range(self.num_evaluation_runs):
+                (sub,) = self._split()
+                seed = int(jr.randint(sub, (), 0, 1_000_000).item())
+                models.append(self.model_factory(params=params, config=ModelConfig(seed=seed)))
+        results, batched = _evaluate_models(models, self.evaluation_steps)
+        self.batched_evaluations += int(batched)
+        R = self.num_evaluation_runs
+        out = []
+        for c in range(len(candidates)):
+            runs = [self._metric_values(r) for r in results[c * R:(c + 1) * R]]
+            out.append(self._summarise(runs))
+        return out
+
+    def _evaluate_params_robust(self, params: Dict[str, float]):
+        return self._evaluate_population([params])[0]
+
+    def _rows(self, pop):
+        host = pop.detach().cpu().numpy()
+        return [{name: float(host[i, j]) for j, name in enumerate(self._names())}
+                for i in range(host.shape[0])]
+
+    # -- calibration loops (jaxabm/analysis.py:1281-1580) --------------------------------
+
+    def calibrate(self, verbose: bool = True) -> Dict[str, float]:
+        if verbose:
+            print(f"Starting calibration with {self.method} method...")
+            print(f"Target metrics: {self.target_metrics}")
+            print(f"Parameter bounds: {self.param_bounds}")
+        return {"es": self._calibrate_evolution_strategies,
+                "pso": self._calibrate_particle_swarm,
+                "cem": self._calibrate_cross_entropy}[self.method](verbose)
+
+    def _elite_step(self, pop, verbose, iteration):
+        scores = [loss for loss, _ in self._evaluate_population(self._rows(pop))]
+        fitness = torch.tensor(scores, dtype=torch.float32)
+        n_elite = int(pop.shape[0] * (self.es_elite_ratio if self.method == "es"
+                                      else self.cem_elite_ratio))
+        elite_idx = torch.sort(fitness, stable=True).indices[:n_elite]
+        elite = pop[elite_idx.to(pop.device)]
+        best_idx = int(elite_idx[0])
+        best_loss = float(fitness[best_idx])
+        if best_loss < self.best_loss:
+            self.best_loss = best_loss
+            self.best_params = self._rows(pop[best_idx:best_idx + 1])[0]
+        if verbose:
+            print(f"\nIteration {iteration + 1}/{self.max_iterations}")
+            print(f"Best loss: {best_loss:.6f}")
+        return elite, best_loss
+
+    def _calibrate_evolution_strategies(self, verbose: bool) -> Dict[str, float]:
+        for it in range(self.max_iterations):
+            elite, best_loss = self._elite_step(self.es_population, verbose, it)
+            (sub,) = self._split()
+            mean = elite.mean(dim=0)
+            noise = jr.normal(sub, tuple(self.es_population.shape)) * np.float32(self.es_sigma)
+            self.es_population = self._clip(mean[None, :] + noise)
+            self.loss_history.append(best_loss)
+            self.param_history.append(dict(self.best_params))
+            self.es_sigma *= 0.995
+            if best_loss < self.tolerance:
+                if verbose:
+                    print("Converged: loss below tolerance")
+                break
+        return self.best_params
+
+    def _calibrate_cross_entropy(self, verbose: bool) -> Dict[str, float]:
+        n = len(self.params)
+        for it in range(self.max_iterations):
+            (sub,) = self._split()
+            pop = jr.normal(sub, (self.cem_population_size, n))
+            pop = self._clip(pop * self.cem_std[None, :] + self.cem_mean[None, :])
+            elite, best_loss = self._elite_step(pop, verbose, it)
+            self.cem_mean = elite.mean(dim=0)
+            self.cem_std = elite.std(dim=0, unbiased=False) + np.float32(1e-6)
+            self.loss_history.append(best_loss)
+            self.param_history.append(dict(self.best_params))
+            self.cem_std = self.cem_std * np.float32(self.cem_noise_decay)
+            if best_loss < self.tolerance:
+                if verbose:
+                    print("Converged: loss below tolerance")
+                break
+        return self.best_params
+
+    def _calibrate_particle_swarm(self, verbose: bool) -> Dict[str, float]:
+        for it in range(self.max_iterations):
+            rows = self._rows(self.pso_positions)
+            evals = self._evaluate_population(rows)
+            for i, (loss, _) in enumerate(evals):
+                if loss < float(self.pso_personal_best_scores[i]):
+                    self.pso_personal_best_scores[i] = loss
+                    self.pso_personal_best[i] = self.pso_positions[i]
+                if loss < self.pso_global_best_score:
+                    self.pso_global_best_score = loss
+                    self.pso_global_best = self.pso_positions[i].clone()
+                    self.best_loss = loss
+                    self.best_params = dict(rows[i])
+            sub1, sub2 = self._split(3)
+            shape = tuple(self.pso_velocities.shape)
+            r1, r2 = jr.uniform(sub1, shape), jr.uniform(sub2, shape)
+            cognitive = np.float32(self.pso_c1) * r1 * (self.pso_personal_best - self.pso_positions)
+            social = np.float32(self.pso_c2) * r2 * (self.pso_global_best[None, :] -
+                                                     self.pso_positions)
+            self.pso_velocities = np.float32(self.pso_w) * self.pso_velocities + cognitive + social
+            self.pso_positions = self._clip(self.pso_positions + self.pso_velocities)
+            self.loss_history.append(float(self.pso_global_best_score))
+            self.param_history.append(dict(self.best_params))
+            if verbose:
+                print(f"\nIteration {it + 1}/{self.max_iterations}")
+                print(f"Best loss: {self.pso_global_best_score:.6f}")
+            if self.pso_global_best_score < self.tolerance:
+                if verbose:
+                    print("Converged: loss below tolerance")
+                break
+        return self.best_params
+
+    def get_calibration_history(self) -> Dict[str, List[Any]]:
+        return {"loss": self.loss_history, "params": self.param_history,
+                "confidence_intervals": self.confidence_intervals}

@@ -75,3 +75,42 @@ def test_sobol_indices_squared_correlation():
 def test_sobol_indices_before_run_raises():
     with pytest.raises(ValueError):
         _bare(np.zeros((3, 1)), None, {"a": (0, 1)}).sobol_indices()
+
+
+def _bare_calibrator(**kw):
+    from jaxabm_gb300.analysis import ModelCalibrator
+    c = ModelCalibrator.__new__(ModelCalibrator)
+    c.target_metrics = kw.get("targets", {"a": 2.0, "b": -1.0})
+    c.metrics_weights = kw.get("weights", {"a": 1.0, "b": 0.5})
+    c.loss_type = kw.get("loss_type", "mse")
+    return c
+
+
+@pytest.mark.parametrize("loss_type,want", [
+    ("mse", (3.0 - 2.0) ** 2 + 0.5 * (-0.5 + 1.0) ** 2),
+    ("mae", 1.0 + 0.5 * 0.5),
+    ("huber", (1.0 - 0.5) + 0.5 * (0.5 * 0.5 ** 2)),
+    ("relative", 1.0 / 2.0 + 0.5 * 0.5 / 1.0),
+])
+def test_calibrator_losses(loss_type, want):
+    """The reference's loss types (jaxabm/analysis.py:401-431); Huber with delta 1."""
+    c = _bare_calibrator(loss_type=loss_type)
+    assert c._compute_loss({"a": 3.0, "b": -0.5, "other": 9.0}) == pytest.approx(want)
+
+
+def test_calibrator_normalized_loss_and_intervals():
+    c = _bare_calibrator()
+    assert c._compute_normalized_loss({"a": 3.0}) == pytest.approx(0.25)
+    loss, ci = c._summarise([{"a": 1.0, "b": -1.0}, {"a": 3.0, "b": -1.0}])
+    assert loss == pytest.approx(0.0)
+    half = 1.96 * 1.0 / np.sqrt(2)
+    assert ci["a"] == pytest.approx((2.0 - half, 2.0 + half))
+    assert ci["b"] == pytest.approx((-1.0, -1.0))
+
+
+def test_calibrator_methods_rejected_before_any_launch():
+    from jaxabm_gb300.analysis import ModelCalibrator
+    with pytest.raises(ValueError):
+        ModelCalibrator(None, {"beta": 0.1}, {"R": 1.0}, method="nope")
+    with pytest.raises(NotImplementedError):
+        ModelCalibrator(None, {"beta": 0.1}, {"R": 1.0}, method="adam")

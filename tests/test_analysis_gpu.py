@@ -72,3 +72,69 @@ def test_non_sir_analysis_runs_serially(cuda):
                       config=jx.ModelConfig(seed=1000 + i)).run()
         assert float(res["mean_x"][i]) == pytest.approx(float(ref["mean_x"][-1]), rel=1e-6)
     assert torch.all(res["missing"] == 0)
+
+
+def _sir_factory(steps_hook=False):
+    import jaxabm_gb300 as jx
+
+    class HookedSIR(jx.SIRModel):
+        """Same model with a no-op step hook: not batchable, runs one by one."""
+
+        def step(self):
+            pass
+
+    cls = HookedSIR if steps_hook else jx.SIRModel
+
+    def factory(params=None, config=None):
+        p = {"n": 1500, "m": 3, "initial_infected": 0.02}
+        p.update(params or {})
+        return cls(p, seed=config.seed)
+    return factory
+
+
+def test_es_population_batched_equals_serial(cuda):
+    """One ES iteration: the 20 x 2 models of the population run as one ensemble and give
+    the same losses, best parameters and next population as the models run one by one."""
+    import jaxabm_gb300 as jx
+    kw = dict(initial_params={"beta": 0.1, "gamma": 0.2}, target_metrics={"R": 900.0},
+              param_bounds={"beta": (0.01, 0.4), "gamma": (0.05, 0.5)}, max_iterations=1,
+              method="es", evaluation_steps=20, num_evaluation_runs=2, seed=7)
+    a = jx.ModelCalibrator(_sir_factory(), **kw)
+    b = jx.ModelCalibrator(_sir_factory(steps_hook=True), **kw)
+    assert torch.equal(a.es_population, b.es_population)
+    pa, pb = a.calibrate(verbose=False), b.calibrate(verbose=False)
+    assert a.batched_evaluations == 1 and b.batched_evaluations == 0
+    assert pa == pb and a.loss_history == b.loss_history
+    assert torch.equal(a.es_population, b.es_population)
+    assert torch.equal(a.key, b.key)
+
+
+@pytest.mark.parametrize("method", ["pso", "cem"])
+def test_population_methods_run_batched(cuda, method):
+    import jaxabm_gb300 as jx
+    c = jx.ModelCalibrator(_sir_factory(), {"beta": 0.1, "gamma": 0.2}, {"R": 900.0},
+                           param_bounds={"beta": (0.01, 0.4), "gamma": (0.05, 0.5)},
+                           max_iterations=2, method=method, evaluation_steps=20,
+                           num_evaluation_runs=1, seed=3)
+    best = c.calibrate(verbose=False)
+    assert c.batched_evaluations == 2
+    assert len(c.loss_history) == 2 and c.loss_history[1] <= c.loss_history[0]
+    tol = 1e-6  # bounds are float32 values
+    assert 0.01 - tol <= best["beta"] <= 0.4 + tol and 0.05 - tol <= best["gamma"] <= 0.5 + tol
+    hist = c.get_calibration_history()
+    assert len(hist["params"]) == 2
+
+
+def test_calibrator_non_sir_runs_serially(cuda):
+    import jaxabm_gb300 as jx
+
+    def factory(params=None, config=None):
+        p = {"n": 200}
+        p.update(params or {})
+        return jx.RandomWalkModel(p, seed=config.seed)
+
+    c = jx.ModelCalibrator(factory, {"sigma": 0.02}, {"mean_x": 0.5},
+                           param_bounds={"sigma": (0.001, 0.1)}, max_iterations=1,
+                           method="es", evaluation_steps=3, num_evaluation_runs=1, seed=1)
+    c.calibrate(verbose=False)
+    assert c.batched_evaluations == 0 and len(c.loss_history) == 1
