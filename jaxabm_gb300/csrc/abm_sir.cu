@@ -35,12 +35,16 @@
 //              all its infected neighbours were seen, then draws for those slots in order
 //              with the lanes of the warp drawing together, stopping at the first firing
 //              draw (rows longer than 32 slots are scanned by the whole warp, 128 slots per
-//              pass, with warp votes).  Changes of both kernels are buffered per warp in
-//              shared memory and appended to the change list 32 at a time; no word is
-//              written, so every decision sees the pre-step states.
-//   push       one thread per change (one warp for rows longer than 32 slots): adds +-1 to
-//              the infected-neighbour count of every neighbour and +1 to the agent's own
-//              compartment.
+//              pass, with warp votes).  Decisions read only the 2-bit compartment copy,
+//              which no kernel writes before the push, so every decision sees the pre-step
+//              states.  A newly infected agent's own word and its neighbours' counts are
+//              updated right away (+1; counts only grow during the kernel, so a hub's count
+//              is not read: its row is scanned to the end).  Changes of both kernels are
+//              buffered per warp in shared memory and appended to the change list 32 at a
+//              time.
+//   push       +1 on the compartment copy of every changed agent; for recoveries also +1
+//              on the agent's own word and -1 on its neighbours' counts (one warp per 32
+//              changes, walking the concatenation of their rows one slot per lane).
 //   finalize   one thread per instance: S/I/R counts of the step from the transitions,
 //              rng = split(rng)[0], t += 1, the next step's collection key, done flag after
 //              the last step; clears the lists.
@@ -204,17 +208,70 @@ __device__ __forceinline__ void buffer_change(bool changed, int2 entry, int2* bu
   }
 }
 
+// Count updates of up to 32 CSR rows, one per lane (len 0: none), by the whole warp: the
+// warp walks the concatenation of the rows 32 slots per pass, slot f belonging to the first
+// lane whose inclusive prefix sum of row lengths exceeds f (a five-step binary search over
+// the lanes' prefix sums), so every lane pushes one slot per pass whatever the row lengths
+// and consecutive lanes read consecutive column entries; kPushPasses passes are in flight.
+// tag = instance << 1 | (1: +1, 0: -1).  Called by all lanes of the warp.
+constexpr int kPushPasses = 4;
+
+__device__ __forceinline__ void push_rows(const abm_sir_instance* __restrict__ insts, int tag,
+                                          int row0, int len, int lane) {
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(kFull, incl, 31);
+  const int shift = row0 - (incl - len);  // column index of concatenated slot f: f + shift
+  for (int base = 0; base < total; base += 32 * kPushPasses) {
+    uint32_t v[kPushPasses];
+    int owner[kPushPasses];
+#pragma unroll
+    for (int u = 0; u < kPushPasses; ++u) {
+      const int f = base + 32 * u + lane;
+      int lo = 0;
+#pragma unroll
+      for (int st = 16; st > 0; st >>= 1) {
+        const int p = __shfl_sync(kFull, incl, lo + st - 1);
+        if (p <= f) lo += st;
+      }
+      const int sh = __shfl_sync(kFull, shift, lo);
+      owner[u] = __shfl_sync(kFull, tag, lo);
+      v[u] = f < total ? ld_col(insts[owner[u] >> 1].adj, f + sh) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kPushPasses; ++u) {
+      if (base + 32 * u + lane < total) {
+        const abm_sir_instance* J = insts + (owner[u] >> 1);
+        add_count(J->words, J->hub_counts, v[u], (owner[u] & 1) ? 1 : -1);
+      }
+    }
+  }
+}
+
+// Adds 1 to the compartment field of agent i's word (S -> I, I -> R).
+__device__ __forceinline__ void bump_word(uint8_t* words, int i) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(words + i);
+  red_add(reinterpret_cast<uint32_t*>(a & ~static_cast<uintptr_t>(3)),
+          1u << (8u * static_cast<uint32_t>(a & 3)));
+}
+
 // Per-instance sums over the lanes of a warp (lanes grouped by instance), added to the
-// group's instance by the group's lowest lane: CSR slots scanned and infections.
+// group's instance by the group's lowest lane: CSR slots scanned, infections, slots pushed.
 __device__ __forceinline__ void add_decided(bool valid, int inst, int scanned, int infected,
-                                            abm_sir_instance* insts, int lane) {
+                                            int pushed, abm_sir_instance* insts, int lane) {
   if (!__any_sync(kFull, scanned != 0 || infected != 0)) return;
   const unsigned group = __match_any_sync(kFull, valid ? inst : -1);
   const int s = __reduce_add_sync(group, scanned);
   const int f = __reduce_add_sync(group, infected);
+  const int p = __reduce_add_sync(group, pushed);
   if (valid && lane == __ffs(group) - 1) {
     if (s) red_add(&insts[inst].edges_scanned, static_cast<unsigned long long>(s));
     if (f) red_add(&insts[inst].step_si, f);
+    if (p) red_add(&insts[inst].edges_pushed, static_cast<unsigned long long>(p));
   }
 }
 
@@ -347,10 +404,12 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
 }
 
 // Susceptible candidates: one lane each scans its CSR row, eight slots per pass (the eight
-// column loads, then the eight neighbour-word loads, issued together), stopping at the
-// first firing draw or once all its infected neighbours were seen; rows longer than 32
-// slots are scanned by the whole warp, 128 slots per pass, with warp votes.  Changes go to
-// the change list; no word is written, so every decision sees the pre-step states.
+// column loads, then the eight neighbour-compartment loads, issued together), stopping at
+// the first firing draw or once all its infected neighbours were seen; rows longer than 32
+// slots are scanned by the whole warp, 128 slots per pass, with warp votes.  Decisions read
+// only the 2-bit compartment copy (unchanged until the push kernel), so every decision sees
+// the pre-step states; the rows of the newly infected agents are pushed (+1) by the warp
+// at the end of each pass, and the changes go to the change list.
 __global__ void __launch_bounds__(kSirThreads, 5)
 sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
   __shared__ int2 sbuf[kWarpsPerCta][kBuf];
@@ -398,13 +457,15 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     const uint32_t* __restrict__ comp = nullptr;
     float beta = 0.f;
     if (valid) {
-      if (cnt == static_cast<int>(kHubMark)) cnt = I->hub_counts[i];
       coll = make_uint2(I->coll[0], I->coll[1]);
       adj = I->adj;
       comp = I->comp;
       beta = I->beta;
       row0 = r0_cur;
       deg = r1_cur - r0_cur;
+      // a hub's count is not read here (infections of this step are already being added
+      // to it): its row is scanned to the end
+      if (cnt == static_cast<int>(kHubMark)) cnt = deg;
       heavy = deg > kHeavyDeg;
       if (!heavy) {
         // slots of infected neighbours (bit k: slot k), read until all `cnt` were seen;
@@ -524,8 +585,13 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
       }
     }
 
+    // newly infected agents: their own compartment field and their neighbours' counts are
+    // updated right away (no decision of this step reads the words or the hub counts); the
+    // 2-bit compartment copy, which the decisions read, changes in the push kernel
+    if (infected) bump_word(insts[inst].words, i);
+    push_rows(insts, inst << 1 | 1, row0, infected ? deg : 0, lane);
     buffer_change(infected, make_int2(inst, (i << 2) | static_cast<int>(kI)), buf, nbuf, L, lane);
-    add_decided(valid, inst, scanned, infected ? 1 : 0, insts, lane);
+    add_decided(valid, inst, scanned, infected ? 1 : 0, infected ? deg : 0, insts, lane);
   }
   flush_changes(buf, nbuf, L, lane);
 }
@@ -570,9 +636,10 @@ __global__ void sir_finalize_kernel(abm_sir_instance* __restrict__ insts, int ni
   if (k < ninst) finalize_one(insts + k);
 }
 
-// Neighbours' infected counts +-1 and own compartment +1 for every change: one thread per
-// change for rows up to kHeavyDeg slots (atomics issued without waiting for results), one
-// warp for longer rows (kHeavyUnroll column loads per lane in flight).
+// Changes of the step after every decision was made: +1 on the 2-bit compartment copy of
+// every changed agent; for recoveries (I -> R) also +1 on the agent's own word and -1 on
+// its neighbours' infected counts (push_rows, one warp per 32 changes).  Infections were
+// pushed by the candidates kernel.
 // With few instances (ninst_fused > 0) the last push CTA to finish also finalizes the
 // step: each CTA takes a ticket when done, and the CTA holding the last one runs after
 // every change was pushed.
@@ -583,67 +650,28 @@ sir_push_kernel(abm_sir_instance* __restrict__ insts, Lists L, int ninst_fused) 
   const int threads = gridDim.x * kSirThreads;
   for (int b = (blockIdx.x * kSirThreads + threadIdx.x) & ~31; b < count; b += threads) {
     const int k = b + lane;
-    const bool valid = k < count;
-    int inst = -1, agent = 0, r0 = 0, r1 = 0, delta = 0;
+    int inst = -1, r0 = 0, len = 0;
     abm_sir_instance* I = insts;
-    if (valid) {
+    if (k < count) {
       const int2 ent = __ldcs(&L.changes[k]);
       inst = ent.x;
-      agent = ent.y >> 2;
+      const int agent = ent.y >> 2;
       I = insts + inst;
-      delta = (ent.y & 3) == static_cast<int>(kI) ? 1 : -1;
-      r0 = __ldcs(I->row_ptr + agent);
-      r1 = __ldcs(I->row_ptr + agent + 1);
-      // S(0) -> I(1) and I(1) -> R(2) both add one to the agent's own compartment field
-      const uintptr_t a = reinterpret_cast<uintptr_t>(I->words + agent);
-      red_add(reinterpret_cast<uint32_t*>(a & ~static_cast<uintptr_t>(3)),
-              1u << (8u * static_cast<uint32_t>(a & 3)));
       red_add(I->comp + (agent >> 4), 1u << (2u * static_cast<uint32_t>(agent & 15)));
+      if ((ent.y & 3) != static_cast<int>(kI)) {  // a recovery
+        bump_word(I->words, agent);
+        r0 = __ldcs(I->row_ptr + agent);
+        len = __ldcs(I->row_ptr + agent + 1) - r0;
+      }
     }
     // slots pushed, summed per instance over the warp's lanes
-    {
+    if (__any_sync(kFull, len != 0)) {
       const unsigned group = __match_any_sync(kFull, inst);
-      const int sum = __reduce_add_sync(group, r1 - r0);
-      if (valid && lane == __ffs(group) - 1 && sum)
+      const int sum = __reduce_add_sync(group, len);
+      if (inst >= 0 && lane == __ffs(group) - 1 && sum)
         red_add(&I->edges_pushed, static_cast<unsigned long long>(sum));
     }
-    const bool heavy = valid && r1 - r0 > kHeavyDeg;
-    if (valid && !heavy) {
-      uint8_t* words = I->words;
-      int32_t* hubs = I->hub_counts;
-      const int32_t* __restrict__ adj = I->adj;
-      for (int e0 = r0; e0 < r1; e0 += kChunk) {
-        uint32_t nb[kChunk];
-#pragma unroll
-        for (int q = 0; q < kChunk; ++q) nb[q] = e0 + q < r1 ? ld_col(adj, e0 + q) : 0u;
-#pragma unroll
-        for (int q = 0; q < kChunk; ++q)
-          if (e0 + q < r1) add_count(words, hubs, nb[q], delta);
-      }
-    }
-    unsigned hmask = __ballot_sync(kFull, heavy);
-    while (hmask) {
-      const int src = __ffs(hmask) - 1;
-      hmask &= hmask - 1;
-      const int hinst = __shfl_sync(kFull, inst, src);
-      const int hr0 = __shfl_sync(kFull, r0, src);
-      const int hr1 = __shfl_sync(kFull, r1, src);
-      const int hdelta = __shfl_sync(kFull, delta, src);
-      uint8_t* words = insts[hinst].words;
-      int32_t* hubs = insts[hinst].hub_counts;
-      const int32_t* __restrict__ adj = insts[hinst].adj;
-      for (int e0 = hr0; e0 < hr1; e0 += 32 * kHeavyUnroll) {
-        uint32_t nb[kHeavyUnroll];
-#pragma unroll
-        for (int u = 0; u < kHeavyUnroll; ++u) {
-          const int e = e0 + 32 * u + lane;
-          nb[u] = e < hr1 ? ld_col(adj, e) : 0u;
-        }
-#pragma unroll
-        for (int u = 0; u < kHeavyUnroll; ++u)
-          if (e0 + 32 * u + lane < hr1) add_count(words, hubs, nb[u], hdelta);
-      }
-    }
+    push_rows(insts, inst >= 0 ? inst << 1 : 0, r0, len, lane);
   }
   if (ninst_fused <= 0) return;
   __shared__ bool last;
