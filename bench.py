@@ -134,7 +134,7 @@ def _reduce(v, world, op):
 class SIREnsembleBench:
     name = "sir_ensemble_4096_ba_m4_n1e3_1e5_t365"
 
-    def __init__(self, rank, count=4096, steps=365, grids=None):
+    def __init__(self, rank, count=4096, steps=365, grids=None, path="auto"):
         from jaxabm_gb300 import ensemble
         self.ensemble = ensemble
         self.count, self.T = count, steps
@@ -143,17 +143,24 @@ class SIREnsembleBench:
         t0 = time.perf_counter()
         self.graphs, self.inits = ensemble.build_instances(spec)
         self.build_s = time.perf_counter() - t0
+        # --grids pins the per-step grid kernels; --path resident / grid pins the path
+        self.resident = {"auto": None, "resident": True, "grid": False}[path]
+        if grids is not None:
+            self.resident = False
         self.batch = ensemble.SIRBatch(self.graphs, self.inits, spec["beta"], spec["gamma"],
-                                       spec["seed"], steps)
+                                       spec["seed"], steps, resident=self.resident)
         from jaxabm_gb300 import autotune
         t0 = time.perf_counter()
-        if grids is None:
-            self.launch = autotune.tune_sir_batch(self.batch)
-            self.picked_by = "jaxabm_gb300.autotune"
-        else:
+        if grids is not None:
             self.batch.set_launch(grids)
             self.launch = tuple(grids)
             self.picked_by = "--grids"
+        elif self.resident:
+            self.launch = ensemble.default_launch()
+            self.picked_by = "--path resident"
+        else:
+            self.launch = autotune.tune_sir_batch(self.batch)
+            self.picked_by = "jaxabm_gb300.autotune"
         self.tune_s = time.perf_counter() - t0
         self.batch.capture(steps)
         self.units_per_step = self.batch.agent_steps
@@ -188,8 +195,10 @@ class SIREnsembleBench:
         its counts out inside the timed region.  Returns ms per step."""
         if getattr(self, "_b2", None) is None:
             self._b2 = self.ensemble.SIRBatch(self.graphs, self.inits, self.spec["beta"],
-                                              self.spec["gamma"], self.spec["seed"], self.T)
+                                              self.spec["gamma"], self.spec["seed"], self.T,
+                                              resident=self.resident)
             self._b2.set_launch(self.batch.launch_cfg)
+            self._b2.set_mode(self.batch.mode)
             self._b2.capture(self.T)
         batches = [self.batch, self._b2]
         comp = torch.cuda.current_stream()
@@ -558,7 +567,7 @@ def run_ours(args):
     jx.set_verbose(False)
     jx.build()
     grids = None if not args.grids else tuple(int(v) for v in args.grids.split(","))
-    wl = WORKLOADS[args.workload](rank, count=args.instances, grids=grids)
+    wl = WORKLOADS[args.workload](rank, count=args.instances, grids=grids, path=args.path)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         wl.reset()
@@ -656,6 +665,7 @@ def run_ours(args):
     out["setup_s"] = {"graph_build": wl.build_s, "autotune": wl.tune_s}
     out["config"]["launch_grids"] = {"sweep": wl.launch[0], "candidates": wl.launch[1],
                                      "push": wl.launch[2], "picked_by": wl.picked_by}
+    out["config"]["path"] = wl.batch.mode
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -720,6 +730,9 @@ def main():
     ap.add_argument("--instances", type=int, default=4096,
                     help="ensemble members (the first K of the 4,096-member specification); "
                          "smaller values are for profiling captures")
+    ap.add_argument("--path", default="auto", choices=["auto", "resident", "grid"],
+                    help="SIR ensemble path: the autotuner's choice, the resident "
+                         "per-instance kernel, or the per-step grid kernels")
     ap.add_argument("--grids", default=None,
                     help="fixed sweep,candidates,push grid sizes instead of the autotuner "
                          "(profiling captures: keeps the launch sequence short)")

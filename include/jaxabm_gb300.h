@@ -281,6 +281,30 @@ ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work
                           const abm_sir_launch* launch, void* changes, size_t changes_bytes,
                           void* stream);
 
+/* Resident path: one CTA (512 threads) per instance at a time, running all of the
+ * instance's steps with its words in shared memory (decisions read neighbours'
+ * compartments there, count updates are shared-memory atomics); no per-step launches.
+ * abm_sir_resident_max_agents: largest instance (agents) it can hold on the current device
+ * (0 without a device).  abm_sir_resident_grid: resident CTAs for instances of up to
+ * max_agents agents (also sets the kernel's shared-memory opt-in; call it before capturing
+ * abm_sir_steps_resident into a CUDA graph); 0 if they do not fit.
+ * abm_sir_resident_scratch_bytes: scratch of abm_sir_steps_resident (a queue counter and, per
+ * CTA, three lists of max_agents entries: changes, susceptible candidates, infected agents). */
+ABM_API int32_t abm_sir_resident_max_agents(void);
+ABM_API int32_t abm_sir_resident_grid(int32_t max_agents);
+ABM_API size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid);
+
+/* Same contract as abm_sir_steps (nsteps steps of every instance with t < steps, identical
+ * results) on the resident path: CTAs take instances in the order order[0..ninst) (device
+ * int32, NULL for index order; largest first balances best) and run each for
+ * min(nsteps, steps - t) steps.  Every instance must have n <= max_agents; one that does
+ * not is left untouched and sets *status (device int32, zeroed by the caller) to 1.  grid
+ * from abm_sir_resident_grid(max_agents); scratch 256-byte aligned. */
+ABM_API int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t* order,
+                                   int32_t max_agents, int32_t nsteps, int32_t grid,
+                                   void* scratch, size_t scratch_bytes, int32_t* status,
+                                   void* stream);
+
 /* Workspace of abm_sir_run for n agents and num_edges = row_ptr[n] CSR entries. */
 ABM_API size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges);
 

@@ -1,5 +1,7 @@
 """Project-written autotuner for the launch schedules of the batched SIR step.
 
+It first times the resident path (one CTA per instance, all steps in one launch) when the
+instances fit it, then tunes the per-step grid kernels, and keeps the faster of the two.
 The per-step kernels (sweep, candidates, push) run over persistent grids whose best size
 depends on the GPU and the workload (number of instances, agents, how much of a step is
 random gathering).  The tuner measures CUDA-graph replays of the actual batch for
@@ -104,7 +106,16 @@ def tune_sir_batch(batch, cache_path=None, reps=1, force=False, log=None):
         hit = load_cache(cache_path).get(key)
         if hit and "grids" in hit:
             batch.set_launch(hit["grids"])
+            if batch.resident_ok:
+                batch.set_mode(hit.get("mode", "grid"))
             return tuple(hit["grids"])
+    resident_ms = None
+    if batch.resident_ok:
+        batch.set_mode("resident")
+        resident_ms = time_replay(batch, reps)
+        if log:
+            log(f"autotune resident: {resident_ms:.2f} ms")
+        batch.set_mode("grid")
     default = ensemble.default_launch()
     best = list(default)
     batch.set_launch(best)
@@ -125,8 +136,12 @@ def tune_sir_batch(batch, cache_path=None, reps=1, force=False, log=None):
             if ms < best_ms:
                 best, best_ms = cfg, ms
     batch.set_launch(best)
+    mode = "resident" if resident_ms is not None and resident_ms <= best_ms else "grid"
+    if batch.resident_ok:
+        batch.set_mode(mode)
     batch.reset()
-    store_cache(cache_path, key, {"grids": list(best), "ms": best_ms,
+    store_cache(cache_path, key, {"grids": list(best), "ms": best_ms, "mode": mode,
+                                  "resident_ms": resident_ms,
                                   "default": list(default), "default_ms": tried[tuple(default)],
                                   "configs_tried": len(tried),
                                   "seconds": time.perf_counter() - t0})

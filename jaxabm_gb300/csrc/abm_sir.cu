@@ -898,6 +898,486 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
   }
 }
 
+// ---- Resident path: one CTA per instance, all of its steps, words in shared memory ------
+//
+// Instances are independent, so a CTA takes one instance at a time (in the caller's
+// order, from a queue counter) and runs all of its steps with the instance's words in
+// shared memory: the sweep reads them there, decisions read the neighbours' compartments
+// there, and count updates are shared-memory atomics.  Only CSR rows, row offsets and hub
+// counts come from global memory.  A step is four phases separated by __syncthreads:
+//   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
+//             the susceptible agents with infected neighbours and the infected agents to
+//             two lists (global scratch of the CTA, L2-resident).
+//   decide    warps take rounds of 32 list entries from a round counter, so that every
+//             warp has work however small the instance: a susceptible agent per lane (rows
+//             longer than 32 slots by the whole warp) or an infected agent's recovery draw
+//             per lane; changes go to the CTA's change list.  Nothing is written to the
+//             words, so every decision sees the pre-step states.
+//   apply     warps take groups of 32 changes: +1 on each changed agent's compartment
+//             field and +-1 on its neighbours' counts (push of the concatenated rows).
+//   finalize  thread 0: S/I/R counts of the step, key chain, next step's key.
+// No CTA waits on another; the results equal the grid path's (integer atomics commute).
+constexpr int kResThreads = 512;
+constexpr int kResChunk = 1024;  // agents per warp chunk, 32 per lane
+
+struct ResState {
+  int inst;        // queue position taken by the CTA
+  int next_chunk;  // chunk counter of the step's sweep
+  int next_round;  // round counter of the step's decisions
+  int next_group;  // group counter of the step's count updates
+  int ns, ni;      // entries in the candidate and infected lists
+  int nchanges;    // entries in the change list
+  int si, ir;      // transitions of the step
+  int num_s, num_i, num_r;
+  uint32_t rng0, rng1, coll0, coll1;
+  unsigned long long scanned, pushed, cands;
+};
+
+// Position of the k-th (0-based) set bit of m; requires k < popc(m).
+__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (k >= c) {
+      k -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// First lane whose inclusive prefix sum `incl` exceeds f (f below the warp total), by a
+// five-step binary search over the lanes; called by all lanes.
+__device__ __forceinline__ int owner_lane(int incl, int f) {
+  int lo = 0;
+#pragma unroll
+  for (int st = 16; st > 0; st >>= 1) {
+    const int p = __shfl_sync(kFull, incl, lo + st - 1);
+    if (p <= f) lo += st;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int warp_inclusive_sum(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += u;
+  }
+  return v;
+}
+
+// +v (already shifted into place) on the aligned 32-bit word of shared memory holding
+// byte i of the words.
+__device__ __forceinline__ void sw_add(uint8_t* sw, int i, uint32_t v) {
+  atomicAdd(reinterpret_cast<uint32_t*>(sw + (i & ~3)), v << (8u * static_cast<uint32_t>(i & 3)));
+}
+
+// Count updates of up to 32 rows of one instance, one per lane (len 0: none; up: +1,
+// else -1), by the whole warp over the concatenated rows, kPushPasses passes in flight.
+__device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj, uint8_t* sw,
+                                                 int32_t* hubs, bool up, int row0, int len,
+                                                 int lane) {
+  const int incl = warp_inclusive_sum(len, lane);
+  const int total = __shfl_sync(kFull, incl, 31);
+  const int shift = row0 - (incl - len);
+  const int sign = up ? 1 : 0;
+  for (int base = 0; base < total; base += 32 * kPushPasses) {
+    uint32_t v[kPushPasses];
+    int d[kPushPasses];
+#pragma unroll
+    for (int u = 0; u < kPushPasses; ++u) {
+      const int f = base + 32 * u + lane;
+      const int lo = owner_lane(incl, f);
+      const int sh = __shfl_sync(kFull, shift, lo);
+      d[u] = __shfl_sync(kFull, sign, lo) ? 1 : -1;
+      v[u] = f < total ? ld_col(adj, f + sh) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kPushPasses; ++u) {
+      if (base + 32 * u + lane < total) {
+        const uint32_t t = v[u] & kIdx;
+        if (v[u] & kTag) red_add(hubs + t, d[u]);
+        else sw_add(sw, static_cast<int>(t), static_cast<uint32_t>(4 * d[u]));
+      }
+    }
+  }
+}
+
+// Appends (agent << 2 | new compartment) of the lanes with `changed` to the change list.
+__device__ __forceinline__ void res_record(bool changed, int agent, uint32_t comp_new,
+                                           uint32_t* changes, int* count, int lane) {
+  const unsigned m = __ballot_sync(kFull, changed);
+  if (!m) return;
+  int base = 0;
+  const int leader = __ffs(m) - 1;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (changed)
+    changes[base + __popc(m & ((1u << lane) - 1u))] = (static_cast<uint32_t>(agent) << 2) | comp_new;
+}
+
+__global__ void __launch_bounds__(kResThreads, 2)
+sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
+                    const int32_t* __restrict__ order, int nsteps, int max_bytes,
+                    int32_t* __restrict__ queue, uint32_t* __restrict__ lists, int cap,
+                    int32_t* __restrict__ status) {
+  extern __shared__ __align__(16) uint8_t sw[];
+  __shared__ ResState S;
+  const int lane = threadIdx.x & 31;
+  // this CTA's lists: changes, susceptible candidates, infected agents (cap entries each)
+  uint32_t* __restrict__ changes = lists + static_cast<size_t>(blockIdx.x) * 3 * cap;
+  uint32_t* __restrict__ slist = changes + cap;
+  uint32_t* __restrict__ ilist = slist + cap;
+  for (;;) {
+    if (threadIdx.x == 0) S.inst = atomicAdd(queue, 1);
+    __syncthreads();
+    const int q = S.inst;
+    __syncthreads();  // every thread holds q before S is rewritten
+    if (q >= ninst) break;
+    abm_sir_instance* I = insts + (order != nullptr ? order[q] : q);
+    const int n = I->n;
+    const int npad = static_cast<int>(round16(n));
+    const int t_begin = I->t;
+    const int t_end = min(I->steps, t_begin + nsteps);
+    if (t_begin >= t_end) continue;  // uniform
+    if (npad > max_bytes || n > cap) {
+      if (threadIdx.x == 0) atomicExch(status, 1);
+      continue;
+    }
+    const int32_t* __restrict__ rp = I->row_ptr;
+    const int32_t* __restrict__ adj = I->adj;
+    int32_t* hubs = I->hub_counts;
+    const float beta = I->beta, gamma = I->gamma;
+    for (int k = threadIdx.x; k < npad / 16; k += kResThreads)
+      reinterpret_cast<uint4*>(sw)[k] = reinterpret_cast<const uint4*>(I->words)[k];
+    if (threadIdx.x == 0) {
+      const uint2 rng = make_uint2(I->rng[0], I->rng[1]);
+      const uint2 c = step_key_of(I, t_begin, rng);
+      S.rng0 = rng.x;
+      S.rng1 = rng.y;
+      S.coll0 = c.x;
+      S.coll1 = c.y;
+      S.num_s = I->num_s;
+      S.num_i = I->num_i;
+      S.num_r = I->num_r;
+      S.si = S.ir = 0;
+      S.ns = S.ni = 0;
+      S.nchanges = 0;
+      S.next_chunk = S.next_round = S.next_group = 0;
+      S.scanned = S.pushed = S.cands = 0;
+    }
+    __syncthreads();
+    const int nchunks = (n + kResChunk - 1) / kResChunk;
+    int t = t_begin;
+    for (; t < t_end; ++t) {
+      if (S.num_i == 0) break;  // uniform: nothing can change any more
+      // ---- sweep: lists of susceptible agents with infected neighbours, infected agents
+      unsigned long long my_cands = 0;
+      for (;;) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(&S.next_chunk, 1);
+        c = __shfl_sync(kFull, c, 0);
+        if (c >= nchunks) break;
+        const int base = c * kResChunk + 32 * lane;
+        uint32_t qw[8];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          if (base + 16 * v + 16 <= npad) {
+            const uint4 x = *reinterpret_cast<const uint4*>(sw + base + 16 * v);
+            qw[4 * v] = x.x;
+            qw[4 * v + 1] = x.y;
+            qw[4 * v + 2] = x.z;
+            qw[4 * v + 3] = x.w;
+          } else {
+#pragma unroll
+            for (int z = 0; z < 4; ++z) qw[4 * v + z] = 0x02020202u;  // beyond the agents: R
+          }
+        }
+        unsigned need_s = 0, need_i = 0, hub_s = 0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const uint32_t b = (qw[j >> 2] >> (8 * (j & 3))) & 0xFFu;
+          const uint32_t s = b & 3u;
+          need_s |= static_cast<unsigned>(s == kS && b >= 4u) << j;
+          need_i |= static_cast<unsigned>(s == kI) << j;
+          hub_s |= static_cast<unsigned>(b == (kHubMark << 2)) << j;
+        }
+        while (hub_s) {
+          const int j = __ffs(hub_s) - 1;
+          hub_s &= hub_s - 1;
+          if (__ldcg(hubs + base + j) <= 0) need_s &= ~(1u << j);
+        }
+        const int ms = __popc(need_s), mi = __popc(need_i);
+        my_cands += ms + mi;
+        // one list position per agent: warp prefix sums, one counter atomic per warp
+        const int both = ms | (mi << 16);
+        const int incl = warp_inclusive_sum(both, lane);
+        const int total = __shfl_sync(kFull, incl, 31);
+        int bs = 0, bi = 0;
+        if (lane == 31) {
+          if (total & 0xFFFF) bs = atomicAdd(&S.ns, total & 0xFFFF);
+          if (total >> 16) bi = atomicAdd(&S.ni, total >> 16);
+        }
+        bs = __shfl_sync(kFull, bs, 31) + ((incl - both) & 0xFFFF);
+        bi = __shfl_sync(kFull, bi, 31) + ((incl - both) >> 16);
+        for (unsigned m = need_s; m; m &= m - 1) slist[bs++] = base + __ffs(m) - 1;
+        for (unsigned m = need_i; m; m &= m - 1) ilist[bi++] = base + __ffs(m) - 1;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) my_cands += __shfl_down_sync(kFull, my_cands, o);
+      if (lane == 0 && my_cands) atomicAdd(&S.cands, my_cands);
+      __syncthreads();
+      // ---- decide: rounds of 32 list entries, taken from a round counter ----------------
+      uint2 next_rng = make_uint2(0, 0), next_coll = make_uint2(0, 0);
+      if (threadIdx.x == 0) {
+        next_rng = abm::split_at(make_uint2(S.rng0, S.rng1), 0);
+        if (t + 1 < I->steps) next_coll = step_key_of(I, t + 1, next_rng);
+      }
+      const uint2 coll = make_uint2(S.coll0, S.coll1);
+      const int ns = S.ns, ni = S.ni;
+      const int rounds_s = (ns + 31) >> 5, rounds = rounds_s + ((ni + 31) >> 5);
+      unsigned long long my_scanned = 0;
+      int my_si = 0, my_ir = 0;
+      for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(&S.next_round, 1);
+        r = __shfl_sync(kFull, r, 0);
+        if (r >= rounds) break;
+        if (r >= rounds_s) {
+          // infected agents: recovery draws
+          const int f = 32 * (r - rounds_s) + lane;
+          bool rec = false;
+          int i = 0;
+          if (f < ni) {
+            i = static_cast<int>(ilist[f]);
+            const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
+            rec = abm::unit_float(abm::bits_at(krec, 0)) < gamma;
+          }
+          my_ir += rec;
+          res_record(rec, i, 2u, changes, &S.nchanges, lane);
+          continue;
+        }
+        // susceptible agents with infected neighbours, one per lane
+        const int f = 32 * r + lane;
+        const bool valid = f < ns;
+        int i = 0, row0 = 0, deg = 0, cnt = 0, scanned = 0;
+        bool infected = false, heavy = false;
+        unsigned imask = 0;
+        if (valid) {
+          i = static_cast<int>(slist[f]);
+          row0 = __ldcs(rp + i);
+          deg = __ldcs(rp + i + 1) - row0;
+          cnt = static_cast<int>(sw[i] >> 2);
+          if (cnt == static_cast<int>(kHubMark)) cnt = deg;  // hubs: scan the whole row
+          heavy = deg > kHeavyDeg;
+          if (!heavy) {
+            int seen = 0, k1 = 0;
+            for (; k1 < deg && seen < cnt; k1 += kChunk) {
+              int nb[kChunk];
+#pragma unroll
+              for (int z = 0; z < kChunk; ++z)
+                nb[z] = k1 + z < deg ? static_cast<int>(ld_col(adj, row0 + k1 + z) & kIdx) : -1;
+#pragma unroll
+              for (int z = 0; z < kChunk; ++z) {
+                const bool inf = nb[z] >= 0 && (sw[nb[z]] & 3u) == kI;
+                imask |= static_cast<unsigned>(inf) << (k1 + z);
+                seen += inf;
+              }
+            }
+            scanned = min(k1, deg);
+          }
+        }
+        if (__any_sync(kFull, imask != 0)) {
+          const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
+          while (__any_sync(kFull, imask != 0)) {
+            if (imask) {
+              const int slot = __ffs(imask) - 1;
+              imask &= imask - 1;
+              if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
+                infected = true;
+                imask = 0;
+              }
+            }
+          }
+        }
+        unsigned hmask = __ballot_sync(kFull, heavy);
+        while (hmask) {
+          const int src = __ffs(hmask) - 1;
+          hmask &= hmask - 1;
+          const int hi = __shfl_sync(kFull, i, src);
+          const int hrow = __shfl_sync(kFull, row0, src);
+          const int hdeg = __shfl_sync(kFull, deg, src);
+          int remaining = __shfl_sync(kFull, cnt, src);
+          const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
+          bool fired = false;
+          int cpos = 0;
+          if (hdeg > kDrawFirstDeg) {
+            // long rows: draws first, a neighbour read only where a draw fires
+            int loaded = 0;
+            for (; cpos < hdeg && !fired; cpos += 32 * kHeavyUnroll) {
+              unsigned fire = 0;
+#pragma unroll
+              for (int u = 0; u < kHeavyUnroll; ++u) {
+                const int slot = cpos + 32 * u + lane;
+                if (slot < hdeg && abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta)
+                  fire |= 1u << u;
+              }
+              uint32_t wv[kHeavyUnroll];
+#pragma unroll
+              for (int u = 0; u < kHeavyUnroll; ++u)
+                wv[u] = (fire >> u) & 1u ? ld_col(adj, hrow + cpos + 32 * u + lane) : 0u;
+              bool hit = false;
+#pragma unroll
+              for (int u = 0; u < kHeavyUnroll; ++u)
+                if ((fire >> u) & 1u) hit |= (sw[wv[u] & kIdx] & 3u) == kI;
+              loaded += __popc(fire);
+              fired = __any_sync(kFull, hit);
+            }
+            loaded = __reduce_add_sync(kFull, loaded);
+            if (lane == src) {
+              infected = fired;
+              scanned = loaded;
+            }
+            continue;
+          }
+          for (; cpos < hdeg && !fired && remaining > 0; cpos += 32 * kHeavyUnroll) {
+            uint32_t wv[kHeavyUnroll];
+#pragma unroll
+            for (int u = 0; u < kHeavyUnroll; ++u) {
+              const int slot = cpos + 32 * u + lane;
+              wv[u] = slot < hdeg ? ld_col(adj, hrow + slot) : kTag;
+            }
+            bool hit = false;
+            int seen = 0;
+#pragma unroll
+            for (int u = 0; u < kHeavyUnroll; ++u) {
+              const int slot = cpos + 32 * u + lane;
+              if (slot < hdeg && (sw[wv[u] & kIdx] & 3u) == kI) {
+                ++seen;
+                if (!hit) hit = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
+              }
+            }
+            fired = __any_sync(kFull, hit);
+            remaining -= __reduce_add_sync(kFull, seen);
+          }
+          if (lane == src) {
+            infected = fired;
+            scanned = min(cpos, hdeg);
+          }
+        }
+        my_scanned += scanned;
+        my_si += infected;
+        res_record(infected, i, kI, changes, &S.nchanges, lane);
+      }
+      my_si = __reduce_add_sync(kFull, my_si);
+      my_ir = __reduce_add_sync(kFull, my_ir);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) my_scanned += __shfl_down_sync(kFull, my_scanned, o);
+      if (lane == 0) {
+        if (my_si) atomicAdd(&S.si, my_si);
+        if (my_ir) atomicAdd(&S.ir, my_ir);
+        if (my_scanned) atomicAdd(&S.scanned, my_scanned);
+      }
+      __syncthreads();
+      // ---- apply: groups of 32 changes, taken from a group counter ------------------------
+      const int nch = S.nchanges;
+      const int groups = (nch + 31) >> 5;
+      int my_pushed = 0;
+      for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&S.next_group, 1);
+        g = __shfl_sync(kFull, g, 0);
+        if (g >= groups) break;
+        const int k = 32 * g + lane;
+        int r0 = 0, len = 0;
+        bool up = false;
+        if (k < nch) {
+          const uint32_t e = changes[k];
+          const int a = static_cast<int>(e >> 2);
+          sw_add(sw, a, 1u);
+          up = (e & 3u) == kI;
+          r0 = __ldcs(rp + a);
+          len = __ldcs(rp + a + 1) - r0;
+        }
+        my_pushed += len;
+        push_rows_shared(adj, sw, hubs, up, r0, len, lane);
+      }
+      my_pushed = __reduce_add_sync(kFull, my_pushed);
+      if (lane == 0 && my_pushed) atomicAdd(&S.pushed, static_cast<unsigned long long>(my_pushed));
+      __syncthreads();
+      // ---- finalize ---------------------------------------------------------------------
+      if (threadIdx.x == 0) {
+        S.num_s -= S.si;
+        S.num_i += S.si - S.ir;
+        S.num_r += S.ir;
+        I->counts[3 * t] = S.num_s;
+        I->counts[3 * t + 1] = S.num_i;
+        I->counts[3 * t + 2] = S.num_r;
+        S.si = S.ir = 0;
+        S.ns = S.ni = 0;
+        S.nchanges = 0;
+        S.next_chunk = S.next_round = S.next_group = 0;
+        S.rng0 = next_rng.x;
+        S.rng1 = next_rng.y;
+        S.coll0 = next_coll.x;
+        S.coll1 = next_coll.y;
+      }
+      __syncthreads();
+    }
+    // steps without an infected agent: constant counts, the key chain still advances
+    for (int u = t + static_cast<int>(threadIdx.x); u < t_end; u += kResThreads) {
+      I->counts[3 * u] = S.num_s;
+      I->counts[3 * u + 1] = S.num_i;
+      I->counts[3 * u + 2] = S.num_r;
+    }
+    if (threadIdx.x == 0 && t < t_end) {
+      uint2 r = make_uint2(S.rng0, S.rng1);
+      for (int u = t; u < t_end; ++u) r = abm::split_at(r, 0);
+      S.rng0 = r.x;
+      S.rng1 = r.y;
+      if (t_end < I->steps) {
+        const uint2 c = step_key_of(I, t_end, r);
+        S.coll0 = c.x;
+        S.coll1 = c.y;
+      }
+    }
+    // write back: words, the 2-bit compartment copy, the descriptor
+    for (int k = threadIdx.x; k < npad / 16; k += kResThreads) {
+      const uint4 x = reinterpret_cast<const uint4*>(sw)[k];
+      reinterpret_cast<uint4*>(I->words)[k] = x;
+      const uint32_t w4[4] = {x.x, x.y, x.z, x.w};
+      uint32_t packed = 0;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) packed |= ((w4[j >> 2] >> (8 * (j & 3))) & 3u) << (2 * j);
+      I->comp[k] = packed;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      I->t = t_end;
+      I->rng[0] = S.rng0;
+      I->rng[1] = S.rng1;
+      I->coll[0] = S.coll0;
+      I->coll[1] = S.coll1;
+      I->num_s = S.num_s;
+      I->num_i = S.num_i;
+      I->num_r = S.num_r;
+      I->step_si = 0;
+      I->step_ir = 0;
+      I->edges_scanned += S.scanned;
+      I->edges_pushed += S.pushed;
+      I->candidates += S.cands;
+      if (t_end == I->steps && I->done_flag) {
+        __threadfence_system();
+        *reinterpret_cast<volatile int32_t*>(I->done_flag) = 1;
+      }
+    }
+    __syncthreads();  // the words in shared memory are rewritten by the next instance
+  }
+}
+
 int default_grid(int nwork) {
   const int cap = abm_host::sm_count() * 8;  // 8 resident 256-thread CTAs per SM
   return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
@@ -948,6 +1428,75 @@ int abm_sir_default_launch(abm_sir_launch* out) {
   out->push_grid = resident_grid(sir_push_kernel, 4);
   out->reserved = 0;
   return ABM_OK;
+}
+
+int32_t abm_sir_resident_max_agents(void) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int64_t room = static_cast<int64_t>(optin) - static_cast<int64_t>(fa.sharedSizeBytes);
+  return room > 0 ? static_cast<int32_t>(room & ~static_cast<int64_t>(15)) : 0;
+}
+
+int32_t abm_sir_resident_grid(int32_t max_agents) {
+  if (max_agents <= 0 || max_agents > abm_sir_resident_max_agents()) return 0;
+  const int bytes = static_cast<int>(round16(max_agents));
+  // the opt-in only ever grows, so launches (and captured graphs) of larger batches stay
+  // valid after a smaller batch asked for its grid
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (fa.maxDynamicSharedSizeBytes < bytes &&
+      cudaFuncSetAttribute(sir_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sir_resident_kernel, kResThreads,
+                                                    bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm * abm_host::sm_count();
+}
+
+size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid) {
+  if (max_agents <= 0 || grid <= 0) return 0;
+  return 256 + static_cast<size_t>(grid) * static_cast<size_t>(round16(max_agents)) * 12;
+}
+
+int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t* order,
+                           int32_t max_agents, int32_t nsteps, int32_t grid, void* scratch,
+                           size_t scratch_bytes, int32_t* status, void* stream) {
+  if (!insts || ninst <= 0 || max_agents <= 0 || nsteps < 0 || grid <= 0 || !scratch || !status)
+    return ABM_ERR_BADARG;
+  if (!abm_host::aligned(insts, 8) || !abm_host::aligned(scratch, 256) ||
+      (order && !abm_host::aligned(order, 4)) || !abm_host::aligned(status, 4))
+    return ABM_ERR_BADARG;
+  if (scratch_bytes < abm_sir_resident_scratch_bytes(max_agents, grid)) return ABM_ERR_WORKSPACE;
+  if (nsteps == 0) return ABM_OK;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const int bytes = static_cast<int>(round16(max_agents));
+  // the shared-memory opt-in is set by abm_sir_resident_grid (not a stream operation, so
+  // not repeated here, where the call may be captured into a CUDA graph)
+  int st = abm_host::record_cuda_error(cudaMemsetAsync(scratch, 0, sizeof(int32_t), s),
+                                       "abm_sir_steps_resident/queue");
+  if (st) return st;
+  sir_resident_kernel<<<grid, kResThreads, bytes, s>>>(
+      insts, ninst, order, nsteps, bytes, static_cast<int32_t*>(scratch),
+      reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + 256), bytes, status);
+  return abm_host::check_launch("abm_sir_steps_resident");
 }
 
 size_t abm_sir_changes_bytes(int64_t max_agents, int64_t max_tiles) {

@@ -128,9 +128,13 @@ class SIRBatch:
         betas, gammas: per-instance parameters
         seeds: per-instance model seeds (key chain of ``Model.initialize``/``step``)
         steps: number of steps every instance runs
+        resident: run on the resident path (``abm_sir_steps_resident``: one CTA per
+            instance at a time, all of its steps, words in shared memory) -- None picks it
+            when every instance fits, False keeps the per-step grid kernels
+            (``abm_sir_steps``), True requires it.  Both give identical results.
     """
 
-    def __init__(self, graphs, init_states, betas, gammas, seeds, steps):
+    def __init__(self, graphs, init_states, betas, gammas, seeds, steps, resident=None):
         check_layout()
         dev = _dev.device()
         k = len(graphs)
@@ -191,6 +195,30 @@ class SIRBatch:
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_steps = None
+        # resident path: instances largest first, one change list per resident CTA
+        L = _lib.load()
+        self.max_n = int(self.n.max())
+        self.order = torch.from_numpy(np.argsort(-self.n, kind="stable").astype(np.int32)).to(dev)
+        self.res_grid = int(L.abm_sir_resident_grid(self.max_n)) if resident is not False else 0
+        self.resident_ok = self.res_grid > 0
+        if resident and not self.resident_ok:
+            raise ValueError(f"an instance of {self.max_n} agents does not fit the resident path "
+                             f"(at most {L.abm_sir_resident_max_agents()})")
+        if self.resident_ok:
+            self.res_scratch = torch.empty(L.abm_sir_resident_scratch_bytes(self.max_n,
+                                                                            self.res_grid),
+                                           dtype=torch.uint8, device=dev)
+            self.res_status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.mode = "resident" if self.resident_ok else "grid"
+
+    def set_mode(self, mode):
+        """``"resident"`` or ``"grid"`` (drops the captured graph)."""
+        if mode not in ("resident", "grid"):
+            raise ValueError(f"unknown SIR batch mode {mode!r}")
+        if mode == "resident" and not self.resident_ok:
+            raise ValueError("this batch cannot run on the resident path")
+        self.mode = mode
+        self._graph = None
 
     def pack(self, stream=None):
         """Words, hub counts and 2-bit compartments of every instance from the int8
@@ -222,7 +250,14 @@ class SIRBatch:
         self.desc.copy_(self.desc0)
 
     def launch(self, nsteps, stream=None):
-        """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps``)."""
+        """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps_resident``
+        or ``abm_sir_steps``)."""
+        if self.mode == "resident":
+            _lib.call("abm_sir_steps_resident", _dev.ptr(self.desc), self.k, _dev.ptr(self.order),
+                      self.max_n, int(nsteps), self.res_grid, _dev.ptr(self.res_scratch),
+                      self.res_scratch.numel(), _dev.ptr(self.res_status),
+                      _dev.stream_handle(stream))
+            return
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
                   self.work.shape[0], None, int(nsteps), self._launch_ptr(), _dev.ptr(self.changes),
                   self.changes.numel(), _dev.stream_handle(stream))
@@ -265,6 +300,8 @@ class SIRBatch:
     def check(self):
         if changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed (workspace smaller than live agents)")
+        if self.resident_ok and int(self.res_status.item()) != 0:
+            raise RuntimeError("an SIR instance was larger than the resident path's capacity")
 
     def final_state(self, i):
         w_off = self._offsets[2]
@@ -275,6 +312,8 @@ class SIRBatch:
         return self.counts[c[i]:c[i + 1]].reshape(self.steps, 3)
 
     def launches_per_run(self):
+        if self.mode == "resident":
+            return 1  # one launch for every step of every instance
         # prepare, then per step sweep, candidates, push and (more than 256 instances)
         # finalize, and a work-list compaction every 8 steps
         per_step = 3 if self.k <= 256 else 4

@@ -37,7 +37,11 @@ def test_results_identical_under_any_launch(cuda, tmp_path):
     graphs = [sir.barabasi_albert(n, 4, s) for n, s in zip(sizes, seeds)]
     inits = [sir.initial_states(n, 0.002, s) for n, s in zip(sizes, seeds)]
     b = ensemble.SIRBatch(graphs, inits, [0.1, 0.2, 0.05], [0.1, 0.1, 0.2], seeds, 40)
-    results = []
+    assert b.mode == "resident"
+    b.run()
+    torch.cuda.synchronize()
+    results = [(b.counts.cpu().numpy().copy(), [b.final_state(i).cpu().numpy() for i in range(3)])]
+    b.set_mode("grid")
     for cfg in (None, (1, 1, 1), (152, 304, 152 * 8), (7, 3, 5)):
         b.set_launch(cfg)
         b.reset()
@@ -52,7 +56,8 @@ def test_results_identical_under_any_launch(cuda, tmp_path):
     cache = str(tmp_path / "tune.json")
     cfg = autotune.tune_sir_batch(b, cache_path=cache)
     assert len(cfg) == 3 and all(v > 0 for v in cfg)
-    assert autotune.load_cache(cache)
+    entry = list(autotune.load_cache(cache).values())[0]
+    assert entry["mode"] in ("resident", "grid") and b.mode == entry["mode"]
     b.run()
     torch.cuda.synchronize()
     assert np.array_equal(b.counts.cpu().numpy(), results[0][0])

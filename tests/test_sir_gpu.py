@@ -107,8 +107,9 @@ def test_sir_model_api(cuda):
 
 
 @pytest.mark.parametrize("use_graph", [False, True])
-def test_sir_batched_equals_alone(cuda, use_graph):
-    """Each instance of a batch is bit-identical to the instance run alone."""
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_sir_batched_equals_alone(cuda, use_graph, path):
+    """Each instance of a batch is bit-identical to the instance run alone, on both paths."""
     from jaxabm_gb300 import ensemble, sir
     sizes = [300, 1000, 4097, 257, 256, 70_000]
     seeds = [11, 12, 13, 14, 15, 16]
@@ -117,9 +118,12 @@ def test_sir_batched_equals_alone(cuda, use_graph):
     graphs = [sir.barabasi_albert(n, 4, s) for n, s in zip(sizes, seeds)]
     inits = [sir.initial_states(n, 0.002, s) for n, s in zip(sizes, seeds)]
     steps = 45
-    b = ensemble.SIRBatch(graphs, inits, betas, gammas, seeds, steps)
+    b = ensemble.SIRBatch(graphs, inits, betas, gammas, seeds, steps,
+                          resident=(path == "resident"))
+    assert b.mode == path
     b.run(use_graph=use_graph)
     torch.cuda.synchronize()
+    b.check()
     for i in range(len(sizes)):
         rng, _ = models.model_keys(seeds[i], 1)
         ref_st, ref_counts, ref_rng = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng,
@@ -184,3 +188,73 @@ def test_sir_repack_is_idempotent(cuda):
                                                 [0.08, 0.15][i], [0.1, 0.2][i])
         assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts)
         assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st)
+
+
+def test_sir_resident_edge_cases_match_oracle(cuda):
+    """Resident path on instances that stress it: hubs (BA m=8, a star, a 64-clique where
+    every agent is a hub), rows longer than 96 slots (draw-first), tiny instances (5 and 17
+    agents: one partial chunk), an instance without infected agents, and stepping in three
+    calls (10 + 7 + the rest).  Compartments, counts, key chains and the 2-bit compartment
+    copy equal the oracle's."""
+    from jaxabm_gb300 import ensemble, sir
+    graphs = [sir.barabasi_albert(3000, 8, 1), _graph("star", 700), _graph("clique", 64),
+              sir.barabasi_albert(5, 2, 3), sir.barabasi_albert(17, 4, 4),
+              sir.barabasi_albert(2000, 4, 5), sir.barabasi_albert(40_000, 4, 6)]
+    n = [len(rp) - 1 for rp, _ in graphs]
+    fr = [0.01, 0.02, 0.1, 0.4, 0.2, 0.0, 0.001]
+    inits = [sir.initial_states(k, f, 30 + i) if f > 0 else np.zeros(k, np.int8)
+             for i, (k, f) in enumerate(zip(n, fr))]
+    seeds = [40 + i for i in range(len(graphs))]
+    betas = [0.05, 0.3, 0.02, 0.5, 0.2, 0.1, 0.07]
+    gammas = [0.1, 0.2, 0.05, 0.3, 0.1, 0.1, 0.1]
+    steps = 60
+    b = ensemble.SIRBatch(graphs, inits, betas, gammas, seeds, steps, resident=True)
+    b.launch(10)
+    b.launch(7)
+    b.launch(steps)
+    torch.cuda.synchronize()
+    b.check()
+    d = b.desc.cpu().numpy().view(ensemble.INSTANCE_DTYPE).reshape(-1)
+    for i in range(len(graphs)):
+        rng, _ = models.model_keys(seeds[i], 1)
+        ref_st, ref_counts, ref_rng = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng,
+                                                      steps, betas[i], gammas[i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), i
+        assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st), i
+        assert np.array_equal(d["rng"][i], ref_rng), i
+        assert d["t"][i] == steps
+        w = b._offsets[2]
+        comp = b.comp[w[i] // 16:w[i + 1] // 16].cpu().numpy().view(np.uint32)
+        unpacked = (comp[:, None] >> (2 * np.arange(16, dtype=np.uint32))) & 3
+        assert np.array_equal(unpacked.reshape(-1)[:n[i]], ref_st.astype(np.uint32)), i
+
+
+def test_sir_resident_rejects_oversize_instance(cuda):
+    """An instance larger than the resident call's max_agents is left untouched and sets the
+    status word; the host picks the grid path for batches that do not fit."""
+    from jaxabm_gb300 import _dev, _lib, ensemble, sir
+    graphs = [sir.barabasi_albert(3000, 4, 1), sir.barabasi_albert(800, 4, 2)]
+    inits = [sir.initial_states(3000, 0.01, 1), sir.initial_states(800, 0.01, 2)]
+    b = ensemble.SIRBatch(graphs, inits, [0.1, 0.1], [0.1, 0.1], [1, 2], 20, resident=True)
+    L = _lib.load()
+    grid = L.abm_sir_resident_grid(1000)
+    assert grid > 0
+    scratch = torch.empty(L.abm_sir_resident_scratch_bytes(1000, grid), dtype=torch.uint8,
+                          device=cuda)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid,
+              _dev.ptr(scratch), scratch.numel(), _dev.ptr(status), None)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+    d = b.desc.cpu().numpy().view(ensemble.INSTANCE_DTYPE).reshape(-1)
+    assert d["t"][0] == 0 and d["t"][1] == 20
+    with pytest.raises(_lib.AbmError):
+        _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid,
+                  _dev.ptr(scratch), 16, _dev.ptr(status), None)
+    big = L.abm_sir_resident_max_agents() + 16
+    g = [sir.barabasi_albert(big, 2, 3)]
+    b2 = ensemble.SIRBatch(g, [sir.initial_states(big, 0.001, 3)], [0.1], [0.1], [3], 2)
+    assert b2.mode == "grid" and not b2.resident_ok
+    with pytest.raises(ValueError):
+        ensemble.SIRBatch(g, [sir.initial_states(big, 0.001, 3)], [0.1], [0.1], [3], 2,
+                          resident=True)
