@@ -1141,35 +1141,57 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       const int rounds_s = (ns + 31) >> 5, rounds = rounds_s + ((ni + 31) >> 5);
       unsigned long long my_scanned = 0;
       int my_si = 0, my_ir = 0;
-      for (;;) {
+      // Rounds are taken two ahead: the list entries of the round after next and the row
+      // offsets of the next round are in flight while a round is decided.
+      auto take = [&]() {
         int r = 0;
         if (lane == 0) r = atomicAdd(&S.next_round, 1);
-        r = __shfl_sync(kFull, r, 0);
-        if (r >= rounds) break;
+        return __shfl_sync(kFull, r, 0);
+      };
+      auto entry_of = [&](int r) {
+        if (r < rounds_s) {
+          const int f = 32 * r + lane;
+          return f < ns ? static_cast<int>(slist[f]) : -1;
+        }
+        const int f = 32 * (r - rounds_s) + lane;
+        return r < rounds && f < ni ? static_cast<int>(ilist[f]) : -1;
+      };
+      int r_cur = take(), r_nxt = take();
+      int e_cur = entry_of(r_cur), e_nxt = entry_of(r_nxt);
+      int a_cur = 0, b_cur = 0;
+      if (r_cur < rounds_s && e_cur >= 0) {
+        a_cur = __ldcs(rp + e_cur);
+        b_cur = __ldcs(rp + e_cur + 1);
+      }
+      for (; r_cur < rounds; r_cur = r_nxt, r_nxt = take(), e_nxt = entry_of(r_nxt)) {
+        const int r = r_cur, e = e_cur;
+        const int ra = a_cur, rb = b_cur;
+        e_cur = e_nxt;
+        a_cur = b_cur = 0;
+        if (r_nxt < rounds_s && e_nxt >= 0) {
+          a_cur = __ldcs(rp + e_nxt);
+          b_cur = __ldcs(rp + e_nxt + 1);
+        }
         if (r >= rounds_s) {
           // infected agents: recovery draws
-          const int f = 32 * (r - rounds_s) + lane;
           bool rec = false;
-          int i = 0;
-          if (f < ni) {
-            i = static_cast<int>(ilist[f]);
-            const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)i), 1);
+          if (e >= 0) {
+            const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)e), 1);
             rec = abm::unit_float(abm::bits_at(krec, 0)) < gamma;
           }
           my_ir += rec;
-          res_record(rec, i, 2u, changes, &S.nchanges, lane);
+          res_record(rec, e, 2u, changes, &S.nchanges, lane);
           continue;
         }
         // susceptible agents with infected neighbours, one per lane
-        const int f = 32 * r + lane;
-        const bool valid = f < ns;
+        const bool valid = e >= 0;
         int i = 0, row0 = 0, deg = 0, cnt = 0, scanned = 0;
         bool infected = false, heavy = false;
         unsigned imask = 0;
         if (valid) {
-          i = static_cast<int>(slist[f]);
-          row0 = __ldcs(rp + i);
-          deg = __ldcs(rp + i + 1) - row0;
+          i = e;
+          row0 = ra;
+          deg = rb - ra;
           cnt = static_cast<int>(sw[i] >> 2);
           if (cnt == static_cast<int>(kHubMark)) cnt = deg;  // hubs: scan the whole row
           heavy = deg > kHeavyDeg;
