@@ -33,16 +33,18 @@ import torch  # noqa: E402
 L2_BYTES = 129 * 1024 * 1024
 
 
-def _profiled_traffic(instances):
-    """DRAM bytes of one full-ensemble replay from the committed ncu launch-list summary
+def _profiled_traffic(instances, path="grid"):
+    """DRAM bytes of one full-ensemble replay from the committed ncu summary of the path
     (only for the full 4,096-instance workload it was captured on)."""
-    p = os.path.join(ROOT, "profiles", "sir_ensemble_4096_launch_list.md")
+    name = ("sir_resident_kernel_ensemble4096.md" if path == "resident"
+            else "sir_ensemble_4096_launch_list.md")
+    p = os.path.join(ROOT, "profiles", name)
     if instances != 4096 or not os.path.exists(p):
         return None, None
     with open(p) as f:
         for line in f:
             if line.startswith("traffic_bytes_per_replay:"):
-                return int(line.split(":")[1]), "profiles/sir_ensemble_4096_launch_list.md"
+                return int(line.split(":")[1]), "profiles/" + name
     return None, None
 
 
@@ -248,6 +250,8 @@ class SIREnsembleBench:
         self.work_stats = {"live_agent_steps": self.batch.live_agent_steps(),
                            "decision_candidates": cands, "csr_slots_scanned": scanned,
                            "csr_slots_pushed": pushed, "compartment_changes": changes}
+        if self.batch.mode == "resident":
+            return self.batch.algorithmic_bytes_resident()
         return self.batch.algorithmic_bytes()
 
     def plain(self, sample=48):
@@ -611,7 +615,7 @@ def run_ours(args):
     hbm_peak, peak_kind = _peaks()
     alg_bytes = wl.algorithmic_bytes()
     achieved = alg_bytes / (ms_local / 1e3) / 1e9
-    traffic, traffic_src = _profiled_traffic(wl.count)
+    traffic, traffic_src = _profiled_traffic(wl.count, wl.batch.mode)
     # the per-unit figure of a whole-graph pass (every agent reads its row each step:
     # 4 B column + 1 B neighbour state per CSR slot, 6 B per agent), which the frontier
     # formulation does not move; its rate can exceed the HBM peak for that reason
@@ -643,8 +647,12 @@ def run_ours(args):
                      "traffic_source": traffic_src,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback",
-                     "kernel": "SIR step sequence (sweep + candidates + push + finalize per "
-                               "step; 365 steps in one CUDA-graph replay), timed as a unit",
+                     "kernel": ("sir_resident_kernel: one launch runs every step of every "
+                                "instance (one CTA per instance at a time, words in shared "
+                                "memory); bound by issue (threefry draws) and latency, not HBM"
+                                if wl.batch.mode == "resident" else
+                                "SIR step sequence (sweep + candidates + push + finalize per "
+                                "step; 365 steps in one CUDA-graph replay), timed as a unit"),
                      "algorithmic_bytes_per_step": alg_bytes,
                      "work_per_step": wl.work_stats,
                      "dense_equivalent": dense},

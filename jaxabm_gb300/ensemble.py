@@ -337,6 +337,19 @@ class SIRBatch:
         i_before = np.concatenate([i0[:, None], counts[:, :-1, 1]], axis=1)
         return int(((i_before > 0).sum(axis=1) * self.n).sum())
 
+    def algorithmic_bytes_resident(self):
+        """HBM bytes the resident path must move (after the run completed): each instance's
+        words read and written once and its 2-bit copy written (2.25 B per agent); per
+        decision a 4-byte list entry written and read and 8 bytes of row offsets (an
+        infected agent reads none, so this over-counts); per CSR slot read by a decision
+        or pushed its 4-byte column (neighbour states and counts live in shared memory);
+        per change a 4-byte entry written and read and 8 bytes of row offsets; S/I/R counts
+        12 B per instance and step."""
+        scanned, pushed, changes, cands = self.edge_stats()
+        words = int(((self.n + 15) // 16 * 16).sum())
+        return int(2.25 * words + 16 * cands + 4 * scanned + 16 * changes + 4 * pushed
+                   + 12 * self.k * self.steps)
+
     def algorithmic_bytes(self):
         """Bytes the run must move (after it completed), each datum at its own size: per
         live agent-step its 1-byte word; per decision candidate 8 bytes (a susceptible
