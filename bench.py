@@ -228,8 +228,7 @@ class SIREnsembleBench:
                 issue_copy(k + 1)
             b = batches[k % 2]
             comp.wait_event(ready[k % 2])
-            b.pack()
-            b.desc.copy_(b.desc0, non_blocking=True)
+            b.rewind_loaded()
             b.replay()
             self.h_counts.copy_(b.counts, non_blocking=True)
             free[k % 2].record(comp)

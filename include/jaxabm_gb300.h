@@ -299,9 +299,18 @@ ABM_API size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid);
  * int32, NULL for index order; largest first balances best) and run each for
  * min(nsteps, steps - t) steps.  Every instance must have n <= max_agents; one that does
  * not is left untouched and sets *status (device int32, zeroed by the caller) to 1.  grid
- * from abm_sir_resident_grid(max_agents); scratch 256-byte aligned. */
+ * from abm_sir_resident_grid(max_agents); scratch 256-byte aligned.
+ * With states8 and words_base (both NULL or both set: int8 compartments of an instance at
+ * the same byte offset from states8 as its words from words_base, as for
+ * abm_sir_pack_batch), an instance at t == 0 builds its words in the kernel from its
+ * compartments (hub marks by degree, hub tags on its columns in place, infected-neighbour
+ * counts, hub counts zeroed) instead of reading words, so no abm_sir_pack_batch is needed
+ * before the call; without them the words and column tags must come from
+ * abm_sir_pack_batch (or an earlier call).  A compartment outside 0..2 (stored as R) or a
+ * column outside 0..n-1 (replaced by a self-loop) sets *status to 1. */
 ABM_API int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t* order,
                                    int32_t max_agents, int32_t nsteps, int32_t grid,
+                                   const int8_t* states8, const uint8_t* words_base,
                                    void* scratch, size_t scratch_bytes, int32_t* status,
                                    void* stream);
 

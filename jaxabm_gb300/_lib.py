@@ -61,7 +61,8 @@ SIGNATURES = {
     "abm_sir_resident_max_agents": (_i32, []),
     "abm_sir_resident_grid": (_i32, [_i32]),
     "abm_sir_resident_scratch_bytes": (_sz, [_i32, _i32]),
-    "abm_sir_steps_resident": (_int, [_p, _i32, _p, _i32, _i32, _i32, _p, _sz, _p, _p]),
+    "abm_sir_steps_resident": (_int, [_p, _i32, _p, _i32, _i32, _i32, _p, _p, _p, _sz, _p,
+                                       _p]),
     "abm_sir_tile_agents": (_i32, []),
     "abm_sir_hub_degree": (_i32, []),
     "abm_sir_run_workspace_bytes": (_sz, [_i64, _i64]),

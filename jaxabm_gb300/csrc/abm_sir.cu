@@ -977,6 +977,8 @@ __device__ __forceinline__ void sw_add(uint8_t* sw, int i, uint32_t v) {
 
 // Count updates of up to 32 rows of one instance, one per lane (len 0: none; up: +1,
 // else -1), by the whole warp over the concatenated rows, kPushPasses passes in flight.
+// A column with the hub tag sends its update to hub_counts.  Columns are within the
+// instance (checked when its words are built).
 __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj, uint8_t* sw,
                                                  int32_t* hubs, bool up, int row0, int len,
                                                  int lane) {
@@ -1022,6 +1024,7 @@ __device__ __forceinline__ void res_record(bool changed, int agent, uint32_t com
 __global__ void __launch_bounds__(kResThreads, 2)
 sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
                     const int32_t* __restrict__ order, int nsteps, int max_bytes,
+                    const int8_t* __restrict__ states8, const uint8_t* words_base,
                     int32_t* __restrict__ queue, uint32_t* __restrict__ lists, int cap,
                     int32_t* __restrict__ status) {
   extern __shared__ __align__(16) uint8_t sw[];
@@ -1048,11 +1051,65 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       continue;
     }
     const int32_t* __restrict__ rp = I->row_ptr;
-    const int32_t* __restrict__ adj = I->adj;
+    int32_t* __restrict__ adj = I->adj;
     int32_t* hubs = I->hub_counts;
     const float beta = I->beta, gamma = I->gamma;
-    for (int k = threadIdx.x; k < npad / 16; k += kResThreads)
-      reinterpret_cast<uint4*>(sw)[k] = reinterpret_cast<const uint4*>(I->words)[k];
+    if (states8 != nullptr && t_begin == 0) {
+      // words built here from the int8 compartments: compartment, hub mark (degree >=
+      // 63, whose count starts at 0 in hub_counts), the columns' hub tags, then every
+      // infected agent adds one to its neighbours' counts
+      const int8_t* __restrict__ st = states8 + (I->words - words_base);
+      for (int k = threadIdx.x; k < npad; k += kResThreads) {
+        uint32_t w = 2u;  // padding: R
+        if (k < n) {
+          int c = st[k];
+          if (c < 0 || c > 2) {
+            atomicExch(status, 1);
+            c = 2;
+          }
+          w = static_cast<uint32_t>(c);
+          if (__ldg(rp + k + 1) - __ldg(rp + k) >= kHubDeg) {
+            w |= kHubMark << 2;
+            hubs[k] = 0;
+          }
+        }
+        sw[k] = static_cast<uint8_t>(w);
+      }
+      __syncthreads();
+      // hub tags on the columns (bit 31 where the neighbour is a hub), in place; a column
+      // outside 0..n-1 is flagged and replaced by a self-loop, as abm_sir_pack does, so that
+      // no step reads outside the instance
+      const int nslots = __ldg(rp + n);
+      for (int k = threadIdx.x; k < nslots; k += kResThreads) {
+        const uint32_t v = static_cast<uint32_t>(adj[k]);
+        uint32_t t = v & kIdx;
+        if (t >= static_cast<uint32_t>(n)) {
+          atomicExch(status, 1);
+          int lo = 0, hi = n - 1;  // the row holding slot k: last i with rp[i] <= k
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rp + mid) <= k) lo = mid;
+            else hi = mid - 1;
+          }
+          t = static_cast<uint32_t>(lo);
+        }
+        const uint32_t want = (sw[t] >> 2) == kHubMark ? (t | kTag) : t;
+        if (want != v) adj[k] = static_cast<int32_t>(want);
+      }
+      __syncthreads();
+      for (int b = threadIdx.x & ~31; b < n; b += kResThreads) {
+        const int k = b + lane;
+        int r0 = 0, len = 0;
+        if (k < n && (sw[k] & 3u) == kI) {
+          r0 = __ldg(rp + k);
+          len = __ldg(rp + k + 1) - r0;
+        }
+        push_rows_shared(adj, sw, hubs, true, r0, len, lane);
+      }
+    } else {
+      for (int k = threadIdx.x; k < npad / 16; k += kResThreads)
+        reinterpret_cast<uint4*>(sw)[k] = reinterpret_cast<const uint4*>(I->words)[k];
+    }
     if (threadIdx.x == 0) {
       const uint2 rng = make_uint2(I->rng[0], I->rng[1]);
       const uint2 c = step_key_of(I, t_begin, rng);
@@ -1499,10 +1556,12 @@ size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid) {
 }
 
 int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t* order,
-                           int32_t max_agents, int32_t nsteps, int32_t grid, void* scratch,
+                           int32_t max_agents, int32_t nsteps, int32_t grid,
+                           const int8_t* states8, const uint8_t* words_base, void* scratch,
                            size_t scratch_bytes, int32_t* status, void* stream) {
   if (!insts || ninst <= 0 || max_agents <= 0 || nsteps < 0 || grid <= 0 || !scratch || !status)
     return ABM_ERR_BADARG;
+  if ((states8 == nullptr) != (words_base == nullptr)) return ABM_ERR_BADARG;
   if (!abm_host::aligned(insts, 8) || !abm_host::aligned(scratch, 256) ||
       (order && !abm_host::aligned(order, 4)) || !abm_host::aligned(status, 4))
     return ABM_ERR_BADARG;
@@ -1516,7 +1575,7 @@ int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t
                                        "abm_sir_steps_resident/queue");
   if (st) return st;
   sir_resident_kernel<<<grid, kResThreads, bytes, s>>>(
-      insts, ninst, order, nsteps, bytes, static_cast<int32_t*>(scratch),
+      insts, ninst, order, nsteps, bytes, states8, words_base, static_cast<int32_t*>(scratch),
       reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + 256), bytes, status);
   return abm_host::check_launch("abm_sir_steps_resident");
 }

@@ -194,7 +194,9 @@ class SIRBatch:
         self.changes = changes_workspace(int(self.n.sum()), self.work.shape[0])
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
+        self._graph_states = None
         self._graph_steps = None
+        self._from_states = False  # the next resident run builds its words from state8
         # resident path: instances largest first, one change list per resident CTA
         L = _lib.load()
         self.max_n = int(self.n.max())
@@ -217,8 +219,15 @@ class SIRBatch:
             raise ValueError(f"unknown SIR batch mode {mode!r}")
         if mode == "resident" and not self.resident_ok:
             raise ValueError("this batch cannot run on the resident path")
+        if mode == "grid" and self.mode != "grid":
+            # the grid kernels need packed words and hub-tagged columns
+            self.pack()
+            self.words0.copy_(self.words)
+            self.hub_counts0.copy_(self.hub_counts)
+            self.comp0.copy_(self.comp)
         self.mode = mode
         self._graph = None
+        self._graph_states = None
 
     def pack(self, stream=None):
         """Words, hub counts and 2-bit compartments of every instance from the int8
@@ -230,12 +239,21 @@ class SIRBatch:
 
     def load_host(self, h_row_ptr, h_col, h_state8, stream=None):
         """Inputs from (pinned) host buffers laid out like ``row_ptr``/``col``/``state8``:
-        copy them in, rebuild the words, hub counts and column tags, and rewind every
-        instance to step 0."""
+        copy them in and rewind every instance to step 0.  The grid path rebuilds the
+        words, hub counts and column tags here; the resident kernel builds each instance's
+        words itself at step 0."""
         self.row_ptr.copy_(h_row_ptr, non_blocking=True)
         self.col.copy_(h_col, non_blocking=True)
         self.state8.copy_(h_state8, non_blocking=True)
-        self.pack(stream)
+        self.rewind_loaded(stream)
+
+    def rewind_loaded(self, stream=None):
+        """After new inputs were copied into ``row_ptr``/``col``/``state8``: rebuild what the
+        path needs (the grid path packs here; the resident kernel builds the words itself
+        at step 0) and rewind every instance to step 0."""
+        if self.mode != "resident":
+            self.pack(stream)
+        self._from_states = self.mode == "resident"
         self.desc.copy_(self.desc0, non_blocking=True)
 
     @property
@@ -243,18 +261,28 @@ class SIRBatch:
         return int(self.n.sum()) * self.steps
 
     def reset(self):
-        """Back to step 0 (words, counters, key chains) without reallocating."""
+        """Back to step 0 (words, counters, key chains) without reallocating: the packed
+        words of step 0 are copied back (device to device), so the next run starts from
+        them."""
         self.words.copy_(self.words0)
         self.hub_counts.copy_(self.hub_counts0)
         self.comp.copy_(self.comp0)
         self.desc.copy_(self.desc0)
+        self._from_states = False
 
-    def launch(self, nsteps, stream=None):
+    def launch(self, nsteps, stream=None, from_states=None):
         """Enqueue ``nsteps`` steps of every live instance (C ABI ``abm_sir_steps_resident``
-        or ``abm_sir_steps``)."""
+        or ``abm_sir_steps``).  On the resident path, ``from_states`` (default: after
+        :meth:`load_host`) has the kernel build the words of instances at step 0 from
+        ``state8`` instead of reading the packed words."""
         if self.mode == "resident":
+            if from_states is None:
+                from_states = self._from_states
+                self._from_states = False
+            st = _dev.ptr(self.state8) if from_states else None
+            wb = _dev.ptr(self.words) if from_states else None
             _lib.call("abm_sir_steps_resident", _dev.ptr(self.desc), self.k, _dev.ptr(self.order),
-                      self.max_n, int(nsteps), self.res_grid, _dev.ptr(self.res_scratch),
+                      self.max_n, int(nsteps), self.res_grid, st, wb, _dev.ptr(self.res_scratch),
                       self.res_scratch.numel(), _dev.ptr(self.res_status),
                       _dev.stream_handle(stream))
             return
@@ -270,23 +298,34 @@ class SIRBatch:
         """Use grid sizes ``cfg`` = (sweep, candidates, push); drops the captured graph."""
         self.launch_cfg = None if cfg is None else tuple(int(v) for v in cfg)
         self._graph = None
+        self._graph_states = None
 
     def capture(self, nsteps):
-        """Capture ``nsteps`` steps into a CUDA graph (replayed by :meth:`replay`)."""
-        torch.cuda.synchronize()
-        s = torch.cuda.Stream()
-        s.wait_stream(torch.cuda.current_stream())
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(s):
-            with torch.cuda.graph(g, stream=s):
-                self.launch(nsteps, s)
-        torch.cuda.current_stream().wait_stream(s)
-        torch.cuda.synchronize()
-        self._graph, self._graph_steps = g, nsteps
-        return g
+        """Capture ``nsteps`` steps into a CUDA graph (replayed by :meth:`replay`); on the
+        resident path a second graph builds the words from ``state8`` (used after
+        :meth:`load_host`)."""
+        def one(from_states):
+            torch.cuda.synchronize()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    self.launch(nsteps, s, from_states=from_states)
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            return g
+        self._graph = one(False)
+        self._graph_states = one(True) if self.mode == "resident" else None
+        self._graph_steps = nsteps
+        return self._graph
 
     def replay(self):
-        self._graph.replay()
+        if self._from_states and self._graph_states is not None:
+            self._graph_states.replay()
+            self._from_states = False
+        else:
+            self._graph.replay()
 
     def run(self, use_graph=True):
         """All ``steps`` steps of every instance."""

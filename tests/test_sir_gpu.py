@@ -242,15 +242,15 @@ def test_sir_resident_rejects_oversize_instance(cuda):
     scratch = torch.empty(L.abm_sir_resident_scratch_bytes(1000, grid), dtype=torch.uint8,
                           device=cuda)
     status = torch.zeros(1, dtype=torch.int32, device=cuda)
-    _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid,
+    _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid, None, None,
               _dev.ptr(scratch), scratch.numel(), _dev.ptr(status), None)
     torch.cuda.synchronize()
     assert int(status.item()) == 1
     d = b.desc.cpu().numpy().view(ensemble.INSTANCE_DTYPE).reshape(-1)
     assert d["t"][0] == 0 and d["t"][1] == 20
     with pytest.raises(_lib.AbmError):
-        _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid,
-                  _dev.ptr(scratch), 16, _dev.ptr(status), None)
+        _lib.call("abm_sir_steps_resident", _dev.ptr(b.desc), 2, None, 1000, 20, grid, None,
+                  None, _dev.ptr(scratch), 16, _dev.ptr(status), None)
     big = L.abm_sir_resident_max_agents() + 16
     g = [sir.barabasi_albert(big, 2, 3)]
     b2 = ensemble.SIRBatch(g, [sir.initial_states(big, 0.001, 3)], [0.1], [0.1], [3], 2)
@@ -258,3 +258,46 @@ def test_sir_resident_rejects_oversize_instance(cuda):
     with pytest.raises(ValueError):
         ensemble.SIRBatch(g, [sir.initial_states(big, 0.001, 3)], [0.1], [0.1], [3], 2,
                           resident=True)
+
+
+def test_sir_resident_builds_words_from_untagged_inputs(cuda):
+    """The resident kernel builds each instance's words at step 0 from the int8
+    compartments, so inputs copied in from the host (columns without hub tags, no pack)
+    give the oracle's results; an out-of-range column (replaced by a self-loop) or
+    compartment (stored as R) is reported through the status word."""
+    from jaxabm_gb300 import ensemble, sir
+    graphs = [sir.barabasi_albert(3000, 8, 7), _graph("star", 500), sir.barabasi_albert(900, 4, 8)]
+    n = [len(rp) - 1 for rp, _ in graphs]
+    inits = [sir.initial_states(k, 0.02, 50 + i) for i, k in enumerate(n)]
+    seeds, betas, gammas, steps = [61, 62, 63], [0.06, 0.3, 0.1], [0.1, 0.2, 0.15], 40
+    b = ensemble.SIRBatch(graphs, inits, betas, gammas, seeds, steps, resident=True)
+    h_rp = torch.from_numpy(np.concatenate([rp for rp, _ in graphs]).astype(np.int32))
+    h_col = torch.from_numpy(np.concatenate([c for _, c in graphs]).astype(np.int32))
+    h_st = torch.from_numpy(b.h_state0.copy())
+    assert (b.col.cpu() < 0).any()  # the packed columns carry hub tags; the host copy does not
+    b.load_host(h_rp, h_col, h_st)
+    b.run()
+    torch.cuda.synchronize()
+    b.check()
+    for i in range(3):
+        rng, _ = models.model_keys(seeds[i], 1)
+        ref_st, ref_counts, _ = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng, steps,
+                                                betas[i], gammas[i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), i
+        assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st), i
+    bad_col = h_col.clone()
+    bad_col[5] = 10_000_000
+    bad_col[7] = -3
+    b.load_host(h_rp, bad_col, h_st)
+    b.run()
+    torch.cuda.synchronize()
+    with pytest.raises(RuntimeError):
+        b.check()
+    b.res_status.zero_()
+    bad_st = h_st.clone()
+    bad_st[3] = 7
+    b.load_host(h_rp, h_col, bad_st)
+    b.run()
+    torch.cuda.synchronize()
+    with pytest.raises(RuntimeError):
+        b.check()
