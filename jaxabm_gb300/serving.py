@@ -2,8 +2,8 @@
 
 Requests (a network, initial compartments, beta, gamma, seed, steps) arrive over time.
 The server keeps every admitted request resident on the device as one instance of the
-batched SIR step (``abm_sir_steps``) and advances all of them together, ``steps_per_tick``
-steps per tick:
+batched SIR step (``abm_sir_steps_resident``, or ``abm_sir_steps`` on the grid path) and
+advances all of them together, ``steps_per_tick`` steps per tick:
 
 * admission: a request is admitted when a descriptor slot is free, its tiles fit the work
   list, and its buffers fit the free device memory (``torch.cuda.mem_get_info``) minus a
@@ -87,12 +87,34 @@ class SIRServer:
         steps_per_tick: steps every resident request advances per tick
         reserve_bytes: device memory kept free at admission
         grid: (sweep, candidates, push) persistent grid sizes, or None for the defaults
+        path: ``"auto"`` (the resident kernel when it can hold ``max_request_agents``),
+            ``"resident"`` or ``"grid"`` (the per-step kernels over the work list)
+        max_request_agents: largest request the resident path accepts (larger requests are
+            rejected at submission on that path)
     """
 
     def __init__(self, max_slots=512, max_tiles=65536, steps_per_tick=16,
-                 reserve_bytes=1 << 30, grid=None):
+                 reserve_bytes=1 << 30, grid=None, path="auto", max_request_agents=100_000):
         check_layout()
         dev = _dev.device()
+        if path not in ("auto", "resident", "grid"):
+            raise ValueError(f"unknown server path {path!r}")
+        L = _lib.load()
+        self.max_request_agents = int(max_request_agents)
+        self.res_grid = (int(L.abm_sir_resident_grid(self.max_request_agents))
+                         if path != "grid" else 0)
+        if path == "resident" and self.res_grid <= 0:
+            raise ValueError(f"the resident path cannot hold requests of "
+                             f"{self.max_request_agents} agents")
+        self.resident = self.res_grid > 0
+        if self.resident:
+            self.res_scratch = torch.empty(
+                L.abm_sir_resident_scratch_bytes(self.max_request_agents, self.res_grid),
+                dtype=torch.uint8, device=dev)
+            self.res_status = torch.zeros(1, dtype=torch.int32, device=dev)
+            # instances in the order the resident CTAs take them: live requests largest first
+            self.order = torch.arange(int(max_slots) + 1, dtype=torch.int32, device=dev)
+            self.h_order = torch.arange(int(max_slots) + 1, dtype=torch.int32).pin_memory()
         self.max_slots = int(max_slots)
         self.max_tiles = int(max_tiles)
         self.steps_per_tick = int(steps_per_tick)
@@ -128,6 +150,13 @@ class SIRServer:
 
     # -- graph ------------------------------------------------------------------------
     def _launch(self):
+        if self.resident:
+            _lib.call("abm_sir_steps_resident", _dev.ptr(self.desc), self.max_slots + 1,
+                      _dev.ptr(self.order), self.max_request_agents, self.steps_per_tick,
+                      self.res_grid, None, None, _dev.ptr(self.res_scratch),
+                      self.res_scratch.numel(), _dev.ptr(self.res_status),
+                      self.stream.cuda_stream)
+            return
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.max_slots + 1, _dev.ptr(self.work),
                   self.max_tiles, _dev.ptr(self.live), self.steps_per_tick, self._launch_ptr(),
                   _dev.ptr(self.changes),
@@ -148,6 +177,9 @@ class SIRServer:
 
     # -- request lifecycle --------------------------------------------------------------
     def submit(self, req: Request) -> None:
+        if self.resident and req.n > self.max_request_agents:
+            raise ValueError(f"request {req.rid} has {req.n} agents; this server's resident "
+                             f"path holds at most {self.max_request_agents}")
         if req.arrival is None:
             req.arrival = time.perf_counter()
         self.queue.append(req)
@@ -165,6 +197,8 @@ class SIRServer:
     def check(self):
         if changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed")
+        if self.resident and int(self.res_status.item()) != 0:
+            raise RuntimeError("a request was larger than the resident path's capacity")
 
     def _admit(self):
         """Admit the longest prefix of the queue that fits (free slots, work-list tiles,
@@ -270,10 +304,16 @@ class SIRServer:
             w[k:k + m, 1] = b
             w[k:k + m, 2] = torch.clamp(b + TILE, max=req.n)
             k += m
+        if self.resident:
+            live = sorted(self.active, key=lambda sl: -self.active[sl].n)
+            rest = [sl for sl in range(self.max_slots + 1) if sl not in self.active]
+            self.h_order.copy_(torch.as_tensor(live + rest, dtype=torch.int32))
         with torch.cuda.stream(self.stream):
             self.work[:max(k, 1)].copy_(w[:max(k, 1)], non_blocking=True)
             self.h_live[0] = k
             self.live.copy_(self.h_live, non_blocking=True)
+            if self.resident:
+                self.order.copy_(self.h_order, non_blocking=True)
             self._work_event = torch.cuda.Event()
             self._work_event.record(self.stream)
         self._work_dirty = False
@@ -325,8 +365,12 @@ class SIRServer:
             while len(self._in_flight) > self.max_ticks_in_flight:
                 self._in_flight.popleft().synchronize()
             self.ticks += 1
-            per_step = 3 if self.max_slots + 1 <= 256 else 4
-            self.launches += per_step * self.steps_per_tick + 1 + (self.steps_per_tick + 7) // 8
+            if self.resident:
+                self.launches += 1
+            else:
+                per_step = 3 if self.max_slots + 1 <= 256 else 4
+                self.launches += (per_step * self.steps_per_tick + 1
+                                  + (self.steps_per_tick + 7) // 8)
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)

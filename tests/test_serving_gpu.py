@@ -25,11 +25,13 @@ def _requests(k, seed0=100, steps=60):
     return reqs
 
 
-def test_results_identical_alone_and_in_mix(cuda):
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_results_identical_alone_and_in_mix(cuda, path):
     from jaxabm_gb300.serving import SIRServer
     reqs = _requests(24)
     # mix: all submitted at once into a small server (forces queueing + slot reuse)
-    srv = SIRServer(max_slots=6, max_tiles=256, steps_per_tick=7)
+    srv = SIRServer(max_slots=6, max_tiles=256, steps_per_tick=7, path=path)
+    assert srv.resident == (path == "resident")
     for r in reqs:
         srv.submit(r)
     srv.drain()
@@ -38,7 +40,8 @@ def test_results_identical_alone_and_in_mix(cuda):
     mixed = {r.rid: (r.counts.numpy().copy(), r.final_state.numpy().copy()) for r in srv.completed}
     # alone: each request by itself through a fresh server
     for r in _requests(24)[::5]:
-        solo = SIRServer(max_slots=1, max_tiles=128, steps_per_tick=13)
+        solo = SIRServer(max_slots=1, max_tiles=128, steps_per_tick=13,
+                         path="grid" if path == "resident" else "resident")
         solo.submit(r)
         solo.drain()
         c, fs = mixed[r.rid]
@@ -86,3 +89,13 @@ def test_admission_by_free_memory(cuda, monkeypatch):
     assert len(srv.active) == 1 and len(srv.queue) == 2
     srv.drain()
     assert len(srv.completed) == 3
+
+
+def test_resident_server_rejects_oversize_request(cuda):
+    from jaxabm_gb300 import sir
+    from jaxabm_gb300.serving import Request, SIRServer
+    srv = SIRServer(max_slots=2, max_tiles=64, steps_per_tick=3, path="resident",
+                    max_request_agents=1000)
+    rp, col = sir.barabasi_albert(1500, 4, 1)
+    with pytest.raises(ValueError):
+        srv.submit(Request(0, rp, col, sir.initial_states(1500, 0.01, 1), 0.1, 0.1, 1, 5))
