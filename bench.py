@@ -297,7 +297,11 @@ class SIREnsembleBench:
                                 torch.from_numpy(self.inits[i]).pin_memory(),
                                 self.spec["beta"][i], self.spec["gamma"][i],
                                 int(self.spec["seed"][i]), self.T))
-        srv = SIRServer(max_slots=4096, max_tiles=1 << 17, steps_per_tick=32)
+        # a real-time stream is served on the per-step grid kernels (every step of a request
+        # spread over the whole GPU: shortest ticks); a burst on the resident kernel (one CTA
+        # per request: highest throughput)
+        path = "resident" if burst else "grid"
+        srv = SIRServer(max_slots=4096, max_tiles=1 << 17, steps_per_tick=32, path=path)
         arrivals = np.zeros(self.count) if burst else self.spec["arrival_s"]
         torch.cuda.synchronize()
         wall = srv.serve(reqs, arrivals)
@@ -315,7 +319,7 @@ class SIREnsembleBench:
                 "requests": len(lat),
                 "arrivals": "all at t=0" if burst else "Poisson, 200 requests/s, real time",
                 "wall_s": wall, "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
-                "results_match_batched": bool(same)}
+                "path": path, "results_match_batched": bool(same)}
 
     def cpu_baseline(self, threads, budget_s=12.0):
         from oracle import coracle, models

@@ -87,14 +87,17 @@ class SIRServer:
         steps_per_tick: steps every resident request advances per tick
         reserve_bytes: device memory kept free at admission
         grid: (sweep, candidates, push) persistent grid sizes, or None for the defaults
-        path: ``"auto"`` (the resident kernel when it can hold ``max_request_agents``),
-            ``"resident"`` or ``"grid"`` (the per-step kernels over the work list)
+        path: ``"grid"`` (the per-step kernels over the work list: every step of a request
+            is spread over the whole GPU, so ticks are short and latency low), ``"resident"``
+            (one CTA per request for all steps of a tick: highest throughput when many
+            requests are resident, longer ticks for large requests) or ``"auto"`` (resident
+            when it can hold ``max_request_agents``)
         max_request_agents: largest request the resident path accepts (larger requests are
             rejected at submission on that path)
     """
 
     def __init__(self, max_slots=512, max_tiles=65536, steps_per_tick=16,
-                 reserve_bytes=1 << 30, grid=None, path="auto", max_request_agents=100_000):
+                 reserve_bytes=1 << 30, grid=None, path="grid", max_request_agents=100_000):
         check_layout()
         dev = _dev.device()
         if path not in ("auto", "resident", "grid"):
