@@ -1205,18 +1205,24 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         if (lane == 0) r = atomicAdd(&S.next_round, 1);
         return __shfl_sync(kFull, r, 0);
       };
+      // susceptible and infected rounds alternate (row-reading rounds wait on memory,
+      // recovery rounds on the ALU), then the rest of the longer list follows
+      const int rounds_i = rounds - rounds_s;
+      const int both = 2 * min(rounds_s, rounds_i);
+      auto is_s = [&](int r) {
+        return r < both ? (r & 1) == 0 : rounds_s > rounds_i;
+      };
+      auto index_of = [&](int r) { return r < both ? r >> 1 : (both >> 1) + (r - both); };
       auto entry_of = [&](int r) {
-        if (r < rounds_s) {
-          const int f = 32 * r + lane;
-          return f < ns ? static_cast<int>(slist[f]) : -1;
-        }
-        const int f = 32 * (r - rounds_s) + lane;
-        return r < rounds && f < ni ? static_cast<int>(ilist[f]) : -1;
+        if (r >= rounds) return -1;
+        const int f = 32 * index_of(r) + lane;
+        if (is_s(r)) return f < ns ? static_cast<int>(slist[f]) : -1;
+        return f < ni ? static_cast<int>(ilist[f]) : -1;
       };
       int r_cur = take(), r_nxt = take();
       int e_cur = entry_of(r_cur), e_nxt = entry_of(r_nxt);
       int a_cur = 0, b_cur = 0;
-      if (r_cur < rounds_s && e_cur >= 0) {
+      if (r_cur < rounds && is_s(r_cur) && e_cur >= 0) {
         a_cur = __ldcs(rp + e_cur);
         b_cur = __ldcs(rp + e_cur + 1);
       }
@@ -1225,11 +1231,11 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         const int ra = a_cur, rb = b_cur;
         e_cur = e_nxt;
         a_cur = b_cur = 0;
-        if (r_nxt < rounds_s && e_nxt >= 0) {
+        if (r_nxt < rounds && is_s(r_nxt) && e_nxt >= 0) {
           a_cur = __ldcs(rp + e_nxt);
           b_cur = __ldcs(rp + e_nxt + 1);
         }
-        if (r >= rounds_s) {
+        if (!is_s(r)) {
           // infected agents: recovery draws
           bool rec = false;
           if (e >= 0) {
