@@ -34,6 +34,39 @@ from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, chang
                        word_bytes)
 
 
+def work_table(slots, sizes, dummy, capacity, tile=TILE):
+    """Work items (slot, begin, end, 0) of the requests at ``slots`` with ``sizes`` agents,
+    ``tile`` agents each, in the given order, padded to ``capacity`` rows with the inactive
+    row ``dummy``: returns (int32[capacity, 4], number of items)."""
+    slots = np.asarray(slots, dtype=np.int64)
+    sizes = np.asarray(sizes, dtype=np.int64)
+    tiles = (sizes + tile - 1) // tile
+    k = int(tiles.sum())
+    if k > capacity:
+        raise ValueError(f"{k} work items exceed the capacity {capacity}")
+    out = np.zeros((capacity, 4), dtype=np.int32)
+    out[:, 0] = dummy
+    if k:
+        owner = np.repeat(np.arange(slots.size), tiles)
+        first = np.repeat(np.cumsum(tiles) - tiles, tiles)
+        begin = (np.arange(k) - first) * tile
+        out[:k, 0] = slots[owner]
+        out[:k, 1] = begin
+        out[:k, 2] = np.minimum(begin + tile, sizes[owner])
+    return out, k
+
+
+def order_table(slots, sizes, total):
+    """Every descriptor row 0..total-1 once: the given slots first, largest request first
+    (ties in the given order), then the other rows in index order."""
+    slots = np.asarray(slots, dtype=np.int64)
+    sizes = np.asarray(sizes, dtype=np.int64)
+    live = slots[np.argsort(-sizes, kind="stable")]
+    rest = np.ones(int(total), dtype=bool)
+    rest[slots] = False
+    return np.concatenate([live, np.nonzero(rest)[0]]).astype(np.int32)
+
+
 class _Group:
     """Device buffers shared by the requests admitted together; every request of the group
     holds it, so the buffers are freed once the last of them has retired."""
@@ -264,8 +297,7 @@ class SIRServer:
         rows["gamma"] = [r.gamma for r in picked]
         rows["num_s"], rows["num_i"], rows["num_r"] = sizes[:, 0], sizes[:, 1], sizes[:, 2]
         work = np.concatenate([tiles_for(slot, int(nk)) for slot, nk in zip(slots, n)])
-        for slot in slots:
-            self.done[slot] = 0
+        self.done.numpy()[np.asarray(slots, dtype=np.int64)] = 0
         h_rows = torch.from_numpy(rows.view(np.int32).reshape(g, -1).copy()).pin_memory()
         h_work = torch.from_numpy(work).pin_memory()
         status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -296,23 +328,15 @@ class SIRServer:
         # the pinned staging buffers may still feed the previous rebuild's copies
         if self._work_event is not None:
             self._work_event.synchronize()
-        w = self.h_work
-        w[:, 0] = self.dummy
-        w[:, 1:] = 0
-        k = 0
-        for slot, req in self.active.items():
-            b = torch.arange(0, req.n, TILE, dtype=torch.int32)
-            m = b.numel()
-            w[k:k + m, 0] = slot
-            w[k:k + m, 1] = b
-            w[k:k + m, 2] = torch.clamp(b + TILE, max=req.n)
-            k += m
+        slots = np.fromiter(self.active.keys(), dtype=np.int64, count=len(self.active))
+        sizes = np.fromiter((r.n for r in self.active.values()), dtype=np.int64,
+                            count=len(self.active))
+        table, k = work_table(slots, sizes, self.dummy, self.max_tiles)
+        self.h_work.numpy()[:] = table
         if self.resident:
-            live = sorted(self.active, key=lambda sl: -self.active[sl].n)
-            rest = [sl for sl in range(self.max_slots + 1) if sl not in self.active]
-            self.h_order.copy_(torch.as_tensor(live + rest, dtype=torch.int32))
+            self.h_order.numpy()[:] = order_table(slots, sizes, self.max_slots + 1)
         with torch.cuda.stream(self.stream):
-            self.work[:max(k, 1)].copy_(w[:max(k, 1)], non_blocking=True)
+            self.work[:max(k, 1)].copy_(self.h_work[:max(k, 1)], non_blocking=True)
             self.h_live[0] = k
             self.live.copy_(self.h_live, non_blocking=True)
             if self.resident:
@@ -323,7 +347,8 @@ class SIRServer:
 
     def _harvest(self):
         """Retire requests whose done flag is up: enqueue their result copies."""
-        finished = [slot for slot in self.active if int(self.done[slot]) == 1]
+        slots = np.fromiter(self.active.keys(), dtype=np.int64, count=len(self.active))
+        finished = slots[self.done.numpy()[slots] == 1].tolist()
         for slot in finished:
             req = self.active.pop(slot)
             group, st, counts = req._bufs

@@ -252,3 +252,24 @@ def test_status_errors_raise():
     with pytest.raises(_lib.AbmError) as e:
         _lib.check(_lib.ABM_ERR_WORKSPACE, "abm_x")
     assert "workspace too small" in str(e.value) and e.value.status == _lib.ABM_ERR_WORKSPACE
+
+
+def test_server_work_and_order_tables():
+    """Host tables of the SIR server: tiles of each resident request in slot order, padded
+    with the inactive row; the resident kernel's order lists live requests largest first
+    (ties in admission order), then every other row once."""
+    import numpy as np
+    from jaxabm_gb300.serving import order_table, work_table
+    table, k = work_table([3, 0, 5], [8192 * 2 + 1, 10, 8192], dummy=9, capacity=8, tile=8192)
+    assert k == 5
+    assert table[:5].tolist() == [[3, 0, 8192, 0], [3, 8192, 16384, 0], [3, 16384, 16385, 0],
+                                  [0, 0, 10, 0], [5, 0, 8192, 0]]
+    assert (table[5:, 0] == 9).all() and (table[5:, 1:] == 0).all()
+    empty, k0 = work_table([], [], dummy=2, capacity=3)
+    assert k0 == 0 and (empty[:, 0] == 2).all()
+    order = order_table([4, 1, 6], [100, 300, 100], total=8)
+    assert order.tolist() == [1, 4, 6, 0, 2, 3, 5, 7]
+    assert sorted(order.tolist()) == list(range(8))
+    import pytest
+    with pytest.raises(ValueError):
+        work_table([0], [8192 * 5], dummy=1, capacity=4)
