@@ -916,6 +916,12 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 //   apply     warps take groups of 32 changes: +1 on each changed agent's compartment
 //             field and +-1 on its neighbours' counts (push of the concatenated rows).
 //   finalize  thread 0: S/I/R counts of the step, key chain, next step's key.
+// Decision rounds alternate between the two lists and are taken two ahead, so that the
+// list entries and row offsets of the next rounds are in flight while one is decided.
+// An instance at step 0 may build its words in the kernel from the int8 compartments
+// (hub marks, column hub tags, initial counts) instead of reading packed words.  The
+// words are written back, with the 2-bit compartment copy, when the instance's steps of
+// the call are done.
 // No CTA waits on another; the results equal the grid path's (integer atomics commute).
 constexpr int kResThreads = 512;
 constexpr int kResChunk = 1024;  // agents per warp chunk, 32 per lane
