@@ -191,7 +191,7 @@ class SIRBatch:
         self.words0 = self.words.clone()
         self.hub_counts0 = self.hub_counts.clone()
         self.comp0 = self.comp.clone()
-        self.changes = changes_workspace(int(self.n.sum()), self.work.shape[0])
+        self.changes = None  # list workspace of the grid path, allocated on first use
         self.launch_cfg = None  # (sweep, candidates, push) grid sizes; None = defaults
         self._graph = None
         self._graph_states = None
@@ -212,6 +212,16 @@ class SIRBatch:
                                            dtype=torch.uint8, device=dev)
             self.res_status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.mode = "resident" if self.resident_ok else "grid"
+        if self.mode == "grid":
+            self._ensure_changes()
+
+    def _ensure_changes(self):
+        """The grid path's list workspace (16 bytes per agent: change and candidate lists),
+        allocated when the batch first takes that path (before any graph capture)."""
+        if self.changes is None:
+            if torch.cuda.is_current_stream_capturing():
+                raise RuntimeError("select the grid path before capturing a graph")
+            self.changes = changes_workspace(int(self.n.sum()), self.work.shape[0])
 
     def set_mode(self, mode):
         """``"resident"`` or ``"grid"`` (drops the captured graph)."""
@@ -220,7 +230,8 @@ class SIRBatch:
         if mode == "resident" and not self.resident_ok:
             raise ValueError("this batch cannot run on the resident path")
         if mode == "grid" and self.mode != "grid":
-            # the grid kernels need packed words and hub-tagged columns
+            # the grid kernels need their list workspace, packed words and hub-tagged columns
+            self._ensure_changes()
             self.pack()
             self.words0.copy_(self.words)
             self.hub_counts0.copy_(self.hub_counts)
@@ -286,6 +297,7 @@ class SIRBatch:
                       self.res_scratch.numel(), _dev.ptr(self.res_status),
                       _dev.stream_handle(stream))
             return
+        self._ensure_changes()
         _lib.call("abm_sir_steps", _dev.ptr(self.desc), self.k, _dev.ptr(self.work),
                   self.work.shape[0], None, int(nsteps), self._launch_ptr(), _dev.ptr(self.changes),
                   self.changes.numel(), _dev.stream_handle(stream))
@@ -337,7 +349,7 @@ class SIRBatch:
             self.launch(self.steps)
 
     def check(self):
-        if changes_overflowed(self.changes):
+        if self.changes is not None and changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed (workspace smaller than live agents)")
         if self.resident_ok and int(self.res_status.item()) != 0:
             raise RuntimeError("an SIR instance was larger than the resident path's capacity")
