@@ -197,6 +197,7 @@ class SIRBatch:
         self._graph_states = None
         self._graph_steps = None
         self._from_states = False  # the next resident run builds its words from state8
+        self._words0_stale = False  # inputs were loaded after the step-0 words were saved
         # resident path: instances largest first, one change list per resident CTA
         L = _lib.load()
         self.max_n = int(self.n.max())
@@ -236,6 +237,7 @@ class SIRBatch:
             self.words0.copy_(self.words)
             self.hub_counts0.copy_(self.hub_counts)
             self.comp0.copy_(self.comp)
+            self._words0_stale = False
         self.mode = mode
         self._graph = None
         self._graph_states = None
@@ -265,6 +267,7 @@ class SIRBatch:
         if self.mode != "resident":
             self.pack(stream)
         self._from_states = self.mode == "resident"
+        self._words0_stale = True  # the saved step-0 words belong to the earlier inputs
         self.desc.copy_(self.desc0, non_blocking=True)
 
     @property
@@ -274,7 +277,21 @@ class SIRBatch:
     def reset(self):
         """Back to step 0 (words, counters, key chains) without reallocating: the packed
         words of step 0 are copied back (device to device), so the next run starts from
-        them."""
+        them.  After :meth:`load_host` brought other inputs, the words of step 0 are
+        rebuilt from them instead (the grid path packs again; the resident kernel builds
+        them at step 0)."""
+        if self._words0_stale:
+            self.desc.copy_(self.desc0)
+            if self.mode == "resident":
+                self._from_states = True
+                return
+            self.pack()
+            self.words0.copy_(self.words)
+            self.hub_counts0.copy_(self.hub_counts)
+            self.comp0.copy_(self.comp)
+            self._words0_stale = False
+            self._from_states = False
+            return
         self.words.copy_(self.words0)
         self.hub_counts.copy_(self.hub_counts0)
         self.comp.copy_(self.comp0)
