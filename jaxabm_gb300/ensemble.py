@@ -252,7 +252,9 @@ class SIRBatch:
 
     def load_host(self, h_row_ptr, h_col, h_state8, stream=None):
         """Inputs from (pinned) host buffers laid out like ``row_ptr``/``col``/``state8``:
-        copy them in and rewind every instance to step 0.  The grid path rebuilds the
+        copy them in and rewind every instance to step 0.  The instances keep their sizes
+        and the S/I/R totals given at construction, so the loaded compartments must have the
+        same totals per instance (other agents may be infected).  The grid path rebuilds the
         words, hub counts and column tags here; the resident kernel builds each instance's
         words itself at step 0."""
         self.row_ptr.copy_(h_row_ptr, non_blocking=True)

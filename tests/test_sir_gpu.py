@@ -301,3 +301,37 @@ def test_sir_resident_builds_words_from_untagged_inputs(cuda):
     torch.cuda.synchronize()
     with pytest.raises(RuntimeError):
         b.check()
+
+
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_sir_reset_after_load_host_keeps_loaded_inputs(cuda, path):
+    """Inputs loaded from the host (other infected agents, the same S/I/R totals) are what
+    a reset() rewinds to, on both paths: the run after the reset equals the oracle on the
+    loaded compartments."""
+    from jaxabm_gb300 import ensemble, sir
+    sizes, seeds = [2500, 900], [71, 72]
+    graphs = [sir.barabasi_albert(k, 4, s) for k, s in zip(sizes, seeds)]
+    first = [sir.initial_states(k, 0.01, s) for k, s in zip(sizes, seeds)]
+    other = [sir.initial_states(k, 0.01, s + 100) for k, s in zip(sizes, seeds)]
+    assert all((a == 1).sum() == (b == 1).sum() for a, b in zip(first, other))
+    betas, gammas, steps = [0.1, 0.15], [0.1, 0.2], 30
+    b = ensemble.SIRBatch(graphs, first, betas, gammas, seeds, steps,
+                          resident=(path == "resident"))
+    w_off = b._offsets[2]
+    h_st = np.zeros(int(w_off[-1]), dtype=np.int8)
+    for i, st in enumerate(other):
+        h_st[w_off[i]:w_off[i] + len(st)] = st
+    h_rp = torch.from_numpy(np.concatenate([rp for rp, _ in graphs]).astype(np.int32))
+    h_col = torch.from_numpy(np.concatenate([c for _, c in graphs]).astype(np.int32))
+    b.load_host(h_rp, h_col, torch.from_numpy(h_st))
+    b.run()
+    b.reset()
+    b.run()
+    torch.cuda.synchronize()
+    b.check()
+    for i in range(2):
+        rng, _ = models.model_keys(seeds[i], 1)
+        ref_st, ref_counts, _ = coracle.sir_run(graphs[i][0], graphs[i][1], other[i], rng, steps,
+                                                betas[i], gammas[i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), (path, i)
+        assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st), (path, i)
