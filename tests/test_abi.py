@@ -43,3 +43,16 @@ def test_bad_arguments_rejected_without_gpu(lib):
     assert lib.abm_randomwalk_run(None, None, 10, None, 5, 0.01, None, None, 0, None) == \
         _lib.ABM_ERR_BADARG
     assert lib.abm_randomwalk_workspace_bytes(10_000, 100) > 0
+
+
+def test_sir_resident_entry_points_without_gpu(lib):
+    """Host-side sizing and argument checks of the resident SIR path need no device: the
+    scratch is a 256-byte queue header plus three 4-byte lists of max_agents (rounded to 16)
+    entries per CTA; without a device no instance fits (0); bad arguments are rejected
+    before any CUDA call."""
+    assert lib.abm_sir_resident_scratch_bytes(1000, 2) == 256 + 2 * 1008 * 12
+    assert lib.abm_sir_resident_scratch_bytes(0, 2) == 0
+    assert lib.abm_sir_resident_scratch_bytes(1000, 0) == 0
+    assert lib.abm_sir_resident_max_agents() >= 0
+    assert lib.abm_sir_steps_resident(None, 1, None, 1000, 5, 2, None, None, None, 0, None,
+                                      None) == _lib.ABM_ERR_BADARG
