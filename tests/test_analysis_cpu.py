@@ -114,3 +114,79 @@ def test_calibrator_methods_rejected_before_any_launch():
         ModelCalibrator(None, {"beta": 0.1}, {"R": 1.0}, method="nope")
     with pytest.raises(NotImplementedError):
         ModelCalibrator(None, {"beta": 0.1}, {"R": 1.0}, method="adam")
+
+
+class _OracleRandom:
+    """The device ``jax.random`` of the package, restated on the oracle for host-only
+    tests of the analysis loops (int32 key tensors, as on the device)."""
+
+    @staticmethod
+    def _np(key):
+        return key.numpy().astype(np.int32).view(np.uint32).reshape(-1)
+
+    @staticmethod
+    def _t(a, dtype=torch.int32):
+        a = np.asarray(a)
+        if a.dtype == np.uint32:
+            a = a.view(np.int32)
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dtype)
+
+    def PRNGKey(self, seed):
+        return self._t(tf.PRNGKey(seed))
+
+    def split(self, key, num=2):
+        return self._t(tf.split(self._np(key), num))
+
+    def uniform(self, key, shape=()):
+        return self._t(tf.uniform(self._np(key), shape).astype(np.float32), torch.float32)
+
+    def normal(self, key, shape=()):
+        return self._t(tf.normal(self._np(key), shape).astype(np.float32), torch.float32)
+
+    def randint(self, key, shape, lo, hi):
+        return self._t(tf.randint(self._np(key), shape, lo, hi))
+
+
+class _ToyModel:
+    """Stands in for a model: its final 'R' is a smooth function of (beta, gamma) plus a
+    seed-dependent wobble, so the population methods have a minimum to find."""
+
+    def __init__(self, params, seed):
+        self.p, self.seed = params, seed
+
+    def run(self, steps=None):
+        b, g = self.p["beta"], self.p["gamma"]
+        wobble = ((self.seed * 2654435761) % 1000) / 1e5
+        return {"R": [0.0, 500.0 * b / g + wobble]}
+
+
+@pytest.mark.parametrize("method", ["es", "pso", "cem"])
+def test_calibrator_population_loops_on_host(monkeypatch, method):
+    """ES, PSO and CEM loops with the oracle's random numbers and a toy model: histories
+    have one entry per iteration (each iteration's best for ES and CEM, the running best
+    for PSO, as in the reference), the kept best is the lowest loss seen, parameters stay
+    in bounds, and the same seed repeats the same run."""
+    from jaxabm_gb300 import analysis
+    monkeypatch.setattr(analysis, "jr", _OracleRandom())
+    monkeypatch.setattr(analysis._dev, "device", lambda: torch.device("cpu"))
+
+    def factory(params=None, config=None):
+        return _ToyModel(params, config.seed)
+
+    def calibrate(seed):
+        c = analysis.ModelCalibrator(factory, {"beta": 0.1, "gamma": 0.2}, {"R": 400.0},
+                                     param_bounds={"beta": (0.01, 0.4), "gamma": (0.05, 0.5)},
+                                     max_iterations=4, method=method, evaluation_steps=5,
+                                     num_evaluation_runs=2, tolerance=-1.0, seed=seed)
+        best = c.calibrate(verbose=False)
+        return c, best
+
+    c, best = calibrate(5)
+    assert len(c.loss_history) == 4 and len(c.param_history) == 4
+    if method == "pso":
+        assert all(b <= a for a, b in zip(c.loss_history, c.loss_history[1:]))
+    assert c.best_loss <= min(c.loss_history)
+    assert 0.01 - 1e-6 <= best["beta"] <= 0.4 + 1e-6 and 0.05 - 1e-6 <= best["gamma"] <= 0.5 + 1e-6
+    assert c.batched_evaluations == 0  # toy models run one by one
+    c2, best2 = calibrate(5)
+    assert best2 == best and c2.loss_history == c.loss_history
