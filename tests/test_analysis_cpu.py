@@ -146,6 +146,10 @@ class _OracleRandom:
     def randint(self, key, shape, lo, hi):
         return self._t(tf.randint(self._np(key), shape, lo, hi))
 
+    def permutation(self, key, x):
+        out = tf.permutation(self._np(key), x.numpy() if torch.is_tensor(x) else x)
+        return torch.from_numpy(np.ascontiguousarray(out))
+
 
 class _ToyModel:
     """Stands in for a model: its final 'R' is a smooth function of (beta, gamma) plus a
@@ -190,3 +194,31 @@ def test_calibrator_population_loops_on_host(monkeypatch, method):
     assert c.batched_evaluations == 0  # toy models run one by one
     c2, best2 = calibrate(5)
     assert best2 == best and c2.loss_history == c.loss_history
+
+
+def test_sensitivity_analysis_on_host(monkeypatch):
+    """SensitivityAnalysis end to end with the oracle's random numbers and toy models (run
+    one by one): samples equal the oracle's Latin hypercube, each sample's model is built
+    with seed 1000 + i, and the result is the last value of each metric."""
+    from jaxabm_gb300 import analysis
+    monkeypatch.setattr(analysis, "jr", _OracleRandom())
+    seeds = []
+
+    def factory(params=None, config=None):
+        seeds.append(config.seed)
+        return _ToyModel(params, config.seed)
+
+    ranges = {"beta": (0.05, 0.3), "gamma": (0.1, 0.4)}
+    sa = analysis.SensitivityAnalysis(factory, ranges, ["R", "missing"], num_samples=12, seed=9)
+    assert np.array_equal(sa.samples.numpy(), lhs_oracle(9, 12, list(ranges.values())))
+    res = sa.run(verbose=False)
+    assert seeds == [1000 + i for i in range(12)] and not sa.batched
+    for i in range(12):
+        want = _ToyModel({"beta": float(sa.samples[i, 0]), "gamma": float(sa.samples[i, 1])},
+                         1000 + i).run()["R"][-1]
+        assert float(res["R"][i]) == pytest.approx(want, rel=1e-6)
+    assert torch.all(res["missing"] == 0)
+    idx = sa.sobol_indices()
+    assert set(idx["R"]) == {"beta", "gamma"}
+    assert all(0.0 <= v <= 1.0 + 1e-6 for v in idx["R"].values())
+    assert idx["R"]["beta"] > 0.1 and idx["R"]["gamma"] > 0.1  # R = 500 beta / gamma
