@@ -90,3 +90,54 @@ def randomwalk_run(seed, n, steps, sigma=0.01):
         x, y = randomwalk_step(x, y, ck[t, 0], sigma)
         means[t] = (x.astype(np.float64).mean(), y.astype(np.float64).mean())
     return x, y, means
+
+
+# ---- SIR on a network --------------------------------------------------------------------
+# Agent (jx.Agent form), agent_key = split(coll_key, N)[i]:
+#   k_inf, k_rec = split(agent_key)
+#   S: becomes I if, for some CSR slot k of its row whose neighbour is I,
+#      uniform(k_inf, (deg,))[k] < beta
+#   I: becomes R if uniform(k_rec) < gamma
+#   R: stays R
+# Every agent reads the pre-step compartments (jaxabm/agent.py:168-177); the S, I, R counts
+# after each step are the metrics.  This is the direct (dense) statement of the rule: every
+# agent evaluates its own draws, whatever its neighbours are.  The C oracle uses the same
+# rule; the GPU kernels evaluate it only where it can change a compartment.
+
+
+def sir_step(state, row_ptr, col, coll_key, beta, gamma):
+    """One synchronous SIR step (small cases: a Python loop over agents)."""
+    st = np.asarray(state, dtype=np.int8)
+    n = st.size
+    beta32, gamma32 = np.float32(beta), np.float32(gamma)
+    akeys = agent_keys(np.asarray(coll_key, dtype=np.uint32), n)
+    new = st.copy()
+    for i in range(n):
+        if st[i] == 2:
+            continue
+        k_inf, k_rec = tfy.split(akeys[i], 2)
+        if st[i] == 1:
+            if tfy.uniform(k_rec, ()) < gamma32:
+                new[i] = 2
+            continue
+        r0, r1 = int(row_ptr[i]), int(row_ptr[i + 1])
+        if r1 == r0:
+            continue
+        infected_nb = st[np.asarray(col[r0:r1], dtype=np.int64)] == 1
+        if infected_nb.any():
+            u = tfy.uniform(k_inf, (r1 - r0,))
+            if np.any(infected_nb & (u < beta32)):
+                new[i] = 1
+    return new
+
+
+def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
+    """``steps`` SIR steps from compartments ``state`` and the model rng (after
+    ``Model.initialize``).  Returns (final compartments, counts int32[steps, 3], rng)."""
+    ck, rng_out = keychain(rng, steps, 1)
+    st = np.array(state, dtype=np.int8, copy=True)
+    counts = np.zeros((steps, 3), dtype=np.int32)
+    for t in range(steps):
+        st = sir_step(st, row_ptr, col, ck[t, 0], beta, gamma)
+        counts[t] = [(st == 0).sum(), (st == 1).sum(), (st == 2).sum()]
+    return st, counts, rng_out

@@ -1,0 +1,66 @@
+"""The C oracle's SIR (the GPU parity checker) against an independent NumPy statement of
+the reference's SIR rule (oracle/models.py) on small graphs: bit-exact compartments,
+per-step counts and key chains.  No GPU."""
+
+import numpy as np
+import pytest
+
+from oracle import coracle, models
+
+
+def _ba(n, m, seed):
+    """Small Barabasi-Albert-like graph (seeded, symmetric CSR) built here in NumPy."""
+    rs = np.random.RandomState(seed)
+    edges = set()
+    for i in range(m, n):
+        targets = rs.choice(i, size=min(m, i), replace=False)
+        for j in targets:
+            edges.add((i, int(j)))
+    return _csr(n, edges)
+
+
+def _csr(n, undirected):
+    rows = [[] for _ in range(n)]
+    for a, b in undirected:
+        rows[a].append(b)
+        rows[b].append(a)
+    rp = np.zeros(n + 1, dtype=np.int32)
+    rp[1:] = np.cumsum([len(r) for r in rows])
+    col = np.array([c for r in rows for c in sorted(r)], dtype=np.int32)
+    return rp, col
+
+
+def _star(n):
+    return _csr(n, {(0, i) for i in range(1, n)})
+
+
+def _clique(n):
+    return _csr(n, {(a, b) for a in range(n) for b in range(a + 1, n)})
+
+
+CASES = [
+    ("ba", lambda: _ba(80, 3, 1), 0.05, 0.2, 0.1, 25, 3),
+    ("ba_dense", lambda: _ba(60, 6, 2), 0.1, 0.3, 0.15, 20, 4),
+    ("star", lambda: _star(40), 0.1, 0.3, 0.1, 20, 5),
+    ("clique64", lambda: _clique(64), 0.05, 0.05, 0.2, 15, 6),
+    ("isolated", lambda: _csr(30, {(0, 1), (2, 3)}), 0.2, 0.5, 0.1, 10, 7),
+]
+
+
+@pytest.mark.parametrize("name,make,frac,beta,gamma,steps,seed", CASES,
+                         ids=[c[0] for c in CASES])
+def test_c_oracle_sir_equals_numpy_statement(name, make, frac, beta, gamma, steps, seed):
+    rp, col = make()
+    n = len(rp) - 1
+    rs = np.random.RandomState(seed)
+    st0 = np.zeros(n, dtype=np.int8)
+    st0[rs.permutation(n)[:max(1, int(frac * n))]] = 1
+    rng, _ = models.model_keys(seed, 1)
+    ref_st, ref_counts, ref_rng = models.sir_run(rp, col, st0, rng, steps, beta, gamma)
+    c_st, c_counts, c_rng = coracle.sir_run(rp, col, st0, rng, steps, beta, gamma)
+    assert np.array_equal(c_counts, ref_counts)
+    assert np.array_equal(c_st, ref_st)
+    assert np.array_equal(c_rng, ref_rng)
+    assert (ref_counts.sum(axis=1) == n).all()
+    if name != "isolated":  # the epidemic spreads, so the comparison covers infections
+        assert ref_counts[-1, 0] < (st0 == 0).sum()
