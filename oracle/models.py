@@ -141,3 +141,61 @@ def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
         st = sir_step(st, row_ptr, col, ck[t, 0], beta, gamma)
         counts[t] = [(st == 0).sum(), (st == 1).sum(), (st == 2).sum()]
     return st, counts, rng_out
+
+
+# ---- Schelling segregation on a torus grid ----------------------------------------------
+# Cell (x, y) of a W x H torus has index x*H + y.  Each step, from the pre-step layout:
+#   an agent is unhappy iff 8 * (same-type Moore neighbours) < 3 * (occupied neighbours);
+#   an unhappy agent i draws idx = min(floor(f32(uniform(agent_key) * e)), e - 1) into the
+#   ascending list of the e empty cells (agent_key = split(coll_key, N)[i]; one correctly
+#   rounded float32 multiply) and claims that cell; the lowest claiming id wins and moves,
+#   the others stay.  Metrics: (unhappy agents, moved agents).
+
+
+def schelling_step(pos, types, W, H, coll_key):
+    """One Schelling step (small cases).  Returns (new positions, (unhappy, moved))."""
+    pos = np.asarray(pos, dtype=np.int64)
+    types = np.asarray(types, dtype=np.int64)
+    n = pos.size
+    grid = np.full(W * H, -1, dtype=np.int64)
+    grid[pos] = types
+    empty = np.nonzero(grid < 0)[0]
+    e = empty.size
+    akeys = agent_keys(np.asarray(coll_key, dtype=np.uint32), n)
+    claims = {}
+    unhappy = 0
+    for i in range(n):
+        x, y = divmod(int(pos[i]), H)
+        same = occ = 0
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                if dx == 0 and dy == 0:
+                    continue
+                c = grid[((x + dx) % W) * H + (y + dy) % H]
+                if c >= 0:
+                    occ += 1
+                    same += int(c == types[i])
+        if 8 * same < 3 * occ:
+            unhappy += 1
+            if e == 0:
+                continue
+            u = np.float32(tfy.uniform(akeys[i], ()))
+            idx = min(int(np.floor(np.float32(u * np.float32(e)))), e - 1)
+            cell = int(empty[idx])
+            if cell not in claims or i < claims[cell]:
+                claims[cell] = i
+    new = pos.copy()
+    for cell, i in claims.items():
+        new[i] = cell
+    return new.astype(np.int32), (unhappy, len(claims))
+
+
+def schelling_run(pos, types, W, H, coll_keys):
+    """Schelling steps with per-step collection keys uint32[steps, 2].  Returns (final
+    positions, stats int32[steps, 2] = (unhappy, moved))."""
+    ck = np.asarray(coll_keys, dtype=np.uint32).reshape(-1, 2)
+    p = np.asarray(pos, dtype=np.int32).copy()
+    stats = np.zeros((ck.shape[0], 2), dtype=np.int32)
+    for t in range(ck.shape[0]):
+        p, stats[t] = schelling_step(p, types, W, H, ck[t])
+    return p, stats

@@ -1,6 +1,6 @@
-"""The C oracle's SIR (the GPU parity checker) against an independent NumPy statement of
-the reference's SIR rule (oracle/models.py) on small graphs: bit-exact compartments,
-per-step counts and key chains.  No GPU."""
+"""The C oracle's SIR and Schelling (the GPU parity checkers) against independent, direct
+NumPy statements of the rules (oracle/models.py) on small cases: bit-exact compartments,
+positions, per-step counts and key chains.  No GPU."""
 
 import numpy as np
 import pytest
@@ -64,3 +64,22 @@ def test_c_oracle_sir_equals_numpy_statement(name, make, frac, beta, gamma, step
     assert (ref_counts.sum(axis=1) == n).all()
     if name != "isolated":  # the epidemic spreads, so the comparison covers infections
         assert ref_counts[-1, 0] < (st0 == 0).sum()
+
+
+@pytest.mark.parametrize("W,H,density,seed,steps", [(12, 10, 0.8, 1, 8), (9, 9, 0.5, 2, 10),
+                                                   (16, 7, 0.9, 3, 6), (5, 5, 0.96, 4, 5)])
+def test_c_oracle_schelling_equals_numpy_statement(W, H, density, seed, steps):
+    """The C oracle's Schelling step (the GPU tests' checker) against the direct NumPy
+    statement of the rule: positions and (unhappy, moved) per step, bit for bit."""
+    rs = np.random.RandomState(seed)
+    n = int(density * W * H)
+    pos = rs.permutation(W * H)[:n].astype(np.int32)
+    types = (np.arange(n) >= n // 2).astype(np.int8)
+    rng, _ = models.model_keys(seed, 1)
+    ck, _ = models.keychain(rng, steps, 1)
+    ck = ck.reshape(steps, 2)
+    ref_pos, ref_stats = models.schelling_run(pos, types, W, H, ck)
+    c_pos, c_stats = coracle.schelling_run(pos, types, W, H, ck)
+    assert np.array_equal(c_stats, ref_stats)
+    assert np.array_equal(c_pos, ref_pos)
+    assert ref_stats[:, 1].sum() > 0  # agents moved, so claims were compared
