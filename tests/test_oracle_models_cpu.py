@@ -83,3 +83,38 @@ def test_c_oracle_schelling_equals_numpy_statement(W, H, density, seed, steps):
     assert np.array_equal(c_stats, ref_stats)
     assert np.array_equal(c_pos, ref_pos)
     assert ref_stats[:, 1].sum() > 0  # agents moved, so claims were compared
+
+
+def test_golden_small_cases():
+    """The committed small-case vectors (tests/golden/oracle_small_cases.npz, written by
+    tests/golden/make_oracle_fixtures.py from the NumPy statements) are reproduced by the
+    NumPy statements and by the C oracle."""
+    import importlib.util
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_oracle_fixtures",
+                                                  os.path.join(here, "make_oracle_fixtures.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    g = np.load(os.path.join(here, "oracle_small_cases.npz"))
+    fresh = mk.cases()
+    assert set(g.files) == set(fresh)
+    for k in g.files:
+        if k.startswith("rw_"):  # floating point: libm may differ across machines
+            np.testing.assert_allclose(fresh[k], g[k], rtol=1e-6, atol=1e-6, err_msg=k)
+        else:
+            assert np.array_equal(g[k], fresh[k]), k
+    rng, _ = models.model_keys(int(g["sir_seed"]), 1)
+    st, counts, r = coracle.sir_run(g["sir_row_ptr"], g["sir_col"], g["sir_state0"], rng,
+                                    int(g["sir_steps"]), float(g["sir_beta"]),
+                                    float(g["sir_gamma"]))
+    assert np.array_equal(st, g["sir_state"]) and np.array_equal(counts, g["sir_counts"])
+    assert np.array_equal(r, g["sir_rng"])
+    assert counts[-1, 0] < (g["sir_state0"] == 0).sum()
+    pos, stats = coracle.schelling_run(g["sch_pos0"], g["sch_types"], int(g["sch_W"]),
+                                       int(g["sch_H"]), g["sch_coll_keys"])
+    assert np.array_equal(pos, g["sch_pos"]) and np.array_equal(stats, g["sch_stats"])
+    rw = coracle.randomwalk_run(0, 100, 5)
+    d = np.abs(rw["x"].astype(np.float64) - g["rw_x"])
+    assert np.minimum(d, 1 - d).max() < 1e-6
+    np.testing.assert_allclose(rw["means"], g["rw_means"], rtol=1e-6)

@@ -1,16 +1,16 @@
 """Pins the PRNG oracle (CPU only).
 
-Known-answer values used here are published ones, restated in the test (no file in this
-repository or container holds them):
+The known-answer values are published ones, restated from the public record in
+``tests/golden/published_known_answers.json``:
 
 * Random123 threefry2x32_20 known-answer vectors (zero key/counter, all-ones, and the
   pi-digits key/counter), the same triples JAX's own test suite checks;
-* outputs printed in the JAX documentation for ``PRNGKey(0)``: legacy-mode
-  ``split`` -> [[4146024105, 967050713], [2718843009, 1272950319]],
-  ``normal(key, (1,))`` -> [-0.20584226], ``uniform(key, (3,))`` ->
-  [0.9653214, 0.31468165, 0.63302994]; partitionable-mode ``split`` ->
-  [[1797259609, 2579123966], [928981903, 3453687069]].
+* outputs printed in the JAX documentation for ``PRNGKey(0)`` (legacy-mode ``split``,
+  ``normal(key, (1,))``, ``uniform(key, (3,))``; partitionable-mode ``split``).
 """
+
+import json
+import os
 
 import numpy as np
 import pytest
@@ -18,11 +18,12 @@ import pytest
 from oracle import coracle, models
 from oracle import threefry as t
 
-KAT = [
-    ((0x00000000, 0x00000000), (0x00000000, 0x00000000), (0x6B200159, 0x99BA4EFE)),
-    ((0xFFFFFFFF, 0xFFFFFFFF), (0xFFFFFFFF, 0xFFFFFFFF), (0x1CB996FC, 0xBB002BE7)),
-    ((0x13198A2E, 0x03707344), (0x243F6A88, 0x85A308D3), (0xC4923A9C, 0x483DF7A0)),
-]
+with open(os.path.join(os.path.dirname(__file__), "golden", "published_known_answers.json")) as _f:
+    GOLDEN = json.load(_f)
+
+KAT = [(tuple(int(v, 16) for v in r["key"]), tuple(int(v, 16) for v in r["counter"]),
+        tuple(int(v, 16) for v in r["output"])) for r in GOLDEN["threefry2x32_20"]]
+JAX0 = GOLDEN["jax_prngkey0"]
 
 
 @pytest.mark.parametrize("key,ctr,expect", KAT)
@@ -43,17 +44,21 @@ def test_prngkey_layout():
     assert t.PRNGKey(2**33 + 5).tolist() == [2, 5]
 
 
+def test_kat_count():
+    assert len(KAT) == 3
+
+
 def test_jax_doc_values_legacy():
     k = t.PRNGKey(0)
-    assert t.split(k, 2, t.LEGACY).tolist() == [[4146024105, 967050713], [2718843009, 1272950319]]
-    np.testing.assert_allclose(t.normal(k, (1,), t.LEGACY), [-0.20584226], rtol=1e-6)
-    np.testing.assert_allclose(t.uniform(k, (3,), mode=t.LEGACY),
-                               [0.9653214, 0.31468165, 0.63302994], rtol=1e-6)
+    assert t.split(k, 2, t.LEGACY).tolist() == JAX0["legacy_split_2"]
+    np.testing.assert_allclose(t.normal(k, (1,), t.LEGACY), JAX0["legacy_normal_1"], rtol=1e-6)
+    np.testing.assert_allclose(t.uniform(k, (3,), mode=t.LEGACY), JAX0["legacy_uniform_3"],
+                               rtol=1e-6)
 
 
 def test_jax_doc_values_partitionable():
     k = t.PRNGKey(0)
-    assert t.split(k, 2).tolist() == [[1797259609, 2579123966], [928981903, 3453687069]]
+    assert t.split(k, 2).tolist() == JAX0["partitionable_split_2"]
 
 
 def test_partitionable_bits_prefix_stable():
