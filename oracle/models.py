@@ -199,3 +199,29 @@ def schelling_run(pos, types, W, H, coll_keys):
     for t in range(ck.shape[0]):
         p, stats[t] = schelling_step(p, types, W, H, ck[t])
     return p, stats
+
+
+# ---- bounded-confidence opinion dynamics --------------------------------------------------
+# Per step, from the pre-step opinions o (every instance b its own mu, eps, tau):
+#   o_i += mu * (sum over neighbours j of s_ij * d_ij) / deg_i,
+#   d_ij = o_j - o_i,  s_ij = sigmoid((eps - |d_ij|) / tau)
+
+
+def opinion_step_f64(o, row_ptr, col, mu, eps, tau):
+    """One synchronous step in float64; o float64[n, B]; mu, eps, tau float64[B]."""
+    o = np.asarray(o, dtype=np.float64)
+    n = o.shape[0]
+    deg = np.diff(np.asarray(row_ptr, dtype=np.int64))
+    src = np.repeat(np.arange(n), deg)
+    d = o[np.asarray(col, dtype=np.int64)] - o[src]
+    s = 1.0 / (1.0 + np.exp(-(np.asarray(eps) - np.abs(d)) / np.asarray(tau)))
+    acc = np.zeros_like(o)
+    np.add.at(acc, src, s * d)
+    return o + np.asarray(mu) * acc / np.maximum(deg, 1)[:, None]
+
+
+def opinion_run_f64(o, row_ptr, col, mu, eps, tau, steps):
+    x = np.array(o, dtype=np.float64, copy=True)
+    for _ in range(steps):
+        x = opinion_step_f64(x, row_ptr, col, mu, eps, tau)
+    return x

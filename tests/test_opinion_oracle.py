@@ -64,3 +64,14 @@ def test_mean_conserved_on_regular_graph(case):
     rp, col, o0, mu, eps, tau, T, _ = case
     b = coracle.opinion_run_f64(o0, rp, col, mu, eps, tau, T)
     np.testing.assert_allclose(b.mean(0), o0.mean(0), atol=1e-12)
+
+
+def test_c_forward_equals_numpy_statement(case):
+    """The C float64 forward (checker of the GPU forward and of the adjoint's recompute)
+    against the direct NumPy statement of the step, within float64 rounding."""
+    from oracle import models
+    rp, col, o0, mu, eps, tau, T, _ = case
+    ref = models.opinion_run_f64(o0, rp, col, mu, eps, tau, 20)
+    got = coracle.opinion_run_f64(o0, rp, col, mu, eps, tau, 20)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-13)
+    assert np.abs(ref - o0).max() > 1e-3  # opinions moved
