@@ -12,7 +12,13 @@ server: p50/p99 latency and throughput), and ``cpu_baseline`` (the C/OpenMP orac
 sample of the instances, host cores).
 
 Prints ONE JSON line on rank 0.  ``--impl reference`` times the CPU port of the same
-workload (the reference itself runs on JAX, which the GPU host does not have).
+workload (the reference itself runs on JAX, which the GPU host does not have), built from
+``oracle/`` alone: its inputs come from the oracle's own generators, and its timed steps
+together run every member of the ensemble once.
+
+The GPU line carries ``parity``: the oracle's results on the first 1,024 members and the
+largest one (from the oracle's own inputs) compared bit for bit with the batched replay;
+any mismatch makes the run exit non-zero after printing the line.
 """
 
 import argparse
@@ -31,21 +37,6 @@ import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
 L2_BYTES = 129 * 1024 * 1024
-
-
-def _profiled_traffic(instances, path="grid"):
-    """DRAM bytes of one full-ensemble replay from the committed ncu summary of the path
-    (only for the full 4,096-instance workload it was captured on)."""
-    name = ("sir_resident_kernel_ensemble4096.md" if path == "resident"
-            else "sir_ensemble_4096_launch_list.md")
-    p = os.path.join(ROOT, "profiles", name)
-    if instances != 4096 or not os.path.exists(p):
-        return None, None
-    with open(p) as f:
-        for line in f:
-            if line.startswith("traffic_bytes_per_replay:"):
-                return int(line.split(":")[1]), "profiles/" + name
-    return None, None
 
 
 def _peaks():
@@ -133,15 +124,31 @@ def _reduce(v, world, op):
 # SIR ensemble (default workload)
 # --------------------------------------------------------------------------------------
 
-class SIREnsembleBench:
-    name = "sir_ensemble_4096_ba_m4_n1e3_1e5_t365"
+ENSEMBLE_NAME = "sir_ensemble_4096_ba_m4_n1e3_1e5_t365"
 
-    def __init__(self, rank, count=4096, steps=365, grids=None, path="auto"):
+
+def ensemble_config(sizes, steps, world, m=4):
+    """The ``config`` of both arms, from the member sizes alone (a BA(m) graph of n nodes
+    has 2 m (n - m) directed edges)."""
+    n = np.asarray(sizes, dtype=np.int64)
+    e = 2 * m * (n - m)
+    return {"workload": ENSEMBLE_NAME, "instances": int(n.size), "steps_per_instance": int(steps),
+            "agents": int(n.sum()), "directed_edges": int(e.sum()),
+            "l2": "inputs larger than L2 (CSR %.2f GB)" % (e.sum() * 4 / 1e9),
+            "parallelism": f"members partitioned across {world} rank(s), balanced by agents"}
+
+
+class SIREnsembleBench:
+    name = ENSEMBLE_NAME
+
+    def __init__(self, rank, world=1, count=4096, steps=365, grids=None, path="auto"):
         from jaxabm_gb300 import ensemble
         self.ensemble = ensemble
-        self.count, self.T = count, steps
-        spec = ensemble.rank_spec(count, rank)  # each rank its own members
+        self.T = steps
+        spec = ensemble.rank_spec(count, rank, world)  # this rank's share of the members
         self.spec = spec
+        self.count = len(spec["n"])
+        self.full_sizes = ensemble.ensemble_spec(4096 if count <= 4096 else count)["n"][:count]
         t0 = time.perf_counter()
         self.graphs, self.inits = ensemble.build_instances(spec)
         self.build_s = time.perf_counter() - t0
@@ -241,14 +248,22 @@ class SIREnsembleBench:
         h2d = (self.h_rp.numel() + self.h_col.numel()) * 4 + self.h_state.numel()
         return h2d, self.h_counts.numel() * 4
 
-    def algorithmic_bytes(self):
+    def final_replay(self):
+        """One more replay from step 0 after the timed legs: its status is checked (bad
+        inputs raise), its counters give the work of a replay, and its results are what
+        the parity check compares."""
         self.batch.reset()
         self.batch.replay()
         torch.cuda.synchronize()
+        self.batch.check()
+
+    def algorithmic_bytes(self):
+        """HBM bytes of the last replay's work (after :meth:`final_replay`)."""
         scanned, pushed, changes, cands = self.batch.edge_stats()
         self.work_stats = {"live_agent_steps": self.batch.live_agent_steps(),
                            "decision_candidates": cands, "csr_slots_scanned": scanned,
                            "csr_slots_pushed": pushed, "compartment_changes": changes}
+        self.work_stats.update(self.batch.threefry_blocks())
         if self.batch.mode == "resident":
             return self.batch.algorithmic_bytes_resident()
         return self.batch.algorithmic_bytes()
@@ -321,21 +336,48 @@ class SIREnsembleBench:
                 "wall_s": wall, "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
                 "path": path, "results_match_batched": bool(same)}
 
-    def cpu_baseline(self, threads, budget_s=12.0):
-        from oracle import coracle, models
+    def oracle_check(self, threads, sample=1024):
+        """The C/OpenMP oracle on this rank's first ``sample`` members and its largest one,
+        each from the oracle's own inputs (``oracle.workloads``), timed on the host cores
+        (``cpu_baseline``) and compared bit for bit with the last replay's per-step counts
+        and final compartments (``parity``)."""
+        from oracle import coracle, models, workloads
         coracle.set_threads(threads)
-        units, secs, k = 0, 0.0, 0
-        while k < self.count and secs < budget_s:
-            rp, col = self.graphs[k]
-            rng, _ = models.model_keys(int(self.spec["seed"][k]), 1)
-            t0 = time.perf_counter()
-            coracle.sir_run(rp, col, self.inits[k], rng, self.T, float(self.spec["beta"][k]),
-                            float(self.spec["gamma"][k]))
-            secs += time.perf_counter() - t0
-            units += (len(rp) - 1) * self.T
-            k += 1
-        return {"value": units / secs, "unit": "agent-steps/s", "cores": threads, "kind": "port",
-                "sample": f"first {k} of {self.count} instances, 365 steps each, C/OpenMP oracle"}
+        ospec = workloads.sir_ensemble_spec(4096 if len(self.full_sizes) <= 4096
+                                            else len(self.full_sizes))
+        local = list(range(min(sample, self.count)))
+        big = int(np.argmax(self.spec["n"]))
+        if big not in local:
+            local.append(big)
+        members = [int(self.spec["member"][k]) for k in local]
+        inputs = workloads.sir_members(ospec, members)
+        b = self.batch
+        counts = b.counts.reshape(b.k, self.T, 3).cpu().numpy()
+        words = self.ensemble.unpack_words(b.words).cpu().numpy()
+        w_off = b._offsets[2]
+        rngs = np.stack([models.model_keys(int(ospec["seed"][i]), 1)[0] for i in members])
+        t0 = time.perf_counter()
+        states, ref_counts, _ = coracle.sir_run_many(
+            [(rp, col) for rp, col, _ in inputs], [st0 for _, _, st0 in inputs], rngs, self.T,
+            ospec["beta"][members], ospec["gamma"][members])
+        secs = time.perf_counter() - t0
+        units = sum(len(st0) for _, _, st0 in inputs) * self.T
+        bad = []
+        for j, (k, i) in enumerate(zip(local, members)):
+            gpu_state = words[w_off[k]:w_off[k] + len(states[j])]
+            if not (np.array_equal(ref_counts[j], counts[k])
+                    and np.array_equal(states[j], gpu_state)):
+                bad.append(i)
+        desc = (f"members {members[0]}..{members[min(sample, self.count) - 1]} (first "
+                f"{min(sample, self.count)} of this rank) and the largest ({members[-1]}, "
+                f"{int(self.spec['n'][big])} agents), {self.T} steps each, C/OpenMP oracle "
+                f"(host threads take whole members) on the oracle's own inputs")
+        cpu = {"value": units / secs, "unit": "agent-steps/s", "cores": threads, "kind": "port",
+               "sample": desc}
+        parity = {"instances_checked": len(local), "mismatches": len(bad),
+                  "mismatched_members": bad[:16], "compared": "all per-step S/I/R counts and "
+                  "final compartments, bit for bit", "sample": desc}
+        return cpu, parity
 
 
 def _time_ms(fn, reps=3, warmup=1):
@@ -565,6 +607,23 @@ WORKLOADS = {"sir_ensemble": SIREnsembleBench}
 DEFAULT_WORKLOAD = "sir_ensemble"
 
 
+def sampler_block_rate(reps=5):
+    """Measured threefry2x32-20 block rate of the K1 sampler (jax.random.uniform over 2^28
+    elements, one block per element, ALU-bound): the issue-side peak of the SIR kernels,
+    whose work is dominated by the same blocks."""
+    from jaxabm_gb300 import _dev, _lib
+    import jaxabm_gb300.random as jr
+    n = 1 << 28
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    key = jr.PRNGKey(0)
+
+    def uni():
+        _lib.call("abm_rng_uniform", _dev.ptr(key), 1, n, 0.0, 1.0, _dev.ptr(out), 1, None)
+    ms = _time_ms(uni, reps=reps, warmup=2)
+    del out
+    return n / (ms / 1e3), ms
+
+
 def run_ours(args):
     world, rank, local = _dist()
     if world > 1:
@@ -574,7 +633,8 @@ def run_ours(args):
     jx.set_verbose(False)
     jx.build()
     grids = None if not args.grids else tuple(int(v) for v in args.grids.split(","))
-    wl = WORKLOADS[args.workload](rank, count=args.instances, grids=grids, path=args.path)
+    wl = WORKLOADS[args.workload](rank, world, count=args.instances, grids=grids,
+                                  path=args.path)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         wl.reset()
@@ -593,6 +653,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     _barrier(world)
     clk = clocks.stop()
+    wl.batch.check()  # a bad input of the timed replays raises here
     ms_local = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
     ms = _reduce(ms_local, world, torch.distributed.ReduceOp.MAX if world > 1 else None)
 
@@ -616,9 +677,11 @@ def run_ours(args):
     units = _reduce(wl.units_per_step, world, torch.distributed.ReduceOp.SUM if world > 1 else None)
     value = units / (ms / 1e3)
     hbm_peak, peak_kind = _peaks()
+    wl.final_replay()
     alg_bytes = wl.algorithmic_bytes()
     achieved = alg_bytes / (ms_local / 1e3) / 1e9
-    traffic, traffic_src = _profiled_traffic(wl.count, wl.batch.mode)
+    blocks = wl.work_stats["blocks"]
+    block_peak, sampler_ms = sampler_block_rate()
     # the per-unit figure of a whole-graph pass (every agent reads its row each step:
     # 4 B column + 1 B neighbour state per CSR slot, 6 B per agent), which the frontier
     # formulation does not move; its rate can exceed the HBM peak for that reason
@@ -632,12 +695,9 @@ def run_ours(args):
     out = {
         "metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "int8",
         "data": "synthetic",
-        "config": {"workload": wl.name, "instances": wl.count, "steps_per_instance": wl.T,
-                   "agents": int(wl.batch.n.sum()), "directed_edges": int(wl.batch.e.sum()),
-                   "l2": "inputs larger than L2 (CSR %.2f GB)" % (wl.batch.e.sum() * 4 / 1e9),
-                   "parallelism": f"instances sharded over {world} GPU(s)"},
+        "config": ensemble_config(wl.full_sizes, wl.T, world),
         "e2e": {"value": units / (e2e_ms / 1e3), "unit": "agent-steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "e2e_pipelined": {"value": units / (e2e_pipe_ms / 1e3), "unit": "agent-steps/s",
@@ -646,8 +706,9 @@ def run_ours(args):
                                   "second stream during step k's replay"},
         "gpu_launches": wl.launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": traffic_src,
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "traffic_note": "DRAM bytes come from ncu captures only (not measurable "
+                                     "in-run); the committed profile summaries give them",
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback",
                      "kernel": ("sir_resident_kernel: one launch runs every step of every "
@@ -659,6 +720,13 @@ def run_ours(args):
                      "algorithmic_bytes_per_step": alg_bytes,
                      "work_per_step": wl.work_stats,
                      "dense_equivalent": dense},
+        "roofline_issue": {"bound": "threefry2x32-20 blocks (ALU issue)",
+                           "achieved": blocks / (ms_local / 1e3), "peak": block_peak,
+                           "unit": "blocks/s", "frac": blocks / (ms_local / 1e3) / block_peak,
+                           "blocks_per_step": blocks,
+                           "peak_kind": "measured in this run: the K1 sampler "
+                                        "(jax.random.uniform, 2^28 elements, one block each, "
+                                        f"{sampler_ms:.3f} ms)"},
         "clocks": clk,
     }
     if not args.quick:
@@ -669,61 +737,80 @@ def run_ours(args):
         out["served_burst"] = wl.served(burst=True)
         out["served_burst"]["served_over_plain"] = (out["served_burst"]["value"]
                                                     / out["plain"]["value"])
-    if rank == 0 and world == 1 and not args.quick:
-        out["cpu_baseline"] = wl.cpu_baseline(os.cpu_count() or 1)
+        wl.final_replay()  # the served legs replay the batch: the parity check reads a fresh run
+    parity = None
+    if rank == 0 and not args.no_parity:
+        cpu, parity = wl.oracle_check(os.cpu_count() or 1)
+        if world == 1:
+            out["cpu_baseline"] = cpu
+        out["parity"] = parity
     if not args.quick or args.models:
         out["models"] = model_lines()
     out["setup_s"] = {"graph_build": wl.build_s, "autotune": wl.tune_s}
-    out["config"]["launch_grids"] = {"sweep": wl.launch[0], "candidates": wl.launch[1],
-                                     "push": wl.launch[2], "picked_by": wl.picked_by}
-    out["config"]["path"] = wl.batch.mode
+    out["launch"] = {"path": wl.batch.mode, "sweep": wl.launch[0], "candidates": wl.launch[1],
+                     "push": wl.launch[2], "picked_by": wl.picked_by}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+    if parity is not None and parity["mismatches"]:
+        sys.exit(3)
 
 
 def run_reference(args):
-    """CPU port of the same workload on all host cores: each step runs a bounded sample of
-    the ensemble's instances (the first ``sample`` members, 365 steps each)."""
+    """The reference's CPU path on the same workload: the C/OpenMP port of the SIR step
+    (the reference itself needs JAX, absent on this host) on all host cores, with inputs
+    from the oracle's own generators.  The members are split into ``--steps`` runs of
+    nearly equal agent totals; timed step k runs run k, so the timed steps together run
+    every member once (warm-up step w runs run w mod steps, untimed)."""
     world, rank, _ = _dist()
     if rank != 0:
         return
-    from jaxabm_gb300 import ensemble
-    from oracle import coracle, models
+    from oracle import coracle, models, workloads
     cores = os.cpu_count() or 1
     coracle.set_threads(cores)
-    count, T, sample = 4096, 365, 64
-    spec = ensemble.ensemble_spec(count)
-    sub = {k: v[:sample] for k, v in spec.items()}
-    graphs, inits = ensemble.build_instances(sub)
-    times, units = [], 0
-    for it in range(args.warmup + args.steps):
+    T = 365
+    spec = workloads.sir_ensemble_spec(4096 if args.instances <= 4096 else args.instances)
+    count = args.instances
+    sizes = spec["n"][:count]
+    runs = workloads.balanced_slices(sizes, args.steps)
+    t0 = time.perf_counter()
+    members = workloads.sir_members(spec, range(count))
+    build_s = time.perf_counter() - t0
+
+    rngs = np.stack([models.model_keys(int(spec["seed"][i]), 1)[0] for i in range(count)])
+
+    def one_step(k):
+        idx = runs[k]
+        coracle.sir_run_many([members[i][:2] for i in idx], [members[i][2] for i in idx],
+                             rngs[idx], T, spec["beta"][idx], spec["gamma"][idx])
+        return int(sizes[idx].sum()) * T
+
+    for w in range(args.warmup):
+        one_step(w % args.steps)
+    units, secs = 0, 0.0
+    for k in range(args.steps):
         t0 = time.perf_counter()
-        u = 0
-        for k in range(sample):
-            rp, col = graphs[k]
-            rng, _ = models.model_keys(int(sub["seed"][k]), 1)
-            coracle.sir_run(rp, col, inits[k], rng, T, float(sub["beta"][k]), float(sub["gamma"][k]))
-            u += (len(rp) - 1) * T
-        dt = time.perf_counter() - t0
-        if it >= args.warmup:
-            times.append(dt)
-            units = u
-    ms = 1e3 * sum(times) / len(times)
-    value = units / (ms / 1e3)
+        units += one_step(k)
+        secs += time.perf_counter() - t0
+    value = units / secs
+    ms = 1e3 * secs / args.steps
     out = {"metric": "agent-steps/s", "value": value, "unit": "agent-steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int8",
+           "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "int8",
            "data": "synthetic", "impl": "reference",
-           "config": {"workload": SIREnsembleBench.name, "parallelism": "host cores"},
+           "config": ensemble_config(sizes, T, world),
            "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": cores,
                             "kind": "port",
-                            "sample": f"first {sample} of {count} ensemble instances per step, "
-                                      f"{T} steps each (C/OpenMP port; the reference needs JAX, "
-                                      f"absent on this host)"},
+                            "sample": f"all {count} members over the {args.steps} timed steps "
+                                      f"(step k runs the k-th of {args.steps} runs of nearly "
+                                      f"equal agent totals), {T} steps each; C/OpenMP port of "
+                                      f"the reference's SIR step (host threads take whole "
+                                      f"members) on the oracle's own inputs (the reference "
+                                      f"needs JAX, absent on this host)"},
            "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
-                   "d2h_bytes_per_step": 0}}
+                   "d2h_bytes_per_step": 0},
+           "setup_s": {"input_build": build_s}}
     print(json.dumps(out), flush=True)
 
 
@@ -744,6 +831,8 @@ def main():
     ap.add_argument("--path", default="auto", choices=["auto", "resident", "grid"],
                     help="SIR ensemble path: the autotuner's choice, the resident "
                          "per-instance kernel, or the per-step grid kernels")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle parity check (profiling captures)")
     ap.add_argument("--grids", default=None,
                     help="fixed sweep,candidates,push grid sizes instead of the autotuner "
                          "(profiling captures: keeps the launch sequence short)")

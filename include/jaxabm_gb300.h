@@ -153,7 +153,7 @@ ABM_API int abm_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t n
                                void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- K5: SIR contagion on a Network ------------------------------------------------- */
-/* Device-side descriptor of one SIR model instance (144 bytes, 8-byte aligned).
+/* Device-side descriptor of one SIR model instance (152 bytes, 8-byte aligned).
  * words holds one byte per agent, (infected neighbours << 2) | compartment (0 S, 1 I,
  * 2 R); an agent of degree >= abm_sir_hub_degree() (a hub) has 63 in the count field and
  * its count in hub_counts[i] (int32[n]).  words is 16-byte aligned and round_up(n, 16)
@@ -169,8 +169,9 @@ ABM_API int abm_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t n
  * S, I, R after each step (int32[steps][3]); step_si/step_ir are the transitions of the
  * step in flight (zero before step 0); done_flag (nullable, may be host-mapped) is set to
  * 1 after the last step; edges_scanned / edges_pushed accumulate the CSR slots read by
- * the decide and push phases and candidates the agents that needed a decision (all zero
- * before step 0). */
+ * the decide and push phases, candidates the agents that needed a decision (susceptible
+ * agents with an infected neighbour and infected agents, summed over steps) and draws the
+ * infection draws made (one threefry2x32 block each; all zero before step 0). */
 typedef struct abm_sir_instance {
   const int32_t* row_ptr;
   int32_t* adj;
@@ -195,7 +196,15 @@ typedef struct abm_sir_instance {
   unsigned long long edges_pushed;
   unsigned long long candidates;
   uint32_t coll[2]; /* collection key of the current step (written by abm_sir_steps) */
+  unsigned long long draws;
 } abm_sir_instance;
+
+/* Bits of the status word of abm_sir_pack, abm_sir_pack_batch and abm_sir_steps_resident
+ * (device int32, zeroed by the caller; bits are OR-ed in, so one word reports every kind
+ * of bad input a call met). */
+#define ABM_SIR_STATUS_OVERSIZE 1        /* instance larger than the resident call's max_agents */
+#define ABM_SIR_STATUS_BAD_COMPARTMENT 2 /* compartment outside 0..2 (stored as R)              */
+#define ABM_SIR_STATUS_BAD_COLUMN 4      /* CSR column outside 0..n-1 (replaced by a self-loop) */
 
 /* A tile of agents [begin, end) of instance `inst` (end - begin <= abm_sir_tile_agents()). */
 typedef struct abm_work_item {
@@ -220,8 +229,9 @@ ABM_API int32_t abm_sir_hub_degree(void);
  * (row_ptr[n] entries, may be col itself) receives the columns with hub tags; words
  * (16-byte aligned, round_up(n,16) bytes), hub_counts (int32[n]) and comp
  * (round_up(n,16)/16 words) as described at abm_sir_instance; sizes (device int32[3])
- * receives the S, I, R totals; *status (device int32) becomes 1 on a compartment outside
- * 0..2 (stored as R) or a column outside 0..n-1 (replaced by a self-loop). */
+ * receives the S, I, R totals; *status (device int32) gets ABM_SIR_STATUS_BAD_COMPARTMENT
+ * for a compartment outside 0..2 (stored as R) and ABM_SIR_STATUS_BAD_COLUMN for a column
+ * outside 0..n-1 (replaced by a self-loop). */
 ABM_API int abm_sir_pack(const int8_t* state, const int32_t* row_ptr, const int32_t* col,
                          int64_t n, int32_t* adj, uint8_t* words, int32_t* hub_counts,
                          uint32_t* comp, int32_t* sizes, int32_t* status, void* stream);
@@ -298,7 +308,8 @@ ABM_API size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid);
  * results) on the resident path: CTAs take instances in the order order[0..ninst) (device
  * int32, NULL for index order; largest first balances best) and run each for
  * min(nsteps, steps - t) steps.  Every instance must have n <= max_agents; one that does
- * not is left untouched and sets *status (device int32, zeroed by the caller) to 1.  grid
+ * not is left untouched and ORs ABM_SIR_STATUS_OVERSIZE into *status (device int32,
+ * zeroed by the caller).  grid
  * from abm_sir_resident_grid(max_agents); scratch 256-byte aligned.
  * With states8 and words_base (both NULL or both set: int8 compartments of an instance at
  * the same byte offset from states8 as its words from words_base, as for
@@ -306,8 +317,9 @@ ABM_API size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid);
  * compartments (hub marks by degree, hub tags on its columns in place, infected-neighbour
  * counts, hub counts zeroed) instead of reading words, so no abm_sir_pack_batch is needed
  * before the call; without them the words and column tags must come from
- * abm_sir_pack_batch (or an earlier call).  A compartment outside 0..2 (stored as R) or a
- * column outside 0..n-1 (replaced by a self-loop) sets *status to 1. */
+ * abm_sir_pack_batch (or an earlier call).  A compartment outside 0..2 (stored as R) ORs
+ * ABM_SIR_STATUS_BAD_COMPARTMENT and a column outside 0..n-1 (replaced by a self-loop)
+ * ABM_SIR_STATUS_BAD_COLUMN into *status. */
 ABM_API int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t* order,
                                    int32_t max_agents, int32_t nsteps, int32_t grid,
                                    const int8_t* states8, const uint8_t* words_base,
@@ -356,6 +368,12 @@ ABM_API int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32
 /* B instances (B a power of two, 4 <= B <= 128) share one symmetric CSR graph; opinions
  * are interleaved o float32[n][B] (16-byte aligned); mu, eps, tau are float32[B].
  * Per step: o_i += mu * (sum_j sigmoid((eps - |o_j - o_i|) / tau) (o_j - o_i)) / deg_i.
+ * The forward is a fixed sequence of float32 operations, each rounded to nearest with no
+ * fused multiply-add: d = o_j - o_i; z = (eps - |d|) * (1 / tau); s = 1 / (1 + exp(-z));
+ * acc = acc + s * d over the row in CSR order; o_i' = o_i + mu * (acc / deg_i); exp is the
+ * table-driven method of Tang (ACM TOMS 15(2), 1989) with x clamped to [-87, 88] (see
+ * abm_opinion_sigmoid).  Results are therefore reproducible bit for bit by any IEEE-754
+ * float32 implementation of the same sequence.
  * The reference trains such models with jit(grad(loss)) through its whole run loop
  * (jaxabm/analysis.py:494-522); these entry points give the forward pass, checkpoints and
  * the hand-written reverse pass. */
@@ -373,6 +391,11 @@ ABM_API int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, cons
 ABM_API int abm_opinion_step(const float* o_in, float* o_out, const int32_t* row_ptr,
                              const int32_t* col, int64_t n, int32_t B, const float* mu,
                              const float* eps, const float* tau, void* stream);
+
+/* s[k] = sigmoid(z[k]) exactly as the forward step evaluates it (n values, device float32),
+ * so the forward's sigmoid can be compared bit for bit with another implementation of the
+ * same sequence. */
+ABM_API int abm_opinion_sigmoid(const float* z, float* s, int64_t n, void* stream);
 
 /* inv_deg float32[n] = 1 / deg_i (0 for isolated nodes), read by abm_opinion_adjoint_step. */
 ABM_API int abm_opinion_inv_degree(const int32_t* row_ptr, int64_t n, float* inv_deg,

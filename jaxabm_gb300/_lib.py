@@ -72,6 +72,7 @@ SIGNATURES = {
     "abm_schelling_run": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _i32, _p, _p, _sz, _p]),
     "abm_opinion_run": (_int, [_p, _p, _p, _p, _i64, _i32, _p, _p, _p, _i32, _i32, _p, _p]),
     "abm_opinion_step": (_int, [_p, _p, _p, _p, _i64, _i32, _p, _p, _p, _p]),
+    "abm_opinion_sigmoid": (_int, [_p, _p, _i64, _p]),
     "abm_opinion_inv_degree": (_int, [_p, _i64, _p, _p]),
     "abm_opinion_moments_workspace_bytes": (_sz, [_i64, _i32]),
     "abm_opinion_moments": (_int, [_p, _i64, _i32, _p, _p, _sz, _p]),

@@ -4,8 +4,12 @@
 // (float32), so a neighbour's B values are one contiguous 4*B-byte row: a group of B/4
 // lanes reads it with 128-bit loads.  Per step, for node i and instance b:
 //   d_j = o_j - o_i;  s_j = sigmoid((eps_b - |d_j|) * (1/tau_b))
-//   o_i' = o_i + mu_b * (sum_j s_j d_j) / deg_i                (fused multiply-adds)
+//   acc = sum_j s_j * d_j  (in CSR order);  o_i' = o_i + mu_b * (acc / deg_i)
 // which is the model o_i += mu * mean_j sigmoid((eps - |o_j - o_i|)/tau) (o_j - o_i).
+// The forward is exact float32 arithmetic in a fixed order: every operation is one IEEE-754
+// operation rounded to nearest (no contraction into fused multiply-adds), the sigmoid is
+// 1 / (1 + exp(-z)) with a correctly rounded reciprocal and the table-driven exponential
+// below, so the C oracle's float32 restatement of the same sequence gives the same bits.
 //
 // Adjoint (reverse mode, the gradient jax.grad of the reference's run loop would give,
 // jaxabm/analysis.py:494-522): with g(d) = s d and g'(d) = s - |d| s (1 - s) / tau,
@@ -33,14 +37,48 @@ __device__ __forceinline__ void ld4(const float* __restrict__ row, int sub, floa
   a[3] = v.w;
 }
 
-// sigmoid((eps - |d|) / tau) with the hardware exponential and reciprocal (__expf,
-// __fdividef): about 2^-21 relative error for |z| <= 10, far inside the FP32 tolerance of
-// the model (the tests bound the states against the FP64 oracle).
-__device__ __forceinline__ float sigmoid_z(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
+// 2^(j/32) for j = 0..31, each the float32 nearest to the exact value.
+__device__ const float kExp2Table[32] = {
+    0x1.000000p+0f, 0x1.059b0ep+0f, 0x1.0b5586p+0f, 0x1.11301ep+0f, 0x1.172b84p+0f,
+    0x1.1d4874p+0f, 0x1.2387a6p+0f, 0x1.29e9e0p+0f, 0x1.306fe0p+0f, 0x1.371a74p+0f,
+    0x1.3dea64p+0f, 0x1.44e086p+0f, 0x1.4bfdaep+0f, 0x1.5342b6p+0f, 0x1.5ab07ep+0f,
+    0x1.6247ecp+0f, 0x1.6a09e6p+0f, 0x1.71f75ep+0f, 0x1.7a1148p+0f, 0x1.82589ap+0f,
+    0x1.8ace54p+0f, 0x1.93737cp+0f, 0x1.9c4918p+0f, 0x1.a5503cp+0f, 0x1.ae89fap+0f,
+    0x1.b7f770p+0f, 0x1.c199bep+0f, 0x1.cb720ep+0f, 0x1.d5818ep+0f, 0x1.dfc974p+0f,
+    0x1.ea4afap+0f, 0x1.f50766p+0f};
+constexpr float kExpK = 0x1.715476p+5f;   // 32 / ln 2
+constexpr float kExpL1 = 0x1.62c000p-6f;  // ln 2 / 32, leading 11 bits
+constexpr float kExpL2 = 0x1.217f7ep-17f; // ln 2 / 32 - kExpL1
+constexpr float kExpC3 = 0x1.555556p-3f;  // 1 / 6
 
-__device__ __forceinline__ float sigmoid_of(float eps, float itau, float d) {
-  return sigmoid_z((eps - fabsf(d)) * itau);
+// exp(x) in float32 by Tang's table-driven method (P. T. P. Tang, "Table-driven
+// implementation of the exponential function in IEEE floating-point arithmetic", ACM TOMS
+// 15(2), 1989): N = rint(x * 32 / ln 2); r = (x - N L1) - N L2 with L1 + L2 = ln 2 / 32 (L1
+// has 11 significant bits, so N L1 and x - N L1 are exact); exp(r) - 1 by its Taylor
+// polynomial r + r^2 (1/2 + r/6) (|r| <= ln 2 / 64: truncation error below 6e-10);
+// exp(x) = 2^(N >> 5) (T[N & 31] + T[N & 31] p).  x is clamped to [-87, 88], so every
+// intermediate is normal and the scaling is an exact add to the exponent field.  About 2 ulp
+// from exp over the clamped range.  T is kExp2Table staged in shared memory.
+__device__ __forceinline__ float exp_table(float x, const float* T) {
+  x = fminf(fmaxf(x, -87.0f), 88.0f);
+  const float nf = rintf(__fmul_rn(x, kExpK));
+  const int N = static_cast<int>(nf);
+  const float r = __fsub_rn(__fsub_rn(x, __fmul_rn(nf, kExpL1)), __fmul_rn(nf, kExpL2));
+  const float p = __fadd_rn(r, __fmul_rn(__fmul_rn(r, r), __fadd_rn(0.5f, __fmul_rn(r, kExpC3))));
+  const float t = T[N & 31];
+  const float e = __fadd_rn(t, __fmul_rn(t, p));
+  return __uint_as_float(__float_as_uint(e) + (static_cast<uint32_t>(N >> 5) << 23));
 }
+
+// sigmoid(z) = 1 / (1 + exp(-z)), reciprocal correctly rounded.
+__device__ __forceinline__ float sigmoid_exact(float z, const float* T) {
+  return __frcp_rn(__fadd_rn(1.0f, exp_table(-z, T)));
+}
+
+// The adjoint's sigmoid: the hardware exponential and reciprocal (__expf, __fdividef, about
+// 2^-21 relative error for |z| <= 10); the adjoint is checked against the float64 gradient
+// and central differences, not bit for bit, and reads states the exact forward produced.
+__device__ __forceinline__ float sigmoid_z(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 template <int LPN>
 __global__ void __launch_bounds__(kOpThreads)
@@ -48,6 +86,9 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
                     const int32_t* __restrict__ rp, const int32_t* __restrict__ col, int n, int B,
                     const float* __restrict__ mu, const float* __restrict__ eps,
                     const float* __restrict__ tau) {
+  __shared__ float T[32];
+  if (threadIdx.x < 32) T[threadIdx.x] = kExp2Table[threadIdx.x];
+  __syncthreads();
   const long long g = (long long)blockIdx.x * kOpThreads + threadIdx.x;
   const int node = (int)(g / LPN);
   const int sub = (int)(g % LPN);
@@ -57,40 +98,52 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
   ld4(eps, sub, ep);
   ld4(tau, sub, it);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) it[c] = 1.0f / it[c];
+  for (int c = 0; c < 4; ++c) it[c] = __frcp_rn(it[c]);
   ld4(o + (size_t)node * B, sub, oi);
   const int r0 = rp[node], r1 = rp[node + 1];
+  // acc += s(d) * d for one neighbour row (instances of this lane)
+  auto edge = [&](const float (&oj)[4]) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float d = __fsub_rn(oj[c], oi[c]);
+      const float s = sigmoid_exact(__fmul_rn(__fsub_rn(ep[c], fabsf(d)), it[c]), T);
+      acc[c] = __fadd_rn(acc[c], __fmul_rn(s, d));
+    }
+  };
   int e = r0;
   // two neighbour rows in flight per iteration; accumulation stays in CSR order
   for (; e + 1 < r1; e += 2) {
     float oa[4], ob[4];
     ld4(o + (size_t)col[e] * B, sub, oa);
     ld4(o + (size_t)col[e + 1] * B, sub, ob);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float da = oa[c] - oi[c];
-      acc[c] = fmaf(sigmoid_of(ep[c], it[c], da), da, acc[c]);
-      const float db = ob[c] - oi[c];
-      acc[c] = fmaf(sigmoid_of(ep[c], it[c], db), db, acc[c]);
-    }
+    edge(oa);
+    edge(ob);
   }
   if (e < r1) {
     float oa[4];
     ld4(o + (size_t)col[e] * B, sub, oa);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float da = oa[c] - oi[c];
-      acc[c] = fmaf(sigmoid_of(ep[c], it[c], da), da, acc[c]);
-    }
+    edge(oa);
   }
   float res[4] = {oi[0], oi[1], oi[2], oi[3]};
   const int deg = r1 - r0;
   if (deg > 0) {
     const float fdeg = (float)deg;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) res[c] = fmaf(m[c], acc[c] / fdeg, oi[c]);
+    for (int c = 0; c < 4; ++c) res[c] = __fadd_rn(oi[c], __fmul_rn(m[c], __fdiv_rn(acc[c], fdeg)));
   }
   reinterpret_cast<float4*>(out + (size_t)node * B)[sub] = make_float4(res[0], res[1], res[2], res[3]);
+}
+
+// The forward's sigmoid over an array (s[k] = sigmoid(z[k]) exactly as the step computes
+// it), for bit-level checks against the oracle.
+__global__ void opinion_sigmoid_kernel(const float* __restrict__ z, float* __restrict__ s,
+                                       long long n) {
+  __shared__ float T[32];
+  if (threadIdx.x < 32) T[threadIdx.x] = kExp2Table[threadIdx.x];
+  __syncthreads();
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x)
+    s[k] = sigmoid_exact(z[k], T);
 }
 
 // One adjoint step: lam_out from lam_in (= lambda^{t+1}) at the forward state o (= o^t);
@@ -329,6 +382,15 @@ int abm_opinion_step(const float* o_in, float* o_out, const int32_t* row_ptr, co
   ABM_OP_DISPATCH(opinion_step_kernel, B / 4, step_blocks(n, B), 0, s, o_in, o_out, row_ptr, col,
                   (int)n, B, mu, eps, tau);
   return abm_host::check_launch("abm_opinion_step");
+}
+
+int abm_opinion_sigmoid(const float* z, float* s, int64_t n, void* stream) {
+  if (!z || !s || n <= 0) return ABM_ERR_BADARG;
+  long long blocks = (n + 255) / 256;
+  const long long cap = (long long)abm_host::sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  opinion_sigmoid_kernel<<<(unsigned)blocks, 256, 0, abm_host::as_stream(stream)>>>(z, s, n);
+  return abm_host::check_launch("abm_opinion_sigmoid");
 }
 
 int abm_opinion_inv_degree(const int32_t* row_ptr, int64_t n, float* inv_deg, void* stream) {

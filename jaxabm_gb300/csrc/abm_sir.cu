@@ -75,7 +75,7 @@ constexpr int kFusedFinalizeMax = 256;             // instances finalized by the
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kS = 0, kI = 1;
 
-static_assert(sizeof(abm_sir_instance) == 144, "abm_sir_instance layout");
+static_assert(sizeof(abm_sir_instance) == 152, "abm_sir_instance layout");
 static_assert(sizeof(abm_work_item) == 16, "abm_work_item layout");
 
 // List workspace: this header, then `capacity` change entries (int2 {inst, agent << 2 |
@@ -260,18 +260,22 @@ __device__ __forceinline__ void bump_word(uint8_t* words, int i) {
 }
 
 // Per-instance sums over the lanes of a warp (lanes grouped by instance), added to the
-// group's instance by the group's lowest lane: CSR slots scanned, infections, slots pushed.
+// group's instance by the group's lowest lane: CSR slots scanned, infections, slots pushed,
+// infection draws.
 __device__ __forceinline__ void add_decided(bool valid, int inst, int scanned, int infected,
-                                            int pushed, abm_sir_instance* insts, int lane) {
-  if (!__any_sync(kFull, scanned != 0 || infected != 0)) return;
+                                            int pushed, int draws, abm_sir_instance* insts,
+                                            int lane) {
+  if (!__any_sync(kFull, scanned != 0 || infected != 0 || draws != 0)) return;
   const unsigned group = __match_any_sync(kFull, valid ? inst : -1);
   const int s = __reduce_add_sync(group, scanned);
   const int f = __reduce_add_sync(group, infected);
   const int p = __reduce_add_sync(group, pushed);
+  const int d = __reduce_add_sync(group, draws);
   if (valid && lane == __ffs(group) - 1) {
     if (s) red_add(&insts[inst].edges_scanned, static_cast<unsigned long long>(s));
     if (f) red_add(&insts[inst].step_si, f);
     if (p) red_add(&insts[inst].edges_pushed, static_cast<unsigned long long>(p));
+    if (d) red_add(&insts[inst].draws, static_cast<unsigned long long>(d));
   }
 }
 
@@ -450,7 +454,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     const abm_sir_instance* I = insts + inst;
     int cnt = static_cast<int>(static_cast<uint32_t>(e.x) >> kInstBits);
     bool infected = false, heavy = false;
-    int row0 = 0, deg = 0, scanned = 0;
+    int row0 = 0, deg = 0, scanned = 0, draws = 0;
     unsigned imask = 0;
     uint2 coll = make_uint2(0, 0);
     const int32_t* __restrict__ adj = nullptr;
@@ -497,6 +501,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
         if (imask) {
           const int slot = __ffs(imask) - 1;
           imask &= imask - 1;
+          ++draws;
           if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
             infected = true;
             imask = 0;
@@ -522,7 +527,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           __shfl_sync(kFull, reinterpret_cast<unsigned long long>(comp), src));
       const uint2 kinf = abm::split_at(abm::split_at(hcoll, (uint64_t)hi), 0);
       bool fired = false;
-      int c = 0;
+      int c = 0, hdraws = 0;
       if (hdeg > kDrawFirstDeg) {
         // long rows: the draws first (ALU only), the neighbour's compartment read only
         // where a draw fires -- a fraction beta of the slots -- in slot order, so the
@@ -533,6 +538,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
 #pragma unroll
           for (int u = 0; u < kHeavyUnroll; ++u) {
             const int slot = c + 32 * u + lane;
+            hdraws += slot < hdeg;
             if (slot < hdeg && abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < hbeta)
               fire |= 1u << u;
           }
@@ -548,9 +554,11 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           fired = __any_sync(kFull, f);
         }
         loaded = __reduce_add_sync(kFull, loaded);
+        hdraws = __reduce_add_sync(kFull, hdraws);
         if (lane == src) {
           infected = fired;
           scanned = loaded;
+          draws = hdraws;
         }
         continue;
       }
@@ -573,15 +581,20 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
           const int slot = c + 32 * u + lane;
           if (slot < hdeg && (wv[u] & 3u) == kI) {
             ++seen;
-            if (!f) f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < hbeta;
+            if (!f) {
+              ++hdraws;
+              f = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < hbeta;
+            }
           }
         }
         fired = __any_sync(kFull, f);
         remaining -= __reduce_add_sync(kFull, seen);
       }
+      hdraws = __reduce_add_sync(kFull, hdraws);
       if (lane == src) {
         infected = fired;
         scanned = min(c, hdeg);
+        draws = hdraws;
       }
     }
 
@@ -591,7 +604,7 @@ sir_candidates_kernel(abm_sir_instance* __restrict__ insts, Lists L) {
     if (infected) bump_word(insts[inst].words, i);
     push_rows(insts, inst << 1 | 1, row0, infected ? deg : 0, lane);
     buffer_change(infected, make_int2(inst, (i << 2) | static_cast<int>(kI)), buf, nbuf, L, lane);
-    add_decided(valid, inst, scanned, infected ? 1 : 0, infected ? deg : 0, insts, lane);
+    add_decided(valid, inst, scanned, infected ? 1 : 0, infected ? deg : 0, draws, insts, lane);
   }
   flush_changes(buf, nbuf, L, lane);
 }
@@ -729,7 +742,7 @@ __device__ __forceinline__ int pack_mark(const int8_t* __restrict__ st,
   }
   const int s = st[i];
   if (s < 0 || s > 2) {
-    atomicExch(bad, 1);
+    atomicOr(bad, ABM_SIR_STATUS_BAD_COMPARTMENT);
     words[i] = 2;
     return -1;
   }
@@ -753,7 +766,7 @@ __device__ __forceinline__ void pack_count(const int32_t* __restrict__ rp, const
     if (t >= static_cast<uint32_t>(n)) {
       // out-of-range column: flagged, and replaced by a self-loop so that no step kernel
       // reads outside the instance
-      atomicExch(bad, 1);
+      atomicOr(bad, ABM_SIR_STATUS_BAD_COLUMN);
       adj[k] = static_cast<int32_t>((words[i] >> 2) == kHubMark ? (static_cast<uint32_t>(i) | kTag)
                                                                 : static_cast<uint32_t>(i));
       continue;
@@ -936,7 +949,7 @@ struct ResState {
   int si, ir;      // transitions of the step
   int num_s, num_i, num_r;
   uint32_t rng0, rng1, coll0, coll1;
-  unsigned long long scanned, pushed, cands;
+  unsigned long long scanned, pushed, cands, draws;
 };
 
 // Position of the k-th (0-based) set bit of m; requires k < popc(m).
@@ -1053,7 +1066,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
     const int t_end = min(I->steps, t_begin + nsteps);
     if (t_begin >= t_end) continue;  // uniform
     if (npad > max_bytes || n > cap) {
-      if (threadIdx.x == 0) atomicExch(status, 1);
+      if (threadIdx.x == 0) atomicOr(status, ABM_SIR_STATUS_OVERSIZE);
       continue;
     }
     const int32_t* __restrict__ rp = I->row_ptr;
@@ -1070,7 +1083,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         if (k < n) {
           int c = st[k];
           if (c < 0 || c > 2) {
-            atomicExch(status, 1);
+            atomicOr(status, ABM_SIR_STATUS_BAD_COMPARTMENT);
             c = 2;
           }
           w = static_cast<uint32_t>(c);
@@ -1090,7 +1103,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         const uint32_t v = static_cast<uint32_t>(adj[k]);
         uint32_t t = v & kIdx;
         if (t >= static_cast<uint32_t>(n)) {
-          atomicExch(status, 1);
+          atomicOr(status, ABM_SIR_STATUS_BAD_COLUMN);
           int lo = 0, hi = n - 1;  // the row holding slot k: last i with rp[i] <= k
           while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -1130,7 +1143,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       S.ns = S.ni = 0;
       S.nchanges = 0;
       S.next_chunk = S.next_round = S.next_group = 0;
-      S.scanned = S.pushed = S.cands = 0;
+      S.scanned = S.pushed = S.cands = S.draws = 0;
     }
     __syncthreads();
     const int nchunks = (n + kResChunk - 1) / kResChunk;
@@ -1203,7 +1216,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       const int ns = S.ns, ni = S.ni;
       const int rounds_s = (ns + 31) >> 5, rounds = rounds_s + ((ni + 31) >> 5);
       unsigned long long my_scanned = 0;
-      int my_si = 0, my_ir = 0;
+      int my_si = 0, my_ir = 0, my_draws = 0;
       // Rounds are taken two ahead: the list entries of the round after next and the row
       // offsets of the next round are in flight while a round is decided.
       auto take = [&]() {
@@ -1287,6 +1300,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             if (imask) {
               const int slot = __ffs(imask) - 1;
               imask &= imask - 1;
+              ++my_draws;
               if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
                 infected = true;
                 imask = 0;
@@ -1313,6 +1327,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
 #pragma unroll
               for (int u = 0; u < kHeavyUnroll; ++u) {
                 const int slot = cpos + 32 * u + lane;
+                my_draws += slot < hdeg;
                 if (slot < hdeg && abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta)
                   fire |= 1u << u;
               }
@@ -1348,7 +1363,10 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
               const int slot = cpos + 32 * u + lane;
               if (slot < hdeg && (sw[wv[u] & kIdx] & 3u) == kI) {
                 ++seen;
-                if (!hit) hit = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
+                if (!hit) {
+                  ++my_draws;
+                  hit = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
+                }
               }
             }
             fired = __any_sync(kFull, hit);
@@ -1365,12 +1383,14 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       }
       my_si = __reduce_add_sync(kFull, my_si);
       my_ir = __reduce_add_sync(kFull, my_ir);
+      my_draws = __reduce_add_sync(kFull, my_draws);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) my_scanned += __shfl_down_sync(kFull, my_scanned, o);
       if (lane == 0) {
         if (my_si) atomicAdd(&S.si, my_si);
         if (my_ir) atomicAdd(&S.ir, my_ir);
         if (my_scanned) atomicAdd(&S.scanned, my_scanned);
+        if (my_draws) atomicAdd(&S.draws, static_cast<unsigned long long>(my_draws));
       }
       __syncthreads();
       // ---- apply: groups of 32 changes, taken from a group counter ------------------------
@@ -1460,6 +1480,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       I->edges_scanned += S.scanned;
       I->edges_pushed += S.pushed;
       I->candidates += S.cands;
+      I->draws += S.draws;
       if (t_end == I->steps && I->done_flag) {
         __threadfence_system();
         *reinterpret_cast<volatile int32_t*>(I->done_flag) = 1;

@@ -25,7 +25,7 @@ from .sir import barabasi_albert, initial_states
 
 TILE = 8192  # agents per work item (abm_sir_tile_agents)
 
-# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 144 bytes
+# numpy view of abm_sir_instance (include/jaxabm_gb300.h), 152 bytes
 INSTANCE_DTYPE = np.dtype([
     ("row_ptr", "<u8"), ("adj", "<u8"), ("words", "<u8"), ("hub_counts", "<u8"),
     ("comp", "<u8"), ("counts", "<u8"), ("done_flag", "<u8"), ("coll_keys", "<u8"),
@@ -33,9 +33,34 @@ INSTANCE_DTYPE = np.dtype([
     ("n", "<i4"), ("t", "<i4"), ("steps", "<i4"), ("beta", "<f4"), ("gamma", "<f4"),
     ("num_s", "<i4"), ("num_i", "<i4"), ("num_r", "<i4"), ("step_si", "<i4"),
     ("step_ir", "<i4"), ("edges_scanned", "<u8"), ("edges_pushed", "<u8"),
-    ("candidates", "<u8"), ("coll", "<u4", (2,)),
+    ("candidates", "<u8"), ("coll", "<u4", (2,)), ("draws", "<u8"),
 ])
-assert INSTANCE_DTYPE.itemsize == 144
+assert INSTANCE_DTYPE.itemsize == 152
+
+# bits of the status word of the pack and resident entry points (ABM_SIR_STATUS_*)
+STATUS_OVERSIZE = 1
+STATUS_BAD_COMPARTMENT = 2
+STATUS_BAD_COLUMN = 4
+
+
+def raise_status(bits, where="SIR batch"):
+    """Raise the error a status word reports (no-op for 0): ``AbmError`` with
+    ABM_ERR_BADARG for an oversize instance or a compartment outside 0..2, ABM_ERR_BOUNDS
+    for a CSR column outside its instance."""
+    bits = int(bits)
+    if not bits:
+        return
+    msgs = []
+    if bits & STATUS_OVERSIZE:
+        msgs.append("an instance has more agents than the resident call's max_agents")
+    if bits & STATUS_BAD_COMPARTMENT:
+        msgs.append("an initial compartment is outside 0..2 (S, I, R); it was run as R")
+    if bits & STATUS_BAD_COLUMN:
+        msgs.append("a CSR column points outside its instance; it was run as a self-loop")
+    code = _lib.ABM_ERR_BOUNDS if bits == STATUS_BAD_COLUMN else _lib.ABM_ERR_BADARG
+    raise _lib.AbmError(code, where, "; ".join(msgs))
+
+
 WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
 
@@ -186,8 +211,11 @@ class SIRBatch:
             np.concatenate([tiles_for(i, int(n)) for i, n in enumerate(self.n)])).to(dev)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.pack()
-        if int(self._status.item()) != 0:
+        bad = int(self._status.item())
+        if bad & STATUS_BAD_COMPARTMENT:
             raise ValueError("initial compartments must be 0 (S), 1 (I) or 2 (R)")
+        if bad & STATUS_BAD_COLUMN:
+            raise ValueError("a CSR column points outside its instance (0..n-1)")
         self.words0 = self.words.clone()
         self.hub_counts0 = self.hub_counts.clone()
         self.comp0 = self.comp.clone()
@@ -281,7 +309,10 @@ class SIRBatch:
         words of step 0 are copied back (device to device), so the next run starts from
         them.  After :meth:`load_host` brought other inputs, the words of step 0 are
         rebuilt from them instead (the grid path packs again; the resident kernel builds
-        them at step 0)."""
+        them at step 0).  The status words are cleared, except what a pack of the loaded
+        inputs reports about them."""
+        if self.resident_ok:
+            self.res_status.zero_()
         if self._words0_stale:
             self.desc.copy_(self.desc0)
             if self.mode == "resident":
@@ -358,20 +389,32 @@ class SIRBatch:
         else:
             self._graph.replay()
 
-    def run(self, use_graph=True):
-        """All ``steps`` steps of every instance."""
+    def run(self, use_graph=True, check=True):
+        """All ``steps`` steps of every instance; with ``check`` (default) waits for them
+        and raises on bad inputs (:meth:`check`)."""
         if use_graph:
             if self._graph is None or self._graph_steps != self.steps:
                 self.capture(self.steps)
             self.replay()
         else:
             self.launch(self.steps)
+        if check:
+            self.check()
+
+    def status(self):
+        """Status bits (``STATUS_*``) the inputs and runs since the last :meth:`reset`
+        raised (synchronises with the device)."""
+        bits = int(self._status.item())
+        if self.resident_ok:
+            bits |= int(self.res_status.item())
+        return bits
 
     def check(self):
+        """Raise if a list overflowed or an input was bad (oversize instance, compartment
+        outside 0..2, CSR column outside its instance); each kind has its own message."""
         if self.changes is not None and changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed (workspace smaller than live agents)")
-        if self.resident_ok and int(self.res_status.item()) != 0:
-            raise RuntimeError("an SIR instance was larger than the resident path's capacity")
+        raise_status(self.status())
 
     def final_state(self, i):
         w_off = self._offsets[2]
@@ -397,6 +440,23 @@ class SIRBatch:
                       - 2 * (self.h_state0 == 2).sum())
         return (int(d["edges_scanned"].sum()), int(d["edges_pushed"].sum()), changes,
                 int(d["candidates"].sum()))
+
+    def threefry_blocks(self):
+        """Threefry2x32-20 blocks the completed run evaluated, from its counters:
+        2 per susceptible decision (the infection key split(split(coll_key, i)[0])), 1 per
+        infection draw, 3 per recovery decision (key and draw), 3 per instance-step for the
+        key chain (step key, collection key, next rng).  Recovery decisions are the
+        infected agents at the start of every step, read from the counts."""
+        d = self.desc.cpu().numpy().view(INSTANCE_DTYPE).reshape(-1)
+        counts = self.counts.reshape(self.k, self.steps, 3).cpu().numpy().astype(np.int64)
+        i0 = np.array([(self.h_state0[o:o + n] == 1).sum() for o, n in
+                       zip(self._offsets[2][:-1], self.n)], dtype=np.int64)
+        i_before = np.concatenate([i0[:, None], counts[:, :-1, 1]], axis=1)
+        rec = int(i_before.sum())
+        sus = int(d["candidates"].sum()) - rec
+        blocks = 2 * sus + int(d["draws"].sum()) + 3 * rec + 3 * int(d["t"].sum())
+        return {"blocks": blocks, "susceptible_decisions": sus, "recovery_decisions": rec,
+                "infection_draws": int(d["draws"].sum())}
 
     def live_agent_steps(self):
         """Agent-steps whose words the sweep reads: steps of an instance that start with at
@@ -458,14 +518,35 @@ def ensemble_spec(count=4096, n_lo=1_000, n_hi=100_000, seed=2, rate=200.0):
     return {"n": n, "beta": beta, "gamma": gamma, "arrival_s": arrivals, "seed": seeds}
 
 
-def rank_spec(count=4096, rank=0, full=4096):
-    """The first ``count`` members of the ensemble specification for one rank of a
-    multi-GPU run: every rank runs its own members (model, graph and infection seeds offset
-    by ``rank * full``), so ranks never share an instance and need no collective."""
-    spec = ensemble_spec(full)
+def partition_members(sizes, world):
+    """Member indices of each of ``world`` ranks: the members split so that every member
+    belongs to exactly one rank and the ranks' agent totals are balanced (largest member
+    first, each to the rank with the fewest agents so far; ties to the lower rank).  Each
+    rank's list is in ascending member order."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    world = int(world)
+    if world < 1:
+        raise ValueError("world must be at least 1")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.empty(sizes.size, dtype=np.int64)
+    for i in np.argsort(-sizes, kind="stable"):
+        r = int(np.argmin(load))
+        owner[i] = r
+        load[r] += sizes[i]
+    return [np.flatnonzero(owner == r) for r in range(world)]
+
+
+def rank_spec(count=4096, rank=0, world=1):
+    """This rank's share of the first ``count`` members of the ensemble specification in a
+    ``world``-rank run: the members are partitioned across the ranks, balanced by agents
+    (:func:`partition_members`), so every member runs on exactly one GPU and the ranks need
+    no collective.  Adds ``member``, the members' indices in the full specification."""
+    spec = ensemble_spec(4096 if count <= 4096 else count)
     spec = {k: v[:count].copy() for k, v in spec.items()}
-    spec["seed"] = spec["seed"] + int(rank) * int(full)
-    return spec
+    mine = partition_members(spec["n"], world)[int(rank)]
+    out = {k: v[mine].copy() for k, v in spec.items()}
+    out["member"] = mine
+    return out
 
 
 def build_instances(spec, m=4, initial_infected=0.001, workers=None):

@@ -29,9 +29,9 @@ import torch
 
 from . import _dev
 from . import _lib
-from .ensemble import (INSTANCE_DTYPE, RNG_WORD, TILE, changes_overflowed, changes_workspace,
-                       check_layout, launch_struct, model_rngs, tiles_for, unpack_words,
-                       word_bytes)
+from .ensemble import (INSTANCE_DTYPE, RNG_WORD, STATUS_BAD_COLUMN, STATUS_BAD_COMPARTMENT, TILE,
+                       changes_overflowed, changes_workspace, check_layout, launch_struct,
+                       model_rngs, raise_status, tiles_for, unpack_words, word_bytes)
 
 
 def work_table(slots, sizes, dummy, capacity, tile=TILE):
@@ -69,17 +69,39 @@ def order_table(slots, sizes, total):
 
 class _Group:
     """Device buffers shared by the requests admitted together; every request of the group
-    holds it, so the buffers are freed once the last of them has retired."""
-    __slots__ = ("bufs",)
+    holds it, so the buffers are freed once the last of them has retired.  ``h_status`` is
+    a pinned copy of the group's pack status (bad compartments or columns), written on the
+    server stream right after the pack."""
+    __slots__ = ("bufs", "h_status")
 
-    def __init__(self, bufs):
+    def __init__(self, bufs, h_status):
         self.bufs = bufs
+        self.h_status = h_status
+
+
+def input_error(req):
+    """The error of a request whose inputs the pack flagged (compartment outside 0..2 or a
+    CSR column outside 0..n-1), found on the host for that request alone; None if its own
+    inputs are fine (another request of its admission group was flagged)."""
+    st = np.asarray(req.state, dtype=np.int8)
+    col = np.asarray(req.col, dtype=np.int64)
+    bits = 0
+    if st.size and (st.min() < 0 or st.max() > 2):
+        bits |= STATUS_BAD_COMPARTMENT
+    if col.size and (col.min() < 0 or col.max() >= req.n):
+        bits |= STATUS_BAD_COLUMN
+    if not bits:
+        return None
+    try:
+        raise_status(bits, f"request {req.rid}")
+    except _lib.AbmError as err:
+        return err
 
 
 class Request:
     __slots__ = ("rid", "row_ptr", "col", "state", "beta", "gamma", "seed", "steps",
                  "arrival", "admitted", "finished", "counts", "final_state", "_slot",
-                 "_bufs", "_event", "keep_state")
+                 "_bufs", "_event", "keep_state", "error")
 
     def __init__(self, rid, row_ptr, col, state, beta, gamma, seed, steps, arrival=None,
                  keep_state=False):
@@ -92,6 +114,7 @@ class Request:
         self.counts = None
         self.final_state = None
         self.keep_state = keep_state
+        self.error = None  # AbmError when the request's inputs were bad (set at harvest)
         self._slot = None
         self._bufs = None
         self._event = None
@@ -231,10 +254,12 @@ class SIRServer:
         return free + torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
 
     def check(self):
+        """Raise if the change list overflowed or the resident kernel reported a bad
+        instance (bad inputs of single requests are reported on the request: ``error``)."""
         if changes_overflowed(self.changes):
             raise RuntimeError("SIR change list overflowed")
-        if self.resident and int(self.res_status.item()) != 0:
-            raise RuntimeError("a request was larger than the resident path's capacity")
+        if self.resident:
+            raise_status(int(self.res_status.item()), "SIR server (resident path)")
 
     def _admit(self):
         """Admit the longest prefix of the queue that fits (free slots, work-list tiles,
@@ -308,11 +333,13 @@ class SIRServer:
             d_work = h_work.to(dev, non_blocking=True)
             _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(d_work), work.shape[0],
                       _dev.ptr(st8), _dev.ptr(words), _dev.ptr(status), s.cuda_stream)
+            h_status = torch.zeros(1, dtype=torch.int32).pin_memory()
+            h_status.copy_(status, non_blocking=True)
             # staging buffers stay alive until the copies and the pack have run
             done_ev = torch.cuda.Event()
             done_ev.record(s)
         group = _Group((rp, col, st8, words, hubs, comp, counts, h_rows, h_work, d_work,
-                        status, done_ev))
+                        status, done_ev), h_status)
         now = time.perf_counter()
         for k, (req, slot) in enumerate(zip(picked, slots)):
             req._slot = slot
@@ -352,6 +379,10 @@ class SIRServer:
         for slot in finished:
             req = self.active.pop(slot)
             group, st, counts = req._bufs
+            # the request's last step ran after its group's pack, so the pinned status copy
+            # is in place
+            if int(group.h_status[0]):
+                req.error = input_error(req)
             with torch.cuda.stream(self.stream):
                 req.counts = torch.empty((req.steps, 3), dtype=torch.int32).pin_memory()
                 req.counts.copy_(counts.view(req.steps, 3), non_blocking=True)

@@ -171,3 +171,31 @@ void orc_sir_run(const int32_t* rp, const int32_t* col, int64_t n, int8_t* state
   rng[0] = r.a;
   rng[1] = r.b;
 }
+
+/* Many independent SIR models (an ensemble): the host threads take whole instances
+ * (largest first, dynamic schedule) and each instance runs orc_sir_run on its thread
+ * (the nested parallel loop inside runs with one thread), so small instances keep every
+ * core busy.  Arrays of per-instance pointers and parameters; rngs uint32[ninst][2] and
+ * states are updated in place as by orc_sir_run. */
+void orc_sir_run_many(int64_t ninst, const int32_t* const* rps, const int32_t* const* cols,
+                      const int64_t* ns, int8_t* const* states, uint32_t* rngs, int32_t steps,
+                      const float* betas, const float* gammas, int32_t* const* counts) {
+  int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (size_t)(ninst > 0 ? ninst : 1));
+  for (int64_t i = 0; i < ninst; ++i) order[i] = i;
+  for (int64_t i = 1; i < ninst; ++i) { /* insertion sort by size, descending */
+    const int64_t v = order[i];
+    int64_t j = i;
+    while (j > 0 && ns[order[j - 1]] < ns[v]) {
+      order[j] = order[j - 1];
+      --j;
+    }
+    order[j] = v;
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < ninst; ++k) {
+    const int64_t i = order[k];
+    orc_sir_run(rps[i], cols[i], ns[i], states[i], rngs + 2 * i, steps, betas[i], gammas[i],
+                counts[i]);
+  }
+  free(order);
+}

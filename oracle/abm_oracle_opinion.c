@@ -16,8 +16,55 @@
 #include <stdlib.h>
 #include <string.h>
 
-/* float32 forward with the GPU kernel's operation order (fmaf accumulation, multiply by
- * float32(1/tau)); differs from the GPU only by the last bits of expf. */
+/* float32 exponential by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2), 1989),
+ * every operation a single float32 operation rounded to nearest (built with
+ * -ffp-contract=off, so nothing is fused):
+ *   x clamped to [-87, 88]; N = rint(x * 32/ln2); r = (x - N L1) - N L2 with
+ *   L1 + L2 = ln2/32 (L1 of 11 significant bits: N L1 and x - N L1 are exact);
+ *   p = r + r^2 (1/2 + r/6)  (Taylor; |r| <= ln2/64);
+ *   exp(x) = 2^(N >> 5) (T[N & 31] + T[N & 31] p),  T[j] = 2^(j/32) rounded to float32;
+ * the scaling by 2^(N >> 5) adds to the exponent field (exact: the result stays normal). */
+static const float orc_exp2_tab[32] = {
+    0x1.000000p+0f, 0x1.059b0ep+0f, 0x1.0b5586p+0f, 0x1.11301ep+0f, 0x1.172b84p+0f,
+    0x1.1d4874p+0f, 0x1.2387a6p+0f, 0x1.29e9e0p+0f, 0x1.306fe0p+0f, 0x1.371a74p+0f,
+    0x1.3dea64p+0f, 0x1.44e086p+0f, 0x1.4bfdaep+0f, 0x1.5342b6p+0f, 0x1.5ab07ep+0f,
+    0x1.6247ecp+0f, 0x1.6a09e6p+0f, 0x1.71f75ep+0f, 0x1.7a1148p+0f, 0x1.82589ap+0f,
+    0x1.8ace54p+0f, 0x1.93737cp+0f, 0x1.9c4918p+0f, 0x1.a5503cp+0f, 0x1.ae89fap+0f,
+    0x1.b7f770p+0f, 0x1.c199bep+0f, 0x1.cb720ep+0f, 0x1.d5818ep+0f, 0x1.dfc974p+0f,
+    0x1.ea4afap+0f, 0x1.f50766p+0f};
+
+static float orc_expf_tang(float x) {
+  x = fminf(fmaxf(x, -87.0f), 88.0f);
+  const float nf = rintf(x * 0x1.715476p+5f);
+  const int32_t N = (int32_t)nf;
+  const float r = (x - nf * 0x1.62c000p-6f) - nf * 0x1.217f7ep-17f;
+  const float p = r + (r * r) * (0.5f + r * 0x1.555556p-3f);
+  const float t = orc_exp2_tab[N & 31];
+  const float e = t + t * p;
+  uint32_t bits;
+  memcpy(&bits, &e, 4);
+  bits += (uint32_t)(N >> 5) << 23;
+  float out;
+  memcpy(&out, &bits, 4);
+  return out;
+}
+
+static float orc_sigmoid32(float z) { return 1.0f / (1.0f + orc_expf_tang(-z)); }
+
+/* The exponential and the sigmoid over arrays, and the table (CPU checks). */
+void orc_expf_tang_array(const float* x, float* y, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) y[i] = orc_expf_tang(x[i]);
+}
+
+void orc_sigmoid32_array(const float* z, float* s, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) s[i] = orc_sigmoid32(z[i]);
+}
+
+void orc_exp2_table(float* out) { memcpy(out, orc_exp2_tab, sizeof(orc_exp2_tab)); }
+
+/* float32 forward: the fixed operation sequence of the model (see orc_expf_tang), per step
+ * and node i, instance b: d = o_j - o_i; z = (eps - |d|) * (1/tau); s = 1 / (1 + exp(-z));
+ * acc = acc + s * d over the CSR row in order; o_i' = o_i + mu * (acc / deg_i). */
 void orc_opinion_run_f32(float* o, const int32_t* rp, const int32_t* col, int64_t n, int32_t B,
                          const float* mu, const float* eps, const float* tau, int32_t steps) {
   float* nxt = (float*)malloc(sizeof(float) * (size_t)n * B);
@@ -25,20 +72,26 @@ void orc_opinion_run_f32(float* o, const int32_t* rp, const int32_t* col, int64_
   for (int b = 0; b < B; ++b) itau[b] = 1.0f / tau[b];
   float* cur = o;
   for (int32_t t = 0; t < steps; ++t) {
-#pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < n; ++i) {
-      const int32_t r0 = rp[i], r1 = rp[i + 1];
-      for (int b = 0; b < B; ++b) {
-        const float oi = cur[i * B + b];
-        float acc = 0.0f;
+#pragma omp parallel
+    {
+      float* acc = (float*)malloc(sizeof(float) * (size_t)B);
+#pragma omp for schedule(static)
+      for (int64_t i = 0; i < n; ++i) {
+        const int32_t r0 = rp[i], r1 = rp[i + 1];
+        const float* oi = cur + i * B;
+        for (int b = 0; b < B; ++b) acc[b] = 0.0f;
+        /* every instance accumulates its own sum in CSR order */
         for (int32_t e = r0; e < r1; ++e) {
-          const float d = cur[(int64_t)col[e] * B + b] - oi;
-          const float z = (eps[b] - fabsf(d)) * itau[b];
-          const float s = 1.0f / (1.0f + expf(-z));
-          acc = fmaf(s, d, acc);
+          const float* oj = cur + (int64_t)col[e] * B;
+          for (int b = 0; b < B; ++b) {
+            const float d = oj[b] - oi[b];
+            acc[b] = acc[b] + orc_sigmoid32((eps[b] - fabsf(d)) * itau[b]) * d;
+          }
         }
-        nxt[i * B + b] = (r1 > r0) ? fmaf(mu[b], acc / (float)(r1 - r0), oi) : oi;
+        for (int b = 0; b < B; ++b)
+          nxt[i * B + b] = (r1 > r0) ? oi[b] + mu[b] * (acc[b] / (float)(r1 - r0)) : oi[b];
       }
+      free(acc);
     }
     float* tmp = cur;
     cur = nxt;
@@ -56,19 +109,25 @@ void orc_opinion_run_f32(float* o, const int32_t* rp, const int32_t* col, int64_
 static void step_f64(const double* cur, double* nxt, const int32_t* rp, const int32_t* col,
                      int64_t n, int32_t B, const double* mu, const double* eps,
                      const double* tau) {
-#pragma omp parallel for schedule(static)
-  for (int64_t i = 0; i < n; ++i) {
-    const int32_t r0 = rp[i], r1 = rp[i + 1];
-    for (int b = 0; b < B; ++b) {
-      const double oi = cur[i * B + b];
-      double acc = 0.0;
+#pragma omp parallel
+  {
+    double* acc = (double*)malloc(sizeof(double) * (size_t)B);
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t r0 = rp[i], r1 = rp[i + 1];
+      const double* oi = cur + i * B;
+      for (int b = 0; b < B; ++b) acc[b] = 0.0;
       for (int32_t e = r0; e < r1; ++e) {
-        const double d = cur[(int64_t)col[e] * B + b] - oi;
-        const double s = 1.0 / (1.0 + exp(-(eps[b] - fabs(d)) / tau[b]));
-        acc += s * d;
+        const double* oj = cur + (int64_t)col[e] * B;
+        for (int b = 0; b < B; ++b) {
+          const double d = oj[b] - oi[b];
+          acc[b] += d / (1.0 + exp(-(eps[b] - fabs(d)) / tau[b]));
+        }
       }
-      nxt[i * B + b] = (r1 > r0) ? oi + mu[b] * acc / (double)(r1 - r0) : oi;
+      for (int b = 0; b < B; ++b)
+        nxt[i * B + b] = (r1 > r0) ? oi[b] + mu[b] * acc[b] / (double)(r1 - r0) : oi[b];
     }
+    free(acc);
   }
 }
 

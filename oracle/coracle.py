@@ -86,6 +86,27 @@ def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
     return st, counts, r
 
 
+def sir_run_many(graphs, states, rngs, steps, betas, gammas):
+    """Many SIR runs at once (``graphs`` [(row_ptr, col)], ``states`` int8 arrays, ``rngs``
+    uint32[k, 2]), the host threads taking whole instances.  Returns (final states, counts
+    int32[k, steps, 3], advanced rngs), each equal to ``sir_run`` of that instance."""
+    k = len(graphs)
+    rps = [np.ascontiguousarray(g[0], dtype=np.int32) for g in graphs]
+    cols = [np.ascontiguousarray(g[1], dtype=np.int32) for g in graphs]
+    sts = [np.array(s, dtype=np.int8, copy=True) for s in states]
+    r = np.array(rngs, dtype=np.uint32, copy=True).reshape(k, 2)
+    counts = np.zeros((k, steps, 3), dtype=np.int32)
+    ns = np.array([s.size for s in sts], dtype=np.int64)
+    vp = ctypes.c_void_p * max(k, 1)
+    lib().orc_sir_run_many(ctypes.c_int64(k), vp(*[a.ctypes.data for a in rps]),
+                           vp(*[a.ctypes.data for a in cols]), _p(ns),
+                           vp(*[a.ctypes.data for a in sts]), _p(r), ctypes.c_int32(steps),
+                           _p(np.ascontiguousarray(betas, dtype=np.float32)),
+                           _p(np.ascontiguousarray(gammas, dtype=np.float32)),
+                           vp(*[counts[i].ctypes.data for i in range(k)]))
+    return sts, counts, r
+
+
 def schelling_run(pos, types, W, H, coll_keys):
     """Schelling steps with the given per-step collection keys uint32[steps, 2].
     Returns (final positions, stats int32[steps, 2] = (unhappy, moved))."""
@@ -103,8 +124,30 @@ def _params(dtype, *arrs):
     return [np.ascontiguousarray(a, dtype=dtype) for a in arrs]
 
 
+def expf_tang(x):
+    """float32 exp by the oracle's table-driven method (the forward's exponential)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty_like(x)
+    lib().orc_expf_tang_array(_p(x), _p(y), ctypes.c_int64(x.size))
+    return y
+
+
+def sigmoid32(z):
+    """float32 sigmoid 1 / (1 + exp(-z)) exactly as the float32 forward evaluates it."""
+    z = np.ascontiguousarray(z, dtype=np.float32)
+    s = np.empty_like(z)
+    lib().orc_sigmoid32_array(_p(z), _p(s), ctypes.c_int64(z.size))
+    return s
+
+
+def exp2_table():
+    out = np.empty(32, np.float32)
+    lib().orc_exp2_table(_p(out))
+    return out
+
+
 def opinion_run_f32(o, row_ptr, col, mu, eps, tau, steps):
-    """Float32 forward (GPU operation order); o float32[n, B]."""
+    """Float32 forward (the model's fixed operation sequence); o float32[n, B]."""
     x = np.array(o, dtype=np.float32, copy=True, order="C")
     n, B = x.shape
     rp, cl = _params(np.int32, row_ptr, col)

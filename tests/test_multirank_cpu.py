@@ -1,6 +1,7 @@
-"""The multi-GPU path of the ensemble (instances sharded over ranks, no data-path
-collective; only the timing and unit reductions of the benchmark) with world_size 2 on the
-gloo backend, on CPU."""
+"""The multi-GPU path of the ensemble (the 4,096 members partitioned across ranks, balanced
+by agents, no data-path collective; only the timing and unit reductions of the benchmark)
+with world_size 2 on the gloo backend, on CPU.  Unmeasured on hardware: every GPU call of
+this build has one GPU."""
 
 import os
 import socket
@@ -22,8 +23,9 @@ def _worker(rank, world, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     from jaxabm_gb300 import ensemble
-    spec = ensemble.rank_spec(64, rank)
-    seeds = torch.tensor(spec["seed"], dtype=torch.int64)
+    spec = ensemble.rank_spec(4096, rank, world)
+    seeds = torch.full((4096,), -1, dtype=torch.int64)
+    seeds[:len(spec["seed"])] = torch.tensor(spec["seed"], dtype=torch.int64)
     gathered = [torch.zeros_like(seeds) for _ in range(world)]
     dist.all_gather(gathered, seeds)
     units = torch.tensor([float(spec["n"].sum() * 365)], dtype=torch.float64)
@@ -48,7 +50,26 @@ def test_two_rank_sharding_gloo():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert len(np.unique(seeds)) == len(seeds) == 128  # disjoint members
-    # both ranks run the same sizes (weak scaling), so the sum is twice one rank's units
-    assert units == pytest.approx(2 * n0.sum() * 365)
+    # the union of the ranks' members is every member exactly once
+    seeds = seeds[seeds >= 0]
+    assert len(seeds) == 4096 and np.array_equal(np.sort(seeds), np.arange(4096))
+    from jaxabm_gb300 import ensemble
+    full = ensemble.ensemble_spec(4096)
+    assert units == pytest.approx(full["n"].sum() * 365)  # all ranks together: the whole job
+    assert abs(n0.sum() - full["n"].sum() / 2) < full["n"].max()  # balanced by agents
     assert ms == 101.0  # the slowest rank defines the step time
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 8])
+def test_partition_covers_members_once(world):
+    from jaxabm_gb300 import ensemble
+    spec = ensemble.ensemble_spec(4096)
+    parts = ensemble.partition_members(spec["n"], world)
+    allm = np.concatenate(parts)
+    assert np.array_equal(np.sort(allm), np.arange(4096))
+    loads = np.array([spec["n"][p].sum() for p in parts])
+    assert loads.max() - loads.min() <= spec["n"].max()
+    for r in range(world):
+        rs = ensemble.rank_spec(4096, r, world)
+        assert np.array_equal(rs["member"], parts[r])
+        assert np.array_equal(rs["seed"], parts[r])

@@ -264,7 +264,8 @@ def test_sir_resident_builds_words_from_untagged_inputs(cuda):
     """The resident kernel builds each instance's words at step 0 from the int8
     compartments, so inputs copied in from the host (columns without hub tags, no pack)
     give the oracle's results; an out-of-range column (replaced by a self-loop) or
-    compartment (stored as R) is reported through the status word."""
+    compartment (stored as R) makes run() raise, each with its own code and message."""
+    from jaxabm_gb300 import _lib
     from jaxabm_gb300 import ensemble, sir
     graphs = [sir.barabasi_albert(3000, 8, 7), _graph("star", 500), sir.barabasi_albert(900, 4, 8)]
     n = [len(rp) - 1 for rp, _ in graphs]
@@ -289,18 +290,52 @@ def test_sir_resident_builds_words_from_untagged_inputs(cuda):
     bad_col[5] = 10_000_000
     bad_col[7] = -3
     b.load_host(h_rp, bad_col, h_st)
-    b.run()
-    torch.cuda.synchronize()
-    with pytest.raises(RuntimeError):
-        b.check()
-    b.res_status.zero_()
+    with pytest.raises(_lib.AbmError, match="CSR column points outside") as err:
+        b.run()
+    assert err.value.status == _lib.ABM_ERR_BOUNDS
+    assert b.status() == ensemble.STATUS_BAD_COLUMN
+    b.reset()
+    assert b.status() == 0
     bad_st = h_st.clone()
     bad_st[3] = 7
     b.load_host(h_rp, h_col, bad_st)
+    with pytest.raises(_lib.AbmError, match="compartment is outside 0..2") as err:
+        b.run()
+    assert err.value.status == _lib.ABM_ERR_BADARG
+    assert b.status() == ensemble.STATUS_BAD_COMPARTMENT
+    # good inputs again: the status is cleared and the run equals the oracle
+    b.load_host(h_rp, h_col, h_st)
+    b.reset()
     b.run()
-    torch.cuda.synchronize()
-    with pytest.raises(RuntimeError):
-        b.check()
+    for i in range(3):
+        rng, _ = models.model_keys(seeds[i], 1)
+        _, ref_counts, _ = coracle.sir_run(graphs[i][0], graphs[i][1], inits[i], rng, steps,
+                                           betas[i], gammas[i])
+        assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), i
+
+
+def test_sir_grid_path_reports_bad_inputs(cuda):
+    """The grid path's pack reports a bad column and a bad compartment of loaded inputs;
+    run() raises with the matching code, and the construction rejects both up front."""
+    from jaxabm_gb300 import _lib, ensemble, sir
+    graphs = [sir.barabasi_albert(800, 4, 3), sir.barabasi_albert(500, 4, 4)]
+    inits = [sir.initial_states(800, 0.02, 1), sir.initial_states(500, 0.02, 2)]
+    b = ensemble.SIRBatch(graphs, inits, [0.1, 0.1], [0.1, 0.1], [1, 2], 10, resident=False)
+    h_rp = torch.from_numpy(np.concatenate([rp for rp, _ in graphs]).astype(np.int32))
+    h_col = torch.from_numpy(np.concatenate([c for _, c in graphs]).astype(np.int32))
+    bad_col = h_col.clone()
+    bad_col[-1] = 500  # the second instance has agents 0..499
+    b.load_host(h_rp, bad_col, torch.from_numpy(b.h_state0.copy()))
+    with pytest.raises(_lib.AbmError) as err:
+        b.run()
+    assert err.value.status == _lib.ABM_ERR_BOUNDS
+    bad = [inits[0].copy(), inits[1]]
+    bad[0][10] = -1
+    with pytest.raises(ValueError, match="compartments"):
+        ensemble.SIRBatch(graphs, bad, [0.1, 0.1], [0.1, 0.1], [1, 2], 10, resident=False)
+    g2 = [graphs[0], (graphs[1][0], np.where(graphs[1][1] == 3, 9999, graphs[1][1]))]
+    with pytest.raises(ValueError, match="CSR column"):
+        ensemble.SIRBatch(g2, inits, [0.1, 0.1], [0.1, 0.1], [1, 2], 10, resident=False)
 
 
 @pytest.mark.parametrize("path", ["resident", "grid"])
@@ -335,3 +370,33 @@ def test_sir_reset_after_load_host_keeps_loaded_inputs(cuda, path):
                                                 betas[i], gammas[i])
         assert np.array_equal(b.counts_of(i).cpu().numpy(), ref_counts), (path, i)
         assert np.array_equal(b.final_state(i).cpu().numpy(), ref_st), (path, i)
+
+
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_sir_headline_ensemble_slice_matches_oracle(cuda, path):
+    """Members of the 4,096-instance benchmark ensemble (the first 64 and the largest, member
+    2461 with 99,619 agents; BA m=4, Sobol (beta, gamma), 365 steps): the GPU runs them as
+    one batch from the package's inputs, the C oracle runs each alone from the oracle's own
+    inputs; every per-step S/I/R count and every final compartment is bit-identical."""
+    from jaxabm_gb300 import ensemble
+    from oracle import workloads
+    spec = ensemble.ensemble_spec(4096)
+    idx = list(range(64)) + [int(np.argmax(spec["n"]))]
+    sub = {k: v[idx] for k, v in spec.items()}
+    graphs, inits = ensemble.build_instances(sub)
+    b = ensemble.SIRBatch(graphs, inits, sub["beta"], sub["gamma"], sub["seed"], 365,
+                          resident=(path == "resident"))
+    assert b.mode == path
+    b.run()
+    counts = b.counts.reshape(len(idx), 365, 3).cpu().numpy()
+    ospec = workloads.sir_ensemble_spec(4096)
+    members = workloads.sir_members(ospec, idx)
+    for k, i in enumerate(idx):
+        rp, col, st0 = members[k]
+        assert np.array_equal(rp, graphs[k][0]) and np.array_equal(st0, inits[k])
+        rng, _ = models.model_keys(int(ospec["seed"][i]), 1)
+        ref_st, ref_counts, _ = coracle.sir_run(rp, col, st0, rng, 365, float(ospec["beta"][i]),
+                                                float(ospec["gamma"][i]))
+        assert np.array_equal(counts[k], ref_counts), (path, i)
+        assert np.array_equal(b.final_state(k).cpu().numpy(), ref_st), (path, i)
+    assert int(b.n.max()) == int(spec["n"].max()) == 99_619
