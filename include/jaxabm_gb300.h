@@ -244,6 +244,21 @@ ABM_API int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_ite
                                int32_t nwork, const int8_t* states8, const uint8_t* words_base,
                                int32_t* status, void* stream);
 
+/* Adds the S, I and R totals of every instance's int8 compartments (laid out as for
+ * abm_sir_pack_batch) to its descriptor's num_s / num_i / num_r, which the caller zeroes
+ * first; compartments outside 0..2 are not counted.  Lets a server admit requests without
+ * counting their compartments on the host. */
+ABM_API int abm_sir_count_batch(abm_sir_instance* insts, const abm_work_item* work,
+                                int32_t nwork, const int8_t* states8, const uint8_t* words_base,
+                                void* stream);
+
+/* count independent copies on one stream, one cudaMemcpyAsync each (host to device when
+ * to_device is non-zero, else device to host): dst[k] <- src[k], bytes[k] bytes (0 skips the
+ * entry).  Host buffers should be page-locked for the copies to be asynchronous.  One call
+ * replaces a host loop of copy calls when a server admits or retires many requests. */
+ABM_API int abm_copy_segments(int64_t count, void* const* dst, const void* const* src,
+                              const size_t* bytes, int32_t to_device, void* stream);
+
 /* int8 compartments of n packed words. */
 ABM_API int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream);
 
@@ -368,12 +383,12 @@ ABM_API int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32
 /* B instances (B a power of two, 4 <= B <= 128) share one symmetric CSR graph; opinions
  * are interleaved o float32[n][B] (16-byte aligned); mu, eps, tau are float32[B].
  * Per step: o_i += mu * (sum_j sigmoid((eps - |o_j - o_i|) / tau) (o_j - o_i)) / deg_i.
- * The forward is a fixed sequence of float32 operations, each rounded to nearest with no
- * fused multiply-add: d = o_j - o_i; z = (eps - |d|) * (1 / tau); s = 1 / (1 + exp(-z));
- * acc = acc + s * d over the row in CSR order; o_i' = o_i + mu * (acc / deg_i); exp is the
- * table-driven method of Tang (ACM TOMS 15(2), 1989) with x clamped to [-87, 88] (see
- * abm_opinion_sigmoid).  Results are therefore reproducible bit for bit by any IEEE-754
- * float32 implementation of the same sequence.
+ * The forward is a fixed sequence of float32 operations, each rounded to nearest (fused
+ * multiply-adds only where written): d = o_j - o_i; z = (eps - |d|) * (1 / tau);
+ * s = 1 / (1 + exp(-z)); acc = fma(s, d, acc) over the row in CSR order;
+ * o_i' = fma(mu, acc / deg_i, o_i); exp is the table-driven method of Tang (ACM TOMS 15(2),
+ * 1989) with x clamped to [-87, 88] (see abm_opinion_sigmoid).  Results are therefore
+ * reproducible bit for bit by any IEEE-754 float32 implementation of the same sequence.
  * The reference trains such models with jit(grad(loss)) through its whole run loop
  * (jaxabm/analysis.py:494-522); these entry points give the forward pass, checkpoints and
  * the hand-written reverse pass. */
@@ -446,8 +461,12 @@ ABM_API int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx,
  * library until the process exits.  Limit: n <= 67,108,864 (2^26); larger n returns
  * ABM_ERR_BADARG (use abm_select_indices).  The first call on each device looks up the
  * array's device address (cudaGetSymbolAddress, with that device current); make that first
- * call before any stream capture.  All calls share the one array, so calls that overlap
- * on the GPU (other streams, other host threads) race: serialise them on one stream. */
+ * call before any stream capture.  The address is kept with the id of the CUDA context it
+ * belongs to; the first call in a new context of the device (after cudaDeviceReset, or
+ * once the primary context was destroyed and created again) looks it up again, so make
+ * that call outside any stream capture too.  All calls share the one array, so calls that
+ * overlap on the GPU (other streams, other host threads) race: serialise them on one
+ * stream. */
 ABM_API int abm_select_indices_noalloc(const uint8_t* mask, int64_t n, int32_t* out_idx,
                                        int64_t* count, void* stream);
 
@@ -462,7 +481,8 @@ ABM_API int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_byte
 #define ABM_REDUCE_MIN 2
 #define ABM_REDUCE_MAX 3
 ABM_API size_t abm_reduce_workspace_bytes(int64_t n);
-/* *out (device float) = op over x[0..n); sums accumulate in float64. */
+/* *out (device float) = op over x[0..n); sums accumulate in float64; min and max return
+ * NaN when any input is NaN (as jnp.min / jnp.max do). */
 ABM_API int abm_reduce_f32(const float* x, int64_t n, int op, float* out, void* workspace,
                            size_t workspace_bytes, void* stream);
 

@@ -154,8 +154,8 @@ def _evaluate_models(models, steps):
 
 
 class ModelCalibrator:
-    """Population-based calibration of model parameters (jaxabm/analysis.py:290-1580,
-    methods ``"es"``, ``"pso"`` and ``"cem"``).
+    """Calibration of model parameters (jaxabm/analysis.py:290-1580): gradient methods
+    ``"adam"`` and ``"sgd"`` and population methods ``"es"``, ``"pso"`` and ``"cem"``.
 
     The constructor, ``calibrate``, the loss functions, the robust evaluation (mean metrics
     over ``num_evaluation_runs`` runs with seeds ``randint(subkey, (), 0, 1_000_000)``,
@@ -165,13 +165,19 @@ class ModelCalibrator:
     chain advances in the reference's order) and, for SIR models, all of them run as one
     ensemble.  ``batched_evaluations`` counts the iterations that did.
 
-    Gradient methods (``"adam"``, ``"sgd"``: ``jit(grad)`` through ``model.run``) and the
-    reinforcement-learning methods are not provided: the differentiable model of this
-    engine calibrates through ``opinion.OpinionLoss`` (a ``torch.autograd.Function`` with the
-    hand-written adjoint), and the RL policies are not agent-step work.
+    Gradient methods follow ``_calibrate_gradient`` (jaxabm/analysis.py:1309-1394): the
+    loss of a run with ``ModelConfig(seed=42)`` and its gradient, an Adam (beta1 0.9, beta2
+    0.999, eps 1e-8) or SGD update, clipping to the bounds, a robust evaluation, history,
+    and early stopping on ``tolerance`` and ``patience``.  The reference differentiates
+    ``model.run`` with ``jit(grad(loss_fn))`` (:489-531); here the model must be
+    differentiable on the engine -- it provides ``final_metrics_vjp`` (``OpinionModel``: the
+    hand-written adjoint kernel with checkpoints) -- and the loss's derivative with respect
+    to the final metrics is taken on the host.  The reinforcement-learning and Bayesian
+    methods are not agent-step work and are not provided.
     """
 
     POPULATION_METHODS = ("es", "pso", "cem")
+    GRADIENT_METHODS = ("adam", "sgd")
 
     def __init__(self, model_factory, initial_params: Dict[str, float],
                  target_metrics: Dict[str, float], param_bounds=None, metrics_weights=None,
@@ -222,14 +228,13 @@ class ModelCalibrator:
     # -- setup (jaxabm/analysis.py:376-399, 533-597) --------------------------------------
 
     def _check_method(self):
-        if self.method not in self.POPULATION_METHODS:
-            known = ("adam", "sgd", "bayesian", "q_learning", "policy_gradient",
-                     "actor_critic", "multi_agent_rl", "dqn")
+        if self.method not in self.POPULATION_METHODS + self.GRADIENT_METHODS:
+            known = ("bayesian", "q_learning", "policy_gradient", "actor_critic",
+                     "multi_agent_rl", "dqn")
             if self.method in known:
                 raise NotImplementedError(
                     f"calibration method {self.method!r} is not provided by this engine; "
-                    f"population methods: {', '.join(self.POPULATION_METHODS)} (gradients of "
-                    "the opinion model: opinion.OpinionLoss)")
+                    f"methods: {', '.join(self.GRADIENT_METHODS + self.POPULATION_METHODS)}")
             raise ValueError(f"Unknown calibration method: {self.method}")
 
     def _setup_optimization_method(self):
@@ -237,7 +242,13 @@ class ModelCalibrator:
         n = len(self.params)
         init = torch.tensor([float(self.params[k]) for k in self._names()],
                             dtype=torch.float32)
-        if self.method == "es":
+        if self.method in self.GRADIENT_METHODS:
+            # jaxabm/analysis.py:524-531
+            self.adam_m = np.zeros(n)
+            self.adam_v = np.zeros(n)
+            self.adam_beta1, self.adam_beta2, self.adam_eps = 0.9, 0.999, 1e-8
+            self.adam_t = 0
+        elif self.method == "es":
             self.es_population_size, self.es_sigma, self.es_elite_ratio = 20, 0.1, 0.2
             (sub,) = self._split()
             pop = jr.normal(sub, (self.es_population_size, n)) * self.es_sigma
@@ -283,6 +294,45 @@ class ModelCalibrator:
                 raise ValueError(f"Unknown loss type: {self.loss_type}")
             loss += weight * metric_loss
         return loss
+
+    def _loss_gradient(self, metrics: Dict[str, float]) -> Dict[str, float]:
+        """d loss / d metric value of :meth:`_compute_loss` for each target metric present
+        (derivatives of the four loss types; |x| and the Huber kink use sign(x))."""
+        out = {}
+        for metric, target in self.target_metrics.items():
+            if metric not in metrics:
+                continue
+            r, w = metrics[metric] - target, self.metrics_weights[metric]
+            if self.loss_type == "mse":
+                d = 2.0 * r
+            elif self.loss_type == "mae":
+                d = float(np.sign(r))
+            elif self.loss_type == "huber":
+                d = r if abs(r) <= 1.0 else float(np.sign(r))
+            elif self.loss_type == "relative":
+                d = float(np.sign(r)) / (abs(target) + 1e-8)
+            else:
+                raise ValueError(f"Unknown loss type: {self.loss_type}")
+            out[metric] = w * d
+        return out
+
+    def loss_and_grad(self, params_flat):
+        """(loss, gradient float64[n_params]) of the reference's gradient objective at
+        ``params_flat``: the model built with ``ModelConfig(seed=42)``, run for
+        ``evaluation_steps`` steps, loss of the last value of each target metric (0 for a
+        metric the model does not report), differentiated through the model's adjoint."""
+        names = self._names()
+        params = {name: float(params_flat[i]) for i, name in enumerate(names)}
+        model = self.model_factory(params=params, config=ModelConfig(seed=42))
+        if not hasattr(model, "final_metrics_vjp"):
+            raise NotImplementedError(
+                f"gradient calibration needs a differentiable model (one with "
+                f"final_metrics_vjp, such as OpinionModel); {type(model).__name__} has none")
+        final, vjp = model.final_metrics_vjp(names, steps=self.evaluation_steps)
+        metrics = {m: float(final.get(m, 0.0)) for m in self.target_metrics}
+        loss = self._compute_loss(metrics)
+        grads = vjp(self._loss_gradient(metrics))
+        return float(loss), np.array([grads[name] for name in names], dtype=np.float64)
 
     def _compute_normalized_loss(self, metrics: Dict[str, float]) -> float:
         total = 0.0
@@ -348,9 +398,59 @@ class ModelCalibrator:
             print(f"Starting calibration with {self.method} method...")
             print(f"Target metrics: {self.target_metrics}")
             print(f"Parameter bounds: {self.param_bounds}")
-        return {"es": self._calibrate_evolution_strategies,
+        return {"adam": self._calibrate_gradient, "sgd": self._calibrate_gradient,
+                "es": self._calibrate_evolution_strategies,
                 "pso": self._calibrate_particle_swarm,
                 "cem": self._calibrate_cross_entropy}[self.method](verbose)
+
+    def _calibrate_gradient(self, verbose: bool) -> Dict[str, float]:
+        """Adam or SGD on the adjoint gradient (jaxabm/analysis.py:1309-1394)."""
+        names = self._names()
+        params_flat = np.array([float(self.params[k]) for k in names], dtype=np.float64)
+        no_improvement = 0
+        for it in range(self.max_iterations):
+            if verbose:
+                print(f"\nIteration {it + 1}/{self.max_iterations}")
+            _, grads = self.loss_and_grad(params_flat)
+            if np.any(np.isnan(grads)):
+                if verbose:
+                    print("NaN gradients detected, stopping optimization")
+                break
+            if self.method == "adam":
+                self.adam_t += 1
+                self.adam_m = self.adam_beta1 * self.adam_m + (1 - self.adam_beta1) * grads
+                self.adam_v = self.adam_beta2 * self.adam_v + (1 - self.adam_beta2) * grads ** 2
+                m_hat = self.adam_m / (1 - self.adam_beta1 ** self.adam_t)
+                v_hat = self.adam_v / (1 - self.adam_beta2 ** self.adam_t)
+                params_flat = params_flat - self.learning_rate * m_hat / (np.sqrt(v_hat)
+                                                                          + self.adam_eps)
+            else:
+                params_flat = params_flat - self.learning_rate * grads
+            for i, (lo, hi) in enumerate(self.param_bounds.values()):
+                params_flat[i] = min(max(params_flat[i], float(lo)), float(hi))
+            for i, name in enumerate(names):
+                self.params[name] = float(params_flat[i])
+            loss, ci = self._evaluate_params_robust(self.params)
+            self.param_history.append(dict(self.params))
+            self.loss_history.append(loss)
+            self.confidence_intervals.append(ci)
+            if loss < self.best_loss:
+                self.best_loss = loss
+                self.best_params = dict(self.params)
+                no_improvement = 0
+            else:
+                no_improvement += 1
+            if verbose:
+                print(f"Loss: {loss:.6f} (best: {self.best_loss:.6f})")
+            if loss < self.tolerance:
+                if verbose:
+                    print("Converged: loss below tolerance")
+                break
+            if no_improvement >= self.patience:
+                if verbose:
+                    print("Early stopping: no improvement")
+                break
+        return self.best_params
 
     def _elite_step(self, pop, verbose, iteration):
         scores = [loss for loss, _ in self._evaluate_population(self._rows(pop))]

@@ -7,9 +7,10 @@
 //   acc = sum_j s_j * d_j  (in CSR order);  o_i' = o_i + mu_b * (acc / deg_i)
 // which is the model o_i += mu * mean_j sigmoid((eps - |o_j - o_i|)/tau) (o_j - o_i).
 // The forward is exact float32 arithmetic in a fixed order: every operation is one IEEE-754
-// operation rounded to nearest (no contraction into fused multiply-adds), the sigmoid is
-// 1 / (1 + exp(-z)) with a correctly rounded reciprocal and the table-driven exponential
-// below, so the C oracle's float32 restatement of the same sequence gives the same bits.
+// operation rounded to nearest -- add, multiply, fused multiply-add (one rounding, written
+// out where it is used, never left to the compiler), correctly rounded reciprocal and
+// division -- and the sigmoid is 1 / (1 + exp(-z)) with the table-driven exponential below,
+// so the C oracle's float32 restatement of the same sequence gives the same bits.
 //
 // Adjoint (reverse mode, the gradient jax.grad of the reference's run loop would give,
 // jaxabm/analysis.py:494-522): with g(d) = s d and g'(d) = s - |d| s (1 - s) / tau,
@@ -53,20 +54,21 @@ constexpr float kExpC3 = 0x1.555556p-3f;  // 1 / 6
 
 // exp(x) in float32 by Tang's table-driven method (P. T. P. Tang, "Table-driven
 // implementation of the exponential function in IEEE floating-point arithmetic", ACM TOMS
-// 15(2), 1989): N = rint(x * 32 / ln 2); r = (x - N L1) - N L2 with L1 + L2 = ln 2 / 32 (L1
-// has 11 significant bits, so N L1 and x - N L1 are exact); exp(r) - 1 by its Taylor
-// polynomial r + r^2 (1/2 + r/6) (|r| <= ln 2 / 64: truncation error below 6e-10);
-// exp(x) = 2^(N >> 5) (T[N & 31] + T[N & 31] p).  x is clamped to [-87, 88], so every
-// intermediate is normal and the scaling is an exact add to the exponent field.  About 2 ulp
-// from exp over the clamped range.  T is kExp2Table staged in shared memory.
+// 15(2), 1989): N = rint(x * 32 / ln 2); r = fma(-N, L2, fma(-N, L1, x)) with
+// L1 + L2 = ln 2 / 32 (L1 has 11 significant bits, so x - N L1 is exact); exp(r) - 1 by its
+// Taylor polynomial p = fma(r^2, fma(r, 1/6, 1/2), r) (|r| <= ln 2 / 64: truncation error
+// below 6e-10); exp(x) = 2^(N >> 5) fma(T[N & 31], p, T[N & 31]).  x is clamped to
+// [-87, 88], so every intermediate is normal and the scaling is an exact add to the
+// exponent field.  About 1 ulp from exp over the clamped range.  T is kExp2Table staged in
+// shared memory.
 __device__ __forceinline__ float exp_table(float x, const float* T) {
   x = fminf(fmaxf(x, -87.0f), 88.0f);
   const float nf = rintf(__fmul_rn(x, kExpK));
   const int N = static_cast<int>(nf);
-  const float r = __fsub_rn(__fsub_rn(x, __fmul_rn(nf, kExpL1)), __fmul_rn(nf, kExpL2));
-  const float p = __fadd_rn(r, __fmul_rn(__fmul_rn(r, r), __fadd_rn(0.5f, __fmul_rn(r, kExpC3))));
+  const float r = __fmaf_rn(-nf, kExpL2, __fmaf_rn(-nf, kExpL1, x));
+  const float p = __fmaf_rn(__fmul_rn(r, r), __fmaf_rn(r, kExpC3, 0.5f), r);
   const float t = T[N & 31];
-  const float e = __fadd_rn(t, __fmul_rn(t, p));
+  const float e = __fmaf_rn(t, p, t);
   return __uint_as_float(__float_as_uint(e) + (static_cast<uint32_t>(N >> 5) << 23));
 }
 
@@ -107,7 +109,7 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
     for (int c = 0; c < 4; ++c) {
       const float d = __fsub_rn(oj[c], oi[c]);
       const float s = sigmoid_exact(__fmul_rn(__fsub_rn(ep[c], fabsf(d)), it[c]), T);
-      acc[c] = __fadd_rn(acc[c], __fmul_rn(s, d));
+      acc[c] = __fmaf_rn(s, d, acc[c]);
     }
   };
   int e = r0;
@@ -129,7 +131,7 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
   if (deg > 0) {
     const float fdeg = (float)deg;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) res[c] = __fadd_rn(oi[c], __fmul_rn(m[c], __fdiv_rn(acc[c], fdeg)));
+    for (int c = 0; c < 4; ++c) res[c] = __fmaf_rn(m[c], __fdiv_rn(acc[c], fdeg), oi[c]);
   }
   reinterpret_cast<float4*>(out + (size_t)node * B)[sub] = make_float4(res[0], res[1], res[2], res[3]);
 }
@@ -146,19 +148,28 @@ __global__ void opinion_sigmoid_kernel(const float* __restrict__ z, float* __res
     s[k] = sigmoid_exact(z[k], T);
 }
 
-// One adjoint step: lam_out from lam_in (= lambda^{t+1}) at the forward state o (= o^t);
-// gpart[cta][b][3] += this CTA's lambda * dF/d(mu, eps, tau).
+// One adjoint step over instance columns [c0, c0 + 4 LPN): lam_out from lam_in
+// (= lambda^{t+1}) at the forward state o (= o^t); gpart[cta][b][3] += this CTA's lambda *
+// dF/d(mu, eps, tau).  A launch covers at most kAdjCols columns, so the opinion and adjoint
+// rows it gathers (kAdjCols floats per node each) stay in L2 across the step.
 template <int LPN>
 __global__ void __launch_bounds__(kOpThreads, 4)
 opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ lam_in,
                        float* __restrict__ lam_out, const int32_t* __restrict__ rp,
                        const int32_t* __restrict__ col, const float* __restrict__ inv_deg, int n,
-                       int B, const float* __restrict__ mu, const float* __restrict__ eps,
+                       int B, int c0, const float* __restrict__ mu, const float* __restrict__ eps,
                        const float* __restrict__ tau, double* __restrict__ gpart) {
   extern __shared__ float sg[];  // [kOpThreads][12]: this thread's 4 instances x 3 params
   const long long g = (long long)blockIdx.x * kOpThreads + threadIdx.x;
   const int node = (int)(g / LPN);
   const int sub = (int)(g % LPN);
+  // this launch's columns: rows are read from column c0 on
+  o += c0;
+  lam_in += c0;
+  lam_out += c0;
+  mu += c0;
+  eps += c0;
+  tau += c0;
   float gm[4] = {0.f, 0.f, 0.f, 0.f}, ge[4] = {0.f, 0.f, 0.f, 0.f}, gt[4] = {0.f, 0.f, 0.f, 0.f};
   if (node < n) {
     float m[4], ep[4], it[4], oi[4], li[4], li_d[4];
@@ -238,9 +249,9 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     const int s_ = q / 12, v = q % 12;
     float acc = 0.0f;
     for (int k = 0; k < kNodes; ++k) acc += sg[(size_t)(k * LPN + s_) * 12 + v];
-    // v: param*4 + component; instance b = 4*s_ + component
+    // v: param*4 + component; instance b = c0 + 4*s_ + component
     const int param = v / 4, c = v % 4;
-    const int b = 4 * s_ + c;
+    const int b = c0 + 4 * s_ + c;
     gpart[((size_t)blockIdx.x * B + b) * 3 + param] += (double)acc;
   }
 }
@@ -310,6 +321,11 @@ __global__ void inv_degree_kernel(const int32_t* __restrict__ rp, int n, float* 
 }
 
 bool valid_batch(int B) { return B >= 4 && B <= 128 && (B & (B - 1)) == 0; }
+
+// Instance columns per adjoint launch (a step of a wider batch is several launches).
+constexpr int kAdjCols = 32;
+
+int adjoint_cols(int B) { return B < kAdjCols ? B : kAdjCols; }
 
 int step_blocks(int64_t n, int B) {
   const long long threads = n * (long long)(B / 4);
@@ -441,7 +457,7 @@ int abm_opinion_adjoint_init(const float* o, int64_t n, int32_t B, const double*
 
 size_t abm_opinion_grad_workspace_bytes(int64_t n, int32_t B) {
   if (n <= 0 || !valid_batch(B)) return 0;
-  return (size_t)step_blocks(n, B) * B * 3 * sizeof(double);
+  return (size_t)step_blocks(n, adjoint_cols(B)) * B * 3 * sizeof(double);
 }
 
 int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out,
@@ -460,19 +476,24 @@ int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out
       !abm_host::aligned(grad_partials, 8))
     return ABM_ERR_WORKSPACE;
   cudaStream_t s = abm_host::as_stream(stream);
-  const int lpn = B / 4;
-  const int blocks = step_blocks(n, B);
+  const int cols = adjoint_cols(B);
+  const int lpn = cols / 4;
+  const int blocks = step_blocks(n, cols);
   const size_t smem = (size_t)kOpThreads * 12 * sizeof(float);
-  ABM_OP_DISPATCH(opinion_adjoint_kernel, lpn, blocks, smem, s, o, lam_in, lam_out, row_ptr, col,
-                  inv_deg, (int)n, B, mu, eps, tau, grad_partials);
-  return abm_host::check_launch("abm_opinion_adjoint_step");
+  for (int c0 = 0; c0 < B; c0 += cols) {
+    ABM_OP_DISPATCH(opinion_adjoint_kernel, lpn, blocks, smem, s, o, lam_in, lam_out, row_ptr,
+                    col, inv_deg, (int)n, B, c0, mu, eps, tau, grad_partials);
+    const int st = abm_host::check_launch("abm_opinion_adjoint_step");
+    if (st) return st;
+  }
+  return ABM_OK;
 }
 
 int abm_opinion_grad_reduce(const double* grad_partials, int64_t n, int32_t B, double* grads,
                             void* stream) {
   if (!grad_partials || !grads || n <= 0 || !valid_batch(B)) return ABM_ERR_BADARG;
   cudaStream_t s = abm_host::as_stream(stream);
-  const int parts = step_blocks(n, B);
+  const int parts = step_blocks(n, adjoint_cols(B));
   sum_partials_kernel<<<(B * 3 + 127) / 128, 128, 0, s>>>(grad_partials, parts, B * 3, 1.0, grads);
   return abm_host::check_launch("abm_opinion_grad_reduce");
 }

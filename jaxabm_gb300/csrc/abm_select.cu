@@ -173,23 +173,32 @@ __global__ void gather_rows_bytes(const uint8_t* __restrict__ src, const int32_t
 // ---- reductions -------------------------------------------------------------------------
 constexpr int kRedThreads = 256;
 
-// op: 0 sum, 1 mean, 2 min, 3 max.  Sums accumulate in double in a fixed tree.
+// min and max that return NaN when either operand is NaN (as jnp.min / jnp.max do; fmin
+// and fmax would drop it).
+__device__ __forceinline__ double nan_min(double a, double b) {
+  return (a != a || b != b) ? a + b : fmin(a, b);
+}
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return (a != a || b != b) ? a + b : fmax(a, b);
+}
+
+__device__ __forceinline__ double combine(int op, double a, double b) {
+  return op == 2 ? nan_min(a, b) : (op == 3 ? nan_max(a, b) : a + b);
+}
+
+// op: 0 sum, 1 mean, 2 min, 3 max.  Sums accumulate in double in a fixed tree; a NaN
+// anywhere makes every result NaN.
 __global__ void __launch_bounds__(kRedThreads)
 reduce_partial_kernel(const float* __restrict__ x, int64_t n, int op, double* __restrict__ part) {
   __shared__ double s[kRedThreads];
   double acc = (op == 2) ? INFINITY : (op == 3 ? -INFINITY : 0.0);
   for (int64_t i = blockIdx.x * (int64_t)kRedThreads + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * kRedThreads) {
-    const double v = x[i];
-    acc = op == 2 ? fmin(acc, v) : (op == 3 ? fmax(acc, v) : acc + v);
-  }
+       i += (int64_t)gridDim.x * kRedThreads)
+    acc = combine(op, acc, static_cast<double>(x[i]));
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int o = kRedThreads / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      const double a = s[threadIdx.x], b = s[threadIdx.x + o];
-      s[threadIdx.x] = op == 2 ? fmin(a, b) : (op == 3 ? fmax(a, b) : a + b);
-    }
+    if (threadIdx.x < o) s[threadIdx.x] = combine(op, s[threadIdx.x], s[threadIdx.x + o]);
     __syncthreads();
   }
   if (threadIdx.x == 0) part[blockIdx.x] = s[0];
@@ -199,8 +208,7 @@ __global__ void reduce_final_kernel(const double* __restrict__ part, int nparts,
                                     float* __restrict__ out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double acc = (op == 2) ? INFINITY : (op == 3 ? -INFINITY : 0.0);
-  for (int b = 0; b < nparts; ++b)
-    acc = op == 2 ? fmin(acc, part[b]) : (op == 3 ? fmax(acc, part[b]) : acc + part[b]);
+  for (int b = 0; b < nparts; ++b) acc = combine(op, acc, part[b]);
   if (op == 1) acc /= (double)n;
   *out = (float)acc;
 }
@@ -319,23 +327,57 @@ static __device__ __align__(256) unsigned char g_select_scratch[kNoAllocScratchB
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};  // context id of each address
 
-// Device address of g_select_scratch on the current device.  In host code the symbol names
-// a host-side stand-in, so the address must come from the runtime: looked up once per
-// device (with that device current) and cached.
+// Unique id of the calling thread's current CUDA context (the driver's cuCtxGetCurrent and
+// cuCtxGetId, reached through the runtime's entry-point query, so the library links only
+// the runtime).  Ids are never reused, so a context torn down and created again (for example
+// after cudaDeviceReset) has a new id.  0 when the driver cannot say.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_noalloc_mu
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0) return id;
+  return 0;
+}
+
+// Device address of g_select_scratch in the current device's context.  In host code the
+// symbol names a host-side stand-in, so the address must come from the runtime: looked up
+// with that device current, and cached with the id of the context it belongs to.  A call
+// in another context of the device (the primary context was reset and created again) looks
+// the address up again, so no call writes through an address of a destroyed context.
 int noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return abm_host::record_cuda_error(e, "abm_select_indices_noalloc/device");
   if (dev < 0 || dev >= kNoAllocMaxDevices) return ABM_ERR_BADARG;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
+  const unsigned long long ctx = current_context_id();  // 0 before the context is current
+  if (g_noalloc_addr[dev] == nullptr || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_select_scratch);
+    e = cudaGetSymbolAddress(&p, g_select_scratch);  // makes the primary context current
     if (e != cudaSuccess || p == nullptr)
       return abm_host::record_cuda_error(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
                                          "abm_select_indices_noalloc/cudaGetSymbolAddress");
     g_noalloc_addr[dev] = p;
+    g_noalloc_ctx[dev] = current_context_id();
   }
   *out = g_noalloc_addr[dev];
   return ABM_OK;

@@ -863,6 +863,41 @@ __global__ void sir_pack_comp_tiles_kernel(const abm_sir_instance* __restrict__ 
   }
 }
 
+// S, I and R totals of every instance from its int8 compartments (the descriptors'
+// num_s/num_i/num_r, zeroed by the caller): per tile and CTA in shared memory, then one
+// atomic add per compartment.  Compartments outside 0..2 are not counted (the pack reports
+// them).
+__global__ void sir_count_tiles_kernel(abm_sir_instance* __restrict__ insts,
+                                       const int4* __restrict__ work, int nwork,
+                                       const int8_t* __restrict__ states8,
+                                       const uint8_t* __restrict__ words_base) {
+  __shared__ int sc[3];
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+    if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const int4 item = work[w];
+    abm_sir_instance* I = insts + item.x;
+    const int8_t* st = states8 + (I->words - words_base);
+    int c[3] = {0, 0, 0};
+    for (int i = item.y + threadIdx.x; i < item.z; i += blockDim.x) {
+      const int v = st[i];
+      if (v >= 0 && v <= 2) ++c[v];
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int tot = __reduce_add_sync(kFull, c[q]);
+      if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&sc[q], tot);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (sc[0]) atomicAdd(&I->num_s, sc[0]);
+      if (sc[1]) atomicAdd(&I->num_i, sc[1]);
+      if (sc[2]) atomicAdd(&I->num_r, sc[2]);
+    }
+    __syncthreads();  // sc is reset for the next tile
+  }
+}
+
 __global__ void sir_unpack_kernel(const uint8_t* __restrict__ words, int n,
                                   int8_t* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1664,6 +1699,30 @@ int abm_sir_pack_batch(const abm_sir_instance* insts, const abm_work_item* work,
   sir_pack_count_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, s>>>(insts, w4, nwork,
                                                                           status);
   return abm_host::check_launch("abm_sir_pack_batch/count");
+}
+
+int abm_sir_count_batch(abm_sir_instance* insts, const abm_work_item* work, int32_t nwork,
+                        const int8_t* states8, const uint8_t* words_base, void* stream) {
+  if (!insts || !work || nwork <= 0 || !states8 || !words_base) return ABM_ERR_BADARG;
+  if (!abm_host::aligned(insts, 8) || !abm_host::aligned(work, 16)) return ABM_ERR_BADARG;
+  sir_count_tiles_kernel<<<default_grid(nwork), kSirThreads, 0, abm_host::as_stream(stream)>>>(
+      insts, reinterpret_cast<const int4*>(work), nwork, states8, words_base);
+  return abm_host::check_launch("abm_sir_count_batch");
+}
+
+int abm_copy_segments(int64_t count, void* const* dst, const void* const* src,
+                      const size_t* bytes, int32_t to_device, void* stream) {
+  if (count < 0 || (count > 0 && (!dst || !src || !bytes))) return ABM_ERR_BADARG;
+  cudaStream_t s = abm_host::as_stream(stream);
+  const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  for (int64_t k = 0; k < count; ++k) {
+    if (bytes[k] == 0) continue;
+    if (!dst[k] || !src[k]) return ABM_ERR_BADARG;
+    const int st = abm_host::record_cuda_error(cudaMemcpyAsync(dst[k], src[k], bytes[k], kind, s),
+                                               "abm_copy_segments");
+    if (st) return st;
+  }
+  return ABM_OK;
 }
 
 int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream) {

@@ -63,6 +63,7 @@ def raise_status(bits, where="SIR batch"):
 
 WORDS = INSTANCE_DTYPE.itemsize // 4
 RNG_WORD = INSTANCE_DTYPE.fields["rng"][1] // 4  # int32 column of rng[0]
+STEPS_WORD = INSTANCE_DTYPE.fields["steps"][1] // 4  # int32 column of steps
 
 
 def check_layout():

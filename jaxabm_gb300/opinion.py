@@ -103,6 +103,26 @@ class OpinionBatch:
         self.ckpts, self.ckpt_every, self.steps_done = ck, ckpt_every, steps
         return self.o
 
+    def forward_with_moments(self, steps):
+        """``steps`` forward steps from the initial state (no checkpoints), with the raw
+        moments after every step: float64[steps, B_user, 4]."""
+        self.reset()
+        dev = self.o.device
+        rows = torch.empty((steps, self.B, 4), dtype=torch.float64, device=dev)
+        ws = _dev.workspace(_lib.load().abm_opinion_moments_workspace_bytes(self.n, self.B))
+        cur, nxt = self.o, self.tmp
+        for t in range(steps):
+            _lib.call("abm_opinion_step", _dev.ptr(cur), _dev.ptr(nxt), _dev.ptr(self.rp),
+                      _dev.ptr(self.col), self.n, self.B, _dev.ptr(self.mu), _dev.ptr(self.eps),
+                      _dev.ptr(self.tau), _dev.stream_handle())
+            _lib.call("abm_opinion_moments", _dev.ptr(nxt), self.n, self.B, _dev.ptr(rows[t]),
+                      _dev.ptr(ws), ws.numel(), _dev.stream_handle())
+            cur, nxt = nxt, cur
+        if cur is not self.o:
+            self.o.copy_(cur)
+        self.ckpts, self.ckpt_every, self.steps_done = None, None, steps
+        return rows[:, :self.B_user]
+
     def moments(self, o=None):
         """Raw moments float64[B_user, 4] of the current (or given) state."""
         o = self.o if o is None else o
@@ -120,15 +140,23 @@ class OpinionBatch:
     def backward(self, target, grad_loss=None):
         """d loss_b / d (mu_b, eps_b, tau_b) -> float64[B_user, 3] after :meth:`forward`
         with checkpoints; ``grad_loss`` (float64[B_user]) scales each instance."""
-        if self.ckpts is None:
-            raise RuntimeError("forward(steps, ckpt_every) must run first")
         dev = self.o.device
-        T, k = self.steps_done, self.ckpt_every
         m = self.moments()
         t = torch.as_tensor(target, dtype=torch.float64, device=dev).reshape(-1, 4)
         dldm = 0.5 * (m - t)
         if grad_loss is not None:
             dldm = dldm * torch.as_tensor(grad_loss, dtype=torch.float64, device=dev).reshape(-1, 1)
+        return self.backward_moments(dldm)
+
+    def backward_moments(self, dldm):
+        """Vector-Jacobian product of the final raw moments: given d loss_b / d m_k
+        (float64[B_user, 4]) after :meth:`forward` with checkpoints, returns
+        d loss_b / d (mu_b, eps_b, tau_b) as float64[B_user, 3] by the reverse sweep."""
+        if self.ckpts is None:
+            raise RuntimeError("forward(steps, ckpt_every) must run first")
+        dev = self.o.device
+        T, k = self.steps_done, self.ckpt_every
+        dldm = torch.as_tensor(dldm, dtype=torch.float64, device=dev).reshape(-1, 4)
         dl = torch.zeros((self.B, 4), dtype=torch.float64, device=dev)
         dl[:self.B_user] = dldm
         lam = torch.empty_like(self.o)
@@ -188,9 +216,11 @@ class OpinionLoss(torch.autograd.Function):
 # ---- single-model API --------------------------------------------------------------------
 
 class OpinionKernel(StepKernel):
+    """Registered step of ``OpinionAgent``.  Metrics ``m1``..``m4``: the raw moments
+    mean_i o_i^k of the opinions after each step (float64 accumulation)."""
     name = "opinion"
     attributes = ("opinion",)
-    metrics = ()
+    metrics = ("m1", "m2", "m3", "m4")
     params = {"mu": 0.3, "eps": 0.2, "tau": 0.02}
 
     def init(self, n, init_key, params, env):
@@ -201,11 +231,12 @@ class OpinionKernel(StepKernel):
         steps = coll_keys.reshape(-1, 2).shape[0]
         b = OpinionBatch(env["network_row_ptr"], env["network_col"], states["opinion"],
                          [params["mu"]], [params["eps"]], [params["tau"]])
-        b.forward(steps)
-        return {"opinion": b.o[:, 0].contiguous()}, None
+        rows = b.forward_with_moments(steps)
+        return {"opinion": b.o[:, 0].contiguous()}, rows[:, 0, :]
 
     def step(self, states, coll_key, params, env):
-        return self.run(states, coll_key.reshape(1, 2), params, env)
+        new, rows = self.run(states, coll_key.reshape(1, 2), params, env)
+        return new, rows[0]
 
 
 class OpinionAgent(Agent):
@@ -220,18 +251,69 @@ register_step(OpinionAgent, OpinionKernel())
 
 class OpinionModel(Model):
     """Parameters: ``n`` (2^18), ``degree`` (16, random regular graph), ``mu``, ``eps``,
-    ``tau``, ``steps`` (200), ``seed``."""
+    ``tau``, ``steps`` (200), ``seed`` (initial opinions), ``graph_seed`` (the graph;
+    default ``seed``).  Metrics ``m1``..``m4``: raw opinion moments after each step.
+
+    Differentiable: :meth:`final_metrics_vjp` gives the moments after ``steps`` steps and
+    their vector-Jacobian product with respect to ``mu``, ``eps``, ``tau`` (the hand-written
+    adjoint), which ``ModelCalibrator(method="adam" | "sgd")`` uses in place of the
+    reference's ``jit(grad(loss))`` through ``model.run`` (jaxabm/analysis.py:489-531)."""
+
+    DIFFERENTIABLE = ("mu", "eps", "tau")
 
     def setup(self):
         from .sir import random_regular
         n = int(self.p.get("n", 1 << 18))
-        rp, col = random_regular(n, int(self.p.get("degree", 16)), int(self.seed))
+        rp, col = random_regular(n, int(self.p.get("degree", 16)),
+                                 int(self.p.get("graph_seed", self.seed)))
         self.network = Network(self)
         self.network.from_csr(rp, col)
         self.agents = self.add_agents(n, OpinionAgent, name="people",
                                       mu=float(self.p.get("mu", 0.3)),
                                       eps=float(self.p.get("eps", 0.2)),
                                       tau=float(self.p.get("tau", 0.02)))
+
+
+    def final_metrics_vjp(self, names, steps=None, ckpt_every=20):
+        """(metrics, vjp) of a run of ``steps`` steps (default: the model's): ``metrics``
+        maps ``m1``..``m4`` to the raw moments after the last step (the values ``run``
+        records last); ``vjp(dl_dmetrics)`` maps d loss / d metric (a dict, missing metrics
+        0) to d loss / d parameter for ``names`` (a subset of mu, eps, tau), by the adjoint
+        with a checkpoint every ``ckpt_every`` steps."""
+        bad = [k for k in names if k not in self.DIFFERENTIABLE]
+        if bad:
+            raise ValueError(f"parameters {bad} are not differentiable in OpinionModel "
+                             f"(differentiable: {', '.join(self.DIFFERENTIABLE)})")
+        if self._hooks() != (None, None):
+            raise ValueError("a model with Python step hooks has no adjoint")
+        from .core import ModelConfig
+        from .model import Model as JaxModel
+        steps = int(self.steps if steps is None else steps)
+        # set up and initialise exactly as run() does (same graph, key chain and states)
+        self.setup()
+        jm = JaxModel(params=self.p, config=ModelConfig(steps=steps, seed=self.seed))
+        for name, agent_list in self._agent_lists.items():
+            jm.add_agent_collection(name, agent_list.collection)
+        for name, value in self.env.state.items():
+            jm.add_env_state(name, value)
+        jm.initialize()
+        if len(jm.agent_collections) != 1:
+            raise ValueError("the adjoint covers models with one agent collection")
+        coll = next(iter(jm.agent_collections.values()))
+        if not isinstance(coll.kernel, OpinionKernel):
+            raise ValueError("the adjoint covers OpinionAgent collections")
+        par, env = coll.params, coll._env
+        b = OpinionBatch(env["network_row_ptr"], env["network_col"], coll.states["opinion"],
+                         [par["mu"]], [par["eps"]], [par["tau"]])
+        b.forward(steps, max(1, min(int(ckpt_every), steps)))
+        m = b.moments()[0].cpu().numpy()
+        metrics = {f"m{k + 1}": float(m[k]) for k in range(4)}
+
+        def vjp(dl_dmetrics):
+            d = np.array([[float(dl_dmetrics.get(f"m{k + 1}", 0.0)) for k in range(4)]])
+            g = b.backward_moments(d)[0].cpu().numpy()
+            return {k: float(g[self.DIFFERENTIABLE.index(k)]) for k in names}
+        return metrics, vjp
 
 
 def calibration_params(count=64, base=(0.3, 0.2, 0.02), spread=0.2, seed=0):

@@ -29,9 +29,10 @@ import torch
 
 from . import _dev
 from . import _lib
-from .ensemble import (INSTANCE_DTYPE, RNG_WORD, STATUS_BAD_COLUMN, STATUS_BAD_COMPARTMENT, TILE,
-                       changes_overflowed, changes_workspace, check_layout, launch_struct,
-                       model_rngs, raise_status, tiles_for, unpack_words, word_bytes)
+from .ensemble import (INSTANCE_DTYPE, RNG_WORD, STATUS_BAD_COLUMN, STATUS_BAD_COMPARTMENT,
+                       STEPS_WORD, TILE, changes_overflowed, changes_workspace, check_layout,
+                       launch_struct, model_rngs, raise_status, tiles_for, unpack_words,
+                       word_bytes)
 
 
 def work_table(slots, sizes, dummy, capacity, tile=TILE):
@@ -71,12 +72,38 @@ class _Group:
     """Device buffers shared by the requests admitted together; every request of the group
     holds it, so the buffers are freed once the last of them has retired.  ``h_status`` is
     a pinned copy of the group's pack status (bad compartments or columns), written on the
-    server stream right after the pack."""
-    __slots__ = ("bufs", "h_status")
+    server stream right after the pack; ``h_counts`` is the group's pinned result buffer
+    (every request's per-step counts at its offset)."""
+    __slots__ = ("bufs", "h_status", "h_counts")
 
-    def __init__(self, bufs, h_status):
+    def __init__(self, bufs, h_status, h_counts):
         self.bufs = bufs
         self.h_status = h_status
+        self.h_counts = h_counts
+
+
+def _host_span(a, dtype):
+    """(array, address, bytes) of host array ``a`` as a contiguous ``dtype`` array: ``a``
+    itself when it already is one (numpy or CPU tensor), else a converted copy, which the
+    caller keeps alive until the copies that read it were issued."""
+    if isinstance(a, torch.Tensor):
+        if a.is_cuda:
+            raise ValueError("request arrays must be host arrays")
+        want = {np.int32: torch.int32, np.int8: torch.int8}[dtype]
+        if a.dtype != want or not a.is_contiguous():
+            a = a.to(want).contiguous()
+        return a, a.data_ptr(), a.numel() * a.element_size()
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a, a.ctypes.data, a.nbytes
+
+
+def copy_segments(dst, src, nbytes, to_device, stream):
+    """One ``abm_copy_segments`` call for many copies (address lists as numpy uint64)."""
+    dst = np.ascontiguousarray(dst, dtype=np.uint64)
+    src = np.ascontiguousarray(src, dtype=np.uint64)
+    nbytes = np.ascontiguousarray(nbytes, dtype=np.uint64)
+    _lib.call("abm_copy_segments", dst.size, dst.ctypes.data, src.ctypes.data, nbytes.ctypes.data,
+              1 if to_device else 0, stream.cuda_stream)
 
 
 def input_error(req):
@@ -99,14 +126,20 @@ def input_error(req):
 
 
 class Request:
+    """One simulation request: a CSR network (``row_ptr`` int32[n+1], ``col`` int32[E]),
+    initial int8 compartments ``state``, parameters, model seed and steps.  Arrays are host
+    arrays (numpy or CPU tensors; page-locked tensors copy asynchronously), int32 / int8
+    and contiguous; they must stay unchanged until the request is admitted."""
     __slots__ = ("rid", "row_ptr", "col", "state", "beta", "gamma", "seed", "steps",
                  "arrival", "admitted", "finished", "counts", "final_state", "_slot",
-                 "_bufs", "_event", "keep_state", "error")
+                 "_bufs", "_event", "keep_state", "error", "_n", "_e", "cancelled")
 
     def __init__(self, rid, row_ptr, col, state, beta, gamma, seed, steps, arrival=None,
                  keep_state=False):
         self.rid = rid
         self.row_ptr, self.col, self.state = row_ptr, col, state
+        self._n = len(row_ptr) - 1
+        self._e = len(col)
         self.beta, self.gamma, self.seed, self.steps = float(beta), float(gamma), int(seed), int(steps)
         self.arrival = arrival
         self.admitted = None
@@ -115,16 +148,17 @@ class Request:
         self.final_state = None
         self.keep_state = keep_state
         self.error = None  # AbmError when the request's inputs were bad (set at harvest)
+        self.cancelled = False
         self._slot = None
         self._bufs = None
         self._event = None
 
     @property
     def n(self):
-        return len(self.row_ptr) - 1
+        return self._n
 
     def device_bytes(self):
-        n, e = self.n, len(self.col)
+        n, e = self._n, self._e
         # CSR; int8 compartments, word bytes, hub counts and 2-bit compartments (each padded
         # to 16 agents); per-step counts
         return 4 * (n + 1) + 4 * e + 6 * word_bytes(n) + word_bytes(n) // 4 + 12 * self.steps
@@ -198,6 +232,8 @@ class SIRServer:
         self.queue = collections.deque()
         self.retiring = []
         self.completed = []
+        self.cancelled = []  # requests withdrawn by cancel()
+        self._cancelling = []  # (slot, event): slots freed once their in-flight ticks ran
         self.ticks = 0
         self.launches = 0
         self._work_dirty = False
@@ -244,7 +280,7 @@ class SIRServer:
         self.queue.append(req)
 
     def _tiles(self, req):
-        return (req.n + TILE - 1) // TILE
+        return (req._n + TILE - 1) // TILE
 
     @staticmethod
     def free_bytes():
@@ -284,9 +320,9 @@ class SIRServer:
             self.queue.popleft()
         g = len(picked)
         dev, s = self.desc.device, self.stream
-        n = np.array([r.n for r in picked], dtype=np.int64)
-        e = np.array([len(r.col) for r in picked], dtype=np.int64)
-        steps = np.array([r.steps for r in picked], dtype=np.int64)
+        n = np.fromiter((r._n for r in picked), dtype=np.int64, count=g)
+        e = np.fromiter((r._e for r in picked), dtype=np.int64, count=g)
+        steps = np.fromiter((r.steps for r in picked), dtype=np.int64, count=g)
         wb = (n + 15) // 16 * 16
         rp_off = np.concatenate([[0], np.cumsum(n + 1)])
         col_off = np.concatenate([[0], np.cumsum(e)])
@@ -301,13 +337,21 @@ class SIRServer:
             hubs = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
             comp = torch.empty(int(w_off[-1]) // 16, dtype=torch.int32, device=dev)
             counts = torch.zeros(int(c_off[-1]), dtype=torch.int32, device=dev)
-            for k, r in enumerate(picked):
-                rp[rp_off[k]:rp_off[k + 1]].copy_(torch.as_tensor(r.row_ptr), non_blocking=True)
-                col[col_off[k]:col_off[k + 1]].copy_(torch.as_tensor(r.col), non_blocking=True)
-                st8[w_off[k]:w_off[k] + n[k]].copy_(torch.as_tensor(r.state), non_blocking=True)
+            # every request's three arrays in one call (one cudaMemcpyAsync each); converted
+            # copies stay referenced by `spans` until the call has issued every copy (a copy
+            # from pageable memory has read its source when the call returns)
+            spans = [(_host_span(r.row_ptr, np.int32), _host_span(r.col, np.int32),
+                      _host_span(r.state, np.int8)) for r in picked]
+            src = np.array([[a[1] for a in sp] for sp in spans], dtype=np.uint64)
+            nbytes = np.array([[a[2] for a in sp] for sp in spans], dtype=np.uint64)
+            if np.any(nbytes[:, 0] != 4 * (n + 1)) or np.any(nbytes[:, 1] != 4 * e) \
+                    or np.any(nbytes[:, 2] != n):
+                raise ValueError("a request's row_ptr, col and state disagree in size")
+            dst = np.stack([rp.data_ptr() + 4 * rp_off[:-1], col.data_ptr() + 4 * col_off[:-1],
+                            st8.data_ptr() + w_off[:-1]], axis=1).astype(np.uint64)
+            copy_segments(dst.reshape(-1), src.reshape(-1), nbytes.reshape(-1), True, s)
+            del spans
             rngs = model_rngs([r.seed for r in picked])
-        sizes = np.array([np.bincount(np.asarray(r.state, dtype=np.int8).astype(np.int64),
-                                      minlength=3)[:3] for r in picked], dtype=np.int32)
         rows = np.zeros(g, dtype=INSTANCE_DTYPE)
         rows["row_ptr"] = rp.data_ptr() + 4 * rp_off[:-1]
         rows["adj"] = col.data_ptr() + 4 * col_off[:-1]
@@ -320,17 +364,23 @@ class SIRServer:
         rows["steps"] = steps
         rows["beta"] = [r.beta for r in picked]
         rows["gamma"] = [r.gamma for r in picked]
-        rows["num_s"], rows["num_i"], rows["num_r"] = sizes[:, 0], sizes[:, 1], sizes[:, 2]
+        # num_s / num_i / num_r stay 0 here: abm_sir_count_batch adds them on the device
         work = np.concatenate([tiles_for(slot, int(nk)) for slot, nk in zip(slots, n)])
         self.done.numpy()[np.asarray(slots, dtype=np.int64)] = 0
-        h_rows = torch.from_numpy(rows.view(np.int32).reshape(g, -1).copy()).pin_memory()
-        h_work = torch.from_numpy(work).pin_memory()
+        h_rows = torch.empty((g, INSTANCE_DTYPE.itemsize // 4), dtype=torch.int32,
+                             pin_memory=True)
+        h_rows.numpy()[:] = rows.view(np.int32).reshape(g, -1)
+        h_work = torch.empty(work.shape, dtype=torch.int32, pin_memory=True)
+        h_work.numpy()[:] = work
+        h_counts = torch.empty(int(c_off[-1]), dtype=torch.int32, pin_memory=True)
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         with torch.cuda.stream(s):
             d_rows = h_rows.to(dev, non_blocking=True)
             d_rows[:, RNG_WORD:RNG_WORD + 2] = rngs
             self.desc.index_copy_(0, torch.as_tensor(slots, device=dev), d_rows)
             d_work = h_work.to(dev, non_blocking=True)
+            _lib.call("abm_sir_count_batch", _dev.ptr(self.desc), _dev.ptr(d_work),
+                      work.shape[0], _dev.ptr(st8), _dev.ptr(words), s.cuda_stream)
             _lib.call("abm_sir_pack_batch", _dev.ptr(self.desc), _dev.ptr(d_work), work.shape[0],
                       _dev.ptr(st8), _dev.ptr(words), _dev.ptr(status), s.cuda_stream)
             h_status = torch.zeros(1, dtype=torch.int32).pin_memory()
@@ -339,12 +389,11 @@ class SIRServer:
             done_ev = torch.cuda.Event()
             done_ev.record(s)
         group = _Group((rp, col, st8, words, hubs, comp, counts, h_rows, h_work, d_work,
-                        status, done_ev), h_status)
+                        status, done_ev), h_status, h_counts)
         now = time.perf_counter()
         for k, (req, slot) in enumerate(zip(picked, slots)):
             req._slot = slot
-            req._bufs = (group, words[w_off[k]:w_off[k] + n[k]],
-                         counts[c_off[k]:c_off[k + 1]])
+            req._bufs = (group, int(w_off[k]), int(c_off[k]))
             req.admitted = now
             self.active[slot] = req
             self._tiles_used += self._tiles(req)
@@ -373,28 +422,37 @@ class SIRServer:
         self._work_dirty = False
 
     def _harvest(self):
-        """Retire requests whose done flag is up: enqueue their result copies."""
+        """Retire requests whose done flag is up: their counts (and final states when kept)
+        are copied into their group's pinned result buffer, all of them in one call."""
         slots = np.fromiter(self.active.keys(), dtype=np.int64, count=len(self.active))
         finished = slots[self.done.numpy()[slots] == 1].tolist()
-        for slot in finished:
-            req = self.active.pop(slot)
-            group, st, counts = req._bufs
-            # the request's last step ran after its group's pack, so the pinned status copy
-            # is in place
-            if int(group.h_status[0]):
-                req.error = input_error(req)
+        if finished:
+            dst, src, nbytes = [], [], []
             with torch.cuda.stream(self.stream):
-                req.counts = torch.empty((req.steps, 3), dtype=torch.int32).pin_memory()
-                req.counts.copy_(counts.view(req.steps, 3), non_blocking=True)
-                if req.keep_state:
-                    req.final_state = torch.empty(req.n, dtype=torch.int8).pin_memory()
-                    req.final_state.copy_(unpack_words(st, req.n, self.stream), non_blocking=True)
+                for slot in finished:
+                    req = self.active.pop(slot)
+                    group, w0, c0 = req._bufs
+                    counts_dev, words_dev = group.bufs[6], group.bufs[3]
+                    req.counts = group.h_counts[c0:c0 + 3 * req.steps].view(req.steps, 3)
+                    dst.append(req.counts.data_ptr())
+                    src.append(counts_dev.data_ptr() + 4 * c0)
+                    nbytes.append(12 * req.steps)
+                    if req.keep_state:
+                        req.final_state = torch.empty(req.n, dtype=torch.int8, pin_memory=True)
+                        st = unpack_words(words_dev[w0:w0 + req.n], req.n, self.stream)
+                        req.final_state.copy_(st, non_blocking=True)
+                    # the request's last step ran after its group's pack, so the pinned
+                    # status copy is in place
+                    if int(group.h_status[0]):
+                        req.error = input_error(req)
+                    self.retiring.append(req)
+                    self._tiles_used -= self._tiles(req)
+                    self.free_slots.append(slot)
+                copy_segments(dst, src, nbytes, False, self.stream)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
-            req._event = ev
-            self.retiring.append(req)
-            self._tiles_used -= self._tiles(req)
-            self.free_slots.append(slot)
+            for req in self.retiring[len(self.retiring) - len(finished):]:
+                req._event = ev
             self._work_dirty = True
         still = []
         for req in self.retiring:
@@ -409,6 +467,7 @@ class SIRServer:
     def tick(self) -> None:
         """Admit what fits, advance every resident request by steps_per_tick steps, and
         harvest completions."""
+        self._free_cancelled_slots()
         self._harvest()
         self._admit()
         if self._work_dirty:
@@ -430,6 +489,44 @@ class SIRServer:
                 per_step = 3 if self.max_slots + 1 <= 256 else 4
                 self.launches += (per_step * self.steps_per_tick + 1
                                   + (self.steps_per_tick + 7) // 8)
+
+    def cancel(self, rid) -> bool:
+        """Withdraw request ``rid``: a queued request is dropped; an admitted one stops at
+        the next tick -- its descriptor's step count is set to 0 on the server stream, so no
+        kernel advances it any more, and its slot is reused once the ticks already enqueued
+        have run (their last writes to the slot are then done).  Returns whether ``rid``
+        was queued or running; cancelled requests go to ``cancelled`` without results."""
+        for req in list(self.queue):
+            if req.rid == rid:
+                self.queue.remove(req)
+                req.cancelled = True
+                self.cancelled.append(req)
+                return True
+        for slot, req in list(self.active.items()):
+            if req.rid == rid:
+                del self.active[slot]
+                with torch.cuda.stream(self.stream):
+                    self.desc[slot, STEPS_WORD] = 0
+                    ev = torch.cuda.Event()
+                    ev.record(self.stream)
+                req.cancelled = True
+                req._bufs = None
+                self.cancelled.append(req)
+                self._cancelling.append((slot, ev))
+                self._tiles_used -= self._tiles(req)
+                self._work_dirty = True
+                return True
+        return False
+
+    def _free_cancelled_slots(self):
+        still = []
+        for slot, ev in self._cancelling:
+            if ev.query():
+                self.done.numpy()[slot] = 0
+                self.free_slots.append(slot)
+            else:
+                still.append((slot, ev))
+        self._cancelling = still
 
     def idle(self) -> bool:
         return not (self.queue or self.active or self.retiring)

@@ -15,14 +15,25 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int orc_opinion_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
 
 /* float32 exponential by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2), 1989),
  * every operation a single float32 operation rounded to nearest (built with
- * -ffp-contract=off, so nothing is fused):
- *   x clamped to [-87, 88]; N = rint(x * 32/ln2); r = (x - N L1) - N L2 with
- *   L1 + L2 = ln2/32 (L1 of 11 significant bits: N L1 and x - N L1 are exact);
- *   p = r + r^2 (1/2 + r/6)  (Taylor; |r| <= ln2/64);
- *   exp(x) = 2^(N >> 5) (T[N & 31] + T[N & 31] p),  T[j] = 2^(j/32) rounded to float32;
+ * -ffp-contract=off, so only the fmaf calls written out are fused):
+ *   x clamped to [-87, 88]; N = rint(x * 32/ln2); r = fma(-N, L2, fma(-N, L1, x)) with
+ *   L1 + L2 = ln2/32 (L1 of 11 significant bits: x - N L1 is exact);
+ *   p = fma(r^2, fma(r, 1/6, 1/2), r)  (Taylor; |r| <= ln2/64);
+ *   exp(x) = 2^(N >> 5) fma(T[N & 31], p, T[N & 31]),  T[j] = 2^(j/32) rounded to float32;
  * the scaling by 2^(N >> 5) adds to the exponent field (exact: the result stays normal). */
 static const float orc_exp2_tab[32] = {
     0x1.000000p+0f, 0x1.059b0ep+0f, 0x1.0b5586p+0f, 0x1.11301ep+0f, 0x1.172b84p+0f,
@@ -37,10 +48,10 @@ static float orc_expf_tang(float x) {
   x = fminf(fmaxf(x, -87.0f), 88.0f);
   const float nf = rintf(x * 0x1.715476p+5f);
   const int32_t N = (int32_t)nf;
-  const float r = (x - nf * 0x1.62c000p-6f) - nf * 0x1.217f7ep-17f;
-  const float p = r + (r * r) * (0.5f + r * 0x1.555556p-3f);
+  const float r = fmaf(-nf, 0x1.217f7ep-17f, fmaf(-nf, 0x1.62c000p-6f, x));
+  const float p = fmaf(r * r, fmaf(r, 0x1.555556p-3f, 0.5f), r);
   const float t = orc_exp2_tab[N & 31];
-  const float e = t + t * p;
+  const float e = fmaf(t, p, t);
   uint32_t bits;
   memcpy(&bits, &e, 4);
   bits += (uint32_t)(N >> 5) << 23;
@@ -64,7 +75,7 @@ void orc_exp2_table(float* out) { memcpy(out, orc_exp2_tab, sizeof(orc_exp2_tab)
 
 /* float32 forward: the fixed operation sequence of the model (see orc_expf_tang), per step
  * and node i, instance b: d = o_j - o_i; z = (eps - |d|) * (1/tau); s = 1 / (1 + exp(-z));
- * acc = acc + s * d over the CSR row in order; o_i' = o_i + mu * (acc / deg_i). */
+ * acc = fma(s, d, acc) over the CSR row in order; o_i' = fma(mu, acc / deg_i, o_i). */
 void orc_opinion_run_f32(float* o, const int32_t* rp, const int32_t* col, int64_t n, int32_t B,
                          const float* mu, const float* eps, const float* tau, int32_t steps) {
   float* nxt = (float*)malloc(sizeof(float) * (size_t)n * B);
@@ -85,11 +96,11 @@ void orc_opinion_run_f32(float* o, const int32_t* rp, const int32_t* col, int64_
           const float* oj = cur + (int64_t)col[e] * B;
           for (int b = 0; b < B; ++b) {
             const float d = oj[b] - oi[b];
-            acc[b] = acc[b] + orc_sigmoid32((eps[b] - fabsf(d)) * itau[b]) * d;
+            acc[b] = fmaf(orc_sigmoid32((eps[b] - fabsf(d)) * itau[b]), d, acc[b]);
           }
         }
         for (int b = 0; b < B; ++b)
-          nxt[i * B + b] = (r1 > r0) ? oi[b] + mu[b] * (acc[b] / (float)(r1 - r0)) : oi[b];
+          nxt[i * B + b] = (r1 > r0) ? fmaf(mu[b], acc[b] / (float)(r1 - r0), oi[b]) : oi[b];
       }
       free(acc);
     }
@@ -166,16 +177,12 @@ void orc_opinion_moments_f64(const double* o, int64_t n, int32_t B, double* m) {
   }
 }
 
-/* Loss and its gradient w.r.t. (mu, eps, tau) per instance by the reverse sweep over the
- * stored float64 trajectory.  target: float64[4] (shared) ; loss float64[B]; grads [B][3]. */
-void orc_opinion_grad_f64(const double* o0, const int32_t* rp, const int32_t* col, int64_t n,
-                          int32_t B, const double* mu, const double* eps, const double* tau,
-                          int32_t steps, const double* target, double* loss, double* grads) {
+/* Loss and its gradient w.r.t. (mu, eps, tau) per instance by the float64 reverse sweep
+ * over a stored trajectory traj[(steps+1)][n][B] (float64; owned and freed here). */
+static void reverse_sweep_f64(double* traj, const int32_t* rp, const int32_t* col, int64_t n,
+                              int32_t B, const double* mu, const double* eps, const double* tau,
+                              int32_t steps, const double* target, double* loss, double* grads) {
   const size_t sz = (size_t)n * B;
-  double* traj = (double*)malloc(sizeof(double) * sz * (size_t)(steps + 1));
-  memcpy(traj, o0, sizeof(double) * sz);
-  for (int32_t t = 0; t < steps; ++t)
-    step_f64(traj + (size_t)t * sz, traj + (size_t)(t + 1) * sz, rp, col, n, B, mu, eps, tau);
   const double* oT = traj + (size_t)steps * sz;
   double* m = (double*)malloc(sizeof(double) * 4 * (size_t)B);
   orc_opinion_moments_f64(oT, n, B, m);
@@ -194,31 +201,43 @@ void orc_opinion_grad_f64(const double* o0, const int32_t* rp, const int32_t* co
       for (int k = 0; k < 4; ++k) w[k] = 0.5 * (m[4 * b + k] - target[k]);
       lam[i * B + b] = (w[0] + 2 * w[1] * x + 3 * w[2] * x * x + 4 * w[3] * x * x * x) / n;
     }
+  /* per-thread partial parameter gradients, summed in thread order after the sweep */
+  const int nthreads = orc_opinion_threads();
+  double* part = (double*)calloc((size_t)nthreads * 3 * B, sizeof(double));
   for (int32_t t = steps - 1; t >= 0; --t) {
     const double* o = traj + (size_t)t * sz;
-    for (int64_t i = 0; i < n; ++i) {
-      const int32_t r0 = rp[i], r1 = rp[i + 1];
-      const double di = (double)(r1 - r0);
-      for (int b = 0; b < B; ++b) {
-        const double oi = o[i * B + b], li = lam[i * B + b];
-        double sl = 0, sg = 0, se = 0, st = 0;
-        for (int32_t e = r0; e < r1; ++e) {
-          const int32_t j = col[e];
-          const double d = o[(int64_t)j * B + b] - oi, a = fabs(d);
-          const double z = (eps[b] - a) / tau[b];
-          const double s = 1.0 / (1.0 + exp(-z)), sp = s * (1 - s);
-          const double gp = s - a * sp / tau[b];
-          const double dj = (double)(rp[j + 1] - rp[j]);
-          sl += gp * (lam[(int64_t)j * B + b] / dj - li / di);
-          sg += s * d;
-          se += sp / tau[b] * d;
-          st += -sp * z / tau[b] * d;
-        }
-        lam2[i * B + b] = li + mu[b] * sl;
-        if (r1 > r0) {
-          grads[3 * b] += li * sg / di;
-          grads[3 * b + 1] += li * mu[b] * se / di;
-          grads[3 * b + 2] += li * mu[b] * st / di;
+#pragma omp parallel num_threads(nthreads)
+    {
+#ifdef _OPENMP
+      double* gp_part = part + (size_t)omp_get_thread_num() * 3 * B;
+#else
+      double* gp_part = part;
+#endif
+#pragma omp for schedule(static)
+      for (int64_t i = 0; i < n; ++i) {
+        const int32_t r0 = rp[i], r1 = rp[i + 1];
+        const double di = (double)(r1 - r0);
+        for (int b = 0; b < B; ++b) {
+          const double oi = o[i * B + b], li = lam[i * B + b];
+          double sl = 0, sg = 0, se = 0, st = 0;
+          for (int32_t e = r0; e < r1; ++e) {
+            const int32_t j = col[e];
+            const double d = o[(int64_t)j * B + b] - oi, a = fabs(d);
+            const double z = (eps[b] - a) / tau[b];
+            const double s = 1.0 / (1.0 + exp(-z)), sp = s * (1 - s);
+            const double gp = s - a * sp / tau[b];
+            const double dj = (double)(rp[j + 1] - rp[j]);
+            sl += gp * (lam[(int64_t)j * B + b] / dj - li / di);
+            sg += s * d;
+            se += sp / tau[b] * d;
+            st += -sp * z / tau[b] * d;
+          }
+          lam2[i * B + b] = li + mu[b] * sl;
+          if (r1 > r0) {
+            gp_part[3 * b] += li * sg / di;
+            gp_part[3 * b + 1] += li * mu[b] * se / di;
+            gp_part[3 * b + 2] += li * mu[b] * st / di;
+          }
         }
       }
     }
@@ -226,8 +245,53 @@ void orc_opinion_grad_f64(const double* o0, const int32_t* rp, const int32_t* co
     lam = lam2;
     lam2 = tmp;
   }
+  for (int th = 0; th < nthreads; ++th)
+    for (int q = 0; q < 3 * B; ++q) grads[q] += part[(size_t)th * 3 * B + q];
+  free(part);
   free(traj);
   free(m);
   free(lam);
   free(lam2);
+}
+
+/* Loss and gradient along the float64 trajectory from o0.  target: float64[4] (shared);
+ * loss float64[B]; grads [B][3]. */
+void orc_opinion_grad_f64(const double* o0, const int32_t* rp, const int32_t* col, int64_t n,
+                          int32_t B, const double* mu, const double* eps, const double* tau,
+                          int32_t steps, const double* target, double* loss, double* grads) {
+  const size_t sz = (size_t)n * B;
+  double* traj = (double*)malloc(sizeof(double) * sz * (size_t)(steps + 1));
+  memcpy(traj, o0, sizeof(double) * sz);
+  for (int32_t t = 0; t < steps; ++t)
+    step_f64(traj + (size_t)t * sz, traj + (size_t)(t + 1) * sz, rp, col, n, B, mu, eps, tau);
+  reverse_sweep_f64(traj, rp, col, n, B, mu, eps, tau, steps, target, loss, grads);
+}
+
+/* The same float64 reverse sweep along the float32 trajectory from o0 (the states the
+ * float32 forward visits, which is what a float32 adjoint differentiates): the float32
+ * states are computed by the float32 forward, widened to float64, and the sweep runs in
+ * float64 over them. */
+void orc_opinion_grad_f64_along_f32(const float* o0, const int32_t* rp, const int32_t* col,
+                                    int64_t n, int32_t B, const float* mu, const float* eps,
+                                    const float* tau, int32_t steps, const double* target,
+                                    double* loss, double* grads) {
+  const size_t sz = (size_t)n * B;
+  double* traj = (double*)malloc(sizeof(double) * sz * (size_t)(steps + 1));
+  float* cur = (float*)malloc(sizeof(float) * sz);
+  memcpy(cur, o0, sizeof(float) * sz);
+  double* mu64 = (double*)malloc(sizeof(double) * 3 * (size_t)B);
+  double* eps64 = mu64 + B;
+  double* tau64 = eps64 + B;
+  for (int b = 0; b < B; ++b) {
+    mu64[b] = mu[b];
+    eps64[b] = eps[b];
+    tau64[b] = tau[b];
+  }
+  for (int32_t t = 0; t <= steps; ++t) {
+    for (size_t q = 0; q < sz; ++q) traj[(size_t)t * sz + q] = cur[q];
+    if (t < steps) orc_opinion_run_f32(cur, rp, col, n, B, mu, eps, tau, 1);
+  }
+  free(cur);
+  reverse_sweep_f64(traj, rp, col, n, B, mu64, eps64, tau64, steps, target, loss, grads);
+  free(mu64);
 }

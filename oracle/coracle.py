@@ -188,3 +188,19 @@ def opinion_grad_f64(o0, row_ptr, col, mu, eps, tau, steps, target):
                                _p(m), _p(e), _p(t), ctypes.c_int32(steps), _p(tg), _p(loss),
                                _p(grads))
     return loss, grads
+
+
+def opinion_grad_f64_along_f32(o0, row_ptr, col, mu, eps, tau, steps, target):
+    """(loss float64[B], grads float64[B, 3]) by the float64 reverse sweep along the float32
+    trajectory (the states the float32 forward visits, widened to float64)."""
+    x = np.ascontiguousarray(o0, dtype=np.float32)
+    n, B = x.shape
+    rp, cl = _params(np.int32, row_ptr, col)
+    m, e, t = _params(np.float32, mu, eps, tau)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    loss = np.zeros(B)
+    grads = np.zeros((B, 3))
+    lib().orc_opinion_grad_f64_along_f32(_p(x), _p(rp), _p(cl), ctypes.c_int64(n),
+                                         ctypes.c_int32(B), _p(m), _p(e), _p(t),
+                                         ctypes.c_int32(steps), _p(tg), _p(loss), _p(grads))
+    return loss, grads

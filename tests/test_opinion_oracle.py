@@ -75,3 +75,36 @@ def test_c_forward_equals_numpy_statement(case):
     got = coracle.opinion_run_f64(o0, rp, col, mu, eps, tau, 20)
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-13)
     assert np.abs(ref - o0).max() > 1e-3  # opinions moved
+
+
+def test_exp_table_is_correctly_rounded():
+    """The 32 entries of the table-driven exponential are 2^(j/32) rounded to the nearest
+    float32 (checked with 50-digit decimal arithmetic)."""
+    from decimal import Decimal, getcontext
+    from fractions import Fraction
+    getcontext().prec = 50
+    ln2 = Decimal(2).ln()
+    table = coracle.exp2_table()
+    for j in range(32):
+        exact = Fraction((ln2 * j / 32).exp())
+        t = Fraction(float(table[j]))
+        half_ulp = Fraction(float(np.spacing(np.float32(table[j])))) / 2
+        assert abs(t - exact) <= half_ulp, j
+
+
+def test_exp_and_sigmoid_accuracy():
+    """The float32 exponential is within 1.05 ulp of exp on [-87, 88]; the sigmoid within
+    2e-7 relative for |z| <= 86; out-of-range and special inputs are clamped
+    (exp(x) for x < -87 is exp(-87), for x > 88 exp(88); NaN reads as -87)."""
+    x = np.linspace(-87, 88, 2_000_001).astype(np.float32)
+    y = coracle.expf_tang(x).astype(np.float64)
+    ref = np.exp(x.astype(np.float64))
+    assert (np.abs(y - ref) / np.spacing(ref.astype(np.float32))).max() < 1.05
+    z = np.linspace(-86, 86, 2_000_001).astype(np.float32)
+    s = coracle.sigmoid32(z).astype(np.float64)
+    sr = 1.0 / (1.0 + np.exp(-z.astype(np.float64)))
+    assert (np.abs(s - sr) / sr).max() < 2e-7
+    edge = coracle.expf_tang(np.array([-1000, -87, 88, 1000, np.nan, -np.inf, np.inf],
+                                      np.float32))
+    assert edge[0] == edge[1] == edge[4] == edge[5] and edge[2] == edge[3] == edge[6]
+    assert np.isfinite(edge).all()

@@ -138,3 +138,36 @@ def test_many_keys(nkeys, count):
     s = _u32(jr.split(dk, count))
     rs = np.stack([t.split(k, count, t.PARTITIONABLE) for k in keys])
     assert np.array_equal(s, rs)
+
+
+@pytest.mark.parametrize("partitionable", [True, False])
+@pytest.mark.parametrize("n,width,height,seed", [(58_982, 256, 256, 1), (1000, 7, 13, 0),
+                                                 (5, 1 << 20, 3, 42)])
+def test_grid_position_agents_matches_oracle(cuda, partitionable, n, width, height, seed):
+    """Grid.position_agents without positions (jaxabm/agentpy.py:496-527): x = randint(
+    PRNGKey(seed), (n,), 0, width) with the unsplit key and y = randint(split(key)[1], (n,),
+    0, height), equal to the oracle's randint; positions may coincide, as in the
+    reference."""
+    import jaxabm_gb300 as jx
+    from oracle import threefry as tf
+    mode = tf.PARTITIONABLE if partitionable else tf.LEGACY
+    jx.random.set_partitionable(partitionable)
+    try:
+        class M(jx.Model):
+            def setup(self):
+                self.walkers = self.add_agents(n, jx.RandomWalker, name="walkers")
+                self.grid = jx.Grid(self, (width, height))
+
+        m = M({"seed": seed})
+        m.setup()
+        m.grid.position_agents(m.walkers)
+        pos = m.walkers.collection._states["position"].cpu().numpy()
+    finally:
+        jx.random.set_partitionable(True)
+    key = tf.PRNGKey(seed)
+    x = tf.randint(key, (n,), 0, width, mode)
+    y = tf.randint(tf.split(key, 2, mode)[1], (n,), 0, height, mode)
+    assert pos.shape == (n, 2)
+    assert np.array_equal(pos[:, 0], x) and np.array_equal(pos[:, 1], y)
+    assert pos[:, 0].min() >= 0 and pos[:, 0].max() < width
+    assert pos[:, 1].min() >= 0 and pos[:, 1].max() < height

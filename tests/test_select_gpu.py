@@ -66,6 +66,20 @@ def test_reduce(cuda, op):
     np.testing.assert_allclose(out, ref, rtol=1e-6)
 
 
+@pytest.mark.parametrize("where", [0, 5, 77_777, 123_456])
+def test_reduce_propagates_nan(cuda, where):
+    """A NaN anywhere makes sum, mean, min and max NaN, as jnp.sum / mean / min / max do."""
+    from jaxabm_gb300.select import reduce
+    x = np.random.RandomState(1).randn(123_457).astype(np.float32)
+    x[where] = np.nan
+    d = torch.from_numpy(x).cuda()
+    for op in range(4):
+        assert np.isnan(float(reduce(d, op))), op
+    x[where] = 0.5  # without the NaN: ordinary results again
+    d = torch.from_numpy(x).cuda()
+    assert float(reduce(d, 2)) == x.min() and float(reduce(d, 3)) == x.max()
+
+
 def test_select_agentlist_api(cuda):
     import jaxabm_gb300 as jx
 

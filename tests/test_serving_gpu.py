@@ -99,3 +99,62 @@ def test_resident_server_rejects_oversize_request(cuda):
     rp, col = sir.barabasi_albert(1500, 4, 1)
     with pytest.raises(ValueError):
         srv.submit(Request(0, rp, col, sir.initial_states(1500, 0.01, 1), 0.1, 0.1, 1, 5))
+
+
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_bad_request_reports_its_error_and_others_finish(cuda, path):
+    """A request whose network has a column outside its agents, and one with a compartment
+    outside 0..2, each come back with an AbmError naming the fault; the other requests of
+    the same admission group finish with the oracle's results."""
+    from jaxabm_gb300 import _lib
+    from jaxabm_gb300.serving import SIRServer
+    reqs = _requests(6, seed0=300, steps=30)
+    bad_col = reqs[2]
+    bad_col.col = bad_col.col.copy()
+    bad_col.col[3] = bad_col.n + 5
+    bad_st = reqs[4]
+    bad_st.state = bad_st.state.copy()
+    bad_st.state[0] = 9
+    srv = SIRServer(max_slots=8, max_tiles=256, steps_per_tick=10, path=path)
+    for r in reqs:
+        srv.submit(r)
+    srv.drain()
+    done = {r.rid: r for r in srv.completed}
+    assert done[2].error is not None and done[2].error.status == _lib.ABM_ERR_BOUNDS
+    assert "CSR column" in str(done[2].error)
+    assert done[4].error is not None and "compartment" in str(done[4].error)
+    for rid in (0, 1, 3, 5):
+        r = done[rid]
+        assert r.error is None
+        rng, _ = models.model_keys(r.seed, 1)
+        _, ref_counts, _ = coracle.sir_run(r.row_ptr, r.col, r.state, rng, r.steps, r.beta,
+                                           r.gamma)
+        assert np.array_equal(r.counts.numpy(), ref_counts), rid
+
+
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_cancel_queued_and_running_requests(cuda, path):
+    """cancel() drops a queued request and stops a running one between ticks; its slot is
+    reused, and every other request still equals the oracle."""
+    from jaxabm_gb300.serving import SIRServer
+    reqs = _requests(8, seed0=400, steps=80)
+    srv = SIRServer(max_slots=3, max_tiles=64, steps_per_tick=5, path=path)
+    for r in reqs:
+        srv.submit(r)
+    srv.tick()
+    srv.tick()
+    running = next(iter(srv.active.values())).rid
+    queued = srv.queue[-1].rid
+    assert srv.cancel(running) and srv.cancel(queued)
+    assert not srv.cancel(10_000)
+    srv.drain()
+    assert sorted(r.rid for r in srv.cancelled) == sorted([running, queued])
+    assert all(r.cancelled for r in srv.cancelled)
+    finished = {r.rid: r for r in srv.completed}
+    assert set(finished) == {r.rid for r in reqs} - {running, queued}
+    for rid, r in finished.items():
+        rng, _ = models.model_keys(r.seed, 1)
+        ref_st, ref_counts, _ = coracle.sir_run(r.row_ptr, r.col, r.state, rng, r.steps, r.beta,
+                                                r.gamma)
+        assert np.array_equal(r.counts.numpy(), ref_counts), rid
+        assert np.array_equal(r.final_state.numpy(), ref_st), rid
