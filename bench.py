@@ -438,7 +438,8 @@ def model_lines():
         _lib.call("abm_schelling_place", _dev.ptr(p), _dev.ptr(t8), n, W, H, _dev.ptr(grid),
                   _dev.ptr(ca), _dev.ptr(status), None)
         _lib.call("abm_schelling_run", _dev.ptr(p), _dev.ptr(t8), n, W, H, _dev.ptr(grid),
-                  _dev.ptr(ca), _dev.ptr(ck), T, _dev.ptr(stats), _dev.ptr(ws), ws.numel(), None)
+                  _dev.ptr(ca), _dev.ptr(ck), T, 3, 8, _dev.ptr(stats), _dev.ptr(ws), ws.numel(),
+                  None)
     ms = _time_ms(sch, reps=3)
     out["schelling_256x256_t200"] = {"agent_steps_per_s": n * T / (ms / 1e3), "ms_per_run": ms,
                                      "launches_per_run": 3}

@@ -121,6 +121,22 @@ ABM_API int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* co
                        float sigma, float* means, void* workspace, size_t workspace_bytes,
                        void* stream);
 
+/* Batches of `members` independent random-walk models of n agents each, in one launch
+ * (the ensembles of Model.batch_run / SensitivityAnalysis.run, jaxabm/agentpy.py:1116-1152,
+ * jaxabm/analysis.py:97-165, which the reference runs one model after another): member m
+ * holds x, y at [m * n, (m + 1) * n), its init key init_keys[m] (uint32[members][2]), its
+ * collection keys coll_keys[m] (uint32[members][steps][2]), sigma sigmas[m] (device
+ * float32[members]) and means[m] (float32[members][steps][2]).  Every member's result
+ * equals abm_randomwalk_init / abm_randomwalk_run of that member alone, bit for bit.
+ * 1 <= members <= 65535. */
+ABM_API int abm_randomwalk_init_batch(float* x, float* y, int64_t n, int32_t members,
+                                      const uint32_t* init_keys, void* stream);
+ABM_API size_t abm_randomwalk_batch_workspace_bytes(int64_t n, int32_t steps, int32_t members);
+ABM_API int abm_randomwalk_run_batch(float* x, float* y, int64_t n, int32_t members,
+                                     const uint32_t* coll_keys, int32_t steps,
+                                     const float* sigmas, float* means, void* workspace,
+                                     size_t workspace_bytes, void* stream);
+
 /* ---- Network construction (HOST memory; native setup code) ------------------------- */
 /* Directed-entry count 2*m*(n-m) of a Barabasi-Albert graph, or -1 for bad sizes. */
 ABM_API int64_t abm_graph_ba_num_edges(int64_t n, int32_t m);
@@ -367,17 +383,46 @@ ABM_API int abm_schelling_place(const int32_t* pos, const int8_t* type, int64_t 
                                 void* stream);
 
 /* `steps` synchronous Schelling steps with per-step collection keys coll_keys
- * uint32[steps][2]: an agent is unhappy iff 8*same < 3*occupied over its Moore-8 torus
- * neighbours; each unhappy agent draws idx = min(floor(uniform(agent_key) * e), e - 1)
- * into the ascending list of the e pre-step empty cells and claims that cell; the lowest
- * claiming id moves.  pos, grid and cell_agent are updated in place; stats int32[steps][2]
- * receives (unhappy, moved) per step.  Replaces the vmapped Agent.step of the Schelling
- * model (examples/models/schelling_model.py:33-68, jaxabm/agent.py:168-177) with the
+ * uint32[steps][2]: an agent is unhappy iff thr_den*same < thr_num*occupied over its
+ * Moore-8 torus neighbours (same/occupied below the threshold thr_num/thr_den; the
+ * example's similarity_threshold, examples/models/schelling_model.py:36-40, as an exact
+ * fraction, 0 <= thr_num, 0 < thr_den, both <= 2^27); each unhappy agent draws
+ * idx = min(floor(uniform(agent_key) * e), e - 1) into the ascending list of the e
+ * pre-step empty cells and claims that cell; the lowest claiming id moves.  pos, grid and
+ * cell_agent are updated in place; stats int32[steps][2] receives (unhappy, moved) per
+ * step.  Replaces the vmapped Agent.step of the Schelling model
+ * (examples/models/schelling_model.py:33-68, jaxabm/agent.py:168-177) with the
  * neighbourhood rule and relocation it leaves as placeholders. */
 ABM_API int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, int32_t H,
                               int8_t* grid, int32_t* cell_agent, const uint32_t* coll_keys,
-                              int32_t steps, int32_t* stats, void* workspace,
-                              size_t workspace_bytes, void* stream);
+                              int32_t steps, int32_t thr_num, int32_t thr_den, int32_t* stats,
+                              void* workspace, size_t workspace_bytes, void* stream);
+
+/* One model of a Schelling batch (device descriptor, 8-byte aligned): its arrays as for
+ * abm_schelling_run (grid and cell_agent placed by abm_schelling_place), its key chain
+ * coll_keys uint32[steps][2], stats int32[steps][2], a workspace of
+ * abm_schelling_workspace_bytes(n, W, H) bytes (256-byte aligned, no set-up needed), n
+ * agents and its threshold. */
+typedef struct abm_schelling_member {
+  int32_t* pos;
+  const int8_t* type;
+  int8_t* grid;
+  int32_t* cell_agent;
+  const uint32_t* coll_keys;
+  int32_t* stats;
+  void* workspace;
+  int64_t n;
+  int32_t thr_num;
+  int32_t thr_den;
+} abm_schelling_member;
+
+/* `count` Schelling models of one W x H grid (W*H <= 2^18) in one launch, one
+ * thread-block cluster per model (the ensembles of Model.batch_run / SensitivityAnalysis,
+ * jaxabm/agentpy.py:1116-1152, jaxabm/analysis.py:97-165, which the reference runs one
+ * model after another).  Each model's result equals abm_schelling_run of it alone.
+ * members: device array of count descriptors (count <= 8191). */
+ABM_API int abm_schelling_run_batch(const abm_schelling_member* members, int32_t count,
+                                    int32_t W, int32_t H, int32_t steps, void* stream);
 
 /* ---- K8: differentiable bounded-confidence opinion model ---------------------------- */
 /* B instances (B a power of two, 4 <= B <= 128) share one symmetric CSR graph; opinions

@@ -46,6 +46,9 @@ SIGNATURES = {
     "abm_randomwalk_init": (_int, [_p, _p, _i64, _p, _p]),
     "abm_randomwalk_workspace_bytes": (_sz, [_i64, _i32]),
     "abm_randomwalk_run": (_int, [_p, _p, _i64, _p, _i32, _f32, _p, _p, _sz, _p]),
+    "abm_randomwalk_init_batch": (_int, [_p, _p, _i64, _i32, _p, _p]),
+    "abm_randomwalk_batch_workspace_bytes": (_sz, [_i64, _i32, _i32]),
+    "abm_randomwalk_run_batch": (_int, [_p, _p, _i64, _i32, _p, _i32, _p, _p, _p, _sz, _p]),
     "abm_graph_ba_num_edges": (_i64, [_i64, _i32]),
     "abm_graph_barabasi_albert": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
     "abm_graph_random_regular": (_int, [_i64, _i32, _u64, _p, _p, _i64]),
@@ -71,7 +74,9 @@ SIGNATURES = {
     "abm_sir_run": (_int, [_p, _p, _i64, _i64, _p, _p, _i32, _f32, _f32, _p, _p, _sz, _p]),
     "abm_schelling_workspace_bytes": (_sz, [_i64, _i32, _i32]),
     "abm_schelling_place": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _p]),
-    "abm_schelling_run": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _i32, _p, _p, _sz, _p]),
+    "abm_schelling_run": (_int, [_p, _p, _i64, _i32, _i32, _p, _p, _p, _i32, _i32, _i32, _p, _p,
+                                 _sz, _p]),
+    "abm_schelling_run_batch": (_int, [_p, _i32, _i32, _i32, _i32, _p]),
     "abm_opinion_run": (_int, [_p, _p, _p, _p, _i64, _i32, _p, _p, _p, _i32, _i32, _p, _p]),
     "abm_opinion_step": (_int, [_p, _p, _p, _p, _i64, _i32, _p, _p, _p, _p]),
     "abm_opinion_sigmoid": (_int, [_p, _p, _i64, _p]),

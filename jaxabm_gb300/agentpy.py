@@ -573,13 +573,25 @@ class Model:
         return results
 
     def batch_run(self, parameter_ranges: Dict[str, List[Any]], repetitions: int = 1):
-        """Every parameter combination, ``repetitions`` runs each (jaxabm/agentpy.py:1116-1152).
-        Batched SIR ensembles run on :mod:`jaxabm_gb300.ensemble` instead."""
+        """Every parameter combination, ``repetitions`` runs each (jaxabm/agentpy.py:1116-1152):
+        run ``r`` of a combination is ``self.__class__(params, seed=self.seed + r)``.  The
+        reference runs them one after another; here models of a batchable family (SIR,
+        random walk, Schelling, opinion; no Python hooks) run as one batched ensemble
+        (:func:`jaxabm_gb300.batching.run_ensemble`), each result equal to that model's own
+        ``run()``; other models run one by one."""
+        from .batching import run_ensemble
         names = list(parameter_ranges.keys())
-        results = {}
+        keys, models = [], []
         for values in itertools.product(*parameter_ranges.values()):
             params = dict(self.p)
             params.update(zip(names, values))
-            reps = [self.__class__(params, seed=self.seed + r).run() for r in range(repetitions)]
-            results[tuple(values)] = reps
+            for r in range(repetitions):
+                keys.append(tuple(values))
+                models.append(self.__class__(params, seed=self.seed + r))
+        runs = run_ensemble(models) if self._hooks() == (None, None) else None
+        if runs is None:
+            runs = [m.run() for m in models]
+        results = {}
+        for values, res in zip(keys, runs):
+            results.setdefault(values, []).append(res)
         return results

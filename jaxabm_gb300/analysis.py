@@ -5,9 +5,9 @@
 one model per sample built by ``model_factory(params=..., config=ModelConfig(seed=1000 + i))``,
 the last value of each metric of interest, and squared correlation coefficients as the
 sensitivity indices.  The reference runs the samples one after another; here, when every
-sample's model is a batchable SIR model, all of them run as one ensemble (one CUDA-graph
-replay for every member and step, ``sir.run_ensemble``) and each member's result equals
-that model's own ``run()``.  Other models run one by one, as in the reference.
+sample's model belongs to a batchable family (SIR, random walk, Schelling, opinion; see
+``batching.run_ensemble``), all of them run as one ensemble and each member's result
+equals that model's own ``run()``.  Other models run one by one, as in the reference.
 ``ModelCalibrator`` evaluates each iteration's population (every candidate times every
 evaluation run) the same way.
 """
@@ -93,8 +93,8 @@ class SensitivityAnalysis:
 
     def run(self, verbose: bool = True) -> Dict[str, torch.Tensor]:
         """Run one model per sample and collect the last value of each metric of interest
-        (jaxabm/analysis.py:97-165).  Batchable SIR models run as one ensemble."""
-        from .sir import run_ensemble
+        (jaxabm/analysis.py:97-165).  Batchable models run as one ensemble."""
+        from .batching import run_ensemble
         if verbose:
             print(f"Running sensitivity analysis with {self.num_samples} samples...")
         pairs = self._models()
@@ -141,9 +141,9 @@ class SensitivityAnalysis:
 
 
 def _evaluate_models(models, steps):
-    """Run ``models`` for ``steps`` steps each: batchable SIR models as one ensemble
-    (``sir.run_ensemble``), anything else one by one.  Returns (results, batched)."""
-    from .sir import run_ensemble
+    """Run ``models`` for ``steps`` steps each: batchable models as one ensemble
+    (``batching.run_ensemble``), anything else one by one.  Returns (results, batched)."""
+    from .batching import run_ensemble
     for m in models:
         if hasattr(m, "steps"):
             m.steps = steps

@@ -270,18 +270,20 @@ __global__ void opinion_adjoint_init_kernel(const float* __restrict__ o, int n, 
   }
 }
 
-// Raw moments: per-CTA partials in double, then a fixed-order final sum.
-__global__ void __launch_bounds__(kOpThreads)
-opinion_moments_partial_kernel(const float* __restrict__ o, int n, int B, int rows_per_cta,
-                               double* __restrict__ part) {
-  // thread t handles instance column b = t % B for rows r0 + t / B, stepping kOpThreads / B rows
-  extern __shared__ double sm[];  // [kOpThreads][4]
-  const int per = kOpThreads / B;  // B <= kOpThreads and divides it
-  const int b = threadIdx.x % B, r = threadIdx.x / B;
+// Raw moments: thread b of CTA c sums instance column b over rows [kMomRows c,
+// kMomRows (c + 1)) in row order (float64), then the partials are summed over CTAs in
+// CTA order.  The order of every sum depends only on n, not on the batch width B, so a
+// column's moments are the same in a batch of any width.
+constexpr int kMomRows = 64;
+
+__global__ void opinion_moments_partial_kernel(const float* __restrict__ o, int n, int B,
+                                               double* __restrict__ part) {
+  const int b = threadIdx.x;
+  if (b >= B) return;
   double a1 = 0, a2 = 0, a3 = 0, a4 = 0;
-  const int r0 = blockIdx.x * rows_per_cta;
-  const int r1 = min(n, r0 + rows_per_cta);
-  for (int i = r0 + r; i < r1; i += per) {
+  const int r0 = blockIdx.x * kMomRows;
+  const int r1 = min(n, r0 + kMomRows);
+  for (int i = r0; i < r1; ++i) {
     const double x = o[(size_t)i * B + b];
     const double x2 = x * x;
     a1 += x;
@@ -289,18 +291,11 @@ opinion_moments_partial_kernel(const float* __restrict__ o, int n, int B, int ro
     a3 += x2 * x;
     a4 += x2 * x2;
   }
-  double* mine = sm + 4 * threadIdx.x;
-  mine[0] = a1;
-  mine[1] = a2;
-  mine[2] = a3;
-  mine[3] = a4;
-  __syncthreads();
-  if (threadIdx.x < B) {
-    double s[4] = {0, 0, 0, 0};
-    for (int k = 0; k < per; ++k)
-      for (int q = 0; q < 4; ++q) s[q] += sm[4 * (k * B + threadIdx.x) + q];
-    for (int q = 0; q < 4; ++q) part[((size_t)blockIdx.x * B + threadIdx.x) * 4 + q] = s[q];
-  }
+  double* out = part + ((size_t)blockIdx.x * B + b) * 4;
+  out[0] = a1;
+  out[1] = a2;
+  out[2] = a3;
+  out[3] = a4;
 }
 
 __global__ void sum_partials_kernel(const double* __restrict__ part, int nparts, int width,
@@ -418,8 +413,7 @@ int abm_opinion_inv_degree(const int32_t* row_ptr, int64_t n, float* inv_deg, vo
 
 size_t abm_opinion_moments_workspace_bytes(int64_t n, int32_t B) {
   if (n <= 0 || !valid_batch(B)) return 0;
-  const int rows_per_cta = 1024;
-  const int64_t parts = (n + rows_per_cta - 1) / rows_per_cta;
+  const int64_t parts = (n + kMomRows - 1) / kMomRows;
   return (size_t)parts * B * 4 * sizeof(double);
 }
 
@@ -430,11 +424,9 @@ int abm_opinion_moments(const float* o, int64_t n, int32_t B, double* moments, v
       !abm_host::aligned(workspace, 8))
     return ABM_ERR_WORKSPACE;
   cudaStream_t s = abm_host::as_stream(stream);
-  const int rows_per_cta = 1024;
-  const int parts = (int)((n + rows_per_cta - 1) / rows_per_cta);
+  const int parts = (int)((n + kMomRows - 1) / kMomRows);
   double* part = static_cast<double*>(workspace);
-  opinion_moments_partial_kernel<<<parts, kOpThreads, kOpThreads * 4 * sizeof(double), s>>>(
-      o, (int)n, B, rows_per_cta, part);
+  opinion_moments_partial_kernel<<<parts, (B + 31) / 32 * 32, 0, s>>>(o, (int)n, B, part);
   int st = abm_host::check_launch("abm_opinion_moments/partial");
   if (st) return st;
   sum_partials_kernel<<<(B * 4 + 127) / 128, 128, 0, s>>>(part, parts, B * 4, 1.0 / (double)n,

@@ -9,6 +9,10 @@
 // AgentCollection.update (jaxabm/agent.py:156-177) and metrics_fn (jaxabm/model.py:193-200).
 // The whole run is one launch: agents are independent between steps, so every thread keeps
 // its agent's (x, y) in registers for all steps and only the per-step reductions leave it.
+// A batch of independent models (members of one size, each with its own key chain and
+// sigma) runs in the same launch: blockIdx.y selects the member, whose arrays follow the
+// previous member's, and each member's blocks and reduction tree are those of a run alone,
+// so every member's states and means equal its solo run bit for bit.
 
 #include "abm_common.cuh"
 
@@ -21,7 +25,9 @@ constexpr int kChunk = 64;  // steps whose keys / warp sums are staged in shared
 __global__ void __launch_bounds__(kBlock) rw_init_kernel(float* __restrict__ x,
                                                          float* __restrict__ y, int64_t n,
                                                          const uint32_t* __restrict__ init_key) {
-  const uint2 key = abm::load_key(init_key);
+  x += blockIdx.y * n;
+  y += blockIdx.y * n;
+  const uint2 key = abm::load_key(init_key + 2 * (size_t)blockIdx.y);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const uint2 ak = abm::split_at(key, (uint64_t)i);
@@ -31,11 +37,35 @@ __global__ void __launch_bounds__(kBlock) rw_init_kernel(float* __restrict__ x,
   }
 }
 
-__global__ void __launch_bounds__(kBlock) rw_run_kernel(float* __restrict__ x,
-                                                        float* __restrict__ y, int64_t n,
-                                                        const uint32_t* __restrict__ coll_keys,
-                                                        int32_t steps, float sigma,
-                                                        float2* __restrict__ partial) {
+// Member blockIdx.y's x, y (n each), key chain (steps keys), sigma and partial sums.
+struct Member {
+  float* x;
+  float* y;
+  const uint32_t* keys;
+  float sigma;
+  float2* partial;
+};
+
+__device__ __forceinline__ Member member_of(float* x, float* y, int64_t n,
+                                            const uint32_t* coll_keys, int32_t steps,
+                                            float sigma, const float* sigmas, float2* partial) {
+  const int64_t m = blockIdx.y;
+  return Member{x + m * n, y + m * n, coll_keys + 2 * (size_t)steps * m,
+                sigmas ? sigmas[m] : sigma, partial + (size_t)steps * gridDim.x * m};
+}
+
+__global__ void __launch_bounds__(kBlock) rw_run_kernel(float* __restrict__ x_all,
+                                                        float* __restrict__ y_all, int64_t n,
+                                                        const uint32_t* __restrict__ keys_all,
+                                                        int32_t steps, float sigma0,
+                                                        const float* __restrict__ sigmas,
+                                                        float2* __restrict__ partial_all) {
+  const Member M = member_of(x_all, y_all, n, keys_all, steps, sigma0, sigmas, partial_all);
+  float* __restrict__ x = M.x;
+  float* __restrict__ y = M.y;
+  const uint32_t* __restrict__ coll_keys = M.keys;
+  const float sigma = M.sigma;
+  float2* __restrict__ partial = M.partial;
   __shared__ uint2 skeys[kChunk];
   __shared__ float2 swarp[kChunk][kWarps];
   const int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x;
@@ -87,9 +117,15 @@ constexpr int kWideAgents = 32;
 constexpr int64_t kWideBelow = 1 << 17;  // agent count below which the wide kernel is used
 
 __global__ void __launch_bounds__(kWideThreads)
-rw_run_wide_kernel(float* __restrict__ x, float* __restrict__ y, int64_t n,
-                   const uint32_t* __restrict__ coll_keys, int32_t steps, float sigma,
-                   float2* __restrict__ partial) {
+rw_run_wide_kernel(float* __restrict__ x_all, float* __restrict__ y_all, int64_t n,
+                   const uint32_t* __restrict__ keys_all, int32_t steps, float sigma0,
+                   const float* __restrict__ sigmas, float2* __restrict__ partial_all) {
+  const Member M = member_of(x_all, y_all, n, keys_all, steps, sigma0, sigmas, partial_all);
+  float* __restrict__ x = M.x;
+  float* __restrict__ y = M.y;
+  const uint32_t* __restrict__ coll_keys = M.keys;
+  const float sigma = M.sigma;
+  float2* __restrict__ partial = M.partial;
   __shared__ float2 snoise[kChunk][kWideAgents];
   const int64_t a0 = (int64_t)blockIdx.x * kWideAgents;
   const int lane = threadIdx.x & 31;
@@ -127,11 +163,14 @@ rw_run_wide_kernel(float* __restrict__ x, float* __restrict__ y, int64_t n,
   }
 }
 
-// means[t] = (sum_b partial[t][b]) / n, one block per step, fixed reduction tree.
+// means[t] = (sum_b partial[t][b]) / n, one block per step (and member, blockIdx.y), fixed
+// reduction tree.
 __global__ void rw_means_kernel(const float2* __restrict__ partial, int nblocks, int64_t n,
                                 float2* __restrict__ means) {
   __shared__ float2 s[kBlock];
   const int t = blockIdx.x;
+  partial += (size_t)gridDim.x * nblocks * blockIdx.y;
+  means += (size_t)gridDim.x * blockIdx.y;
   float sx = 0.f, sy = 0.f;
   for (int b = threadIdx.x; b < nblocks; b += kBlock) {
     const float2 p = partial[(int64_t)t * nblocks + b];
@@ -161,43 +200,74 @@ int64_t rw_blocks(int64_t n) {
 
 extern "C" {
 
-int abm_randomwalk_init(float* x, float* y, int64_t n, const uint32_t* init_key, void* stream) {
-  if (!x || !y || !init_key || n <= 0) return ABM_ERR_BADARG;
+int abm_randomwalk_init_batch(float* x, float* y, int64_t n, int32_t members,
+                              const uint32_t* init_keys, void* stream) {
+  if (!x || !y || !init_keys || n <= 0 || members <= 0 || members > 65535) return ABM_ERR_BADARG;
   int64_t blocks = rw_blocks(n);
   const int64_t cap = (int64_t)abm_host::sm_count() * 16;
   if (blocks > cap) blocks = cap;
-  rw_init_kernel<<<(unsigned)blocks, kBlock, 0, abm_host::as_stream(stream)>>>(x, y, n, init_key);
+  rw_init_kernel<<<dim3((unsigned)blocks, (unsigned)members), kBlock, 0,
+                   abm_host::as_stream(stream)>>>(x, y, n, init_keys);
   return abm_host::check_launch("abm_randomwalk_init");
 }
 
-size_t abm_randomwalk_workspace_bytes(int64_t n, int32_t steps) {
-  if (n <= 0 || steps <= 0) return 0;
-  return (size_t)rw_blocks(n) * (size_t)steps * sizeof(float2);
+int abm_randomwalk_init(float* x, float* y, int64_t n, const uint32_t* init_key, void* stream) {
+  return abm_randomwalk_init_batch(x, y, n, 1, init_key, stream);
 }
 
-int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* coll_keys, int32_t steps,
-                       float sigma, float* means, void* workspace, size_t workspace_bytes,
-                       void* stream) {
-  if (!x || !y || !coll_keys || !means || n <= 0 || steps < 0) return ABM_ERR_BADARG;
+size_t abm_randomwalk_batch_workspace_bytes(int64_t n, int32_t steps, int32_t members) {
+  if (n <= 0 || steps <= 0 || members <= 0) return 0;
+  return (size_t)rw_blocks(n) * (size_t)steps * sizeof(float2) * (size_t)members;
+}
+
+size_t abm_randomwalk_workspace_bytes(int64_t n, int32_t steps) {
+  return abm_randomwalk_batch_workspace_bytes(n, steps, 1);
+}
+
+namespace {
+int run_members(float* x, float* y, int64_t n, int32_t members, const uint32_t* coll_keys,
+                int32_t steps, float sigma, const float* sigmas, float* means, void* workspace,
+                size_t workspace_bytes, void* stream) {
+  if (!x || !y || !coll_keys || !means || n <= 0 || steps < 0 || members <= 0 ||
+      members > 65535)
+    return ABM_ERR_BADARG;
   if (!abm_host::aligned(means, 8)) return ABM_ERR_BADARG;
   if (steps == 0) return ABM_OK;
   const int64_t blocks = rw_blocks(n);
   if (blocks > 0x7FFFFFFF) return ABM_ERR_BADARG;
-  const size_t need = abm_randomwalk_workspace_bytes(n, steps);
+  const size_t need = abm_randomwalk_batch_workspace_bytes(n, steps, members);
   if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 8))
     return ABM_ERR_WORKSPACE;
   cudaStream_t s = abm_host::as_stream(stream);
   float2* partial = static_cast<float2*>(workspace);
+  const dim3 grid((unsigned)blocks, (unsigned)members);
   if (n < kWideBelow)
-    rw_run_wide_kernel<<<(unsigned)blocks, kWideThreads, 0, s>>>(x, y, n, coll_keys, steps, sigma,
-                                                                partial);
+    rw_run_wide_kernel<<<grid, kWideThreads, 0, s>>>(x, y, n, coll_keys, steps, sigma, sigmas,
+                                                     partial);
   else
-    rw_run_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(x, y, n, coll_keys, steps, sigma, partial);
+    rw_run_kernel<<<grid, kBlock, 0, s>>>(x, y, n, coll_keys, steps, sigma, sigmas, partial);
   int st = abm_host::check_launch("abm_randomwalk_run");
   if (st) return st;
-  rw_means_kernel<<<(unsigned)steps, kBlock, 0, s>>>(partial, (int)blocks, n,
-                                                     reinterpret_cast<float2*>(means));
+  rw_means_kernel<<<dim3((unsigned)steps, (unsigned)members), kBlock, 0, s>>>(
+      partial, (int)blocks, n, reinterpret_cast<float2*>(means));
   return abm_host::check_launch("abm_randomwalk_means");
+}
+}  // namespace
+
+int abm_randomwalk_run(float* x, float* y, int64_t n, const uint32_t* coll_keys, int32_t steps,
+                       float sigma, float* means, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  return run_members(x, y, n, 1, coll_keys, steps, sigma, nullptr, means, workspace,
+                     workspace_bytes, stream);
+}
+
+int abm_randomwalk_run_batch(float* x, float* y, int64_t n, int32_t members,
+                             const uint32_t* coll_keys, int32_t steps, const float* sigmas,
+                             float* means, void* workspace, size_t workspace_bytes,
+                             void* stream) {
+  if (!sigmas) return ABM_ERR_BADARG;
+  return run_members(x, y, n, members, coll_keys, steps, 0.0f, sigmas, means, workspace,
+                     workspace_bytes, stream);
 }
 
 }  // extern "C"

@@ -5,7 +5,8 @@
 // cell_agent[c] = occupant id or -1.  Agent semantics per step (partitionable jax.random,
 // agent_key = split(coll_key, n)[i], jaxabm/agent.py:156):
 //   occ  = occupied Moore-8 neighbours, same = those of the agent's type;
-//   unhappy iff 8 * same < 3 * occ         (same/occ < 37.5%, exact in integers)
+//   unhappy iff den * same < num * occ     (same/occ below the threshold num/den, exact in
+//                                           integers; the workload's 37.5% is 3/8)
 //   an unhappy agent draws idx = min(floor(uniform(agent_key) * e), e - 1) (one float32
 //   multiply) into the pre-step list of the e empty cells in ascending cell order, and
 //   claims that cell; of several claimants of one cell the lowest agent id moves, the
@@ -36,8 +37,9 @@ constexpr int32_t kPending = -2;
 
 __global__ void __launch_bounds__(kRowThreads)
 schelling_scan_kernel(const int8_t* __restrict__ grid, const int32_t* __restrict__ cell_agent,
-                      int32_t W, int32_t H, int32_t* __restrict__ target,
-                      int32_t* __restrict__ row_empty, int32_t* __restrict__ stats_t) {
+                      int32_t W, int32_t H, int32_t thr_num, int32_t thr_den,
+                      int32_t* __restrict__ target, int32_t* __restrict__ row_empty,
+                      int32_t* __restrict__ stats_t) {
   extern __shared__ int8_t rows[];  // 3 x H
   __shared__ int sred[2][kRowThreads / 32];
   const int x = blockIdx.x;
@@ -64,7 +66,7 @@ schelling_scan_kernel(const int8_t* __restrict__ grid, const int32_t* __restrict
       occ += nb[k] >= 0;
       same += nb[k] == g;
     }
-    const bool u = 8 * same < 3 * occ;
+    const bool u = thr_den * same < thr_num * occ;
     unhappy += u;
     target[cell_agent[(size_t)x * H + y]] = u ? kPending : -1;
   }
@@ -208,12 +210,40 @@ __device__ __forceinline__ int block_sum(int v, int* sred) {
   return total;  // valid in thread 0
 }
 
-__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
-schelling_cluster_kernel(int32_t* __restrict__ pos, const int8_t* __restrict__ type, int32_t n,
-                         int32_t W, int32_t H, int8_t* grid, int32_t* cell_agent,
-                         const uint32_t* __restrict__ coll_keys, int32_t steps,
-                         int32_t* __restrict__ stats, int32_t* target, int32_t* claim,
-                         int32_t* empty_list, int32_t* unhappy_list, int32_t* unhappy_count) {
+// One model's arrays for the cluster body.
+struct ClusterModel {
+  int32_t* pos;
+  const int8_t* type;
+  int32_t n;
+  int8_t* grid;
+  int32_t* cell_agent;
+  const uint32_t* coll_keys;
+  int32_t* stats;
+  int32_t* target;
+  int32_t* claim;
+  int32_t* empty_list;
+  int32_t* unhappy_list;
+  int32_t* unhappy_count;
+  int32_t thr_num, thr_den;
+};
+
+// Every step of one model on the calling cluster.  With `init`, the cluster first sets its
+// claims to "no claim" and zeroes its statistics and counters (the batched launch, whose
+// models have no host-side set-up); otherwise the host did that.
+__device__ void schelling_cluster_body(const ClusterModel& Mdl, int32_t W, int32_t H,
+                                       int32_t steps, bool init) {
+  int32_t* __restrict__ pos = Mdl.pos;
+  const int8_t* __restrict__ type = Mdl.type;
+  int8_t* grid = Mdl.grid;
+  int32_t* cell_agent = Mdl.cell_agent;
+  const uint32_t* __restrict__ coll_keys = Mdl.coll_keys;
+  int32_t* __restrict__ stats = Mdl.stats;
+  int32_t* target = Mdl.target;
+  int32_t* claim = Mdl.claim;
+  int32_t* empty_list = Mdl.empty_list;
+  int32_t* unhappy_list = Mdl.unhappy_list;
+  int32_t* unhappy_count = Mdl.unhappy_count;
+  const int32_t thr_num = Mdl.thr_num, thr_den = Mdl.thr_den;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ int8_t srows[];  // this CTA's grid rows with one halo row on each side
   __shared__ int swarp[kClusterWarps];
@@ -232,6 +262,12 @@ schelling_cluster_kernel(int32_t* __restrict__ pos, const int8_t* __restrict__ t
   const int x_lo = cta_c0 / H;
   const int x_hi = cta_c1 > cta_c0 ? (cta_c1 - 1) / H : x_lo;
   const int nrows = x_hi - x_lo + 3;
+  if (init) {
+    for (int c = g; c < C; c += nthreads) claim[c] = kNoClaim;
+    for (int k = g; k < 2 * steps; k += nthreads) stats[k] = 0;
+    if (g < 2) unhappy_count[g] = 0;
+    cluster.sync();
+  }
   for (int t = 0; t < steps; ++t) {
     const int32_t* ucount = unhappy_count + (t & 1);
     if (g == 0) unhappy_count[(t + 1) & 1] = 0;  // the counter of the next step
@@ -264,7 +300,7 @@ schelling_cluster_kernel(int32_t* __restrict__ pos, const int8_t* __restrict__ t
         occ += nb[k] >= 0;
         same += nb[k] == gv;
       }
-      if (8 * same < 3 * occ) {
+      if (thr_den * same < thr_num * occ) {
         ++unhappy;
         const int i = __ldcg(cell_agent + c);
         unhappy_list[atomicAdd(const_cast<int32_t*>(ucount), 1)] = i;
@@ -347,6 +383,57 @@ schelling_cluster_kernel(int32_t* __restrict__ pos, const int8_t* __restrict__ t
   }
 }
 
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+schelling_cluster_kernel(ClusterModel Mdl, int32_t W, int32_t H, int32_t steps) {
+  schelling_cluster_body(Mdl, W, H, steps, false);
+}
+
+// Workspace layout of one model (abm_schelling_workspace_bytes), usable on both sides.
+struct Workspace {
+  int32_t* claim;
+  int32_t* target;
+  int32_t* row_empty;
+  int32_t* empty_list;
+  int32_t* unhappy_list;
+  int32_t* e_total;
+  int32_t* bad;
+  int32_t* unhappy_count;  // two counters, one per step parity
+};
+
+__host__ __device__ inline size_t round256(size_t v) { return (v + 255) / 256 * 256; }
+
+__host__ __device__ inline Workspace carve(void* ws, int64_t n, int32_t W, int32_t H) {
+  char* p = static_cast<char*>(ws);
+  const size_t C = (size_t)W * H;
+  Workspace w;
+  w.claim = reinterpret_cast<int32_t*>(p);
+  p += round256(C * 4);
+  w.target = reinterpret_cast<int32_t*>(p);
+  p += round256((size_t)n * 4);
+  w.row_empty = reinterpret_cast<int32_t*>(p);
+  p += round256((size_t)W * 4);
+  w.empty_list = reinterpret_cast<int32_t*>(p);
+  p += round256(C * 4);
+  w.unhappy_list = reinterpret_cast<int32_t*>(p);
+  p += round256((size_t)n * 4);
+  w.e_total = reinterpret_cast<int32_t*>(p);
+  w.bad = w.e_total + 1;
+  w.unhappy_count = w.e_total + 2;
+  return w;
+}
+
+// Many models of one grid shape: cluster m runs member m (abm_schelling_member) entirely.
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+schelling_cluster_batch_kernel(const abm_schelling_member* __restrict__ members, int32_t W,
+                               int32_t H, int32_t steps) {
+  const abm_schelling_member& m = members[blockIdx.x / kClusterCtas];
+  const Workspace w = carve(m.workspace, m.n, W, H);
+  const ClusterModel Mdl{m.pos, m.type, (int32_t)m.n, m.grid, m.cell_agent, m.coll_keys,
+                         m.stats, w.target, w.claim, w.empty_list, w.unhappy_list,
+                         w.unhappy_count, m.thr_num, m.thr_den};
+  schelling_cluster_body(Mdl, W, H, steps, true);
+}
+
 // Bytes of the staged rows of one CTA of schelling_cluster_kernel.
 size_t cluster_smem_bytes(int32_t W, int32_t H) {
   const int64_t C = (int64_t)W * H;
@@ -383,37 +470,6 @@ __global__ void schelling_place_agents_kernel(int32_t n, int32_t C, const int32_
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
-struct Workspace {
-  int32_t* claim;
-  int32_t* target;
-  int32_t* row_empty;
-  int32_t* empty_list;
-  int32_t* unhappy_list;
-  int32_t* e_total;
-  int32_t* bad;
-  int32_t* unhappy_count;  // two counters, one per step parity
-};
-
-Workspace carve(void* ws, int64_t n, int32_t W, int32_t H) {
-  char* p = static_cast<char*>(ws);
-  const size_t C = (size_t)W * H;
-  Workspace w;
-  w.claim = reinterpret_cast<int32_t*>(p);
-  p += align256(C * 4);
-  w.target = reinterpret_cast<int32_t*>(p);
-  p += align256((size_t)n * 4);
-  w.row_empty = reinterpret_cast<int32_t*>(p);
-  p += align256((size_t)W * 4);
-  w.empty_list = reinterpret_cast<int32_t*>(p);
-  p += align256(C * 4);
-  w.unhappy_list = reinterpret_cast<int32_t*>(p);
-  p += align256((size_t)n * 4);
-  w.e_total = reinterpret_cast<int32_t*>(p);
-  w.bad = w.e_total + 1;
-  w.unhappy_count = w.e_total + 2;
-  return w;
-}
-
 }  // namespace
 
 extern "C" {
@@ -443,11 +499,19 @@ int abm_schelling_place(const int32_t* pos, const int8_t* type, int64_t n, int32
   return abm_host::check_launch("abm_schelling_place/agents");
 }
 
+namespace {
+bool valid_threshold(int32_t num, int32_t den) {
+  return den > 0 && num >= 0 && num <= (1 << 27) && den <= (1 << 27);
+}
+}  // namespace
+
 int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, int32_t H,
                       int8_t* grid, int32_t* cell_agent, const uint32_t* coll_keys, int32_t steps,
-                      int32_t* stats, void* workspace, size_t workspace_bytes, void* stream) {
+                      int32_t thr_num, int32_t thr_den, int32_t* stats, void* workspace,
+                      size_t workspace_bytes, void* stream) {
   if (!pos || !type || !grid || !cell_agent || !coll_keys || !stats || n <= 0 || W < 3 ||
-      H < 3 || (int64_t)W * H > 0x7FFFFFFFll || n > (int64_t)W * H || steps < 0 || H > 16384)
+      H < 3 || (int64_t)W * H > 0x7FFFFFFFll || n > (int64_t)W * H || steps < 0 || H > 16384 ||
+      !valid_threshold(thr_num, thr_den))
     return ABM_ERR_BADARG;
   if (!workspace || workspace_bytes < abm_schelling_workspace_bytes(n, W, H) ||
       !abm_host::aligned(workspace, 256))
@@ -472,17 +536,18 @@ int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, in
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)rows_bytes);
     if (e != cudaSuccess) return abm_host::record_cuda_error(e, "abm_schelling_run/cluster smem");
-    schelling_cluster_kernel<<<kClusterCtas, kClusterThreads, rows_bytes, s>>>(
-        pos, type, (int32_t)n, W, H, grid, cell_agent, coll_keys, steps, stats, w.target, w.claim,
-        w.empty_list, w.unhappy_list, w.unhappy_count);
+    const ClusterModel Mdl{pos, type, (int32_t)n, grid, cell_agent, coll_keys, stats, w.target,
+                           w.claim, w.empty_list, w.unhappy_list, w.unhappy_count, thr_num,
+                           thr_den};
+    schelling_cluster_kernel<<<kClusterCtas, kClusterThreads, rows_bytes, s>>>(Mdl, W, H, steps);
     return abm_host::check_launch("abm_schelling_run/cluster");
   }
   const unsigned agent_blocks = (unsigned)((n + kAgentThreads - 1) / kAgentThreads);
   const size_t smem = 3 * (size_t)H;
   for (int32_t t = 0; t < steps; ++t) {
     int32_t* stats_t = stats + 2 * (size_t)t;
-    schelling_scan_kernel<<<W, kRowThreads, smem, s>>>(grid, cell_agent, W, H, w.target,
-                                                      w.row_empty, stats_t);
+    schelling_scan_kernel<<<W, kRowThreads, smem, s>>>(grid, cell_agent, W, H, thr_num, thr_den,
+                                                      w.target, w.row_empty, stats_t);
     if ((st = abm_host::check_launch("abm_schelling_run/scan"))) return st;
     schelling_empties_kernel<<<W, kRowThreads, 0, s>>>(grid, W, H, w.row_empty, w.empty_list,
                                                       w.e_total);
@@ -495,6 +560,24 @@ int abm_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, in
     if ((st = abm_host::check_launch("abm_schelling_run/resolve"))) return st;
   }
   return ABM_OK;
+}
+
+int abm_schelling_run_batch(const abm_schelling_member* members, int32_t count, int32_t W,
+                            int32_t H, int32_t steps, void* stream) {
+  if (!members || count <= 0 || count > 65535 / kClusterCtas || W < 3 || H < 3 || steps < 0 ||
+      !abm_host::aligned(members, 8))
+    return ABM_ERR_BADARG;
+  if ((int64_t)W * H > kClusterMaxCells || cluster_smem_bytes(W, H) > kClusterMaxRowBytes)
+    return ABM_ERR_BADARG;  // larger grids: abm_schelling_run per model
+  if (steps == 0) return ABM_OK;
+  const size_t rows_bytes = cluster_smem_bytes(W, H);
+  cudaError_t e = cudaFuncSetAttribute(schelling_cluster_batch_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)rows_bytes);
+  if (e != cudaSuccess) return abm_host::record_cuda_error(e, "abm_schelling_run_batch/smem");
+  schelling_cluster_batch_kernel<<<count * kClusterCtas, kClusterThreads, rows_bytes,
+                                   abm_host::as_stream(stream)>>>(members, W, H, steps);
+  return abm_host::check_launch("abm_schelling_run_batch");
 }
 
 }  // extern "C"

@@ -326,3 +326,49 @@ def calibration_params(count=64, base=(0.3, 0.2, 0.02), spread=0.2, seed=0):
 
 
 HIDDEN_PARAMS = (0.25, 0.15, 0.025)
+
+
+def ensemble_member(model):
+    """``(n, degree, graph_seed, mu, eps, tau, seed, steps)`` of an ``OpinionModel`` that
+    can run as a batch member, else None."""
+    if not isinstance(model, OpinionModel) or model._hooks() != (None, None) \
+            or type(model).setup is not OpinionModel.setup:
+        return None
+    p = model.p
+    return (int(p.get("n", 1 << 18)), int(p.get("degree", 16)),
+            int(p.get("graph_seed", model.seed)), float(p.get("mu", 0.3)),
+            float(p.get("eps", 0.2)), float(p.get("tau", 0.02)), int(model.seed),
+            int(model.steps))
+
+
+def run_ensemble(models):
+    """Opinion models that share a graph (same ``n``, ``degree`` and ``graph_seed``) and step
+    count run as the columns of one ``OpinionBatch`` (up to 128 per batch): each column
+    has its own parameters and initial opinions, and equals its model's own ``run()``
+    (keys ``step``, ``m1``..``m4``, ``agents.people.opinion``) bit for bit.  Returns None
+    unless every model is a batchable ``OpinionModel``."""
+    from .agentpy import Results
+    from .sir import random_regular
+    specs = [ensemble_member(m) for m in models]
+    if any(s is None for s in specs):
+        return None
+    out = [None] * len(models)
+    groups = {}
+    for k, s in enumerate(specs):
+        groups.setdefault((s[0], s[1], s[2], s[7]), []).append(k)
+    for (n, degree, graph_seed, steps), idx in groups.items():
+        rp, col = random_regular(n, degree, graph_seed)
+        for c0 in range(0, len(idx), 128):
+            part = idx[c0:c0 + 128]
+            o0 = torch.stack([initial_opinions(n, specs[k][6]) for k in part], dim=1)
+            b = OpinionBatch(rp, col, o0, [specs[k][3] for k in part],
+                             [specs[k][4] for k in part], [specs[k][5] for k in part])
+            rows = b.forward_with_moments(steps).cpu().numpy() if steps > 0 else None
+            final = b.o[:, :len(part)].cpu().numpy()
+            for j, k in enumerate(part):
+                data = {"agents.people.opinion": final[:, j].copy()}
+                if steps > 0:
+                    data = {"step": list(range(1, steps + 1)),
+                            **{f"m{q + 1}": rows[:, j, q].tolist() for q in range(4)}, **data}
+                out[k] = Results(data)
+    return out

@@ -12,6 +12,7 @@ with per-step metrics ``mean_x``/``mean_y`` (the reference computes these in a P
 run execute in one launch of ``abm_randomwalk_run``.
 """
 
+import numpy as np
 import torch
 
 from . import _dev
@@ -79,3 +80,60 @@ class RandomWalkModel(Model):
     def setup(self):
         self.walkers = self.add_agents(int(self.p.get("n", 10_000)), RandomWalker,
                                        name="walkers", sigma=float(self.p.get("sigma", 0.01)))
+
+
+def ensemble_member(model):
+    """``(n, sigma, seed, steps)`` of a ``RandomWalkModel`` that can run as a batch member
+    (no Python hooks, the class's own ``setup``), else None."""
+    if not isinstance(model, RandomWalkModel) or model._hooks() != (None, None) \
+            or type(model).setup is not RandomWalkModel.setup:
+        return None
+    p = model.p
+    return (int(p.get("n", 10_000)), float(p.get("sigma", 0.01)), int(model.seed),
+            int(model.steps))
+
+
+def run_ensemble(models):
+    """Random-walk models run as batches of one launch sequence each (members of one size and
+    step count together: ``abm_randomwalk_init_batch`` / ``abm_randomwalk_run_batch``);
+    returns one ``Results`` per model, equal to that model's own ``run()`` (keys ``step``,
+    ``mean_x``, ``mean_y``, ``agents.walkers.x``, ``agents.walkers.y``), or None unless
+    every model is a batchable ``RandomWalkModel``."""
+    from .agentpy import Results
+    specs = [ensemble_member(m) for m in models]
+    if any(s is None for s in specs):
+        return None
+    out = [None] * len(models)
+    groups = {}
+    for k, (n, _, _, steps) in enumerate(specs):
+        groups.setdefault((n, steps), []).append(k)
+    for (n, steps), idx in groups.items():
+        M = len(idx)
+        seeds = np.array([specs[k][2] for k in idx], dtype=np.uint64)
+        keys = np.stack([(seeds >> np.uint64(32)).astype(np.uint32),
+                         (seeds & np.uint64(0xFFFFFFFF)).astype(np.uint32)], axis=1)
+        pair = jrandom.split(_dev.keys_from_numpy(keys), 2)  # Model.initialize, one collection
+        rng, init = pair[:, 0].contiguous(), pair[:, 1].contiguous()
+        x = _dev.empty((M, n), torch.float32)
+        y = _dev.empty((M, n), torch.float32)
+        _lib.call("abm_randomwalk_init_batch", _dev.ptr(x), _dev.ptr(y), n, M, _dev.ptr(init),
+                  _dev.stream_handle())
+        if steps > 0:
+            ck = jrandom.keychain(rng, steps, 1).reshape(M, steps, 2).contiguous()
+            sig = torch.tensor([specs[k][1] for k in idx], dtype=torch.float32,
+                               device=x.device)
+            means = _dev.empty((M, steps, 2), torch.float32)
+            ws = _dev.workspace(_lib.load().abm_randomwalk_batch_workspace_bytes(n, steps, M))
+            _lib.call("abm_randomwalk_run_batch", _dev.ptr(x), _dev.ptr(y), n, M, _dev.ptr(ck),
+                      steps, _dev.ptr(sig), _dev.ptr(means), _dev.ptr(ws), ws.numel(),
+                      _dev.stream_handle())
+            host_means = means.cpu().numpy()
+        hx, hy = x.cpu().numpy(), y.cpu().numpy()
+        for j, k in enumerate(idx):
+            data = {"agents.walkers.x": hx[j], "agents.walkers.y": hy[j]}
+            if steps > 0:
+                data = {"step": list(range(1, steps + 1)),
+                        "mean_x": host_means[j, :, 0].tolist(),
+                        "mean_y": host_means[j, :, 1].tolist(), **data}
+            out[k] = Results(data)
+    return out

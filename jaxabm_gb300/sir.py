@@ -159,42 +159,13 @@ class SIRModel(Model):
         return (g[0], g[1], init, float(p.get("beta", 0.05)), float(p.get("gamma", 0.1)),
                 seed, int(self.steps))
 
-    def batch_run(self, parameter_ranges, repetitions=1):
-        """Every parameter combination, ``repetitions`` runs each, as ONE batched launch
-        sequence of the ensemble engine (the reference runs them one after another,
-        jaxabm/agentpy.py:1116-1152).  Run r of a combination uses seed ``self.seed + r``,
-        as the serial loop does, so each result equals that run done alone.  Subclasses
-        with Python hooks (``step``, ``update_state``, ``compute_metrics``) take the serial
-        path."""
-        import itertools
-
-        if self._hooks() != (None, None):
-            return super().batch_run(parameter_ranges, repetitions)
-        names = list(parameter_ranges.keys())
-        keys, models = [], []
-        for values in itertools.product(*parameter_ranges.values()):
-            for r in range(repetitions):
-                p = dict(self.p)
-                p.update(zip(names, values))
-                keys.append(tuple(values))
-                models.append(self.__class__(p, seed=self.seed + r))
-        if not models:
-            return {}
-        runs = run_ensemble(models)
-        if runs is None:
-            return super().batch_run(parameter_ranges, repetitions)
-        results = {}
-        for values, res in zip(keys, runs):
-            results.setdefault(values, []).append(res)
-        return results
-
 
 def run_ensemble(models):
     """Run SIR models as one batched launch sequence (``ensemble.SIRBatch``: every member and
     step in one CUDA-graph replay) and return one ``Results`` per model, each equal to that
     model's own ``run()`` (keys ``step``, ``S``, ``I``, ``R``, ``agents.people.state``).
-    Returns None unless every model is a batchable ``SIRModel`` (``ensemble_member``) and all
-    run the same number of steps."""
+    Members with different step counts run as one batch per step count.  Returns None
+    unless every model is a batchable ``SIRModel`` (``ensemble_member``)."""
     from .agentpy import Results
     from .ensemble import SIRBatch
     cache, members = {}, []
@@ -203,23 +174,24 @@ def run_ensemble(models):
         if spec is None:
             return None
         members.append(spec)
-    if not members:
-        return []
-    steps = {spec[6] for spec in members}
-    if len(steps) != 1:
-        return None
-    steps = steps.pop()
-    batch = SIRBatch([(s[0], s[1]) for s in members], [s[2] for s in members],
-                     [s[3] for s in members], [s[4] for s in members],
-                     [s[5] for s in members], steps)
-    batch.run()
-    batch.check()
-    counts = batch.counts.reshape(len(members), steps, 3).cpu().numpy()
-    out = []
-    for k in range(len(members)):
-        data = {"step": list(range(1, steps + 1)),
-                "S": counts[k, :, 0].tolist(), "I": counts[k, :, 1].tolist(),
-                "R": counts[k, :, 2].tolist(),
-                "agents.people.state": batch.final_state(k).cpu().numpy()}
-        out.append(Results(data))
+    out = [None] * len(members)
+    by_steps = {}
+    for k, spec in enumerate(members):
+        by_steps.setdefault(spec[6], []).append(k)
+    for steps, idx in by_steps.items():
+        grp = [members[k] for k in idx]
+        if steps == 0:
+            for k, spec in zip(idx, grp):
+                out[k] = Results({"agents.people.state": np.asarray(spec[2], np.int8).copy()})
+            continue
+        batch = SIRBatch([(s[0], s[1]) for s in grp], [s[2] for s in grp],
+                         [s[3] for s in grp], [s[4] for s in grp], [s[5] for s in grp], steps)
+        batch.run()
+        counts = batch.counts.reshape(len(grp), steps, 3).cpu().numpy()
+        for j, k in enumerate(idx):
+            data = {"step": list(range(1, steps + 1)),
+                    "S": counts[j, :, 0].tolist(), "I": counts[j, :, 1].tolist(),
+                    "R": counts[j, :, 2].tolist(),
+                    "agents.people.state": batch.final_state(j).cpu().numpy()}
+            out[k] = Results(data)
     return out

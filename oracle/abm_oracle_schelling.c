@@ -3,7 +3,9 @@
  * Parity status: UNPINNED against the reference -- the reference's Schelling agent is a
  * placeholder (examples/models/schelling_model.py:54-68: `satisfied = jnp.array([True])`,
  * agents never move), so the rule restated here is the workload's definition:
- *   unhappy iff 8*same < 3*occupied over the Moore-8 torus neighbours (37.5%);
+ *   unhappy iff den*same < num*occupied over the Moore-8 torus neighbours (same/occupied
+ *   below the threshold num/den, e.g. 3/8 = 37.5%; the example's similarity_threshold,
+ *   examples/models/schelling_model.py:36-40, as an exact fraction);
  *   unhappy agent i draws idx = min(floor(f32(uniform(split(coll_key, n)[i]) * e)), e-1)
  *   into the ascending pre-step empty-cell list; lowest claiming id moves.
  * Agents are visited in ascending id order, so "first claim wins" is "lowest id wins".
@@ -15,7 +17,8 @@
 #include "abm_oracle_common.h"
 
 void orc_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, int32_t H,
-                       const uint32_t* coll_keys, int32_t steps, int32_t* stats) {
+                       const uint32_t* coll_keys, int32_t steps, int32_t thr_num,
+                       int32_t thr_den, int32_t* stats) {
   const int64_t C = (int64_t)W * H;
   int8_t* grid = (int8_t*)malloc((size_t)C);
   int32_t* owner = (int32_t*)malloc(sizeof(int32_t) * (size_t)C);
@@ -45,7 +48,7 @@ void orc_schelling_run(int32_t* pos, const int8_t* type, int64_t n, int32_t W, i
           same += v == g;
         }
       target[i] = -1;
-      if (8 * same < 3 * occ) {
+      if ((int64_t)thr_den * same < (int64_t)thr_num * occ) {
         ++unhappy;
         if (e > 0) {
           const float u = unit_float(bits_at(split_at(ck, (uint64_t)i), 0));

@@ -107,8 +107,9 @@ def sir_run_many(graphs, states, rngs, steps, betas, gammas):
     return sts, counts, r
 
 
-def schelling_run(pos, types, W, H, coll_keys):
-    """Schelling steps with the given per-step collection keys uint32[steps, 2].
+def schelling_run(pos, types, W, H, coll_keys, threshold=(3, 8)):
+    """Schelling steps with the given per-step collection keys uint32[steps, 2]; an agent is
+    unhappy iff den * same < num * occupied for ``threshold`` = (num, den).
     Returns (final positions, stats int32[steps, 2] = (unhappy, moved))."""
     p = np.array(pos, dtype=np.int32, copy=True)
     ty = np.ascontiguousarray(types, dtype=np.int8)
@@ -116,7 +117,9 @@ def schelling_run(pos, types, W, H, coll_keys):
     steps = ck.shape[0]
     stats = np.zeros((steps, 2), dtype=np.int32)
     lib().orc_schelling_run(_p(p), _p(ty), ctypes.c_int64(p.size), ctypes.c_int32(W),
-                            ctypes.c_int32(H), _p(ck), ctypes.c_int32(steps), _p(stats))
+                            ctypes.c_int32(H), _p(ck), ctypes.c_int32(steps),
+                            ctypes.c_int32(int(threshold[0])), ctypes.c_int32(int(threshold[1])),
+                            _p(stats))
     return p, stats
 
 

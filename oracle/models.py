@@ -145,15 +145,17 @@ def sir_run(row_ptr, col, state, rng, steps, beta, gamma):
 
 # ---- Schelling segregation on a torus grid ----------------------------------------------
 # Cell (x, y) of a W x H torus has index x*H + y.  Each step, from the pre-step layout:
-#   an agent is unhappy iff 8 * (same-type Moore neighbours) < 3 * (occupied neighbours);
+#   an agent is unhappy iff den * (same-type Moore neighbours) < num * (occupied neighbours)
+#   for the threshold num/den (the workload: 3/8);
 #   an unhappy agent i draws idx = min(floor(f32(uniform(agent_key) * e)), e - 1) into the
 #   ascending list of the e empty cells (agent_key = split(coll_key, N)[i]; one correctly
 #   rounded float32 multiply) and claims that cell; the lowest claiming id wins and moves,
 #   the others stay.  Metrics: (unhappy agents, moved agents).
 
 
-def schelling_step(pos, types, W, H, coll_key):
+def schelling_step(pos, types, W, H, coll_key, threshold=(3, 8)):
     """One Schelling step (small cases).  Returns (new positions, (unhappy, moved))."""
+    num, den = threshold
     pos = np.asarray(pos, dtype=np.int64)
     types = np.asarray(types, dtype=np.int64)
     n = pos.size
@@ -175,7 +177,7 @@ def schelling_step(pos, types, W, H, coll_key):
                 if c >= 0:
                     occ += 1
                     same += int(c == types[i])
-        if 8 * same < 3 * occ:
+        if den * same < num * occ:
             unhappy += 1
             if e == 0:
                 continue
@@ -190,14 +192,14 @@ def schelling_step(pos, types, W, H, coll_key):
     return new.astype(np.int32), (unhappy, len(claims))
 
 
-def schelling_run(pos, types, W, H, coll_keys):
+def schelling_run(pos, types, W, H, coll_keys, threshold=(3, 8)):
     """Schelling steps with per-step collection keys uint32[steps, 2].  Returns (final
     positions, stats int32[steps, 2] = (unhappy, moved))."""
     ck = np.asarray(coll_keys, dtype=np.uint32).reshape(-1, 2)
     p = np.asarray(pos, dtype=np.int32).copy()
     stats = np.zeros((ck.shape[0], 2), dtype=np.int32)
     for t in range(ck.shape[0]):
-        p, stats[t] = schelling_step(p, types, W, H, ck[t])
+        p, stats[t] = schelling_step(p, types, W, H, ck[t], threshold)
     return p, stats
 
 

@@ -273,3 +273,20 @@ def test_server_work_and_order_tables():
     import pytest
     with pytest.raises(ValueError):
         work_table([0], [8192 * 5], dummy=1, capacity=4)
+
+
+def test_schelling_threshold_fraction():
+    from jaxabm_gb300.schelling import threshold_fraction
+    assert threshold_fraction(0.375) == (3, 8)
+    assert threshold_fraction(0.5) == (1, 2)
+    assert threshold_fraction(0.3) == (3, 10)
+    assert threshold_fraction((5, 8)) == (5, 8)
+    assert threshold_fraction(0) == (0, 1) and threshold_fraction(1) == (1, 1)
+    # decisions depend on the threshold only through same/occ with occ <= 8
+    for t in (0.1, 0.3, 0.37, 0.51, 0.74, 0.999):
+        num, den = threshold_fraction(t)
+        for occ in range(1, 9):
+            for same in range(occ + 1):
+                assert (den * same < num * occ) == (same / occ < t), (t, same, occ)
+    with pytest.raises(ValueError):
+        threshold_fraction((1, 0))

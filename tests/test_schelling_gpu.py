@@ -18,7 +18,7 @@ def _keys(seed, steps):
     return ck, ref.reshape(steps, 2)
 
 
-def _run_abi(pos, types, W, H, ck):
+def _run_abi(pos, types, W, H, ck, threshold=(3, 8)):
     from jaxabm_gb300 import _dev, _lib
     n = len(pos)
     p = torch.from_numpy(pos.astype(np.int32)).cuda()
@@ -34,7 +34,8 @@ def _run_abi(pos, types, W, H, ck):
     wsb = _lib.load().abm_schelling_workspace_bytes(n, W, H)
     ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
     _lib.call("abm_schelling_run", _dev.ptr(p), _dev.ptr(t), n, W, H, _dev.ptr(grid), _dev.ptr(ca),
-              _dev.ptr(ck), steps, _dev.ptr(stats), _dev.ptr(ws), wsb, None)
+              _dev.ptr(ck), steps, threshold[0], threshold[1], _dev.ptr(stats), _dev.ptr(ws),
+              wsb, None)
     torch.cuda.synchronize()
     return p.cpu().numpy(), stats.cpu().numpy(), grid.cpu().numpy(), ca.cpu().numpy()
 
@@ -58,6 +59,23 @@ def test_schelling_small_bit_exact(cuda, W, H, density, steps, seed):
     assert np.array_equal(grid, g)
     assert np.array_equal(ca[rp], np.arange(len(pos)))
     assert (ca >= 0).sum() == len(pos)
+
+
+@pytest.mark.parametrize("W,H,threshold", [(40, 40, (1, 2)), (64, 32, (2, 3)), (50, 50, (0, 1)),
+                                           (600, 500, (5, 8)), (30, 30, (1, 1))])
+def test_schelling_other_thresholds(cuda, W, H, threshold):
+    """Thresholds other than 3/8 (1/2 as in the reference example's default, 2/3, 0: nobody
+    unhappy, 5/8 on the four-launch path, 1: everyone with an unlike neighbour unhappy)
+    equal the oracle's run with the same (num, den)."""
+    from jaxabm_gb300.schelling import initial_layout
+    pos, types = initial_layout(W, H, 0.8, 0.5, 11)
+    ck, ckref = _keys(11, 20)
+    p, stats, _, _ = _run_abi(pos, types, W, H, ck, threshold)
+    rp, rstats = coracle.schelling_run(pos, types, W, H, ckref, threshold)
+    assert np.array_equal(stats, rstats)
+    assert np.array_equal(p, rp)
+    if threshold[0] == 0:
+        assert stats[:, 0].sum() == 0
 
 
 def test_schelling_full_config(cuda):
@@ -85,6 +103,19 @@ def test_schelling_model_api(cuda):
     assert np.array_equal(np.array([res["unhappy"], res["moved"]]).T, rstats)
     assert np.array_equal(res["agents.agents.position"], rp)
     assert np.array_equal(res["agents.agents.type"], types)
+
+
+def test_schelling_model_threshold_param(cuda):
+    """SchellingModel(threshold=...) reaches the kernel as an exact fraction."""
+    import jaxabm_gb300 as jx
+    from jaxabm_gb300.schelling import initial_layout
+    res = jx.SchellingModel({"width": 40, "height": 40, "steps": 15, "seed": 2,
+                             "threshold": 0.5}).run()
+    pos, types = initial_layout(40, 40, 0.9, 0.5, 2)
+    _, ckref = _keys(2, 15)
+    rp, rstats = coracle.schelling_run(pos, types, 40, 40, ckref, (1, 2))
+    assert np.array_equal(np.array([res["unhappy"], res["moved"]]).T, rstats)
+    assert np.array_equal(res["agents.agents.position"], rp)
 
 
 def test_schelling_rejects_collisions(cuda):
