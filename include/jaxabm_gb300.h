@@ -497,6 +497,44 @@ ABM_API size_t abm_select_workspace_bytes(int64_t n);
 ABM_API int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t* count,
                                void* workspace, size_t workspace_bytes, void* stream);
 
+/* Compaction by a simple condition, without a mask array: the condition is a postfix
+ * program of at most 16 operations over at most 4 attribute arrays of n entries.
+ * ABM_SELECT_LT..NE push (attrs[op.attr][i] <op> op.value) -- float32 attributes compare
+ * in float32 with value rounded to float32 (as a float32 array compared with a Python
+ * number does), integer attributes compare exactly; ABM_SELECT_AND / OR pop two flags and
+ * push one; ABM_SELECT_NOT flips the top.  The program must leave exactly one flag.
+ * Output as abm_select_indices (ascending indices, *count), workspace of
+ * abm_select_workspace_bytes(n).  Replaces the eager boolean mask of AgentList.select /
+ * AgentCollection.filter (jaxabm/agentpy.py:316-345, jaxabm/agent.py:213-243) for
+ * conditions such as (s["x"] > 0.5) & ~(s["state"] == 2). */
+#define ABM_SELECT_LT 1
+#define ABM_SELECT_LE 2
+#define ABM_SELECT_GT 3
+#define ABM_SELECT_GE 4
+#define ABM_SELECT_EQ 5
+#define ABM_SELECT_NE 6
+#define ABM_SELECT_AND 7
+#define ABM_SELECT_OR 8
+#define ABM_SELECT_NOT 9
+#define ABM_SELECT_F32 0
+#define ABM_SELECT_I32 1
+#define ABM_SELECT_I8 2
+#define ABM_SELECT_U8 3
+typedef struct abm_select_attr {
+  const void* data; /* device array of n entries */
+  int32_t dtype;    /* ABM_SELECT_F32 / I32 / I8 / U8 (bool) */
+  int32_t reserved;
+} abm_select_attr;
+typedef struct abm_select_op {
+  int32_t code;
+  int32_t attr;  /* attribute index of a comparison */
+  double value;  /* constant of a comparison */
+} abm_select_op;
+ABM_API int abm_select_where(const abm_select_attr* attrs, int32_t nattrs,
+                             const abm_select_op* program, int32_t nops, int64_t n,
+                             int32_t* out_idx, int64_t* count, void* workspace,
+                             size_t workspace_bytes, void* stream);
+
 /* Same result as abm_select_indices, without any workspace and without allocating.
  * No counterpart in the reference (it allocates through JAX for every selection).
  * For callers that cannot allocate device memory when they select: a host application

@@ -90,6 +90,7 @@ SIGNATURES = {
     "abm_opinion_grad_reduce": (_int, [_p, _i64, _i32, _p, _p]),
     "abm_select_workspace_bytes": (_sz, [_i64]),
     "abm_select_indices": (_int, [_p, _i64, _p, _p, _p, _sz, _p]),
+    "abm_select_where": (_int, [_p, _i32, _p, _i32, _i64, _p, _p, _p, _sz, _p]),
     "abm_select_indices_noalloc": (_int, [_p, _i64, _p, _p, _p]),
     "abm_gather_rows": (_int, [_p, _i64, _i64, _p, _i64, _p, _p]),
     "abm_reduce_workspace_bytes": (_sz, [_i64]),

@@ -119,10 +119,11 @@ class AgentCollection:
 
     def filter(self, condition: Callable[[Dict[str, Any]], Any]) -> "AgentCollection":
         """Agents whose ``condition(states)`` mask is true, in ascending id order
-        (jaxabm/agent.py:213-243); compaction runs in the warp-ballot kernel."""
-        from .select import compact_states
-        mask = condition({k: self._states[k] for k in self._states})
-        new_states, count = compact_states(self._states, mask)
+        (jaxabm/agent.py:213-243); compaction runs in the warp-ballot kernels, with simple
+        conditions evaluated inside them (``select.compact_where``)."""
+        from .select import compact_where
+        new_states, count = compact_where({k: self._states[k] for k in self._states},
+                                          condition)
         filtered = AgentCollection.__new__(AgentCollection)
         filtered.agent_type = self.agent_type
         filtered.num_agents = count

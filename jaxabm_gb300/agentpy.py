@@ -28,7 +28,7 @@ from . import random as jrandom
 from .agent import AgentCollection, AgentType
 from .core import ModelConfig, verbose
 from .model import Model as JaxModel
-from .select import compact_states
+from .select import compact_where
 from .utils import convert_to_numpy, format_time
 
 
@@ -143,10 +143,11 @@ class AgentList:
         return self.n
 
     def select(self, condition) -> "AgentList":
-        """Agents satisfying ``condition(states)`` (jaxabm/agentpy.py:316-345)."""
+        """Agents satisfying ``condition(states)`` (jaxabm/agentpy.py:316-345).  A condition
+        made of attribute comparisons with numbers and &, |, ~ runs as a predicate program
+        inside the compaction kernels; any other condition is evaluated into a mask."""
         states = self.states
-        mask = condition(states)
-        new_states, count = compact_states(states, mask)
+        new_states, count = compact_where(states, condition)
         filtered = AgentList.__new__(AgentList)
         filtered.model = self.model
         filtered.n = count

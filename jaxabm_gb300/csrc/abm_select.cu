@@ -170,6 +170,130 @@ __global__ void gather_rows_bytes(const uint8_t* __restrict__ src, const int32_t
   }
 }
 
+// ---- compaction by a predicate program (AgentList.select with a simple condition) --------
+// The condition is a postfix program over at most kPredAttrs attribute arrays: comparisons
+// of one attribute with a constant push a flag, AND / OR pop two and push one, NOT flips
+// the top.  The count and scatter passes evaluate it for their 16 elements per thread, so
+// the boolean mask is never written; the tile scan is the mask path's.
+constexpr int kPredAttrs = 4;
+constexpr int kPredOps = 16;
+
+struct Predicate {
+  const void* attr[kPredAttrs];
+  int32_t dtype[kPredAttrs];
+  int32_t nops;
+  int32_t code[kPredOps];
+  int32_t arg[kPredOps];
+  float value_f32[kPredOps];
+  double value_f64[kPredOps];
+};
+
+template <typename T>
+__device__ __forceinline__ bool compare(T v, T c, int code) {
+  switch (code) {
+    case ABM_SELECT_LT: return v < c;
+    case ABM_SELECT_LE: return v <= c;
+    case ABM_SELECT_GT: return v > c;
+    case ABM_SELECT_GE: return v >= c;
+    case ABM_SELECT_EQ: return v == c;
+    default: return v != c;
+  }
+}
+
+// The program's result for element i (a stack of flags held as bits).
+__device__ __forceinline__ bool eval_predicate(const Predicate& P, int64_t i) {
+  uint32_t stack = 0;
+  int sp = 0;
+  for (int k = 0; k < P.nops; ++k) {
+    const int code = P.code[k];
+    if (code <= ABM_SELECT_NE) {
+      const int a = P.arg[k];
+      bool r;
+      switch (P.dtype[a]) {
+        case ABM_SELECT_F32:
+          r = compare(static_cast<const float*>(P.attr[a])[i], P.value_f32[k], code);
+          break;
+        case ABM_SELECT_I32:
+          r = compare(static_cast<double>(static_cast<const int32_t*>(P.attr[a])[i]),
+                      P.value_f64[k], code);
+          break;
+        case ABM_SELECT_I8:
+          r = compare(static_cast<double>(static_cast<const int8_t*>(P.attr[a])[i]),
+                      P.value_f64[k], code);
+          break;
+        default:
+          r = compare(static_cast<double>(static_cast<const uint8_t*>(P.attr[a])[i]),
+                      P.value_f64[k], code);
+          break;
+      }
+      stack = (stack & ~(1u << sp)) | (static_cast<uint32_t>(r) << sp);
+      ++sp;
+    } else if (code == ABM_SELECT_NOT) {
+      stack ^= 1u << (sp - 1);
+    } else {
+      const uint32_t b = (stack >> (sp - 1)) & 1u, a = (stack >> (sp - 2)) & 1u;
+      const uint32_t r = code == ABM_SELECT_AND ? (a & b) : (a | b);
+      sp -= 1;
+      stack = (stack & ~(1u << (sp - 1))) | (r << (sp - 1));
+    }
+  }
+  return (stack & 1u) != 0;
+}
+
+__device__ __forceinline__ uint32_t predicate_flags(const Predicate& P, int64_t n, int64_t base) {
+  uint32_t bits = 0;
+#pragma unroll 4
+  for (int j = 0; j < kSelPerThread; ++j)
+    if (base + j < n && eval_predicate(P, base + j)) bits |= 1u << j;
+  return bits;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+select_pred_count_kernel(const Predicate P, int64_t n, int32_t* __restrict__ tile_counts) {
+  __shared__ int swarp[kSelThreads / 32];
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kSelPerThread;
+  const int c = __popc(predicate_flags(P, n, base));
+  const int wsum = abm::warp_sum(c);
+  if ((threadIdx.x & 31) == 0) swarp[threadIdx.x >> 5] = wsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kSelThreads / 32; ++w) s += swarp[w];
+    tile_counts[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+select_pred_scatter_kernel(const Predicate P, int64_t n, const int64_t* __restrict__ tile_offsets,
+                           int32_t* __restrict__ out_idx) {
+  __shared__ int swarp[kSelThreads / 32];
+  __shared__ int32_t sidx[kTile];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kSelPerThread;
+  const uint32_t bits = predicate_flags(P, n, base);
+  const int c = __popc(bits);
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) swarp[warp] = incl;
+  __syncthreads();
+  int warp_excl = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < kSelThreads / 32; ++w) {
+    warp_excl += w < warp ? swarp[w] : 0;
+    total += swarp[w];
+  }
+  int pos = warp_excl + (incl - c);
+  for (uint32_t rest = bits; rest; rest &= rest - 1)
+    sidx[pos++] = (int32_t)(base + __ffs(rest) - 1);
+  __syncthreads();
+  int32_t* __restrict__ dst = out_idx + tile_offsets[blockIdx.x];
+  for (int k = threadIdx.x; k < total; k += kSelThreads) dst[k] = sidx[k];
+}
+
 // ---- reductions -------------------------------------------------------------------------
 constexpr int kRedThreads = 256;
 
@@ -257,6 +381,63 @@ int abm_select_indices(const uint8_t* mask, int64_t n, int32_t* out_idx, int64_t
   select_scatter_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(mask, n, vec_ok, tile_offsets,
                                                                 out_idx);
   return abm_host::check_launch("abm_select_indices/scatter");
+}
+
+int abm_select_where(const abm_select_attr* attrs, int32_t nattrs, const abm_select_op* program,
+                     int32_t nops, int64_t n, int32_t* out_idx, int64_t* count, void* workspace,
+                     size_t workspace_bytes, void* stream) {
+  if (!attrs || !program || !out_idx || !count || nattrs <= 0 || nattrs > kPredAttrs ||
+      nops <= 0 || nops > kPredOps || n < 0 || n > 0x7FFFFFFFll)
+    return ABM_ERR_BADARG;
+  Predicate P{};
+  for (int a = 0; a < nattrs; ++a) {
+    if (!attrs[a].data || attrs[a].dtype < ABM_SELECT_F32 || attrs[a].dtype > ABM_SELECT_U8)
+      return ABM_ERR_BADARG;
+    P.attr[a] = attrs[a].data;
+    P.dtype[a] = attrs[a].dtype;
+  }
+  // the program must leave exactly one flag and never pop an empty stack
+  int depth = 0;
+  for (int k = 0; k < nops; ++k) {
+    const int code = program[k].code;
+    if (code >= ABM_SELECT_LT && code <= ABM_SELECT_NE) {
+      if (program[k].attr < 0 || program[k].attr >= nattrs) return ABM_ERR_BADARG;
+      ++depth;
+    } else if (code == ABM_SELECT_NOT) {
+      if (depth < 1) return ABM_ERR_BADARG;
+    } else if (code == ABM_SELECT_AND || code == ABM_SELECT_OR) {
+      if (depth < 2) return ABM_ERR_BADARG;
+      --depth;
+    } else {
+      return ABM_ERR_BADARG;
+    }
+    P.code[k] = code;
+    P.arg[k] = program[k].attr;
+    P.value_f32[k] = static_cast<float>(program[k].value);
+    P.value_f64[k] = program[k].value;
+  }
+  if (depth != 1) return ABM_ERR_BADARG;
+  P.nops = nops;
+  cudaStream_t s = abm_host::as_stream(stream);
+  if (n == 0) {
+    return abm_host::record_cuda_error(cudaMemsetAsync(count, 0, sizeof(int64_t), s),
+                                       "abm_select_where");
+  }
+  const size_t need = abm_select_workspace_bytes(n);
+  if (!workspace || workspace_bytes < need || !abm_host::aligned(workspace, 256))
+    return ABM_ERR_WORKSPACE;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  int32_t* tile_counts = static_cast<int32_t*>(workspace);
+  int64_t* tile_offsets = reinterpret_cast<int64_t*>(
+      static_cast<char*>(workspace) + align_up((size_t)tiles * sizeof(int32_t), 256));
+  select_pred_count_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(P, n, tile_counts);
+  int st = abm_host::check_launch("abm_select_where/count");
+  if (st) return st;
+  select_scan_kernel<<<1, 1024, 0, s>>>(tile_counts, tiles, tile_offsets, count);
+  st = abm_host::check_launch("abm_select_where/scan");
+  if (st) return st;
+  select_pred_scatter_kernel<<<(unsigned)tiles, kSelThreads, 0, s>>>(P, n, tile_offsets, out_idx);
+  return abm_host::check_launch("abm_select_where/scatter");
 }
 
 int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes, const int32_t* idx,

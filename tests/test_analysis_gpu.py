@@ -55,7 +55,7 @@ def test_sir_analysis_runs_batched_and_matches_serial(cuda):
     assert set(idx) == {"I", "R", "S"} and set(idx["R"]) == {"beta", "gamma"}
 
 
-def test_non_sir_analysis_runs_serially(cuda):
+def test_random_walk_analysis_is_batched(cuda):
     import jaxabm_gb300 as jx
 
     def factory(params=None, config=None):
@@ -66,7 +66,7 @@ def test_non_sir_analysis_runs_serially(cuda):
     sa = jx.SensitivityAnalysis(factory, {"sigma": (0.001, 0.05)}, ["mean_x", "missing"],
                                 num_samples=3, seed=1)
     res = sa.run(verbose=False)
-    assert not sa.batched
+    assert sa.batched  # random-walk samples run as one batch, each equal to its own run()
     for i in range(3):
         ref = factory(params={"sigma": float(sa.samples[i, 0])},
                       config=jx.ModelConfig(seed=1000 + i)).run()
@@ -125,7 +125,7 @@ def test_population_methods_run_batched(cuda, method):
     assert len(hist["params"]) == 2
 
 
-def test_calibrator_non_sir_runs_serially(cuda):
+def test_calibrator_random_walk_population_is_batched(cuda):
     import jaxabm_gb300 as jx
 
     def factory(params=None, config=None):
@@ -137,4 +137,4 @@ def test_calibrator_non_sir_runs_serially(cuda):
                            param_bounds={"sigma": (0.001, 0.1)}, max_iterations=1,
                            method="es", evaluation_steps=3, num_evaluation_runs=1, seed=1)
     c.calibrate(verbose=False)
-    assert c.batched_evaluations == 0 and len(c.loss_history) == 1
+    assert c.batched_evaluations == 1 and len(c.loss_history) == 1

@@ -290,3 +290,30 @@ def test_schelling_threshold_fraction():
                 assert (den * same < num * occ) == (same / occ < t), (t, same, occ)
     with pytest.raises(ValueError):
         threshold_fraction((1, 0))
+
+
+def test_select_condition_compiler():
+    """Conditions made of attribute comparisons with numbers and &, |, ~ become postfix
+    predicate programs (a reflected comparison `c < s[a]` is `s[a] > c`; a bool attribute
+    alone is `!= 0`); anything else is left to eager evaluation (None)."""
+    import torch
+    from jaxabm_gb300.select import (SELECT_AND, SELECT_EQ, SELECT_GT, SELECT_LE, SELECT_NE,
+                                     SELECT_NOT, SELECT_OR, compile_condition)
+    st = {"x": torch.zeros(10), "k": torch.zeros(10, dtype=torch.int8),
+          "f": torch.zeros(10, dtype=torch.bool), "d": torch.zeros(10, dtype=torch.float64),
+          "m": torch.zeros((10, 2))}
+    assert compile_condition(lambda s: (s["x"] > 0.5) & ~(s["k"] == 2), st) == (
+        [(SELECT_GT, 0, 0.5), (SELECT_EQ, 1, 2.0), (SELECT_NOT, 0, 0.0), (SELECT_AND, 0, 0.0)],
+        ["x", "k"])
+    assert compile_condition(lambda s: 0.25 < s["x"], st) == ([(SELECT_GT, 0, 0.25)], ["x"])
+    assert compile_condition(lambda s: s["f"], st) == ([(SELECT_NE, 0, 0.0)], ["f"])
+    assert compile_condition(lambda s: (s["x"] > 0.1) | (s["x"] <= 0.9), st) == (
+        [(SELECT_GT, 0, 0.1), (SELECT_LE, 0, 0.9), (SELECT_OR, 0, 0.0)], ["x"])
+    for cond in (lambda s: s["x"] * 2 > 1, lambda s: s["d"] > 1, lambda s: s["m"] > 0,
+                 lambda s: (s["x"] > 0.1) and (s["x"] < 0.5), lambda s: s["x"] > s["x"],
+                 lambda s: torch.ones(10, dtype=torch.bool), lambda s: s.get("x"),
+                 lambda s: s["nope"] > 0):
+        assert compile_condition(cond, st) is None
+    many = lambda s: ((s["x"] > 0) & (s["x"] > 1) & (s["x"] > 2) & (s["x"] > 3) & (s["x"] > 4)
+                      & (s["x"] > 5) & (s["x"] > 6) & (s["x"] > 7) & (s["x"] > 8))  # 17 ops
+    assert compile_condition(many, st) is None

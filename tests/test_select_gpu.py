@@ -93,3 +93,70 @@ def test_select_agentlist_api(cuda):
     y = m.walkers.y.cpu().numpy()
     assert len(sel) == int((y < 0.25).sum())
     assert np.array_equal(sel.y.cpu().numpy(), y[y < 0.25])
+
+
+@pytest.mark.parametrize("n", [1, 15, 4096, 4097, 100_003, 1 << 20])
+def test_select_where_matches_numpy(cuda, n):
+    """Predicate programs over float32, int32, int8 and bool attributes select exactly the
+    indices numpy's boolean evaluation does (float32 compares in float32)."""
+    from jaxabm_gb300.select import select_where
+    rs = np.random.RandomState(n)
+    h = {"x": rs.rand(n).astype(np.float32), "i": rs.randint(-5, 6, n).astype(np.int32),
+         "k": rs.randint(0, 3, n).astype(np.int8), "f": rs.rand(n) < 0.3}
+    st = {k: torch.from_numpy(v).cuda() for k, v in h.items()}
+    conds = [
+        (lambda s: s["x"] > 0.5, lambda s: s["x"] > np.float32(0.5)),
+        (lambda s: (s["x"] >= 0.2) & (s["x"] < 0.6), lambda s: (s["x"] >= np.float32(0.2))
+         & (s["x"] < np.float32(0.6))),
+        (lambda s: ~(s["k"] == 2) | (s["i"] <= -3), lambda s: ~(s["k"] == 2) | (s["i"] <= -3)),
+        (lambda s: s["f"], lambda s: s["f"]),
+        (lambda s: (s["i"] != 0) & s["f"] & (0.1 < s["x"]),
+         lambda s: (s["i"] != 0) & s["f"] & (s["x"] > np.float32(0.1))),
+        (lambda s: s["x"] > 2.0, lambda s: s["x"] > 2.0),  # nothing selected
+        (lambda s: s["x"] >= 0.0, lambda s: s["x"] >= 0.0),  # everything selected
+    ]
+    from jaxabm_gb300 import select as sel
+    for cond, ref in conds:
+        idx, c = select_where(st, cond)
+        assert sel.last_path == "predicate"
+        want = np.nonzero(ref(h))[0]
+        assert c == len(want) and np.array_equal(idx.cpu().numpy(), want)
+
+
+def test_select_uses_predicate_path_and_falls_back(cuda):
+    """AgentList.select runs simple conditions as predicate programs and anything else
+    through an eager mask; both give numpy's selection."""
+    import jaxabm_gb300 as jx
+    from jaxabm_gb300 import select as sel
+
+    class M(jx.Model):
+        def setup(self):
+            self.walkers = self.add_agents(5000, jx.RandomWalker, name="walkers")
+
+    m = M({"steps": 2, "seed": 3})
+    m.run()
+    x, y = m.walkers.x.cpu().numpy(), m.walkers.y.cpu().numpy()
+    a = m.walkers.select(lambda s: (s["x"] < 0.3) | (s["y"] > 0.8))
+    assert sel.last_path == "predicate"
+    keep = (x < np.float32(0.3)) | (y > np.float32(0.8))
+    assert len(a) == keep.sum() and np.array_equal(a.x.cpu().numpy(), x[keep])
+    b = m.walkers.select(lambda s: (s["x"] + s["y"]) > 1.0)
+    assert sel.last_path == "mask"
+    keep = (x + y) > 1.0
+    assert len(b) == keep.sum() and np.array_equal(b.y.cpu().numpy(), y[keep])
+
+
+def test_select_where_rejects_bad_programs(cuda):
+    from jaxabm_gb300 import _lib
+    from jaxabm_gb300.select import ATTR_DTYPE, OP_DTYPE
+    x = torch.rand(100, device="cuda")
+    attrs = np.array([(x.data_ptr(), 0, 0)], dtype=ATTR_DTYPE)
+    idx = torch.empty(100, dtype=torch.int32, device="cuda")
+    cnt = torch.empty(1, dtype=torch.int64, device="cuda")
+    ws = torch.empty(4096, dtype=torch.uint8, device="cuda")
+    L = _lib.load()
+    for prog in ([(7, 0, 0.0)], [(3, 0, 0.5), (3, 0, 0.2)], [(3, 1, 0.5)], [(12, 0, 0.0)]):
+        ops = np.array(prog, dtype=OP_DTYPE)
+        assert L.abm_select_where(attrs.ctypes.data, 1, ops.ctypes.data, len(prog), 100,
+                                  idx.data_ptr(), cnt.data_ptr(), ws.data_ptr(), ws.numel(),
+                                  None) == _lib.ABM_ERR_BADARG, prog
