@@ -372,3 +372,45 @@ def run_ensemble(models):
                             **{f"m{q + 1}": rows[:, j, q].tolist() for q in range(4)}, **data}
                 out[k] = Results(data)
     return out
+
+
+def main(argv=None):
+    """``python -m jaxabm_gb300.opinion``: times one calibration batch -- the forward with a
+    checkpoint every ``--every`` steps, then the reverse sweep -- on a random
+    ``--degree``-regular graph of ``--n`` nodes with ``--instances`` parameter sets, and
+    prints one JSON line per repetition (CUDA events on the current stream)."""
+    import argparse
+    import json
+
+    from . import _build
+    from .sir import random_regular
+    ap = argparse.ArgumentParser(prog="python -m jaxabm_gb300.opinion")
+    ap.add_argument("--n", type=int, default=1 << 18)
+    ap.add_argument("--degree", type=int, default=16)
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--every", type=int, default=20)
+    ap.add_argument("--reps", type=int, default=2)
+    args = ap.parse_args(argv)
+    _build.build()
+    rp, col = random_regular(args.n, args.degree, 0)
+    p = calibration_params(args.instances)
+    b = OpinionBatch(rp, col, initial_opinions(args.n, 0), p[:, 0], p[:, 1], p[:, 2])
+    target = np.array([0.5, 0.3, 0.2, 0.15])
+    for rep in range(args.reps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        b.forward(args.steps, args.every)
+        ev[1].record()
+        g = b.backward(target)
+        ev[2].record()
+        ev[2].synchronize()
+        print(json.dumps({"rep": rep, "n": args.n, "instances": args.instances,
+                          "steps": args.steps, "every": args.every,
+                          "ms_forward": ev[0].elapsed_time(ev[1]),
+                          "ms_reverse": ev[1].elapsed_time(ev[2]),
+                          "grad_sum": float(g.sum())}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
