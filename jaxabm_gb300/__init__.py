@@ -16,6 +16,7 @@ from ._lib import AbmError
 from .agent import AgentCollection, AgentType
 from .agentpy import Agent, AgentList, Environment, Grid, Model, Network, Results
 from .core import ModelConfig, has_cuda, set_verbose, show_info
+from .trace import set_tracing, tracing
 from .model import Model as JaxModel
 from .registry import StepKernel, UnregisteredAgentError, lookup, register_step, unregister_step
 from .utils import convert_to_numpy, format_time
@@ -53,6 +54,6 @@ __all__ = [
     "Agent", "AgentList", "Environment", "Grid", "Network", "Model", "Results",
     "AgentType", "AgentCollection", "JaxModel", "ModelConfig",
     "StepKernel", "UnregisteredAgentError", "register_step", "unregister_step", "lookup",
-    "convert_to_numpy", "format_time", "random", "build", "show_info", "set_verbose",
+    "convert_to_numpy", "format_time", "random", "build", "show_info", "set_verbose", "set_tracing", "tracing",
     "RandomWalker", "RandomWalkModel", "AbmError", "SensitivityAnalysis", "ModelCalibrator",
 ]

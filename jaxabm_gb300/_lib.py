@@ -8,6 +8,7 @@ import ctypes
 import os
 import threading
 
+from . import trace as _trace
 from ._build import LIB_PATH
 
 ABM_OK = 0
@@ -154,6 +155,11 @@ def check(status, where):
 
 
 def call(name, *args):
-    """Call a C-ABI entry point and raise AbmError on a non-zero status."""
+    """Call a C-ABI entry point and raise AbmError on a non-zero status (inside an NVTX
+    range named after the entry point when tracing is on)."""
     fn = getattr(load(), name)
+    if _trace.tracing():
+        with _trace.nvtx_range(name):
+            check(fn(*args), name)
+        return
     check(fn(*args), name)

@@ -12,6 +12,7 @@ import torch
 
 from .core import ModelConfig
 from .registry import lookup
+from .trace import nvtx_range
 
 AgentState = Dict[str, Any]
 
@@ -90,15 +91,18 @@ class AgentCollection:
         if self.model_config is None:
             raise RuntimeError("Model config not set for AgentCollection. Ensure "
                                "Model.initialize() was called.")
-        self._states, self._last_metrics = self.kernel.step(self._states, key, self.params,
-                                                            self._env)
+        with nvtx_range(f"AgentCollection.update {self.kernel.name}"):
+            self._states, self._last_metrics = self.kernel.step(self._states, key, self.params,
+                                                                self._env)
 
     def run_steps(self, coll_keys: torch.Tensor):
         """``coll_keys.shape[0]`` updates as one fused launch sequence; returns the
         per-step metrics tensor [T, m] (or None)."""
         if self._states is None:
             raise ValueError("Agent collection not initialized. Call init() first.")
-        self._states, metrics = self.kernel.run(self._states, coll_keys, self.params, self._env)
+        with nvtx_range(f"AgentCollection.run_steps {self.kernel.name}"):
+            self._states, metrics = self.kernel.run(self._states, coll_keys, self.params,
+                                                    self._env)
         return metrics
 
     def get_states(self) -> Dict[str, Any]:

@@ -543,11 +543,10 @@ class Model:
         return (self.update_state if (has_step or has_update) else None,
                 self.compute_metrics if has_metrics else None)
 
-    def run(self, steps: Optional[int] = None) -> Results:
-        """Set up, run and collect results (jaxabm/agentpy.py:1040-1114)."""
-        if steps is not None:
-            self.steps = steps
-        self._running = True
+    def core_model(self) -> JaxModel:
+        """Run ``setup()`` and return the core :class:`JaxModel` that :meth:`run` drives
+        (its collections and environment are this model's), e.g. to step it piecewise or
+        to checkpoint it with ``state_dict()`` (jaxabm/agentpy.py:1040-1075)."""
         config = ModelConfig(steps=self.steps, collect_interval=1, seed=self.seed)
         self.setup()
         update_fn, metrics_fn = self._hooks()
@@ -558,6 +557,14 @@ class Model:
             self._jax_model.add_agent_collection(name, agent_list.collection)
         for name, value in self.env.state.items():
             self._jax_model.add_env_state(name, value)
+        return self._jax_model
+
+    def run(self, steps: Optional[int] = None) -> Results:
+        """Set up, run and collect results (jaxabm/agentpy.py:1040-1114)."""
+        if steps is not None:
+            self.steps = steps
+        self._running = True
+        self.core_model()
         start = time.time()
         results_dict = self._jax_model.run()
         simulation_time = time.time() - start

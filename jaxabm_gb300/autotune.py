@@ -10,7 +10,8 @@ keeps the fastest, and caches the choice in a JSON file keyed by GPU and workloa
 
 Results never depend on the choice: the model is integer-valued and every kernel's work
 is order-free (commutative integer atomics, per-agent decisions), so any configuration
-produces bit-identical compartments and counts (tests/test_autotune_gpu.py).
+produces bit-identical compartments and counts (tests/test_autotune.py,
+test_results_identical_under_any_launch).
 """
 
 import json

@@ -73,6 +73,18 @@ __device__ __forceinline__ uint32_t legacy_bits_at(uint2 key, uint64_t count, ui
 __device__ __forceinline__ float unit_float(uint32_t b) {
   return __uint_as_float((b >> 9) | 0x3F800000u) - 1.0f;
 }
+// unit_float(b) is m * 2^-23 with m = b >> 9, so for a float p the comparison
+// unit_float(b) < p equals the integer comparison (b >> 9) < unit_threshold(p): the
+// scaling by 2^23 and the ceiling are exact, p >= 1 admits every m, and p <= 0 or NaN
+// admits none.
+__host__ __device__ __forceinline__ uint32_t unit_threshold(float p) {
+  if (!(p > 0.0f)) return 0u;
+  if (p >= 1.0f) return 1u << 23;
+  return static_cast<uint32_t>(ceilf(p * 8388608.0f));
+}
+__device__ __forceinline__ bool unit_below(uint32_t b, uint32_t threshold) {
+  return (b >> 9) < threshold;
+}
 __device__ __forceinline__ float uniform_from_bits(uint32_t b, float lo, float hi) {
   const float span = __fsub_rn(hi, lo);
   const float v = __fadd_rn(__fmul_rn(unit_float(b), span), lo);

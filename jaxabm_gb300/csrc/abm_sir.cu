@@ -952,20 +952,22 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // order, from a queue counter) and runs all of its steps with the instance's words in
 // shared memory: the sweep reads them there, decisions read the neighbours' compartments
 // there, and count updates are shared-memory atomics.  Only CSR rows, row offsets and hub
-// counts come from global memory.  A step is four phases separated by __syncthreads:
+// counts come from global memory.  A step is three phases separated by __syncthreads:
 //   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
 //             the susceptible agents with infected neighbours and the infected agents to
 //             two lists (global scratch of the CTA, L2-resident).
-//   decide    warps take rounds of 32 list entries from a round counter, so that every
-//             warp has work however small the instance: a susceptible agent per lane (rows
-//             longer than 32 slots by the whole warp) or an infected agent's recovery draw
-//             per lane; changes go to the CTA's change list.  Nothing is written to the
-//             words, so every decision sees the pre-step states.
+//   decide    warps take paired rounds from a round counter, so that every warp has work
+//             however small the instance: per lane one susceptible agent (rows longer
+//             than 32 slots by the whole warp) and one infected agent's recovery draw;
+//             the recovery chain and the susceptible agent's key derivation run while its
+//             row is in flight.  Changes go to the CTA's change list.  Nothing is written
+//             to the words, so every decision sees the pre-step states.
 //   apply     warps take groups of 32 changes: +1 on each changed agent's compartment
-//             field and +-1 on its neighbours' counts (push of the concatenated rows).
-//   finalize  thread 0: S/I/R counts of the step, key chain, next step's key.
-// Decision rounds alternate between the two lists and are taken two ahead, so that the
-// list entries and row offsets of the next rounds are in flight while one is decided.
+//             field and +-1 on its neighbours' counts (push of the concatenated rows);
+//             meanwhile thread 0 records the step's S/I/R counts and advances the keys.
+// Rounds are taken two ahead, so that the list entries and row offsets of the next
+// rounds are in flight while one is decided.  Draws compare the 23 random mantissa bits
+// with an integer threshold, which equals the float comparison of jax.random.uniform.
 // An instance at step 0 may build its words in the kernel from the int8 compartments
 // (hub marks, column hub tags, initial counts) instead of reading packed words.  The
 // words are written back, with the 2-bit compartment copy, when the instance's steps of
@@ -1107,7 +1109,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
     const int32_t* __restrict__ rp = I->row_ptr;
     int32_t* __restrict__ adj = I->adj;
     int32_t* hubs = I->hub_counts;
-    const float beta = I->beta, gamma = I->gamma;
+    const uint32_t tbeta = abm::unit_threshold(I->beta), tgamma = abm::unit_threshold(I->gamma);
     if (states8 != nullptr && t_begin == 0) {
       // words built here from the int8 compartments: compartment, hub mark (degree >=
       // 63, whose count starts at 0 in hub_counts), the columns' hub tags, then every
@@ -1185,6 +1187,11 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
     int t = t_begin;
     for (; t < t_end; ++t) {
       if (S.num_i == 0) break;  // uniform: nothing can change any more
+      // counters of the previous step's apply, free since its closing barrier
+      if (threadIdx.x == 0) {
+        S.nchanges = 0;
+        S.next_group = 0;
+      }
       // ---- sweep: lists of susceptible agents with infected neighbours, infected agents
       unsigned long long my_cands = 0;
       for (;;) {
@@ -1241,81 +1248,91 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       for (int o = 16; o > 0; o >>= 1) my_cands += __shfl_down_sync(kFull, my_cands, o);
       if (lane == 0 && my_cands) atomicAdd(&S.cands, my_cands);
       __syncthreads();
-      // ---- decide: rounds of 32 list entries, taken from a round counter ----------------
+      // ---- decide: paired rounds taken from a round counter -----------------------------
+      // Round p holds susceptible entries 32p..32p+31 and infected entries 32p..32p+31, one
+      // of each per lane: the infected entry's recovery chain and the susceptible entry's
+      // key derivation run while its row is in flight.  Entries are loaded two rounds ahead
+      // and row offsets one round ahead.
       uint2 next_rng = make_uint2(0, 0), next_coll = make_uint2(0, 0);
       if (threadIdx.x == 0) {
+        S.next_chunk = 0;  // the sweep is over
         next_rng = abm::split_at(make_uint2(S.rng0, S.rng1), 0);
         if (t + 1 < I->steps) next_coll = step_key_of(I, t + 1, next_rng);
       }
       const uint2 coll = make_uint2(S.coll0, S.coll1);
       const int ns = S.ns, ni = S.ni;
-      const int rounds_s = (ns + 31) >> 5, rounds = rounds_s + ((ni + 31) >> 5);
+      const int rounds = max((ns + 31) >> 5, (ni + 31) >> 5);
       unsigned long long my_scanned = 0;
       int my_si = 0, my_ir = 0, my_draws = 0;
-      // Rounds are taken two ahead: the list entries of the round after next and the row
-      // offsets of the next round are in flight while a round is decided.
       auto take = [&]() {
         int r = 0;
         if (lane == 0) r = atomicAdd(&S.next_round, 1);
         return __shfl_sync(kFull, r, 0);
       };
-      // susceptible and infected rounds alternate (row-reading rounds wait on memory,
-      // recovery rounds on the ALU), then the rest of the longer list follows
-      const int rounds_i = rounds - rounds_s;
-      const int both = 2 * min(rounds_s, rounds_i);
-      auto is_s = [&](int r) {
-        return r < both ? (r & 1) == 0 : rounds_s > rounds_i;
+      auto s_entry = [&](int r) {
+        const int f = 32 * r + lane;
+        return r < rounds && f < ns ? static_cast<int>(slist[f]) : -1;
       };
-      auto index_of = [&](int r) { return r < both ? r >> 1 : (both >> 1) + (r - both); };
-      auto entry_of = [&](int r) {
-        if (r >= rounds) return -1;
-        const int f = 32 * index_of(r) + lane;
-        if (is_s(r)) return f < ns ? static_cast<int>(slist[f]) : -1;
-        return f < ni ? static_cast<int>(ilist[f]) : -1;
+      auto i_entry = [&](int r) {
+        const int f = 32 * r + lane;
+        return r < rounds && f < ni ? static_cast<int>(ilist[f]) : -1;
       };
       int r_cur = take(), r_nxt = take();
-      int e_cur = entry_of(r_cur), e_nxt = entry_of(r_nxt);
+      int es_cur = s_entry(r_cur), ei_cur = i_entry(r_cur);
+      int es_nxt = s_entry(r_nxt), ei_nxt = i_entry(r_nxt);
       int a_cur = 0, b_cur = 0;
-      if (r_cur < rounds && is_s(r_cur) && e_cur >= 0) {
-        a_cur = __ldcs(rp + e_cur);
-        b_cur = __ldcs(rp + e_cur + 1);
+      if (es_cur >= 0) {
+        a_cur = __ldcs(rp + es_cur);
+        b_cur = __ldcs(rp + es_cur + 1);
       }
-      for (; r_cur < rounds; r_cur = r_nxt, r_nxt = take(), e_nxt = entry_of(r_nxt)) {
-        const int r = r_cur, e = e_cur;
+      while (r_cur < rounds) {
+        const int e = es_cur, ei = ei_cur;
         const int ra = a_cur, rb = b_cur;
-        e_cur = e_nxt;
         a_cur = b_cur = 0;
-        if (r_nxt < rounds && is_s(r_nxt) && e_nxt >= 0) {
-          a_cur = __ldcs(rp + e_nxt);
-          b_cur = __ldcs(rp + e_nxt + 1);
+        if (es_nxt >= 0) {
+          a_cur = __ldcs(rp + es_nxt);
+          b_cur = __ldcs(rp + es_nxt + 1);
         }
-        if (!is_s(r)) {
-          // infected agents: recovery draws
-          bool rec = false;
-          if (e >= 0) {
-            const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)e), 1);
-            rec = abm::unit_float(abm::bits_at(krec, 0)) < gamma;
-          }
-          my_ir += rec;
-          res_record(rec, e, 2u, changes, &S.nchanges, lane);
-          continue;
-        }
-        // susceptible agents with infected neighbours, one per lane
+        r_cur = r_nxt;
+        es_cur = es_nxt;
+        ei_cur = ei_nxt;
+        r_nxt = take();
+        es_nxt = s_entry(r_nxt);
+        ei_nxt = i_entry(r_nxt);
+        // susceptible entry (a susceptible agent with infected neighbours): the first
+        // columns of its row are loaded before the draw chains below
         const bool valid = e >= 0;
-        int i = 0, row0 = 0, deg = 0, cnt = 0, scanned = 0;
-        bool infected = false, heavy = false;
+        const int row0 = ra, deg = valid ? rb - ra : 0;
+        int cnt = 0, scanned = 0;
+        bool infected = false;
+        const bool heavy = deg > kHeavyDeg;
         unsigned imask = 0;
+        int nb[kChunk];
+#pragma unroll
+        for (int z = 0; z < kChunk; ++z)
+          nb[z] = !heavy && z < deg ? static_cast<int>(ld_col(adj, row0 + z) & kIdx) : -1;
+        // infected entry: recovery draw
+        bool rec = false;
+        if (ei >= 0) {
+          const uint2 krec = abm::split_at(abm::split_at(coll, (uint64_t)ei), 1);
+          rec = abm::unit_below(abm::bits_at(krec, 0), tgamma);
+        }
+        my_ir += rec;
+        uint2 kinf = make_uint2(0, 0);
         if (valid) {
-          i = e;
-          row0 = ra;
-          deg = rb - ra;
-          cnt = static_cast<int>(sw[i] >> 2);
+          kinf = abm::split_at(abm::split_at(coll, (uint64_t)e), 0);
+          cnt = static_cast<int>(sw[e] >> 2);
           if (cnt == static_cast<int>(kHubMark)) cnt = deg;  // hubs: scan the whole row
-          heavy = deg > kHeavyDeg;
           if (!heavy) {
-            int seen = 0, k1 = 0;
+            int seen = 0;
+#pragma unroll
+            for (int z = 0; z < kChunk; ++z) {
+              const bool inf = nb[z] >= 0 && (sw[nb[z]] & 3u) == kI;
+              imask |= static_cast<unsigned>(inf) << z;
+              seen += inf;
+            }
+            int k1 = kChunk;
             for (; k1 < deg && seen < cnt; k1 += kChunk) {
-              int nb[kChunk];
 #pragma unroll
               for (int z = 0; z < kChunk; ++z)
                 nb[z] = k1 + z < deg ? static_cast<int>(ld_col(adj, row0 + k1 + z) & kIdx) : -1;
@@ -1329,17 +1346,21 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             scanned = min(k1, deg);
           }
         }
-        if (__any_sync(kFull, imask != 0)) {
-          const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)i), 0);
-          while (__any_sync(kFull, imask != 0)) {
-            if (imask) {
-              const int slot = __ffs(imask) - 1;
-              imask &= imask - 1;
-              ++my_draws;
-              if (abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta) {
-                infected = true;
-                imask = 0;
-              }
+        // draws at the infected slots in row order, two per pass; the first that fires
+        // infects (the outcome is the OR over the slots, the count is the sequential one)
+        while (__any_sync(kFull, imask != 0)) {
+          if (imask) {
+            const int s1 = __ffs(imask) - 1;
+            imask &= imask - 1;
+            const bool two = imask != 0;
+            const int s2 = two ? __ffs(imask) - 1 : s1;
+            if (two) imask &= imask - 1;
+            const bool f1 = abm::unit_below(abm::bits_at(kinf, (uint64_t)s1), tbeta);
+            const bool f2 = two && abm::unit_below(abm::bits_at(kinf, (uint64_t)s2), tbeta);
+            my_draws += (f1 || !two) ? 1 : 2;
+            if (f1 || f2) {
+              infected = true;
+              imask = 0;
             }
           }
         }
@@ -1347,11 +1368,11 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         while (hmask) {
           const int src = __ffs(hmask) - 1;
           hmask &= hmask - 1;
-          const int hi = __shfl_sync(kFull, i, src);
           const int hrow = __shfl_sync(kFull, row0, src);
           const int hdeg = __shfl_sync(kFull, deg, src);
           int remaining = __shfl_sync(kFull, cnt, src);
-          const uint2 kinf = abm::split_at(abm::split_at(coll, (uint64_t)hi), 0);
+          const uint2 hk = make_uint2(__shfl_sync(kFull, kinf.x, src),
+                                      __shfl_sync(kFull, kinf.y, src));
           bool fired = false;
           int cpos = 0;
           if (hdeg > kDrawFirstDeg) {
@@ -1363,7 +1384,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
               for (int u = 0; u < kHeavyUnroll; ++u) {
                 const int slot = cpos + 32 * u + lane;
                 my_draws += slot < hdeg;
-                if (slot < hdeg && abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta)
+                if (slot < hdeg && abm::unit_below(abm::bits_at(hk, (uint64_t)slot), tbeta))
                   fire |= 1u << u;
               }
               uint32_t wv[kHeavyUnroll];
@@ -1400,7 +1421,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
                 ++seen;
                 if (!hit) {
                   ++my_draws;
-                  hit = abm::unit_float(abm::bits_at(kinf, (uint64_t)slot)) < beta;
+                  hit = abm::unit_below(abm::bits_at(hk, (uint64_t)slot), tbeta);
                 }
               }
             }
@@ -1414,7 +1435,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         my_scanned += scanned;
         my_si += infected;
-        res_record(infected, i, kI, changes, &S.nchanges, lane);
+        res_record(rec, ei, 2u, changes, &S.nchanges, lane);
+        res_record(infected, e, kI, changes, &S.nchanges, lane);
       }
       my_si = __reduce_add_sync(kFull, my_si);
       my_ir = __reduce_add_sync(kFull, my_ir);
@@ -1431,6 +1453,25 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       // ---- apply: groups of 32 changes, taken from a group counter ------------------------
       const int nch = S.nchanges;
       const int groups = (nch + 31) >> 5;
+      // the step's counts and the next step's keys, by thread 0 while the warps apply (every
+      // field written here was last read before the barrier above; the step loop reads
+      // num_i after the closing barrier)
+      if (threadIdx.x == 0) {
+        const int si = S.si, ir = S.ir;
+        S.num_s -= si;
+        S.num_i += si - ir;
+        S.num_r += ir;
+        I->counts[3 * t] = S.num_s;
+        I->counts[3 * t + 1] = S.num_i;
+        I->counts[3 * t + 2] = S.num_r;
+        S.si = S.ir = 0;
+        S.ns = S.ni = 0;
+        S.next_round = 0;
+        S.rng0 = next_rng.x;
+        S.rng1 = next_rng.y;
+        S.coll0 = next_coll.x;
+        S.coll1 = next_coll.y;
+      }
       int my_pushed = 0;
       for (;;) {
         int g = 0;
@@ -1453,24 +1494,6 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       }
       my_pushed = __reduce_add_sync(kFull, my_pushed);
       if (lane == 0 && my_pushed) atomicAdd(&S.pushed, static_cast<unsigned long long>(my_pushed));
-      __syncthreads();
-      // ---- finalize ---------------------------------------------------------------------
-      if (threadIdx.x == 0) {
-        S.num_s -= S.si;
-        S.num_i += S.si - S.ir;
-        S.num_r += S.ir;
-        I->counts[3 * t] = S.num_s;
-        I->counts[3 * t + 1] = S.num_i;
-        I->counts[3 * t + 2] = S.num_r;
-        S.si = S.ir = 0;
-        S.ns = S.ni = 0;
-        S.nchanges = 0;
-        S.next_chunk = S.next_round = S.next_group = 0;
-        S.rng0 = next_rng.x;
-        S.rng1 = next_rng.y;
-        S.coll0 = next_coll.x;
-        S.coll1 = next_coll.y;
-      }
       __syncthreads();
     }
     // steps without an infected agent: constant counts, the key chain still advances

@@ -22,6 +22,7 @@ from . import _dev
 from . import _lib
 from . import random as jrandom
 from .sir import barabasi_albert, initial_states
+from .trace import nvtx_range
 
 TILE = 8192  # agents per work item (abm_sir_tile_agents)
 
@@ -384,11 +385,12 @@ class SIRBatch:
         return self._graph
 
     def replay(self):
-        if self._from_states and self._graph_states is not None:
-            self._graph_states.replay()
-            self._from_states = False
-        else:
-            self._graph.replay()
+        with nvtx_range("SIRBatch.replay"):
+            if self._from_states and self._graph_states is not None:
+                self._graph_states.replay()
+                self._from_states = False
+            else:
+                self._graph.replay()
 
     def run(self, use_graph=True, check=True):
         """All ``steps`` steps of every instance; with ``check`` (default) waits for them

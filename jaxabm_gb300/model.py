@@ -19,6 +19,7 @@ import torch
 
 from . import random as jrandom
 from .agent import AgentCollection
+from .trace import nvtx_range
 from .core import ModelConfig, verbose
 
 
@@ -26,6 +27,45 @@ def _metric_value(v):
     if isinstance(v, torch.Tensor) and v.numel() == 1:
         return v.reshape(()).item()
     return v
+
+
+def _snapshot(d: Dict[str, Any]) -> Dict[str, Any]:
+    """Copy of a state dict: tensors cloned on their device, nested dicts copied, other
+    values shared (ints, floats, tuples and the like are immutable)."""
+    out = {}
+    for k, v in (d or {}).items():
+        if isinstance(v, torch.Tensor):
+            out[k] = v.detach().clone()
+        elif isinstance(v, dict):
+            out[k] = _snapshot(v)
+        else:
+            out[k] = v
+    return out
+
+
+def _restore(dst: Dict[str, Any], src: Dict[str, Any]) -> Dict[str, Any]:
+    """Write snapshot ``src`` into ``dst``: a tensor of the same shape and dtype is
+    overwritten in place (views of it, such as a grid, stay valid), anything else is
+    replaced by a copy; keys missing from ``src`` are dropped."""
+    out = {}
+    for k, v in src.items():
+        cur = dst.get(k) if dst is not None else None
+        if isinstance(v, torch.Tensor):
+            if (isinstance(cur, torch.Tensor) and cur.shape == v.shape and cur.dtype == v.dtype
+                    and cur.device == v.device):
+                cur.copy_(v)
+                out[k] = cur
+            else:
+                out[k] = v.detach().clone()
+        elif isinstance(v, dict):
+            out[k] = _restore(cur if isinstance(cur, dict) else {}, v)
+        else:
+            out[k] = v
+    if dst is not None:
+        dst.clear()
+        dst.update(out)
+        return dst
+    return out
 
 
 class Model:
@@ -104,6 +144,10 @@ class Model:
 
     def step(self) -> Dict[str, Any]:
         """One step (jaxabm/model.py:146-216)."""
+        with nvtx_range("Model.step"):
+            return self._step()
+
+    def _step(self) -> Dict[str, Any]:
         if not self._is_initialized:
             raise RuntimeError("Model must be initialized before stepping. Call initialize() first.")
         want_update = self._update_state_fn is not None
@@ -147,6 +191,10 @@ class Model:
     def run(self, steps: Optional[int] = None) -> Dict[str, List[Any]]:
         """Run ``steps`` steps and return ``{'step': [...], metric: [...]}``
         (jaxabm/model.py:218-262)."""
+        with nvtx_range("Model.run"):
+            return self._run(steps)
+
+    def _run(self, steps: Optional[int]) -> Dict[str, List[Any]]:
         if not self._is_initialized:
             self.initialize()
         steps_to_run = steps if steps is not None else self.config.steps
@@ -174,6 +222,54 @@ class Model:
                     out[name] = [_metric_value(v) for v in vals]
             return out
         return {}
+
+    # -- checkpoint / resume ------------------------------------------------------------
+    def state_dict(self) -> Dict[str, Any]:
+        """Everything a later :meth:`run` depends on, copied: the step counter, the model
+        key, the environment (its tensors, e.g. a Schelling grid, cloned on the device),
+        every collection's SoA tensors and key, and the collected history.  A model that
+        loads it continues bit for bit like this one (the reference persists only
+        ``Results``, jaxabm/agentpy.py:783-806)."""
+        if not self._is_initialized:
+            raise RuntimeError("Model must be initialized before its state can be saved")
+        return {
+            "time_step": self._time_step,
+            "rng": self._rng.detach().clone(),
+            "env": _snapshot(self._env_state),
+            "collections": {
+                name: {"states": _snapshot(c.states),
+                       "key": c._key.detach().clone() if isinstance(c._key, torch.Tensor)
+                       else c._key}
+                for name, c in self._agent_collections.items()},
+            "history": list(self._history),
+        }
+
+    def load_state_dict(self, state: Dict[str, Any]) -> None:
+        """Resume from :meth:`state_dict` of a model with the same collections (names and
+        agent counts); initialises this model first when needed.  Tensors are written in
+        place where shapes match, so buffers that kernels or views hold stay valid."""
+        if not self._is_initialized:
+            self.initialize()
+        saved = state["collections"]
+        if set(saved) != set(self._agent_collections):
+            raise ValueError(f"state has collections {sorted(saved)}, model has "
+                             f"{sorted(self._agent_collections)}")
+        for name, c in self._agent_collections.items():
+            st = saved[name]["states"]
+            for k, v in st.items():
+                if isinstance(v, torch.Tensor) and v.dim() > 0 and v.shape[0] != c.num_agents:
+                    raise ValueError(f"collection {name!r}: state {k!r} has {v.shape[0]} "
+                                     f"agents, the collection {c.num_agents}")
+        self._rng.copy_(state["rng"])
+        self._time_step = int(state["time_step"])
+        _restore(self._env_state, state["env"])
+        for name, c in self._agent_collections.items():
+            c._states = _restore(c._states, saved[name]["states"])
+            key = saved[name]["key"]
+            c._key = key.detach().clone() if isinstance(key, torch.Tensor) else key
+            c.bind_env(self._env_state)
+        self._history = list(state.get("history", []))
+        self._state = {"env": self._env_state.copy()}
 
     # -- accessors ----------------------------------------------------------------------
     @property

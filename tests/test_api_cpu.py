@@ -317,3 +317,59 @@ def test_select_condition_compiler():
     many = lambda s: ((s["x"] > 0) & (s["x"] > 1) & (s["x"] > 2) & (s["x"] > 3) & (s["x"] > 4)
                       & (s["x"] > 5) & (s["x"] > 6) & (s["x"] > 7) & (s["x"] > 8))  # 17 ops
     assert compile_condition(many, st) is None
+
+
+def test_state_snapshot_and_restore_helpers():
+    """The copy and in-place restore behind Model.state_dict / load_state_dict (CPU
+    tensors stand in for device ones)."""
+    import torch
+    from jaxabm_gb300.model import _restore, _snapshot
+    grid = torch.arange(12, dtype=torch.int8)
+    view = grid.view(3, 4)
+    env = {"grid": view, "shape": (3, 4), "nested": {"a": torch.ones(2)}, "k": 7}
+    snap = _snapshot(env)
+    view.add_(1)
+    env["nested"]["a"].mul_(5)
+    assert torch.equal(snap["grid"], torch.arange(12, dtype=torch.int8).view(3, 4))
+    assert torch.equal(snap["nested"]["a"], torch.ones(2))
+    out = _restore(env, snap)
+    assert out is env and env["grid"] is view  # same shape: written in place
+    assert torch.equal(grid, torch.arange(12, dtype=torch.int8))
+    assert torch.equal(env["nested"]["a"], torch.ones(2)) and env["k"] == 7
+    other = {"grid": torch.zeros(5, dtype=torch.int8)}
+    _restore(other, snap)  # other shape: replaced by a copy
+    assert other["grid"].shape == (3, 4) and other["grid"] is not snap["grid"]
+    assert _restore(None, {"x": 1}) == {"x": 1}
+
+
+def test_state_dict_requires_initialized_model():
+    m = jx.JaxModel()
+    with pytest.raises(RuntimeError):
+        m.state_dict()
+
+
+def test_nvtx_ranges_pair_up(monkeypatch):
+    """With tracing on, every range is pushed and popped, also when the body raises; with
+    tracing off nothing is pushed."""
+    import torch
+    from jaxabm_gb300 import trace
+    log = []
+    monkeypatch.setattr(torch.cuda.nvtx, "range_push", lambda name: log.append(("push", name)))
+    monkeypatch.setattr(torch.cuda.nvtx, "range_pop", lambda: log.append(("pop",)))
+    was = trace.tracing()
+    try:
+        trace.set_tracing(False)
+        with trace.nvtx_range("off"):
+            pass
+        assert log == []
+        jx.set_tracing(True)
+        with trace.nvtx_range("Model.run"):
+            with trace.nvtx_range("abm_sir_run"):
+                pass
+        with pytest.raises(KeyError):
+            with trace.nvtx_range("fails"):
+                raise KeyError("x")
+        assert log == [("push", "Model.run"), ("push", "abm_sir_run"), ("pop",), ("pop",),
+                       ("push", "fails"), ("pop",)]
+    finally:
+        trace.set_tracing(was)
