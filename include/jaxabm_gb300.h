@@ -56,6 +56,19 @@ ABM_API const char* abm_status_string(int status);
 /* Text of the last CUDA error seen by the library on this host thread ("" if none). */
 ABM_API const char* abm_last_cuda_error(void);
 
+/* Range-checked build.  The library compiled with -DABM_CHECKED
+ * (libjaxabm_gb300_checked.so) checks every gather whose index comes from caller data --
+ * CSR row offsets and columns of the opinion kernels, row indices of abm_gather_rows --
+ * and an entry point that met an index outside its array waits for its stream and returns
+ * ABM_ERR_BOUNDS (the access itself is redirected to element 0); abm_bounds_detail() then
+ * names the entry point, the first bad index, its bound and the checking source line.  A
+ * stream being captured into a CUDA graph is not waited for and not checked.  This is the
+ * stand-in for a device memory checker; it has no counterpart in the reference, whose
+ * gathers run inside JAX.  abm_checked_build() is 1 in that build and 0 in the normal one,
+ * where abm_bounds_detail() stays empty. */
+ABM_API const char* abm_bounds_detail(void);
+ABM_API int abm_checked_build(void);
+
 /* SM count and compute capability of the current device. */
 ABM_API int abm_device_info(int* sm_count, int* cc_major, int* cc_minor);
 

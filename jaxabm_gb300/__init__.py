@@ -32,9 +32,11 @@ from .opinion import OpinionAgent, OpinionModel  # noqa: E402
 from .analysis import ModelCalibrator, SensitivityAnalysis  # noqa: E402
 
 
-def build(force: bool = False) -> str:
-    """Compile ``libjaxabm_gb300.so`` for sm_103a (in-tree) and return its path."""
-    return _build_library(force=force)
+def build(force: bool = False, checked: bool = False) -> str:
+    """Compile ``libjaxabm_gb300.so`` for sm_103a (in-tree) and return its path; with
+    ``checked``, the range-checked ``libjaxabm_gb300_checked.so`` (``JAXABM_CHECKED=1``
+    makes the package load it)."""
+    return _build_library(force=force, checked=checked)
 
 
 def has_jax() -> bool:

@@ -3,6 +3,11 @@
 Every ``csrc/*.cu`` and ``csrc/*.cpp`` file is compiled to an object in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a`` and linked into one shared library next
 to this file.  The library links only the CUDA runtime: no torch types cross the ABI.
+
+``build(checked=True)`` compiles the same sources with ``-DABM_CHECKED`` into
+``libjaxabm_gb300_checked.so``: the range-checked build, in which gathers indexed by caller
+data report an out-of-range index as ABM_ERR_BOUNDS (slower: every checked entry point
+waits for its stream).  It is built only on request.
 """
 
 import os
@@ -17,6 +22,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libjaxabm_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
+CHECKED_BUILD_DIR = os.path.join(HERE, "_build_checked")
+CHECKED_LIB_PATH = os.path.join(HERE, "libjaxabm_gb300_checked.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -51,14 +58,14 @@ def _newest(paths):
     return max((os.path.getmtime(p) for p in paths), default=0.0)
 
 
-def up_to_date():
-    if not os.path.exists(LIB_PATH):
+def up_to_date(path=LIB_PATH):
+    if not os.path.exists(path):
         return False
-    return os.path.getmtime(LIB_PATH) >= _newest(sources() + _headers() + [__file__])
+    return os.path.getmtime(path) >= _newest(sources() + _headers() + [__file__])
 
 
-def _compile(nvcc, src, extra):
-    obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+def _compile(nvcc, src, extra, build_dir=BUILD_DIR):
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     cmd = [nvcc] + ARCH_FLAGS + COMMON_FLAGS + extra + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd += ["-Xcompiler", "-pthread"]
@@ -68,29 +75,32 @@ def _compile(nvcc, src, extra):
     return obj, res.stderr
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    """Compile the library if any source is newer than it; return the library path."""
-    if not force and not extra_flags and up_to_date():
-        return LIB_PATH
+def build(force=False, verbose=False, extra_flags=(), checked=False):
+    """Compile the library (the range-checked one with ``checked``) if any source is newer
+    than it; return the library path."""
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    build_dir = CHECKED_BUILD_DIR if checked else BUILD_DIR
+    if not force and not extra_flags and up_to_date(lib_path):
+        return lib_path
     nvcc = nvcc_path()
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(build_dir, exist_ok=True)
     srcs = sources()
-    extra = list(extra_flags)
+    extra = list(extra_flags) + (["-DABM_CHECKED"] if checked else [])
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        results = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
+        results = list(ex.map(lambda s: _compile(nvcc, s, extra, build_dir), srcs))
     objs = [r[0] for r in results]
     if verbose:
         for _, log in results:
             if log.strip():
                 sys.stderr.write(log)
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc] + ARCH_FLAGS + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

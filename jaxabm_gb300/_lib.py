@@ -1,7 +1,9 @@
 """ctypes binding of ``libjaxabm_gb300.so`` (the C ABI declared in include/jaxabm_gb300.h).
 
 The library is required: when it is missing or a symbol is absent, loading raises instead
-of falling back to any other implementation.
+of falling back to any other implementation.  With ``JAXABM_CHECKED=1`` in the
+environment the range-checked build (``libjaxabm_gb300_checked.so``, made by
+``jaxabm_gb300.build(checked=True)``) is loaded instead.
 """
 
 import ctypes
@@ -9,7 +11,7 @@ import os
 import threading
 
 from . import trace as _trace
-from ._build import LIB_PATH
+from ._build import CHECKED_LIB_PATH, LIB_PATH
 
 ABM_OK = 0
 ABM_ERR_BADARG = 1
@@ -36,6 +38,8 @@ SIGNATURES = {
     "abm_version": (_int, []),
     "abm_status_string": (ctypes.c_char_p, [_int]),
     "abm_last_cuda_error": (ctypes.c_char_p, []),
+    "abm_bounds_detail": (ctypes.c_char_p, []),
+    "abm_checked_build": (_int, []),
     "abm_device_info": (_int, [_p, _p, _p]),
     "abm_rng_split": (_int, [_p, _i64, _i64, _p, _int, _p]),
     "abm_rng_bits": (_int, [_p, _i64, _i64, _p, _int, _p]),
@@ -122,7 +126,7 @@ def load(path=None):
     with _lock:
         if _lib is not None and path is None:
             return _lib
-        p = path or LIB_PATH
+        p = path or default_path()
         if not os.path.exists(p):
             raise RuntimeError(
                 f"{os.path.basename(p)} is not built: call jaxabm_gb300.build() "
@@ -135,6 +139,14 @@ def load(path=None):
         if path is None:
             _lib = lib
         return lib
+
+
+def default_path():
+    """The library ``load()`` opens: the range-checked build when ``JAXABM_CHECKED`` is set
+    to a non-zero value, else the normal one."""
+    if os.environ.get("JAXABM_CHECKED", "0") not in ("", "0"):
+        return CHECKED_LIB_PATH
+    return LIB_PATH
 
 
 def status_string(status):
@@ -151,6 +163,8 @@ def check(status, where):
         detail = ""
         if status == ABM_ERR_CUDA:
             detail = load().abm_last_cuda_error().decode()
+        elif status == ABM_ERR_BOUNDS:
+            detail = load().abm_bounds_detail().decode()
         raise AbmError(status, where, detail)
 
 

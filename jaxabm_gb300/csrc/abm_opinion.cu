@@ -103,6 +103,9 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
   for (int c = 0; c < 4; ++c) it[c] = __frcp_rn(it[c]);
   ld4(o + (size_t)node * B, sub, oi);
   const int r0 = rp[node], r1 = rp[node + 1];
+#ifdef ABM_CHECKED
+  const int nslots = rp[n];
+#endif
   // acc += s(d) * d for one neighbour row (instances of this lane)
   auto edge = [&](const float (&oj)[4]) {
 #pragma unroll
@@ -116,14 +119,14 @@ opinion_step_kernel(const float* __restrict__ o, float* __restrict__ out,
   // two neighbour rows in flight per iteration; accumulation stays in CSR order
   for (; e + 1 < r1; e += 2) {
     float oa[4], ob[4];
-    ld4(o + (size_t)col[e] * B, sub, oa);
-    ld4(o + (size_t)col[e + 1] * B, sub, ob);
+    ld4(o + (size_t)ABM_IDX(col[ABM_IDX(e, nslots)], n) * B, sub, oa);
+    ld4(o + (size_t)ABM_IDX(col[ABM_IDX(e + 1, nslots)], n) * B, sub, ob);
     edge(oa);
     edge(ob);
   }
   if (e < r1) {
     float oa[4];
-    ld4(o + (size_t)col[e] * B, sub, oa);
+    ld4(o + (size_t)ABM_IDX(col[ABM_IDX(e, nslots)], n) * B, sub, oa);
     edge(oa);
   }
   float res[4] = {oi[0], oi[1], oi[2], oi[3]};
@@ -181,6 +184,9 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     ld4(o + (size_t)node * B, sub, oi);
     ld4(lam_in + (size_t)node * B, sub, li);
     const int r0 = rp[node], r1 = rp[node + 1];
+#ifdef ABM_CHECKED
+    const int nslots = rp[n];
+#endif
     const float inv_deg_i = inv_deg[node];
 #pragma unroll
     for (int c = 0; c < 4; ++c) li_d[c] = r1 > r0 ? li[c] * inv_deg_i : li[c];
@@ -205,7 +211,8 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
     int e = r0;
     // two neighbours' opinion and adjoint rows in flight per iteration
     for (; e + 1 < r1; e += 2) {
-      const int ja = col[e], jb = col[e + 1];
+      const int ja = static_cast<int>(ABM_IDX(col[ABM_IDX(e, nslots)], n));
+      const int jb = static_cast<int>(ABM_IDX(col[ABM_IDX(e + 1, nslots)], n));
       float oa[4], la[4], ob[4], lb[4];
       ld4(o + (size_t)ja * B, sub, oa);
       ld4(lam_in + (size_t)ja * B, sub, la);
@@ -216,7 +223,7 @@ opinion_adjoint_kernel(const float* __restrict__ o, const float* __restrict__ la
       edge(ob, lb, db);
     }
     if (e < r1) {
-      const int j = col[e];
+      const int j = static_cast<int>(ABM_IDX(col[ABM_IDX(e, nslots)], n));
       float oj[4], lj[4];
       ld4(o + (size_t)j * B, sub, oj);
       ld4(lam_in + (size_t)j * B, sub, lj);
@@ -367,7 +374,7 @@ int abm_opinion_run(float* o, float* o_tmp, const int32_t* row_ptr, const int32_
     }
     ABM_OP_DISPATCH(opinion_step_kernel, lpn, blocks, 0, s, cur, nxt, row_ptr, col, (int)n, B, mu,
                     eps, tau);
-    int st = abm_host::check_launch("abm_opinion_run/step");
+    int st = abm_host::finish(stream, "abm_opinion_run/step");
     if (st) return st;
     float* tmp = cur;
     cur = nxt;
@@ -392,7 +399,7 @@ int abm_opinion_step(const float* o_in, float* o_out, const int32_t* row_ptr, co
   cudaStream_t s = abm_host::as_stream(stream);
   ABM_OP_DISPATCH(opinion_step_kernel, B / 4, step_blocks(n, B), 0, s, o_in, o_out, row_ptr, col,
                   (int)n, B, mu, eps, tau);
-  return abm_host::check_launch("abm_opinion_step");
+  return abm_host::finish(stream, "abm_opinion_step");
 }
 
 int abm_opinion_sigmoid(const float* z, float* s, int64_t n, void* stream) {
@@ -475,7 +482,7 @@ int abm_opinion_adjoint_step(const float* o, const float* lam_in, float* lam_out
   for (int c0 = 0; c0 < B; c0 += cols) {
     ABM_OP_DISPATCH(opinion_adjoint_kernel, lpn, blocks, smem, s, o, lam_in, lam_out, row_ptr,
                     col, inv_deg, (int)n, B, c0, mu, eps, tau, grad_partials);
-    const int st = abm_host::check_launch("abm_opinion_adjoint_step");
+    const int st = abm_host::finish(stream, "abm_opinion_adjoint_step");
     if (st) return st;
   }
   return ABM_OK;

@@ -11,6 +11,7 @@
 namespace {
 
 thread_local char g_last_cuda_error[256] = "";
+thread_local char g_bounds_detail[256] = "";
 
 constexpr int kThreads = 256;
 
@@ -175,6 +176,11 @@ int record_cuda_error(cudaError_t e, const char* where) {
   return ABM_ERR_CUDA;
 }
 int check_launch(const char* where) { return record_cuda_error(cudaGetLastError(), where); }
+void set_bounds_detail(const char* where, long long index, long long bound, long long line) {
+  snprintf(g_bounds_detail, sizeof(g_bounds_detail),
+           "%s: index %lld outside [0, %lld) (checked at source line %lld)", where, index,
+           bound, line);
+}
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
@@ -202,6 +208,16 @@ const char* abm_status_string(int status) {
 }
 
 const char* abm_last_cuda_error(void) { return g_last_cuda_error; }
+
+const char* abm_bounds_detail(void) { return g_bounds_detail; }
+
+int abm_checked_build(void) {
+#ifdef ABM_CHECKED
+  return 1;
+#else
+  return 0;
+#endif
+}
 
 int abm_device_info(int* sm_count, int* cc_major, int* cc_minor) {
   int dev = 0;

@@ -152,21 +152,23 @@ select_scatter_kernel(const uint8_t* __restrict__ mask, int64_t n, bool vec_ok,
 
 // out[r] = src[idx[r]] for rows of `row_bytes` bytes, copied in 4-byte words when possible.
 __global__ void gather_rows_words(const uint32_t* __restrict__ src, const int32_t* __restrict__ idx,
-                                  int64_t count, int64_t row_words, uint32_t* __restrict__ dst) {
+                                  int64_t count, int64_t row_words, uint32_t* __restrict__ dst,
+                                  int64_t nrows_src) {
   const int64_t total = count * row_words;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = g / row_words, w = g - r * row_words;
-    dst[g] = src[(int64_t)idx[r] * row_words + w];
+    dst[g] = src[(int64_t)ABM_IDX(idx[r], nrows_src) * row_words + w];
   }
 }
 __global__ void gather_rows_bytes(const uint8_t* __restrict__ src, const int32_t* __restrict__ idx,
-                                  int64_t count, int64_t row_bytes, uint8_t* __restrict__ dst) {
+                                  int64_t count, int64_t row_bytes, uint8_t* __restrict__ dst,
+                                  int64_t nrows_src) {
   const int64_t total = count * row_bytes;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = g / row_bytes, b = g - r * row_bytes;
-    dst[g] = src[(int64_t)idx[r] * row_bytes + b];
+    dst[g] = src[(int64_t)ABM_IDX(idx[r], nrows_src) * row_bytes + b];
   }
 }
 
@@ -444,7 +446,7 @@ int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes, const
                     int64_t count, void* dst, void* stream) {
   if (!src || !dst || row_bytes <= 0 || count < 0 || nrows_src < 0) return ABM_ERR_BADARG;
   if (count == 0) return ABM_OK;
-  if (!idx) return ABM_ERR_BADARG;
+  if (!idx || nrows_src == 0) return ABM_ERR_BADARG;  // no row to gather from
   cudaStream_t s = abm_host::as_stream(stream);
   const int threads = 256;
   const bool words = row_bytes % 4 == 0 && abm_host::aligned(src, 4) && abm_host::aligned(dst, 4);
@@ -454,11 +456,13 @@ int abm_gather_rows(const void* src, int64_t nrows_src, int64_t row_bytes, const
   if (blocks > cap) blocks = cap;
   if (words)
     gather_rows_words<<<(unsigned)blocks, threads, 0, s>>>(
-        static_cast<const uint32_t*>(src), idx, count, row_bytes / 4, static_cast<uint32_t*>(dst));
+        static_cast<const uint32_t*>(src), idx, count, row_bytes / 4, static_cast<uint32_t*>(dst),
+        nrows_src);
   else
     gather_rows_bytes<<<(unsigned)blocks, threads, 0, s>>>(
-        static_cast<const uint8_t*>(src), idx, count, row_bytes, static_cast<uint8_t*>(dst));
-  return abm_host::check_launch("abm_gather_rows");
+        static_cast<const uint8_t*>(src), idx, count, row_bytes, static_cast<uint8_t*>(dst),
+        nrows_src);
+  return abm_host::finish(stream, "abm_gather_rows");
 }
 
 size_t abm_reduce_workspace_bytes(int64_t n) {

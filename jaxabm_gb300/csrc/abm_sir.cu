@@ -1321,8 +1321,10 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         uint2 kinf = make_uint2(0, 0);
         if (valid) {
           kinf = abm::split_at(abm::split_at(coll, (uint64_t)e), 0);
+          // infected neighbours: the word's count, or a hub's count in global memory
+          // (exact since the last apply; read through L2)
           cnt = static_cast<int>(sw[e] >> 2);
-          if (cnt == static_cast<int>(kHubMark)) cnt = deg;  // hubs: scan the whole row
+          if (cnt == static_cast<int>(kHubMark)) cnt = __ldcg(hubs + e);
           if (!heavy) {
             int seen = 0;
 #pragma unroll
@@ -1373,38 +1375,12 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
           int remaining = __shfl_sync(kFull, cnt, src);
           const uint2 hk = make_uint2(__shfl_sync(kFull, kinf.x, src),
                                       __shfl_sync(kFull, kinf.y, src));
+          // the whole row is scanned (the warp reads 32 x kHeavyUnroll columns per pass
+          // and draws only at infected slots): on the resident kernel this beats drawing
+          // at every slot first, which the grid path does for rows longer than
+          // kDrawFirstDeg
           bool fired = false;
           int cpos = 0;
-          if (hdeg > kDrawFirstDeg) {
-            // long rows: draws first, a neighbour read only where a draw fires
-            int loaded = 0;
-            for (; cpos < hdeg && !fired; cpos += 32 * kHeavyUnroll) {
-              unsigned fire = 0;
-#pragma unroll
-              for (int u = 0; u < kHeavyUnroll; ++u) {
-                const int slot = cpos + 32 * u + lane;
-                my_draws += slot < hdeg;
-                if (slot < hdeg && abm::unit_below(abm::bits_at(hk, (uint64_t)slot), tbeta))
-                  fire |= 1u << u;
-              }
-              uint32_t wv[kHeavyUnroll];
-#pragma unroll
-              for (int u = 0; u < kHeavyUnroll; ++u)
-                wv[u] = (fire >> u) & 1u ? ld_col(adj, hrow + cpos + 32 * u + lane) : 0u;
-              bool hit = false;
-#pragma unroll
-              for (int u = 0; u < kHeavyUnroll; ++u)
-                if ((fire >> u) & 1u) hit |= (sw[wv[u] & kIdx] & 3u) == kI;
-              loaded += __popc(fire);
-              fired = __any_sync(kFull, hit);
-            }
-            loaded = __reduce_add_sync(kFull, loaded);
-            if (lane == src) {
-              infected = fired;
-              scanned = loaded;
-            }
-            continue;
-          }
           for (; cpos < hdeg && !fired && remaining > 0; cpos += 32 * kHeavyUnroll) {
             uint32_t wv[kHeavyUnroll];
 #pragma unroll

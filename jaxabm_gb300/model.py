@@ -256,10 +256,13 @@ class Model:
                              f"{sorted(self._agent_collections)}")
         for name, c in self._agent_collections.items():
             st = saved[name]["states"]
+            cur = c.states or {}
             for k, v in st.items():
-                if isinstance(v, torch.Tensor) and v.dim() > 0 and v.shape[0] != c.num_agents:
-                    raise ValueError(f"collection {name!r}: state {k!r} has {v.shape[0]} "
-                                     f"agents, the collection {c.num_agents}")
+                have = cur.get(k)
+                if (isinstance(v, torch.Tensor) and isinstance(have, torch.Tensor)
+                        and v.shape != have.shape):
+                    raise ValueError(f"collection {name!r}: state {k!r} has shape "
+                                     f"{tuple(v.shape)}, the model's {tuple(have.shape)}")
         self._rng.copy_(state["rng"])
         self._time_step = int(state["time_step"])
         _restore(self._env_state, state["env"])

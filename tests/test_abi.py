@@ -56,3 +56,18 @@ def test_sir_resident_entry_points_without_gpu(lib):
     assert lib.abm_sir_resident_max_agents() >= 0
     assert lib.abm_sir_steps_resident(None, 1, None, 1000, 5, 2, None, None, None, 0, None,
                                       None) == _lib.ABM_ERR_BADARG
+
+
+def test_normal_build_is_not_range_checked(lib):
+    """The normal library reports itself as unchecked and has no bounds detail; the
+    range-checked one is a separate file (built on request)."""
+    assert lib.abm_checked_build() == 0
+    assert lib.abm_bounds_detail() == b""
+    assert _lib.CHECKED_LIB_PATH != _lib.LIB_PATH
+
+
+def test_checked_library_is_chosen_by_the_environment(monkeypatch):
+    monkeypatch.setenv("JAXABM_CHECKED", "1")
+    assert _lib.default_path() == _lib.CHECKED_LIB_PATH
+    monkeypatch.setenv("JAXABM_CHECKED", "0")
+    assert _lib.default_path() == _lib.LIB_PATH
