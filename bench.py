@@ -713,7 +713,8 @@ def run_ours(args):
                      if peak_kind == "measured" else "fallback",
                      "kernel": ("sir_resident_kernel: one launch runs every step of every "
                                 "instance (one CTA per instance at a time, words in shared "
-                                "memory); bound by issue (threefry draws) and latency, not HBM"
+                                "memory); bound by the latency of each warp's dependent work "
+                                "(threefry chains, row loads) at 2 CTAs per SM, not by HBM"
                                 if wl.batch.mode == "resident" else
                                 "SIR step sequence (sweep + candidates + push + finalize per "
                                 "step; 365 steps in one CUDA-graph replay), timed as a unit"),
