@@ -288,6 +288,24 @@ ABM_API int abm_sir_count_batch(abm_sir_instance* insts, const abm_work_item* wo
 ABM_API int abm_copy_segments(int64_t count, void* const* dst, const void* const* src,
                               const size_t* bytes, int32_t to_device, void* stream);
 
+/* One segment of abm_copy_segments_kernel: bytes bytes from src to dst. */
+typedef struct abm_copy_segment {
+  void* dst;
+  const void* src;
+  uint64_t bytes;
+} abm_copy_segment;
+
+/* The same copies as abm_copy_segments, done by one kernel launch instead of one
+ * cudaMemcpyAsync per segment: segs[0..count) is read by the kernel, and every segs[k].dst
+ * and segs[k].src is device memory or page-locked host memory (both are in the device's
+ * address space); this is checked on the host for the table and every pointer
+ * (cudaPointerGetAttributes), and pageable or unknown memory gives ABM_ERR_BADARG before
+ * anything is launched -- copy those through abm_copy_segments.  Segments are copied with
+ * 16-byte accesses where source and destination share their alignment.  When a server
+ * admits or retires thousands of requests at once this replaces thousands of copy calls
+ * (the host link's bandwidth is the same either way). */
+ABM_API int abm_copy_segments_kernel(const abm_copy_segment* segs, int64_t count, void* stream);
+
 /* int8 compartments of n packed words. */
 ABM_API int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream);
 

@@ -64,6 +64,7 @@ SIGNATURES = {
     "abm_sir_pack_batch": (_int, [_p, _p, _i32, _p, _p, _p, _p]),
     "abm_sir_count_batch": (_int, [_p, _p, _i32, _p, _p, _p]),
     "abm_copy_segments": (_int, [_i64, _p, _p, _p, _i32, _p]),
+    "abm_copy_segments_kernel": (_int, [_p, _i64, _p]),
     "abm_sir_unpack": (_int, [_p, _i64, _p, _p]),
     "abm_sir_changes_bytes": (_sz, [_i64, _i64]),
     "abm_sir_steps": (_int, [_p, _i32, _p, _i32, _p, _i32, _p, _p, _sz, _p]),

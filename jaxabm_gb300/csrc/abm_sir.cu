@@ -989,21 +989,6 @@ struct ResState {
   unsigned long long scanned, pushed, cands, draws;
 };
 
-// Position of the k-th (0-based) set bit of m; requires k < popc(m).
-__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
-  int pos = 0;
-#pragma unroll
-  for (int w = 16; w > 0; w >>= 1) {
-    const int c = __popc(m & ((1u << w) - 1u));
-    if (k >= c) {
-      k -= c;
-      m >>= w;
-      pos += w;
-    }
-  }
-  return pos;
-}
-
 // First lane whose inclusive prefix sum `incl` exceeds f (f below the warp total), by a
 // five-step binary search over the lanes; called by all lanes.
 __device__ __forceinline__ int owner_lane(int incl, int f) {
@@ -1214,14 +1199,23 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             for (int z = 0; z < 4; ++z) qw[4 * v + z] = 0x02020202u;  // beyond the agents: R
           }
         }
+        // four agents per 32-bit word at once: per byte, compartment bits (S = 0, I = 1),
+        // count > 0 (adding 0x7F sets bit 7 iff the 6-bit count is non-zero) and hub mark
+        // (count + 1 reaches 64 only for 63); the byte flags (bit 0 of each byte) become
+        // four mask bits by one multiply (partial products land on distinct bits, no carries)
         unsigned need_s = 0, need_i = 0, hub_s = 0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const uint32_t b = (qw[j >> 2] >> (8 * (j & 3))) & 0xFFu;
-          const uint32_t s = b & 3u;
-          need_s |= static_cast<unsigned>(s == kS && b >= 4u) << j;
-          need_i |= static_cast<unsigned>(s == kI) << j;
-          hub_s |= static_cast<unsigned>(b == (kHubMark << 2)) << j;
+        for (int q = 0; q < 8; ++q) {
+          const uint32_t w = qw[q];
+          const uint32_t lo = w & 0x01010101u, hi = (w >> 1) & 0x01010101u;
+          const uint32_t cnt = (w >> 2) & 0x3F3F3F3Fu;
+          const uint32_t isS = ~(lo | hi) & 0x01010101u;
+          const uint32_t isI = lo & ~hi;
+          const uint32_t nz = ((cnt + 0x7F7F7F7Fu) >> 7) & 0x01010101u;
+          const uint32_t hub = ((cnt + 0x01010101u) >> 6) & 0x01010101u;
+          need_s |= (((isS & nz) * 0x01020408u) >> 24 & 0xFu) << (4 * q);
+          need_i |= ((isI * 0x01020408u) >> 24 & 0xFu) << (4 * q);
+          hub_s |= (((isS & hub) * 0x01020408u) >> 24 & 0xFu) << (4 * q);
         }
         while (hub_s) {
           const int j = __ffs(hub_s) - 1;
@@ -1524,6 +1518,39 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
   }
 }
 
+// Segment k of the table is copied by CTA k (grid-stride over segments): head bytes up to
+// a 16-byte boundary, 16-byte vectors, tail bytes when source and destination share their
+// address mod 16, else 4-byte words when they share it mod 4, else bytes.
+__global__ void copy_segments_kernel(const abm_copy_segment* __restrict__ segs, int64_t count) {
+  for (int64_t k = blockIdx.x; k < count; k += gridDim.x) {
+    uint8_t* d = static_cast<uint8_t*>(segs[k].dst);
+    const uint8_t* s = static_cast<const uint8_t*>(segs[k].src);
+    const uint64_t n = segs[k].bytes;
+    const uintptr_t da = reinterpret_cast<uintptr_t>(d), sa = reinterpret_cast<uintptr_t>(s);
+    if ((da & 15) == (sa & 15)) {
+      uint64_t head = (16 - (da & 15)) & 15;
+      if (head > n) head = n;
+      for (uint64_t i = threadIdx.x; i < head; i += blockDim.x) d[i] = s[i];
+      const uint64_t nv = (n - head) / 16;
+      const uint4* sv = reinterpret_cast<const uint4*>(s + head);
+      uint4* dv = reinterpret_cast<uint4*>(d + head);
+      for (uint64_t i = threadIdx.x; i < nv; i += blockDim.x) dv[i] = sv[i];
+      for (uint64_t i = head + nv * 16 + threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+    } else if ((da & 3) == (sa & 3)) {
+      uint64_t head = (4 - (da & 3)) & 3;
+      if (head > n) head = n;
+      for (uint64_t i = threadIdx.x; i < head; i += blockDim.x) d[i] = s[i];
+      const uint64_t nw = (n - head) / 4;
+      const uint32_t* sw4 = reinterpret_cast<const uint32_t*>(s + head);
+      uint32_t* dw4 = reinterpret_cast<uint32_t*>(d + head);
+      for (uint64_t i = threadIdx.x; i < nw; i += blockDim.x) dw4[i] = sw4[i];
+      for (uint64_t i = head + nw * 4 + threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+    } else {
+      for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+    }
+  }
+}
+
 int default_grid(int nwork) {
   const int cap = abm_host::sm_count() * 8;  // 8 resident 256-thread CTAs per SM
   return nwork < cap ? (nwork > 0 ? nwork : 1) : cap;
@@ -1722,6 +1749,37 @@ int abm_copy_segments(int64_t count, void* const* dst, const void* const* src,
     if (st) return st;
   }
   return ABM_OK;
+}
+
+// Device address of a device or page-locked host pointer, or nullptr for anything else
+// (pageable or unknown host memory, which a kernel must not touch).
+static const void* device_view(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  return nullptr;
+}
+
+int abm_copy_segments_kernel(const abm_copy_segment* segs, int64_t count, void* stream) {
+  if (count < 0 || (count > 0 && !segs)) return ABM_ERR_BADARG;
+  if (count == 0) return ABM_OK;
+  const void* table = device_view(segs);
+  if (!table) return ABM_ERR_BADARG;
+  for (int64_t k = 0; k < count; ++k) {
+    if (segs[k].bytes == 0) continue;
+    const void* d = device_view(segs[k].dst);
+    const void* s = device_view(segs[k].src);
+    // the kernel uses the pointers as given: they must be their own device addresses
+    if (d != segs[k].dst || s != segs[k].src) return ABM_ERR_BADARG;
+  }
+  const int64_t grid = count < (1 << 20) ? count : (1 << 20);
+  copy_segments_kernel<<<(unsigned)grid, 256, 0, abm_host::as_stream(stream)>>>(
+      static_cast<const abm_copy_segment*>(table), count);
+  return abm_host::check_launch("abm_copy_segments_kernel");
 }
 
 int abm_sir_unpack(const uint8_t* words, int64_t n, int8_t* state, void* stream) {

@@ -302,6 +302,90 @@ class SIRBatch:
         self._words0_stale = True  # the saved step-0 words belong to the earlier inputs
         self.desc.copy_(self.desc0, non_blocking=True)
 
+    def _chunk_plan(self, chunks):
+        """Index ranges of the overlapped host run (a small first range, so the kernels
+        start early, then ranges of growing byte counts), each with its own order (largest
+        instance first), resident grid, scratch and stream."""
+        if getattr(self, "_chunks", None) is not None and self._chunks[0] == chunks:
+            return self._chunks[1]
+        L = _lib.load()
+        dev = self.row_ptr.device
+        nbytes = 4 * (self.n + 1) + 4 * self.e + self.n
+        cum = np.cumsum(nbytes) / float(nbytes.sum())
+        # cumulative byte fractions at the ends of the ranges: 1/2^(c-1) of the whole for
+        # the first, doubling up to the last
+        ends = [1.0 / (1 << (chunks - 1 - c)) for c in range(chunks)]
+        bounds, start = [], 0
+        for f in ends:
+            stop = max(start + 1, int(np.searchsorted(cum, f - 1e-12) + 1)) if start < self.k \
+                else start
+            stop = min(stop, self.k)
+            if stop > start:
+                bounds.append((start, stop))
+            start = stop
+        if start < self.k:
+            bounds.append((start, self.k))
+        order = np.concatenate([a + np.argsort(-self.n[a:b], kind="stable")
+                                for a, b in bounds]).astype(np.int32)
+        d_order = torch.from_numpy(order).to(dev)
+        plan = []
+        for a, b in bounds:
+            max_n = int(self.n[a:b].max())
+            grid = min(self.res_grid, b - a)
+            scratch = torch.empty(L.abm_sir_resident_scratch_bytes(max_n, grid),
+                                  dtype=torch.uint8, device=dev)
+            plan.append({"range": (a, b), "max_n": max_n, "grid": grid, "scratch": scratch,
+                         "stream": torch.cuda.Stream(), "event": torch.cuda.Event()})
+        self._chunks = (chunks, (plan, d_order, torch.cuda.Stream()))
+        return self._chunks[1]
+
+    def run_from_host(self, h_row_ptr, h_col, h_state8, h_counts=None, chunks=8):
+        """Every step of every instance from page-locked host inputs (laid out like
+        ``row_ptr``/``col``/``state8``), with the host-to-device copies overlapping the
+        kernels (resident path).  The instances are split into ``chunks`` index ranges --
+        the first small, so that kernels start after a few percent of the bytes -- and each
+        range runs as its own resident launch on its own stream as soon as its copies have
+        landed, while the later ranges are still being copied; with ``h_counts`` (page-
+        locked, laid out like ``counts``) each range's counts are copied back as soon as it
+        finishes.  Launches of different ranges share the GPU, so order the instances
+        largest first for the shortest run.  Returns after enqueueing; the results equal
+        :meth:`load_host` followed by :meth:`run`."""
+        if self.mode != "resident":
+            raise ValueError("run_from_host needs the resident path")
+        plan, d_order, copy = self._chunk_plan(int(chunks))
+        rp_off, col_off, w_off, cnt_off = self._offsets
+        cur = torch.cuda.current_stream()
+        self.res_status.zero_()
+        copy.wait_stream(cur)
+        with torch.cuda.stream(copy):
+            self.desc.copy_(self.desc0, non_blocking=True)
+            for c in plan:
+                a, b = c["range"]
+                self.row_ptr[rp_off[a]:rp_off[b]].copy_(h_row_ptr[rp_off[a]:rp_off[b]],
+                                                        non_blocking=True)
+                self.col[col_off[a]:col_off[b]].copy_(h_col[col_off[a]:col_off[b]],
+                                                      non_blocking=True)
+                self.state8[w_off[a]:w_off[b]].copy_(h_state8[w_off[a]:w_off[b]],
+                                                     non_blocking=True)
+                c["event"].record(copy)
+        for c in plan:
+            a, b = c["range"]
+            s = c["stream"]
+            s.wait_event(c["event"])
+            _lib.call("abm_sir_steps_resident", _dev.ptr(self.desc), b - a,
+                      _dev.ptr(d_order) + 4 * a, c["max_n"], self.steps, c["grid"],
+                      _dev.ptr(self.state8), _dev.ptr(self.words), _dev.ptr(c["scratch"]),
+                      c["scratch"].numel(), _dev.ptr(self.res_status), s.cuda_stream)
+            if h_counts is not None:
+                with torch.cuda.stream(s):
+                    h_counts[cnt_off[a]:cnt_off[b]].copy_(self.counts[cnt_off[a]:cnt_off[b]],
+                                                          non_blocking=True)
+        for c in plan:
+            cur.wait_stream(c["stream"])
+        cur.wait_stream(copy)
+        self._from_states = False
+        self._words0_stale = True  # the saved step-0 words belong to the earlier inputs
+
     @property
     def agent_steps(self):
         return int(self.n.sum()) * self.steps

@@ -33,8 +33,7 @@ from . import _lib
 from .trace import nvtx_range
 from .ensemble import (INSTANCE_DTYPE, RNG_WORD, STATUS_BAD_COLUMN, STATUS_BAD_COMPARTMENT,
                        STEPS_WORD, TILE, changes_overflowed, changes_workspace, check_layout,
-                       launch_struct, model_rngs, raise_status, tiles_for, unpack_words,
-                       word_bytes)
+                       launch_struct, model_rngs, raise_status, unpack_words, word_bytes)
 
 
 def work_table(slots, sizes, dummy, capacity, tile=TILE):
@@ -99,13 +98,27 @@ def _host_span(a, dtype):
     return a, a.ctypes.data, a.nbytes
 
 
-def copy_segments(dst, src, nbytes, to_device, stream):
-    """One ``abm_copy_segments`` call for many copies (address lists as numpy uint64)."""
-    dst = np.ascontiguousarray(dst, dtype=np.uint64)
-    src = np.ascontiguousarray(src, dtype=np.uint64)
-    nbytes = np.ascontiguousarray(nbytes, dtype=np.uint64)
+def copy_segments(dst, src, nbytes, to_device, stream, pinned=False):
+    """Many copies in one call (address lists as numpy uint64).  With ``pinned`` (every
+    host side is page-locked) one ``abm_copy_segments_kernel`` launch does them all from a
+    page-locked segment table, which is returned and must stay alive until the stream has
+    run the copy; otherwise ``abm_copy_segments`` issues one copy call per segment (None is
+    returned)."""
+    dst = np.ascontiguousarray(dst, dtype=np.uint64).reshape(-1)
+    src = np.ascontiguousarray(src, dtype=np.uint64).reshape(-1)
+    nbytes = np.ascontiguousarray(nbytes, dtype=np.uint64).reshape(-1)
+    if pinned and dst.size:
+        table = torch.empty((dst.size, 3), dtype=torch.int64, pin_memory=True)
+        t = table.numpy().view(np.uint64)
+        t[:, 0], t[:, 1], t[:, 2] = dst, src, nbytes
+        st = _lib.load().abm_copy_segments_kernel(table.data_ptr(), dst.size, stream.cuda_stream)
+        if st == _lib.ABM_OK:
+            return table
+        if st != _lib.ABM_ERR_BADARG:  # BADARG: memory the kernel may not touch; copy below
+            _lib.check(st, "abm_copy_segments_kernel")
     _lib.call("abm_copy_segments", dst.size, dst.ctypes.data, src.ctypes.data, nbytes.ctypes.data,
               1 if to_device else 0, stream.cuda_stream)
+    return None
 
 
 def input_error(req):
@@ -130,18 +143,20 @@ def input_error(req):
 class Request:
     """One simulation request: a CSR network (``row_ptr`` int32[n+1], ``col`` int32[E]),
     initial int8 compartments ``state``, parameters, model seed and steps.  Arrays are host
-    arrays (numpy or CPU tensors; page-locked tensors copy asynchronously), int32 / int8
-    and contiguous; they must stay unchanged until the request is admitted."""
-    __slots__ = ("rid", "row_ptr", "col", "state", "beta", "gamma", "seed", "steps",
+    arrays (numpy or CPU tensors; page-locked tensors copy asynchronously, and a request
+    whose three arrays are page-locked is copied by the server's gather kernel), int32 /
+    int8 and contiguous; their contents must stay unchanged until the request is admitted
+    (their addresses are taken when the request is made or an array is replaced)."""
+    __slots__ = ("rid", "_row_ptr", "_col", "_state", "beta", "gamma", "seed", "steps",
                  "arrival", "admitted", "finished", "counts", "final_state", "_slot",
-                 "_bufs", "_event", "keep_state", "error", "_n", "_e", "cancelled")
+                 "_bufs", "_event", "keep_state", "error", "_n", "_e", "cancelled", "_spans",
+                 "_pinned")
 
     def __init__(self, rid, row_ptr, col, state, beta, gamma, seed, steps, arrival=None,
                  keep_state=False):
         self.rid = rid
-        self.row_ptr, self.col, self.state = row_ptr, col, state
-        self._n = len(row_ptr) - 1
-        self._e = len(col)
+        self._row_ptr, self._col, self._state = row_ptr, col, state
+        self._refresh()
         self.beta, self.gamma, self.seed, self.steps = float(beta), float(gamma), int(seed), int(steps)
         self.arrival = arrival
         self.admitted = None
@@ -154,6 +169,44 @@ class Request:
         self._slot = None
         self._bufs = None
         self._event = None
+
+    def _refresh(self):
+        """Sizes, and the (array, address, bytes) of each input (a converted copy when the
+        given array is not a contiguous int32 / int8 one) with whether all three are
+        page-locked; redone whenever an input array is replaced."""
+        self._n = len(self._row_ptr) - 1
+        self._e = len(self._col)
+        self._spans = (_host_span(self._row_ptr, np.int32), _host_span(self._col, np.int32),
+                       _host_span(self._state, np.int8))
+        self._pinned = all(isinstance(a[0], torch.Tensor) and a[0].is_pinned()
+                           for a in self._spans)
+
+    @property
+    def row_ptr(self):
+        return self._row_ptr
+
+    @row_ptr.setter
+    def row_ptr(self, v):
+        self._row_ptr = v
+        self._refresh()
+
+    @property
+    def col(self):
+        return self._col
+
+    @col.setter
+    def col(self, v):
+        self._col = v
+        self._refresh()
+
+    @property
+    def state(self):
+        return self._state
+
+    @state.setter
+    def state(self, v):
+        self._state = v
+        self._refresh()
 
     @property
     def n(self):
@@ -243,6 +296,7 @@ class SIRServer:
         self._tiles_used = 0
         self._work_event = None
         self._in_flight = collections.deque()  # events of replayed ticks
+        self._tables = []  # (event, page-locked segment table) of harvest copies in flight
         self.max_ticks_in_flight = 2
         # warm start: the tick graph is captured and replayed once over the empty tables,
         # and the device operations of an admission (key split, row staging, descriptor
@@ -355,20 +409,21 @@ class SIRServer:
             hubs = torch.empty(int(w_off[-1]), dtype=torch.int32, device=dev)
             comp = torch.empty(int(w_off[-1]) // 16, dtype=torch.int32, device=dev)
             counts = torch.zeros(int(c_off[-1]), dtype=torch.int32, device=dev)
-            # every request's three arrays in one call (one cudaMemcpyAsync each); converted
-            # copies stay referenced by `spans` until the call has issued every copy (a copy
-            # from pageable memory has read its source when the call returns)
-            spans = [(_host_span(r.row_ptr, np.int32), _host_span(r.col, np.int32),
-                      _host_span(r.state, np.int8)) for r in picked]
-            src = np.array([[a[1] for a in sp] for sp in spans], dtype=np.uint64)
-            nbytes = np.array([[a[2] for a in sp] for sp in spans], dtype=np.uint64)
+            # every request's three arrays in one call: one gather-kernel launch when all
+            # are page-locked, else one cudaMemcpyAsync each (the requests keep their
+            # converted copies alive; a copy from pageable memory has read its source when
+            # the call returns)
+            src = np.fromiter((a[1] for r in picked for a in r._spans), dtype=np.uint64,
+                              count=3 * g).reshape(g, 3)
+            nbytes = np.fromiter((a[2] for r in picked for a in r._spans), dtype=np.uint64,
+                                 count=3 * g).reshape(g, 3)
             if np.any(nbytes[:, 0] != 4 * (n + 1)) or np.any(nbytes[:, 1] != 4 * e) \
                     or np.any(nbytes[:, 2] != n):
                 raise ValueError("a request's row_ptr, col and state disagree in size")
             dst = np.stack([rp.data_ptr() + 4 * rp_off[:-1], col.data_ptr() + 4 * col_off[:-1],
                             st8.data_ptr() + w_off[:-1]], axis=1).astype(np.uint64)
-            copy_segments(dst.reshape(-1), src.reshape(-1), nbytes.reshape(-1), True, s)
-            del spans
+            table = copy_segments(dst, src, nbytes, True, s,
+                                  pinned=all(r._pinned for r in picked))
             rngs = model_rngs([r.seed for r in picked])
         rows = np.zeros(g, dtype=INSTANCE_DTYPE)
         rows["row_ptr"] = rp.data_ptr() + 4 * rp_off[:-1]
@@ -383,7 +438,7 @@ class SIRServer:
         rows["beta"] = [r.beta for r in picked]
         rows["gamma"] = [r.gamma for r in picked]
         # num_s / num_i / num_r stay 0 here: abm_sir_count_batch adds them on the device
-        work = np.concatenate([tiles_for(slot, int(nk)) for slot, nk in zip(slots, n)])
+        work, _ = work_table(slots, n, self.dummy, int(((n + TILE - 1) // TILE).sum()))
         self.done.numpy()[np.asarray(slots, dtype=np.int64)] = 0
         h_rows = torch.empty((g, INSTANCE_DTYPE.itemsize // 4), dtype=torch.int32,
                              pin_memory=True)
@@ -407,7 +462,7 @@ class SIRServer:
             done_ev = torch.cuda.Event()
             done_ev.record(s)
         group = _Group((rp, col, st8, words, hubs, comp, counts, h_rows, h_work, d_work,
-                        status, done_ev), h_status, h_counts)
+                        status, done_ev, table), h_status, h_counts)
         now = time.perf_counter()
         for k, (req, slot) in enumerate(zip(picked, slots)):
             req._slot = slot
@@ -466,12 +521,16 @@ class SIRServer:
                     self.retiring.append(req)
                     self._tiles_used -= self._tiles(req)
                     self.free_slots.append(slot)
-                copy_segments(dst, src, nbytes, False, self.stream)
+                # every result buffer is page-locked: one gather-kernel launch; its segment
+                # table stays referenced until the copy has run
+                table = copy_segments(dst, src, nbytes, False, self.stream, pinned=True)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
+                self._tables.append((ev, table))
             for req in self.retiring[len(self.retiring) - len(finished):]:
                 req._event = ev
             self._work_dirty = True
+        self._tables = [(ev, t) for ev, t in self._tables if not ev.query()]
         still = []
         for req in self.retiring:
             if req._event.query():
