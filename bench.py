@@ -714,7 +714,12 @@ def run_ours(args):
         "data": "synthetic",
         "config": ensemble_config(wl.full_sizes, wl.T, world),
         "e2e": {"value": units / (e2e_ms / 1e3), "unit": "agent-steps/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": ("SIRBatch.run_from_host: page-locked inputs copied in 8 index "
+                         "ranges, each range's resident launch starting when its copies "
+                         "land, its counts copied back when it ends"
+                         if wl.batch.mode == "resident" else
+                         "SIRBatch.load_host + replay + counts copy")},
         "e2e_pipelined": {"value": units / (e2e_pipe_ms / 1e3), "unit": "agent-steps/s",
                           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                           "note": "two input sets: step k+1's host-to-device copies run on a "
