@@ -173,6 +173,30 @@ __device__ __forceinline__ uint32_t byte_of(const uint32_t (&q)[4 * kVecs], int 
   return (q[j >> 2] >> (8 * (j & 3))) & 0xFFu;
 }
 
+// Flags of 32 agents' words (8 x 32 bits, agent j in byte j): bit j of need_s = susceptible
+// with a non-zero count (hubs included), need_i = infected, hub_s = susceptible hub.
+// Four agents per word at once: per byte, the compartment bits (S = 0, I = 1), count > 0
+// (adding 0x7F sets bit 7 iff the 6-bit count is non-zero) and the hub mark (count + 1
+// reaches 64 only for 63); bit 0 of each byte becomes one mask bit by one multiply (the
+// partial products land on distinct bits, so nothing carries).
+__device__ __forceinline__ void sweep_flags(const uint32_t (&q)[4 * kVecs], unsigned& need_s,
+                                            unsigned& need_i, unsigned& hub_s) {
+  need_s = need_i = hub_s = 0;
+#pragma unroll
+  for (int k = 0; k < 4 * kVecs; ++k) {
+    const uint32_t w = q[k];
+    const uint32_t lo = w & 0x01010101u, hi = (w >> 1) & 0x01010101u;
+    const uint32_t cnt = (w >> 2) & 0x3F3F3F3Fu;
+    const uint32_t is_s = ~(lo | hi) & 0x01010101u;
+    const uint32_t is_i = lo & ~hi;
+    const uint32_t nz = ((cnt + 0x7F7F7F7Fu) >> 7) & 0x01010101u;
+    const uint32_t hub = ((cnt + 0x01010101u) >> 6) & 0x01010101u;
+    need_s |= (((is_s & nz) * 0x01020408u) >> 24 & 0xFu) << (4 * k);
+    need_i |= ((is_i * 0x01020408u) >> 24 & 0xFu) << (4 * k);
+    hub_s |= (((is_s & hub) * 0x01020408u) >> 24 & 0xFu) << (4 * k);
+  }
+}
+
 // Changes buffered per warp in shared memory and appended to the change list 32 at a time
 // (one counter atomic per 32 changes instead of one per pass).
 constexpr int kBuf = 64;
@@ -333,15 +357,8 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
         }
       }
     }
-    unsigned need_s = 0, need_i = 0, hub_s = 0;
-#pragma unroll
-    for (int j = 0; j < kPerThread; ++j) {
-      const uint32_t b = byte_of(q, j);
-      const uint32_t s = b & 3u;
-      need_s |= static_cast<unsigned>(s == kS && b >= 4u) << j;
-      need_i |= static_cast<unsigned>(s == kI) << j;
-      hub_s |= static_cast<unsigned>(b == (kHubMark << 2)) << j;
-    }
+    unsigned need_s, need_i, hub_s;
+    sweep_flags(q, need_s, need_i, hub_s);
     // susceptible hubs need a decision only with infected neighbours (count in hub_counts)
     while (hub_s) {
       const int j = __ffs(hub_s) - 1;
@@ -1199,24 +1216,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             for (int z = 0; z < 4; ++z) qw[4 * v + z] = 0x02020202u;  // beyond the agents: R
           }
         }
-        // four agents per 32-bit word at once: per byte, compartment bits (S = 0, I = 1),
-        // count > 0 (adding 0x7F sets bit 7 iff the 6-bit count is non-zero) and hub mark
-        // (count + 1 reaches 64 only for 63); the byte flags (bit 0 of each byte) become
-        // four mask bits by one multiply (partial products land on distinct bits, no carries)
-        unsigned need_s = 0, need_i = 0, hub_s = 0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const uint32_t w = qw[q];
-          const uint32_t lo = w & 0x01010101u, hi = (w >> 1) & 0x01010101u;
-          const uint32_t cnt = (w >> 2) & 0x3F3F3F3Fu;
-          const uint32_t isS = ~(lo | hi) & 0x01010101u;
-          const uint32_t isI = lo & ~hi;
-          const uint32_t nz = ((cnt + 0x7F7F7F7Fu) >> 7) & 0x01010101u;
-          const uint32_t hub = ((cnt + 0x01010101u) >> 6) & 0x01010101u;
-          need_s |= (((isS & nz) * 0x01020408u) >> 24 & 0xFu) << (4 * q);
-          need_i |= ((isI * 0x01020408u) >> 24 & 0xFu) << (4 * q);
-          hub_s |= (((isS & hub) * 0x01020408u) >> 24 & 0xFu) << (4 * q);
-        }
+        unsigned need_s, need_i, hub_s;
+        sweep_flags(qw, need_s, need_i, hub_s);
         while (hub_s) {
           const int j = __ffs(hub_s) - 1;
           hub_s &= hub_s - 1;
