@@ -352,7 +352,11 @@ class SIRBatch:
         :meth:`load_host` followed by :meth:`run`."""
         if self.mode != "resident":
             raise ValueError("run_from_host needs the resident path")
-        plan, d_order, copy = self._chunk_plan(int(chunks))
+        with nvtx_range("SIRBatch.run_from_host"):
+            self._run_from_host(h_row_ptr, h_col, h_state8, h_counts, int(chunks))
+
+    def _run_from_host(self, h_row_ptr, h_col, h_state8, h_counts, chunks):
+        plan, d_order, copy = self._chunk_plan(chunks)
         rp_off, col_off, w_off, cnt_off = self._offsets
         cur = torch.cuda.current_stream()
         self.res_status.zero_()
