@@ -148,7 +148,7 @@ class Request:
     int8 and contiguous; their contents must stay unchanged until the request is admitted
     (their addresses are taken when the request is made or an array is replaced)."""
     __slots__ = ("rid", "_row_ptr", "_col", "_state", "beta", "gamma", "seed", "steps",
-                 "arrival", "admitted", "finished", "counts", "final_state", "_slot",
+                 "arrival", "admitted", "finished", "_counts", "final_state", "_slot",
                  "_bufs", "_event", "keep_state", "error", "_n", "_e", "cancelled", "_spans",
                  "_pinned")
 
@@ -161,7 +161,7 @@ class Request:
         self.arrival = arrival
         self.admitted = None
         self.finished = None
-        self.counts = None
+        self._counts = None  # (page-locked result buffer, offset) once retired
         self.final_state = None
         self.keep_state = keep_state
         self.error = None  # AbmError when the request's inputs were bad (set at harvest)
@@ -211,6 +211,17 @@ class Request:
     @property
     def n(self):
         return self._n
+
+    @property
+    def counts(self):
+        """Per-step S/I/R counts int32[steps, 3] (a view into the admission group's
+        page-locked result buffer), or None before the request has retired."""
+        c = self._counts
+        if c is None or isinstance(c, torch.Tensor):
+            return c
+        buf, c0 = c
+        self._counts = buf[c0:c0 + 3 * self.steps].view(self.steps, 3)
+        return self._counts
 
     def device_bytes(self):
         n, e = self._n, self._e
@@ -464,12 +475,12 @@ class SIRServer:
         group = _Group((rp, col, st8, words, hubs, comp, counts, h_rows, h_work, d_work,
                         status, done_ev, table), h_status, h_counts)
         now = time.perf_counter()
-        for k, (req, slot) in enumerate(zip(picked, slots)):
+        for req, slot, w0, c0 in zip(picked, slots, w_off[:-1].tolist(), c_off[:-1].tolist()):
             req._slot = slot
-            req._bufs = (group, int(w_off[k]), int(c_off[k]))
+            req._bufs = (group, w0, c0)
             req.admitted = now
             self.active[slot] = req
-            self._tiles_used += self._tiles(req)
+        self._tiles_used += int(((n + TILE - 1) // TILE).sum())
         self._work_dirty = True
         return g
 
@@ -500,17 +511,22 @@ class SIRServer:
         slots = np.fromiter(self.active.keys(), dtype=np.int64, count=len(self.active))
         finished = slots[self.done.numpy()[slots] == 1].tolist()
         if finished:
-            dst, src, nbytes = [], [], []
+            nf = len(finished)
+            dst = np.empty(nf, dtype=np.uint64)
+            src = np.empty(nf, dtype=np.uint64)
+            nbytes = np.empty(nf, dtype=np.uint64)
+            retired = []
             with torch.cuda.stream(self.stream):
-                for slot in finished:
+                for k, slot in enumerate(finished):
                     req = self.active.pop(slot)
                     group, w0, c0 = req._bufs
-                    counts_dev, words_dev = group.bufs[6], group.bufs[3]
-                    req.counts = group.h_counts[c0:c0 + 3 * req.steps].view(req.steps, 3)
-                    dst.append(req.counts.data_ptr())
-                    src.append(counts_dev.data_ptr() + 4 * c0)
-                    nbytes.append(12 * req.steps)
+                    h_counts = group.h_counts
+                    req._counts = (h_counts, c0)  # the view is made on first access
+                    dst[k] = h_counts.data_ptr() + 4 * c0
+                    src[k] = group.bufs[6].data_ptr() + 4 * c0
+                    nbytes[k] = 12 * req.steps
                     if req.keep_state:
+                        words_dev = group.bufs[3]
                         req.final_state = torch.empty(req.n, dtype=torch.int8, pin_memory=True)
                         st = unpack_words(words_dev[w0:w0 + req.n], req.n, self.stream)
                         req.final_state.copy_(st, non_blocking=True)
@@ -518,23 +534,30 @@ class SIRServer:
                     # status copy is in place
                     if int(group.h_status[0]):
                         req.error = input_error(req)
-                    self.retiring.append(req)
-                    self._tiles_used -= self._tiles(req)
-                    self.free_slots.append(slot)
+                    retired.append(req)
+                    self._tiles_used -= (req._n + TILE - 1) // TILE
+                self.free_slots.extend(finished)
                 # every result buffer is page-locked: one gather-kernel launch; its segment
                 # table stays referenced until the copy has run
                 table = copy_segments(dst, src, nbytes, False, self.stream, pinned=True)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
                 self._tables.append((ev, table))
-            for req in self.retiring[len(self.retiring) - len(finished):]:
+            for req in retired:
                 req._event = ev
+            self.retiring.extend(retired)
             self._work_dirty = True
         self._tables = [(ev, t) for ev, t in self._tables if not ev.query()]
-        still = []
+        still, seen = [], {}  # one query per copy event (shared by a harvest's requests)
+        now = None
         for req in self.retiring:
-            if req._event.query():
-                req.finished = time.perf_counter()
+            done = seen.get(id(req._event))
+            if done is None:
+                done = seen[id(req._event)] = req._event.query()
+            if done:
+                if now is None:
+                    now = time.perf_counter()
+                req.finished = now
                 req._bufs = None
                 self.completed.append(req)
             else:
