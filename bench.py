@@ -282,8 +282,8 @@ class SIREnsembleBench:
         return self.batch.algorithmic_bytes()
 
     def plain(self, sample=48):
-        """One simulation per launch sequence (abm_sir_run, the JaxModel.run path), on the
-        first ``sample`` instances, each from device-resident inputs."""
+        """One simulation per call (abm_sir_run, the JaxModel.run path), on the first
+        ``sample`` instances, each from device-resident inputs, one after another."""
         from jaxabm_gb300 import _dev, _lib
         import jaxabm_gb300.random as jr
         L = _lib.load()
@@ -310,7 +310,8 @@ class SIREnsembleBench:
             units += n * self.T
         return {"value": units / secs, "unit": "agent-steps/s",
                 "sample": f"first {min(sample, self.count)} instances, one simulation per "
-                          f"launch sequence (keychain + 2 launches per step)"}
+                          f"call (abm_sir_run, the JaxModel.run path: the key chain, the "
+                          f"pack, then one resident launch of one CTA for all steps)"}
 
     def served(self, burst=False):
         """The request stream through the continuous-batching server: the Poisson arrivals

@@ -391,10 +391,14 @@ ABM_API int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const
 /* Workspace of abm_sir_run for n agents and num_edges = row_ptr[n] CSR entries. */
 ABM_API size_t abm_sir_run_workspace_bytes(int64_t n, int64_t num_edges);
 
-/* One SIR model for `steps` steps (the plain engine: one simulation per launch sequence)
- * with the per-step collection keys coll_keys uint32[steps][2] (abm_keychain, ncoll = 1).
- * The CSR (row_ptr[n+1], col[num_edges]) is only read.  state int8[n] holds the
- * compartments before the run and receives them after it; counts int32[steps][3]. */
+/* One SIR model for `steps` steps (the plain engine: one simulation per call) with the
+ * per-step collection keys coll_keys uint32[steps][2] (abm_keychain, ncoll = 1).  A model
+ * whose one-byte words fit shared memory (abm_sir_resident_max_agents) runs all steps in one
+ * resident launch of one CTA; a larger one steps through the per-step kernels over the whole
+ * GPU.  Both give the same results.  The CSR (row_ptr[n+1], col[num_edges]) is only read.
+ * state int8[n] holds the compartments before the run and receives them after it; counts
+ * int32[steps][3].  Replaces JaxModel.run stepping one SIR collection
+ * (jaxabm/model.py:218-262, jaxabm/agent.py:132-179). */
 ABM_API int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t num_edges,
                         int8_t* state, const uint32_t* coll_keys, int32_t steps, float beta,
                         float gamma, int32_t* counts, void* workspace, size_t workspace_bytes,

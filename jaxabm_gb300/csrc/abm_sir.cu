@@ -1895,8 +1895,18 @@ int abm_sir_run(const int32_t* row_ptr, const int32_t* col, int64_t n, int64_t n
       beta, gamma, misc);
   st = abm_host::check_launch("abm_sir_run/setup");
   if (st) return st;
-  st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr, steps,
-                     nullptr, lists, align256(abm_sir_changes_bytes(n, ntiles)), stream);
+  const size_t lists_bytes = align256(abm_sir_changes_bytes(n, ntiles));
+  // a model whose words fit shared memory runs every step in one launch of one resident CTA
+  // (no per-step launches; the descriptor's per-step keys drive it); larger ones step
+  // through the per-step kernels over the whole GPU
+  if (abm_sir_resident_grid(static_cast<int32_t>(n)) > 0 &&
+      abm_sir_resident_scratch_bytes(static_cast<int32_t>(n), 1) <= lists_bytes) {
+    st = abm_sir_steps_resident(d, 1, nullptr, static_cast<int32_t>(n), steps, 1, nullptr,
+                                nullptr, lists, lists_bytes, misc + 3, stream);
+  } else {
+    st = abm_sir_steps(d, 1, reinterpret_cast<const abm_work_item*>(work), ntiles, nullptr,
+                       steps, nullptr, lists, lists_bytes, stream);
+  }
   if (st) return st;
   return abm_sir_unpack(words, n, state, stream);
 }
