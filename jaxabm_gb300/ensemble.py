@@ -146,6 +146,30 @@ def unpack_words(words, n=None, stream=None):
     return out
 
 
+def chunk_ranges(nbytes, chunks):
+    """Index ranges [a, b) covering 0..len(nbytes) in order, for copying and running a batch
+    in ``chunks`` pieces: range c ends where the cumulative bytes first reach 2^(c+1-chunks)
+    of the total (the first range ~1/2^(chunks-1) of the bytes, each next one doubling),
+    every range holds at least one instance, and empty ranges are dropped."""
+    nbytes = np.asarray(nbytes, dtype=np.float64)
+    k = nbytes.size
+    if k == 0:
+        return []
+    chunks = max(1, int(chunks))
+    cum = np.cumsum(nbytes) / float(nbytes.sum())
+    bounds, start = [], 0
+    for c in range(chunks):
+        if start >= k:
+            break
+        frac = 1.0 / (1 << (chunks - 1 - c))
+        stop = min(k, max(start + 1, int(np.searchsorted(cum, frac - 1e-12)) + 1))
+        bounds.append((start, stop))
+        start = stop
+    if start < k:
+        bounds.append((start, k))
+    return bounds
+
+
 class SIRBatch:
     """A fixed set of SIR instances packed into device buffers.
 
@@ -310,21 +334,7 @@ class SIRBatch:
             return self._chunks[1]
         L = _lib.load()
         dev = self.row_ptr.device
-        nbytes = 4 * (self.n + 1) + 4 * self.e + self.n
-        cum = np.cumsum(nbytes) / float(nbytes.sum())
-        # cumulative byte fractions at the ends of the ranges: 1/2^(c-1) of the whole for
-        # the first, doubling up to the last
-        ends = [1.0 / (1 << (chunks - 1 - c)) for c in range(chunks)]
-        bounds, start = [], 0
-        for f in ends:
-            stop = max(start + 1, int(np.searchsorted(cum, f - 1e-12) + 1)) if start < self.k \
-                else start
-            stop = min(stop, self.k)
-            if stop > start:
-                bounds.append((start, stop))
-            start = stop
-        if start < self.k:
-            bounds.append((start, self.k))
+        bounds = chunk_ranges(4 * (self.n + 1) + 4 * self.e + self.n, chunks)
         order = np.concatenate([a + np.argsort(-self.n[a:b], kind="stable")
                                 for a, b in bounds]).astype(np.int32)
         d_order = torch.from_numpy(order).to(dev)

@@ -71,3 +71,21 @@ def test_ensemble_spec():
     assert s["arrival_s"][0] == 0.0 and np.all(np.diff(s["arrival_s"]) >= 0)
     assert 15.0 < s["arrival_s"][-1] < 26.0
     assert np.array_equal(s["n"], ensemble.ensemble_spec(4096)["n"])
+
+
+def test_chunk_ranges_cover_in_order():
+    """The index ranges of SIRBatch.run_from_host: contiguous, in order, each non-empty,
+    covering every instance once; the first holds about 1/2^(chunks-1) of the bytes."""
+    from jaxabm_gb300.ensemble import chunk_ranges
+    rng = np.random.default_rng(3)
+    for k, chunks in [(1, 8), (3, 8), (11, 3), (4096, 8), (50, 1), (7, 7)]:
+        nbytes = np.sort(rng.integers(100, 10_000, k))[::-1]
+        r = chunk_ranges(nbytes, chunks)
+        assert r[0][0] == 0 and r[-1][1] == k
+        assert all(a < b for a, b in r)
+        assert all(r[i][1] == r[i + 1][0] for i in range(len(r) - 1))
+        assert len(r) <= max(1, chunks)
+        if k >= 4096:
+            first = nbytes[r[0][0]:r[0][1]].sum() / nbytes.sum()
+            assert first <= 2.0 / (1 << (chunks - 1)) + nbytes[0] / nbytes.sum()
+    assert chunk_ranges([], 4) == []
