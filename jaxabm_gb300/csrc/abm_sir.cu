@@ -1116,49 +1116,80 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       // words built here from the int8 compartments: compartment, hub mark (degree >=
       // 63, whose count starts at 0 in hub_counts), the columns' hub tags, then every
       // infected agent adds one to its neighbours' counts
+      // (each loop keeps several independent loads per thread in flight)
       const int8_t* __restrict__ st = states8 + (I->words - words_base);
-      for (int k = threadIdx.x; k < npad; k += kResThreads) {
-        uint32_t w = 2u;  // padding: R
-        if (k < n) {
-          int c = st[k];
-          if (c < 0 || c > 2) {
-            atomicOr(status, ABM_SIR_STATUS_BAD_COMPARTMENT);
-            c = 2;
-          }
-          w = static_cast<uint32_t>(c);
-          if (__ldg(rp + k + 1) - __ldg(rp + k) >= kHubDeg) {
-            w |= kHubMark << 2;
-            hubs[k] = 0;
+      constexpr int kWordsIn = 4, kColsIn = 8;
+      for (int k0 = threadIdx.x; k0 < npad; k0 += kResThreads * kWordsIn) {
+        int c[kWordsIn], a[kWordsIn], e[kWordsIn];
+#pragma unroll
+        for (int u = 0; u < kWordsIn; ++u) {
+          const int k = k0 + kResThreads * u;
+          c[u] = 2;
+          a[u] = e[u] = 0;
+          if (k < n) {
+            c[u] = st[k];
+            a[u] = __ldg(rp + k);
+            e[u] = __ldg(rp + k + 1);
           }
         }
-        sw[k] = static_cast<uint8_t>(w);
+#pragma unroll
+        for (int u = 0; u < kWordsIn; ++u) {
+          const int k = k0 + kResThreads * u;
+          if (k >= npad) continue;
+          uint32_t w = 2u;  // padding: R
+          if (k < n) {
+            int cc = c[u];
+            if (cc < 0 || cc > 2) {
+              atomicOr(status, ABM_SIR_STATUS_BAD_COMPARTMENT);
+              cc = 2;
+            }
+            w = static_cast<uint32_t>(cc);
+            if (e[u] - a[u] >= kHubDeg) {
+              w |= kHubMark << 2;
+              hubs[k] = 0;
+            }
+          }
+          sw[k] = static_cast<uint8_t>(w);
+        }
       }
       __syncthreads();
       // hub tags on the columns (bit 31 where the neighbour is a hub), in place; a column
       // outside 0..n-1 is flagged and replaced by a self-loop, as abm_sir_pack does, so that
       // no step reads outside the instance
       const int nslots = __ldg(rp + n);
-      for (int k = threadIdx.x; k < nslots; k += kResThreads) {
-        const uint32_t v = static_cast<uint32_t>(adj[k]);
-        uint32_t t = v & kIdx;
-        if (t >= static_cast<uint32_t>(n)) {
-          atomicOr(status, ABM_SIR_STATUS_BAD_COLUMN);
-          int lo = 0, hi = n - 1;  // the row holding slot k: last i with rp[i] <= k
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(rp + mid) <= k) lo = mid;
-            else hi = mid - 1;
-          }
-          t = static_cast<uint32_t>(lo);
+      for (int k0 = threadIdx.x; k0 < nslots; k0 += kResThreads * kColsIn) {
+        uint32_t v[kColsIn];
+#pragma unroll
+        for (int u = 0; u < kColsIn; ++u) {
+          const int k = k0 + kResThreads * u;
+          v[u] = k < nslots ? static_cast<uint32_t>(adj[k]) : 0u;
         }
-        const uint32_t want = (sw[t] >> 2) == kHubMark ? (t | kTag) : t;
-        if (want != v) adj[k] = static_cast<int32_t>(want);
+#pragma unroll
+        for (int u = 0; u < kColsIn; ++u) {
+          const int k = k0 + kResThreads * u;
+          if (k >= nslots) continue;
+          uint32_t t = v[u] & kIdx;
+          if (t >= static_cast<uint32_t>(n)) {
+            atomicOr(status, ABM_SIR_STATUS_BAD_COLUMN);
+            int lo = 0, hi = n - 1;  // the row holding slot k: last i with rp[i] <= k
+            while (lo < hi) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (__ldg(rp + mid) <= k) lo = mid;
+              else hi = mid - 1;
+            }
+            t = static_cast<uint32_t>(lo);
+          }
+          const uint32_t want = (sw[t] >> 2) == kHubMark ? (t | kTag) : t;
+          if (want != v[u]) adj[k] = static_cast<int32_t>(want);
+        }
       }
       __syncthreads();
       for (int b = threadIdx.x & ~31; b < n; b += kResThreads) {
         const int k = b + lane;
+        const bool inf = k < n && (sw[k] & 3u) == kI;
+        if (!__any_sync(kFull, inf)) continue;  // uniform: no infected agent here
         int r0 = 0, len = 0;
-        if (k < n && (sw[k] & 3u) == kI) {
+        if (inf) {
           r0 = __ldg(rp + k);
           len = __ldg(rp + k + 1) - r0;
         }
