@@ -1249,10 +1249,20 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         unsigned need_s, need_i, hub_s;
         sweep_flags(qw, need_s, need_i, hub_s);
+        // susceptible hubs need a decision only with infected neighbours (their count in
+        // hub_counts): four counts read at a time
         while (hub_s) {
-          const int j = __ffs(hub_s) - 1;
-          hub_s &= hub_s - 1;
-          if (__ldcg(hubs + base + j) <= 0) need_s &= ~(1u << j);
+          int jj[4];
+          int32_t hc[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            jj[u] = hub_s ? __ffs(hub_s) - 1 : -1;
+            hub_s &= hub_s - 1;
+            hc[u] = jj[u] >= 0 ? __ldcg(hubs + base + jj[u]) : 1;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (jj[u] >= 0 && hc[u] <= 0) need_s &= ~(1u << jj[u]);
         }
         const int ms = __popc(need_s), mi = __popc(need_i);
         my_cands += ms + mi;
