@@ -330,8 +330,13 @@ class SIRBatch:
         """Index ranges of the overlapped host run (a small first range, so the kernels
         start early, then ranges of growing byte counts), each with its own order (largest
         instance first), resident grid, scratch and stream."""
-        if getattr(self, "_chunks", None) is not None and self._chunks[0] == chunks:
-            return self._chunks[1]
+        if getattr(self, "_chunks", None) is not None:
+            if self._chunks[0] == chunks:
+                return self._chunks[1]
+            # the old plan's scratch may still be in use on its streams: finish them before
+            # it is released to the allocator
+            torch.cuda.synchronize()
+            self._chunks = None
         L = _lib.load()
         dev = self.row_ptr.device
         bounds = chunk_ranges(4 * (self.n + 1) + 4 * self.e + self.n, chunks)
