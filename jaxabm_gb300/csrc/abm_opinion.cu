@@ -51,20 +51,27 @@ constexpr float kExpK = 0x1.715476p+5f;   // 32 / ln 2
 constexpr float kExpL1 = 0x1.62c000p-6f;  // ln 2 / 32, leading 11 bits
 constexpr float kExpL2 = 0x1.217f7ep-17f; // ln 2 / 32 - kExpL1
 constexpr float kExpC3 = 0x1.555556p-3f;  // 1 / 6
+constexpr float kExpRound = 0x1.8p+23f;   // 1.5 * 2^23
 
 // exp(x) in float32 by Tang's table-driven method (P. T. P. Tang, "Table-driven
 // implementation of the exponential function in IEEE floating-point arithmetic", ACM TOMS
 // 15(2), 1989): N = rint(x * 32 / ln 2); r = fma(-N, L2, fma(-N, L1, x)) with
 // L1 + L2 = ln 2 / 32 (L1 has 11 significant bits, so x - N L1 is exact); exp(r) - 1 by its
 // Taylor polynomial p = fma(r^2, fma(r, 1/6, 1/2), r) (|r| <= ln 2 / 64: truncation error
-// below 6e-10); exp(x) = 2^(N >> 5) fma(T[N & 31], p, T[N & 31]).  x is clamped to
+// below 6e-10); exp(x) = 2^(N >> 5) fma(T[N & 31], p, T[N & 31]).  N is computed without
+// a rounding or conversion instruction (below), with the same value as rint.  x is clamped to
 // [-87, 88], so every intermediate is normal and the scaling is an exact add to the
 // exponent field.  About 1 ulp from exp over the clamped range.  T is kExp2Table staged in
 // shared memory.
 __device__ __forceinline__ float exp_table(float x, const float* T) {
   x = fminf(fmaxf(x, -87.0f), 88.0f);
-  const float nf = rintf(__fmul_rn(x, kExpK));
-  const int N = static_cast<int>(nf);
+  // rint(x * 32 / ln 2) without a rounding or conversion instruction: adding 1.5 * 2^23 to
+  // a float of magnitude below 2^22 leaves its nearest integer (ties to even, as rint) in
+  // the low mantissa bits; subtracting it back is exact, and the bit patterns' difference
+  // is that integer (|x * 32 / ln 2| <= 4064 here)
+  const float shifted = __fadd_rn(__fmul_rn(x, kExpK), kExpRound);
+  const float nf = __fsub_rn(shifted, kExpRound);
+  const int N = __float_as_int(shifted) - __float_as_int(kExpRound);
   const float r = __fmaf_rn(-nf, kExpL2, __fmaf_rn(-nf, kExpL1, x));
   const float p = __fmaf_rn(__fmul_rn(r, r), __fmaf_rn(r, kExpC3, 0.5f), r);
   const float t = T[N & 31];
