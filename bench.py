@@ -349,7 +349,10 @@ class SIREnsembleBench:
                 "requests": len(lat),
                 "arrivals": "all at t=0" if burst else "Poisson, 200 requests/s, real time",
                 "wall_s": wall, "ticks": srv.ticks, "steps_per_tick": srv.steps_per_tick,
-                "path": path, "results_match_batched": bool(same)}
+                "path": path, "results_match_batched": bool(same),
+                "note": ("the server's capacity: every request submitted at t=0" if burst else
+                         "bounded by the arrival rate: the stream offers "
+                         f"{units / float(np.max(arrivals)):.3g} agent-steps/s")}
 
     def oracle_check(self, threads, sample=1024):
         """The C/OpenMP oracle on this rank's first ``sample`` members and its largest one,
