@@ -1034,7 +1034,9 @@ __device__ __forceinline__ void sw_add(uint8_t* sw, int i, uint32_t v) {
 }
 
 // Count updates of up to 32 rows of one instance, one per lane (len 0: none; up: +1,
-// else -1), by the whole warp over the concatenated rows, kPushPasses passes in flight.
+// else -1), by the whole warp over the concatenated rows, kResPushPasses passes in flight
+// (six here, four on the grid path: each measured best on its path).
+constexpr int kResPushPasses = 6;
 // A column with the hub tag sends its update to hub_counts.  Columns are within the
 // instance (checked when its words are built).
 __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj, uint8_t* sw,
@@ -1044,11 +1046,11 @@ __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj
   const int total = __shfl_sync(kFull, incl, 31);
   const int shift = row0 - (incl - len);
   const int sign = up ? 1 : 0;
-  for (int base = 0; base < total; base += 32 * kPushPasses) {
-    uint32_t v[kPushPasses];
-    int d[kPushPasses];
+  for (int base = 0; base < total; base += 32 * kResPushPasses) {
+    uint32_t v[kResPushPasses];
+    int d[kResPushPasses];
 #pragma unroll
-    for (int u = 0; u < kPushPasses; ++u) {
+    for (int u = 0; u < kResPushPasses; ++u) {
       const int f = base + 32 * u + lane;
       const int lo = owner_lane(incl, f);
       const int sh = __shfl_sync(kFull, shift, lo);
@@ -1056,7 +1058,7 @@ __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj
       v[u] = f < total ? ld_col(adj, f + sh) : 0u;
     }
 #pragma unroll
-    for (int u = 0; u < kPushPasses; ++u) {
+    for (int u = 0; u < kResPushPasses; ++u) {
       if (base + 32 * u + lane < total) {
         const uint32_t t = v[u] & kIdx;
         if (v[u] & kTag) red_add(hubs + t, d[u]);
