@@ -158,3 +158,37 @@ def test_cancel_queued_and_running_requests(cuda, path):
                                                 r.gamma)
         assert np.array_equal(r.counts.numpy(), ref_counts), rid
         assert np.array_equal(r.final_state.numpy(), ref_st), rid
+
+
+@pytest.mark.parametrize("path", ["resident", "grid"])
+def test_page_locked_requests_take_the_gather_copies(cuda, path):
+    """Requests whose arrays are page-locked tensors are admitted and retired through the
+    one-launch gather copy (abm_copy_segments_kernel); numpy requests in the same server go
+    through per-array copies.  Every result equals its oracle run either way."""
+    from jaxabm_gb300.serving import Request, SIRServer
+    base = _requests(10, seed0=700, steps=40)
+    reqs = []
+    for r in base:
+        if r.rid % 2 == 0:  # every other request page-locked
+            r = Request(r.rid, torch.from_numpy(np.asarray(r.row_ptr)).pin_memory(),
+                        torch.from_numpy(np.asarray(r.col)).pin_memory(),
+                        torch.from_numpy(np.asarray(r.state)).pin_memory(),
+                        r.beta, r.gamma, r.seed, r.steps)
+            assert r._pinned
+        else:
+            assert not r._pinned
+        reqs.append(r)
+    srv = SIRServer(max_slots=4, max_tiles=128, steps_per_tick=9, path=path)
+    for r in reqs[:5]:
+        srv.submit(r)
+    srv.tick()
+    for r in reqs[5:]:
+        srv.submit(r)
+    srv.drain()
+    srv.check()
+    assert len(srv.completed) == len(reqs)
+    for r in srv.completed:
+        rng, _ = models.model_keys(r.seed, 1)
+        _, ref_counts, _ = coracle.sir_run(np.asarray(r.row_ptr), np.asarray(r.col),
+                                           np.asarray(r.state), rng, r.steps, r.beta, r.gamma)
+        assert np.array_equal(r.counts.numpy(), ref_counts), r.rid

@@ -435,3 +435,12 @@ def test_sir_run_from_host_overlapped_equals_oracle(cuda, chunks):
     b.reset()
     b.run()
     assert np.array_equal(b.counts.cpu().numpy(), h_counts.numpy())
+
+
+def test_sir_run_from_host_needs_the_resident_path(cuda):
+    from jaxabm_gb300 import ensemble, sir
+    g = [sir.barabasi_albert(500, 4, 1)]
+    st = [sir.initial_states(500, 0.02, 1)]
+    b = ensemble.SIRBatch(g, st, [0.1], [0.1], [1], 10, resident=False)
+    with pytest.raises(ValueError):
+        b.run_from_host(torch.zeros(1), torch.zeros(1), torch.zeros(1))
