@@ -197,6 +197,28 @@ __device__ __forceinline__ void sweep_flags(const uint32_t (&q)[4 * kVecs], unsi
   }
 }
 
+// Clears from need_s the susceptible hubs (bits of hub_s) whose count in hubs[] (agent j at
+// hubs[j]) is not positive: a hub needs a decision only with infected neighbours.  Four
+// counts are read at a time, through L2 (the counts change under atomics of this launch on
+// the resident path).
+__device__ __forceinline__ unsigned drop_idle_hubs(unsigned need_s, unsigned hub_s,
+                                                   const int32_t* hubs) {
+  while (hub_s) {
+    int jj[4];
+    int32_t hc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      jj[u] = hub_s ? __ffs(hub_s) - 1 : -1;
+      hub_s &= hub_s - 1;
+      hc[u] = jj[u] >= 0 ? __ldcg(hubs + jj[u]) : 1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (jj[u] >= 0 && hc[u] <= 0) need_s &= ~(1u << jj[u]);
+  }
+  return need_s;
+}
+
 // Changes buffered per warp in shared memory and appended to the change list 32 at a time
 // (one counter atomic per 32 changes instead of one per pass).
 constexpr int kBuf = 64;
@@ -359,12 +381,7 @@ sir_sweep_kernel(abm_sir_instance* __restrict__ insts, const int4* __restrict__ 
     }
     unsigned need_s, need_i, hub_s;
     sweep_flags(q, need_s, need_i, hub_s);
-    // susceptible hubs need a decision only with infected neighbours (count in hub_counts)
-    while (hub_s) {
-      const int j = __ffs(hub_s) - 1;
-      hub_s &= hub_s - 1;
-      if (hubs[base + j] <= 0) need_s &= ~(1u << j);
-    }
+    need_s = drop_idle_hubs(need_s, hub_s, hubs + base);
     // both counts scanned at once (16 bits each): warp scan, then block totals
     const int mine = __popc(need_s) | (__popc(need_i) << 16);
     int incl = mine;
@@ -1251,21 +1268,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         unsigned need_s, need_i, hub_s;
         sweep_flags(qw, need_s, need_i, hub_s);
-        // susceptible hubs need a decision only with infected neighbours (their count in
-        // hub_counts): four counts read at a time
-        while (hub_s) {
-          int jj[4];
-          int32_t hc[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            jj[u] = hub_s ? __ffs(hub_s) - 1 : -1;
-            hub_s &= hub_s - 1;
-            hc[u] = jj[u] >= 0 ? __ldcg(hubs + base + jj[u]) : 1;
-          }
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (jj[u] >= 0 && hc[u] <= 0) need_s &= ~(1u << jj[u]);
-        }
+        need_s = drop_idle_hubs(need_s, hub_s, hubs + base);
         const int ms = __popc(need_s), mi = __popc(need_i);
         my_cands += ms + mi;
         // one list position per agent: warp prefix sums, one counter atomic per warp
