@@ -156,10 +156,12 @@ class SIREnsembleBench:
         self.resident = {"auto": None, "resident": True, "grid": False}[path]
         if grids is not None:
             self.resident = False
-        # batch members largest first (batch position pos[k] holds this rank's member k):
-        # the resident kernel takes the largest first anyway, and the end-to-end leg's
-        # index-range copies then land in the order the kernel needs them
-        self.perm = np.argsort(-np.asarray(spec["n"]), kind="stable")
+        # batch members longest first by predicted device time (batch position pos[k] holds
+        # this rank's member k): the resident kernel takes them in that order anyway, and
+        # the end-to-end leg's index-range copies then land in the order the kernel needs
+        self.costs = ensemble.member_costs(self.graphs, self.inits, spec["beta"],
+                                           spec["gamma"], steps)
+        self.perm = np.argsort(-self.costs, kind="stable")
         self.pos = np.empty_like(self.perm)
         self.pos[self.perm] = np.arange(self.perm.size)
         self.batch = self._make_batch()

@@ -51,6 +51,8 @@
 // Integer atomics commute, so every result is exact and independent of scheduling.  No
 // kernel waits on anything.
 
+#include <algorithm>
+
 #include "abm_common.cuh"
 
 namespace {
@@ -989,7 +991,9 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // counts come from global memory.  A step is three phases separated by __syncthreads:
 //   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
 //             the susceptible agents with infected neighbours and the infected agents to
-//             two lists (global scratch of the CTA, L2-resident).
+//             two lists (their first entries in shared memory after the words, as many as
+//             fit without lowering the CTAs per SM; the rest in the CTA's global scratch,
+//             L2-resident).
 //   decide    warps take paired rounds from a round counter, so that every warp has work
 //             however small the instance: per lane one susceptible agent (rows longer
 //             than 32 slots by the whole warp) and one infected agent's recovery draw;
@@ -1085,9 +1089,21 @@ __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj
   }
 }
 
+// Entry k of a CTA list: the first scap entries are in shared memory (sl), the rest in the
+// CTA's global list (gl, indexed from 0 like the shared part).
+__device__ __forceinline__ void list_put(uint32_t* sl, uint32_t* gl, int scap, int k, uint32_t v) {
+  if (k < scap) sl[k] = v;
+  else gl[k] = v;
+}
+__device__ __forceinline__ uint32_t list_get(const uint32_t* sl, const uint32_t* gl, int scap,
+                                             int k) {
+  return k < scap ? sl[k] : gl[k];
+}
+
 // Appends (agent << 2 | new compartment) of the lanes with `changed` to the change list.
 __device__ __forceinline__ void res_record(bool changed, int agent, uint32_t comp_new,
-                                           uint32_t* changes, int* count, int lane) {
+                                           uint32_t* s_changes, uint32_t* changes, int scap,
+                                           int* count, int lane) {
   const unsigned m = __ballot_sync(kFull, changed);
   if (!m) return;
   int base = 0;
@@ -1095,7 +1111,8 @@ __device__ __forceinline__ void res_record(bool changed, int agent, uint32_t com
   if (lane == leader) base = atomicAdd(count, __popc(m));
   base = __shfl_sync(kFull, base, leader);
   if (changed)
-    changes[base + __popc(m & ((1u << lane) - 1u))] = (static_cast<uint32_t>(agent) << 2) | comp_new;
+    list_put(s_changes, changes, scap, base + __popc(m & ((1u << lane) - 1u)),
+             (static_cast<uint32_t>(agent) << 2) | comp_new);
 }
 
 __global__ void __launch_bounds__(kResThreads, 2)
@@ -1103,14 +1120,18 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
                     const int32_t* __restrict__ order, int nsteps, int max_bytes,
                     const int8_t* __restrict__ states8, const uint8_t* words_base,
                     int32_t* __restrict__ queue, uint32_t* __restrict__ lists, int cap,
-                    int32_t* __restrict__ status) {
+                    int scap, int32_t* __restrict__ status) {
   extern __shared__ __align__(16) uint8_t sw[];
   __shared__ ResState S;
   const int lane = threadIdx.x & 31;
-  // this CTA's lists: changes, susceptible candidates, infected agents (cap entries each)
+  // this CTA's lists: changes, susceptible candidates, infected agents (cap entries each);
+  // the first scap entries of each are kept in shared memory after the words
   uint32_t* __restrict__ changes = lists + static_cast<size_t>(blockIdx.x) * 3 * cap;
   uint32_t* __restrict__ slist = changes + cap;
   uint32_t* __restrict__ ilist = slist + cap;
+  uint32_t* s_changes = reinterpret_cast<uint32_t*>(sw + max_bytes);
+  uint32_t* s_slist = s_changes + scap;
+  uint32_t* s_ilist = s_slist + scap;
   for (;;) {
     if (threadIdx.x == 0) S.inst = atomicAdd(queue, 1);
     __syncthreads();
@@ -1282,8 +1303,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         bs = __shfl_sync(kFull, bs, 31) + ((incl - both) & 0xFFFF);
         bi = __shfl_sync(kFull, bi, 31) + ((incl - both) >> 16);
-        for (unsigned m = need_s; m; m &= m - 1) slist[bs++] = base + __ffs(m) - 1;
-        for (unsigned m = need_i; m; m &= m - 1) ilist[bi++] = base + __ffs(m) - 1;
+        for (unsigned m = need_s; m; m &= m - 1) list_put(s_slist, slist, scap, bs++, base + __ffs(m) - 1);
+        for (unsigned m = need_i; m; m &= m - 1) list_put(s_ilist, ilist, scap, bi++, base + __ffs(m) - 1);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) my_cands += __shfl_down_sync(kFull, my_cands, o);
@@ -1312,11 +1333,11 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       };
       auto s_entry = [&](int r) {
         const int f = 32 * r + lane;
-        return r < rounds && f < ns ? static_cast<int>(slist[f]) : -1;
+        return r < rounds && f < ns ? static_cast<int>(list_get(s_slist, slist, scap, f)) : -1;
       };
       auto i_entry = [&](int r) {
         const int f = 32 * r + lane;
-        return r < rounds && f < ni ? static_cast<int>(ilist[f]) : -1;
+        return r < rounds && f < ni ? static_cast<int>(list_get(s_ilist, ilist, scap, f)) : -1;
       };
       int r_cur = take(), r_nxt = take();
       int es_cur = s_entry(r_cur), ei_cur = i_entry(r_cur);
@@ -1452,8 +1473,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         my_scanned += scanned;
         my_si += infected;
-        res_record(rec, ei, 2u, changes, &S.nchanges, lane);
-        res_record(infected, e, kI, changes, &S.nchanges, lane);
+        res_record(rec, ei, 2u, s_changes, changes, scap, &S.nchanges, lane);
+        res_record(infected, e, kI, s_changes, changes, scap, &S.nchanges, lane);
       }
       my_si = __reduce_add_sync(kFull, my_si);
       my_ir = __reduce_add_sync(kFull, my_ir);
@@ -1499,7 +1520,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         int r0 = 0, len = 0;
         bool up = false;
         if (k < nch) {
-          const uint32_t e = changes[k];
+          const uint32_t e = list_get(s_changes, changes, scap, k);
           const int a = static_cast<int>(e >> 2);
           sw_add(sw, a, 1u);
           up = (e & 3u) == kI;
@@ -1631,6 +1652,35 @@ Lists carve_lists(void* ws, size_t bytes, int64_t max_tiles) {
   return L;
 }
 
+// Entries of each CTA list kept in shared memory after the words (at most kResListShared,
+// a multiple of 32): what is left of the SM's shared memory once the CTAs per SM that the
+// words allow have their words, static shared memory and per-block reservation, less a
+// slack for the allocation granularity.  0 when nothing is left or a query fails.  The
+// opt-in must already cover `bytes`.
+constexpr int kResListShared = 2048;
+
+int res_list_cap(int bytes) {
+  int dev = 0, smem_sm = 0, reserved = 0, per_sm = 0;
+  cudaFuncAttributes fa;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) !=
+          cudaSuccess ||
+      cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sir_resident_kernel, kResThreads,
+                                                    bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (per_sm <= 0) return 0;
+  const int64_t room = static_cast<int64_t>(smem_sm / per_sm) - reserved -
+                       static_cast<int64_t>(fa.sharedSizeBytes) - bytes - 256;
+  if (room < 12 * 32) return 0;
+  return static_cast<int>(std::min<int64_t>(kResListShared, room / 12) & ~int64_t{31});
+}
+
+
 }  // namespace
 
 extern "C" {
@@ -1671,20 +1721,26 @@ int32_t abm_sir_resident_grid(int32_t max_agents) {
   const int bytes = static_cast<int>(round16(max_agents));
   // the opt-in only ever grows, so launches (and captured graphs) of larger batches stay
   // valid after a smaller batch asked for its grid
-  cudaFuncAttributes fa;
-  if (cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess) {
+  auto raise_optin = [](int want) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess) return false;
+    return fa.maxDynamicSharedSizeBytes >= want ||
+           cudaFuncSetAttribute(sir_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                want) == cudaSuccess;
+  };
+  if (!raise_optin(bytes)) {
     cudaGetLastError();
     return 0;
   }
-  if (fa.maxDynamicSharedSizeBytes < bytes &&
-      cudaFuncSetAttribute(sir_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           bytes) != cudaSuccess) {
+  // then room for the shared list heads (sized not to lower the CTAs per SM)
+  const int smem = bytes + 12 * res_list_cap(bytes);
+  if (!raise_optin(smem)) {
     cudaGetLastError();
     return 0;
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sir_resident_kernel, kResThreads,
-                                                    bytes) != cudaSuccess) {
+                                                    smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -1711,13 +1767,22 @@ int abm_sir_steps_resident(abm_sir_instance* insts, int32_t ninst, const int32_t
   cudaStream_t s = abm_host::as_stream(stream);
   const int bytes = static_cast<int>(round16(max_agents));
   // the shared-memory opt-in is set by abm_sir_resident_grid (not a stream operation, so
-  // not repeated here, where the call may be captured into a CUDA graph)
+  // not repeated here, where the call may be captured into a CUDA graph); the shared list
+  // heads take what the opt-in leaves, up to the size that function allowed for
+  int scap = res_list_cap(bytes);
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, sir_resident_kernel) != cudaSuccess) {
+    cudaGetLastError();
+    scap = 0;
+  } else {
+    scap = std::max(0, std::min(scap, (fa.maxDynamicSharedSizeBytes - bytes) / 12 & ~31));
+  }
   int st = abm_host::record_cuda_error(cudaMemsetAsync(scratch, 0, sizeof(int32_t), s),
                                        "abm_sir_steps_resident/queue");
   if (st) return st;
-  sir_resident_kernel<<<grid, kResThreads, bytes, s>>>(
+  sir_resident_kernel<<<grid, kResThreads, bytes + 12 * scap, s>>>(
       insts, ninst, order, nsteps, bytes, states8, words_base, static_cast<int32_t*>(scratch),
-      reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + 256), bytes, status);
+      reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + 256), bytes, scap, status);
   return abm_host::check_launch("abm_sir_steps_resident");
 }
 

@@ -170,6 +170,62 @@ def chunk_ranges(nbytes, chunks):
     return bounds
 
 
+# Fixed cost of one step of a member on the resident path (its three barriers and the
+# dependent loads of its phases), counted in list entries: fitted per-member device times
+# give ~10 us per active step and a few hundredths of a microsecond per list entry.
+STEP_COST_ENTRIES = 256
+
+
+def excess_degrees(row_ptrs):
+    """<k^2>/<k> - 1 of each CSR graph: the mean number of further neighbours of an agent
+    reached along an edge, the branching factor of a contagion on the graph."""
+    out = np.zeros(len(row_ptrs), dtype=np.float64)
+    for j, rp in enumerate(row_ptrs):
+        deg = np.diff(np.asarray(rp, dtype=np.int64)).astype(np.float64)
+        tot = deg.sum()
+        out[j] = (deg * deg).sum() / tot - 1.0 if tot > 0 else 0.0
+    return out
+
+
+def predicted_costs(n, num_s, num_i, betas, gammas, k_exc, steps):
+    """Predicted resident-path time of each member, in list entries, from a mean-field SIR
+    recursion on its excess degree k: per step an S agent is infected with probability
+    1 - (1 - beta i)^k and an infected one recovers with probability gamma; a member is
+    active while its expected infected count is at least 1/2, and an active step costs
+    ``STEP_COST_ENTRIES`` plus its expected list entries (infected agents and susceptible
+    agents with an infected neighbour).  Used only to order the members (longest first),
+    which never changes results: a long-lived epidemic on a small graph can take longer
+    than a quick one on a large graph, and started last it would run alone at the end."""
+    n = np.maximum(np.asarray(n, dtype=np.float64), 1.0)
+    i = np.asarray(num_i, dtype=np.float64) / n
+    s = np.asarray(num_s, dtype=np.float64) / n
+    beta = np.asarray(betas, dtype=np.float64)
+    gamma = np.asarray(gammas, dtype=np.float64)
+    k = np.maximum(np.asarray(k_exc, dtype=np.float64), 0.0)
+    cost = np.zeros_like(n)
+    alive = np.ones(n.shape, dtype=bool)
+    for _ in range(int(steps)):
+        alive &= i * n >= 0.5
+        if not alive.any():
+            break
+        cost += np.where(alive, STEP_COST_ENTRIES + n * (i + s * (1.0 - (1.0 - i) ** k)), 0.0)
+        new_i = s * (1.0 - (1.0 - beta * i) ** k)
+        new_r = gamma * i
+        s = s - new_i
+        i = i + new_i - new_r
+    return cost
+
+
+def member_costs(graphs, init_states, betas, gammas, steps):
+    """:func:`predicted_costs` of SIR members given as host (row_ptr, col) graphs and int8
+    compartments."""
+    num_s = np.array([int((np.asarray(st) == 0).sum()) for st in init_states], dtype=np.int64)
+    num_i = np.array([int((np.asarray(st) == 1).sum()) for st in init_states], dtype=np.int64)
+    n = np.array([len(rp) - 1 for rp, _ in graphs], dtype=np.int64)
+    return predicted_costs(n, num_s, num_i, betas, gammas,
+                           excess_degrees([rp for rp, _ in graphs]), steps)
+
+
 class SIRBatch:
     """A fixed set of SIR instances packed into device buffers.
 
@@ -252,10 +308,13 @@ class SIRBatch:
         self._graph_steps = None
         self._from_states = False  # the next resident run builds its words from state8
         self._words0_stale = False  # inputs were loaded after the step-0 words were saved
-        # resident path: instances largest first, one change list per resident CTA
+        # resident path: instances longest first by predicted time (mean-field cost model),
+        # one change list per resident CTA
         L = _lib.load()
         self.max_n = int(self.n.max())
-        self.order = torch.from_numpy(np.argsort(-self.n, kind="stable").astype(np.int32)).to(dev)
+        self.cost = predicted_costs(self.n, sizes[:, 0], sizes[:, 1], betas, gammas,
+                                    excess_degrees([rp for rp, _ in graphs]), self.steps)
+        self.order = torch.from_numpy(np.argsort(-self.cost, kind="stable").astype(np.int32)).to(dev)
         self.res_grid = int(L.abm_sir_resident_grid(self.max_n)) if resident is not False else 0
         self.resident_ok = self.res_grid > 0
         if resident and not self.resident_ok:
@@ -328,8 +387,8 @@ class SIRBatch:
 
     def _chunk_plan(self, chunks):
         """Index ranges of the overlapped host run (a small first range, so the kernels
-        start early, then ranges of growing byte counts), each with its own order (largest
-        instance first), resident grid, scratch and stream."""
+        start early, then ranges of growing byte counts), each with its own order (longest
+        predicted time first), resident grid, scratch and stream."""
         if getattr(self, "_chunks", None) is not None:
             if self._chunks[0] == chunks:
                 return self._chunks[1]
@@ -340,7 +399,7 @@ class SIRBatch:
         L = _lib.load()
         dev = self.row_ptr.device
         bounds = chunk_ranges(4 * (self.n + 1) + 4 * self.e + self.n, chunks)
-        order = np.concatenate([a + np.argsort(-self.n[a:b], kind="stable")
+        order = np.concatenate([a + np.argsort(-self.cost[a:b], kind="stable")
                                 for a, b in bounds]).astype(np.int32)
         d_order = torch.from_numpy(order).to(dev)
         plan = []
@@ -363,7 +422,7 @@ class SIRBatch:
         landed, while the later ranges are still being copied; with ``h_counts`` (page-
         locked, laid out like ``counts``) each range's counts are copied back as soon as it
         finishes.  Launches of different ranges share the GPU, so order the instances
-        largest first for the shortest run.  Returns after enqueueing; the results equal
+        longest first (:func:`member_costs`) for the shortest run.  Returns after enqueueing; the results equal
         :meth:`load_host` followed by :meth:`run`."""
         if self.mode != "resident":
             raise ValueError("run_from_host needs the resident path")

@@ -89,3 +89,33 @@ def test_chunk_ranges_cover_in_order():
             first = nbytes[r[0][0]:r[0][1]].sum() / nbytes.sum()
             assert first <= 2.0 / (1 << (chunks - 1)) + nbytes[0] / nbytes.sum()
     assert chunk_ranges([], 4) == []
+
+
+def test_excess_degrees():
+    """<k^2>/<k> - 1: k - 1 on a k-regular graph; on a star (centre degree n-1, n-1 leaves
+    of degree 1) ((n-1)^2 + (n-1)) / (2(n-1)) - 1 = n/2 - 1; 0 without edges."""
+    n, k = 64, 6
+    rp = np.arange(n + 1, dtype=np.int32) * k
+    star = np.concatenate([[0, n - 1], n - 1 + np.arange(1, n)]).astype(np.int32)
+    e = ensemble.excess_degrees([rp, star, np.zeros(5, np.int32)])
+    assert e[0] == pytest.approx(k - 1)
+    assert e[1] == pytest.approx(n / 2 - 1)
+    assert e[2] == 0.0
+
+
+def test_predicted_costs_order_members():
+    """The resident path's member order: no infected agent costs nothing; at equal
+    parameters a larger member costs more; a slow epidemic on a small graph outlasts (and
+    out-costs) a quick one on a graph six times larger."""
+    n = np.array([10_000, 20_000, 5_000, 30_000, 5_000])
+    num_i = np.array([10, 20, 5, 30, 0])
+    num_s = n - num_i
+    beta = np.array([0.05, 0.05, 0.011, 0.2, 0.05])
+    gamma = np.array([0.1, 0.1, 0.067, 0.3, 0.1])
+    k = np.full(5, 20.0)
+    c = ensemble.predicted_costs(n, num_s, num_i, beta, gamma, k, 365)
+    assert c[4] == 0.0
+    assert c[1] > c[0] > 0
+    assert c[2] > c[3]
+    # at least one active step's fixed cost for every member with an infected agent
+    assert np.all(c[:4] >= ensemble.STEP_COST_ENTRIES)
