@@ -1239,6 +1239,26 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       for (int k = threadIdx.x; k < npad / 16; k += kResThreads)
         reinterpret_cast<uint4*>(sw)[k] = reinterpret_cast<const uint4*>(I->words)[k];
     }
+    // row offsets staged in shared memory after the words where they fit (the smaller
+    // members of a batch): the row lookups of every step are then shared-memory loads
+    const bool staged = npad + 4 * (n + 1) <= max_bytes;
+    const int32_t* srp = reinterpret_cast<const int32_t*>(sw + npad);
+    if (staged) {
+      for (int k0 = threadIdx.x; k0 <= n; k0 += 4 * kResThreads) {
+        int32_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = k0 + kResThreads * u;
+          v[u] = k <= n ? __ldg(rp + k) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = k0 + kResThreads * u;
+          if (k <= n) reinterpret_cast<int32_t*>(sw + npad)[k] = v[u];
+        }
+      }
+    }
+    auto row_at = [&](int k) { return staged ? srp[k] : __ldcs(rp + k); };
     if (threadIdx.x == 0) {
       const uint2 rng = make_uint2(I->rng[0], I->rng[1]);
       const uint2 c = step_key_of(I, t_begin, rng);
@@ -1344,16 +1364,16 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       int es_nxt = s_entry(r_nxt), ei_nxt = i_entry(r_nxt);
       int a_cur = 0, b_cur = 0;
       if (es_cur >= 0) {
-        a_cur = __ldcs(rp + es_cur);
-        b_cur = __ldcs(rp + es_cur + 1);
+        a_cur = row_at(es_cur);
+        b_cur = row_at(es_cur + 1);
       }
       while (r_cur < rounds) {
         const int e = es_cur, ei = ei_cur;
         const int ra = a_cur, rb = b_cur;
         a_cur = b_cur = 0;
         if (es_nxt >= 0) {
-          a_cur = __ldcs(rp + es_nxt);
-          b_cur = __ldcs(rp + es_nxt + 1);
+          a_cur = row_at(es_nxt);
+          b_cur = row_at(es_nxt + 1);
         }
         r_cur = r_nxt;
         es_cur = es_nxt;
@@ -1524,8 +1544,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
           const int a = static_cast<int>(e >> 2);
           sw_add(sw, a, 1u);
           up = (e & 3u) == kI;
-          r0 = __ldcs(rp + a);
-          len = __ldcs(rp + a + 1) - r0;
+          r0 = row_at(a);
+          len = row_at(a + 1) - r0;
         }
         my_pushed += len;
         push_rows_shared(adj, sw, hubs, up, r0, len, lane);
