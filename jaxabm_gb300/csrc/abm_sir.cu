@@ -988,7 +988,9 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // order, from a queue counter) and runs all of its steps with the instance's words in
 // shared memory: the sweep reads them there, decisions read the neighbours' compartments
 // there, and count updates are shared-memory atomics.  Only CSR rows, row offsets and hub
-// counts come from global memory.  A step is three phases separated by __syncthreads:
+// counts come from global memory, and the row offsets of a member whose words leave room
+// for them are staged in shared memory too.  A step is three phases separated by
+// __syncthreads:
 //   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
 //             the susceptible agents with infected neighbours and the infected agents to
 //             two lists (their first entries in shared memory after the words, as many as
@@ -1010,7 +1012,9 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // (hub marks, column hub tags, initial counts) instead of reading packed words.  The
 // words are written back, with the 2-bit compartment copy, when the instance's steps of
 // the call are done.
-// No CTA waits on another; the results equal the grid path's (integer atomics commute).
+// The host orders the members longest first by a predicted device time; the order never
+// changes results.  No CTA waits on another; the results equal the grid path's (integer
+// atomics commute).
 constexpr int kResThreads = 512;
 constexpr int kResChunk = 1024;  // agents per warp chunk, 32 per lane
 
