@@ -358,7 +358,8 @@ ABM_API int abm_sir_steps(abm_sir_instance* insts, int32_t ninst, const abm_work
  * compartments there, count updates are shared-memory atomics); no per-step launches.
  * abm_sir_resident_max_agents: largest instance (agents) it can hold on the current device
  * (0 without a device).  abm_sir_resident_grid: resident CTAs for instances of up to
- * max_agents agents (also sets the kernel's shared-memory opt-in; call it before capturing
+ * max_agents agents (also sets the kernel's shared-memory opt-in, which covers the words
+ * and the lists' first entries kept in shared memory; call it before capturing
  * abm_sir_steps_resident into a CUDA graph); 0 if they do not fit.
  * abm_sir_resident_scratch_bytes: scratch of abm_sir_steps_resident (a queue counter and, per
  * CTA, three lists of max_agents entries: changes, susceptible candidates, infected agents). */
@@ -368,8 +369,9 @@ ABM_API size_t abm_sir_resident_scratch_bytes(int32_t max_agents, int32_t grid);
 
 /* Same contract as abm_sir_steps (nsteps steps of every instance with t < steps, identical
  * results) on the resident path: CTAs take instances in the order order[0..ninst) (device
- * int32, NULL for index order; largest first balances best) and run each for
- * min(nsteps, steps - t) steps.  Every instance must have n <= max_agents; one that does
+ * int32, NULL for index order; longest running first balances best -- SIRBatch predicts
+ * each instance's time from its size, excess degree and beta/gamma -- and the order never
+ * changes results) and run each for min(nsteps, steps - t) steps.  Every instance must have n <= max_agents; one that does
  * not is left untouched and ORs ABM_SIR_STATUS_OVERSIZE into *status (device int32,
  * zeroed by the caller).  grid
  * from abm_sir_resident_grid(max_agents); scratch 256-byte aligned.
