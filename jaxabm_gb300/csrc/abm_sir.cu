@@ -200,9 +200,9 @@ __device__ __forceinline__ void sweep_flags(const uint32_t (&q)[4 * kVecs], unsi
 }
 
 // Clears from need_s the susceptible hubs (bits of hub_s) whose count in hubs[] (agent j at
-// hubs[j]) is not positive: a hub needs a decision only with infected neighbours.  Four
-// counts are read at a time, through L2 (the counts change under atomics of this launch on
-// the resident path).
+// hubs[j]) is not positive: a hub needs a decision only with infected neighbours (the grid
+// path's sweep; its candidates kernel draws at every slot of a long row first, so an idle
+// hub would cost a whole row of draws there).  Four counts are read at a time, through L2.
 __device__ __forceinline__ unsigned drop_idle_hubs(unsigned need_s, unsigned hub_s,
                                                    const int32_t* hubs) {
   while (hub_s) {
@@ -992,9 +992,10 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // for them are staged in shared memory too.  A step is three phases separated by
 // __syncthreads:
 //   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
-//             the susceptible agents with infected neighbours and the infected agents to
-//             two lists (their first entries in shared memory after the words, as many as
-//             fit without lowering the CTAs per SM; the rest in the CTA's global scratch,
+//             the susceptible agents with infected neighbours (and every susceptible hub,
+//             whose count only its decision reads) and the infected agents to two lists
+//             (their first entries in shared memory after the words, as many as fit
+//             without lowering the CTAs per SM; the rest in the CTA's global scratch,
 //             L2-resident).
 //   decide    warps take paired rounds from a round counter, so that every warp has work
 //             however small the instance: per lane one susceptible agent (rows longer
@@ -1311,9 +1312,10 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             for (int z = 0; z < 4; ++z) qw[4 * v + z] = 0x02020202u;  // beyond the agents: R
           }
         }
+        // every susceptible hub is listed (its count is read by its decision, which scans
+        // nothing when the count is 0): cheaper here than reading the hub counts
         unsigned need_s, need_i, hub_s;
         sweep_flags(qw, need_s, need_i, hub_s);
-        need_s = drop_idle_hubs(need_s, hub_s, hubs + base);
         const int ms = __popc(need_s), mi = __popc(need_i);
         my_cands += ms + mi;
         // one list position per agent: warp prefix sums, one counter atomic per warp
