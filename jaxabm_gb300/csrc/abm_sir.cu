@@ -66,7 +66,8 @@ constexpr int kTile = kSirThreads * kPerThread;    // 8192 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr int kHeavyUnroll = 4;                    // slots per lane per pass of a warp row scan
 constexpr int kDrawFirstDeg = 96;                  // rows longer than this draw before reading
-constexpr int kChunk = 8;                          // row slots per scan pass
+constexpr int kChunk = 8;                          // row slots per scan pass (grid path)
+constexpr int kResScan = 5;                        // row slots per scan pass (resident path)
 constexpr int kHubDeg = 63;                        // degree from which a count is a hub count
 constexpr uint32_t kHubMark = 63;                  // count field of a hub's word
 constexpr uint32_t kTag = 0x80000000u;             // column entry of a hub neighbour
@@ -1395,9 +1396,9 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         bool infected = false;
         const bool heavy = deg > kHeavyDeg;
         unsigned imask = 0;
-        int nb[kChunk];
+        int nb[kResScan];
 #pragma unroll
-        for (int z = 0; z < kChunk; ++z)
+        for (int z = 0; z < kResScan; ++z)
           nb[z] = !heavy && z < deg ? static_cast<int>(ld_col(adj, row0 + z) & kIdx) : -1;
         // infected entry: recovery draw
         bool rec = false;
@@ -1416,20 +1417,22 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
           if (!heavy) {
             int seen = 0;
 #pragma unroll
-            for (int z = 0; z < kChunk; ++z) {
+            for (int z = 0; z < kResScan; ++z) {
               const bool inf = nb[z] >= 0 && (sw[nb[z]] & 3u) == kI;
               imask |= static_cast<unsigned>(inf) << z;
               seen += inf;
             }
-            int k1 = kChunk;
-            for (; k1 < deg && seen < cnt; k1 += kChunk) {
+            int k1 = kResScan;
+            for (; k1 < deg && seen < cnt; k1 += kResScan) {
 #pragma unroll
-              for (int z = 0; z < kChunk; ++z)
+              for (int z = 0; z < kResScan; ++z)
                 nb[z] = k1 + z < deg ? static_cast<int>(ld_col(adj, row0 + k1 + z) & kIdx) : -1;
 #pragma unroll
-              for (int z = 0; z < kChunk; ++z) {
+              for (int z = 0; z < kResScan; ++z) {
                 const bool inf = nb[z] >= 0 && (sw[nb[z]] & 3u) == kI;
-                imask |= static_cast<unsigned>(inf) << (k1 + z);
+                // slots past the row (k1 + z may reach 34 for a 32-slot row) are never
+                // infected; the mask keeps their shift defined
+                imask |= static_cast<unsigned>(inf) << ((k1 + z) & 31);
                 seen += inf;
               }
             }
