@@ -65,6 +65,7 @@ constexpr int kSub = 32 * kPerThread;              // 1024 agents per warp and t
 constexpr int kTile = kSirThreads * kPerThread;    // 8192 agents per work item
 constexpr int kHeavyDeg = 32;
 constexpr int kHeavyUnroll = 4;                    // slots per lane per pass of a warp row scan
+constexpr int kResHeavyUnroll = 2;                 // the same on the resident path
 constexpr int kDrawFirstDeg = 96;                  // rows longer than this draw before reading
 constexpr int kChunk = 8;                          // row slots per scan pass (grid path)
 constexpr int kResScan = 5;                        // row slots per scan pass (resident path)
@@ -1466,23 +1467,23 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
           int remaining = __shfl_sync(kFull, cnt, src);
           const uint2 hk = make_uint2(__shfl_sync(kFull, kinf.x, src),
                                       __shfl_sync(kFull, kinf.y, src));
-          // the whole row is scanned (the warp reads 32 x kHeavyUnroll columns per pass
+          // the whole row is scanned (the warp reads 32 x kResHeavyUnroll columns per pass
           // and draws only at infected slots): on the resident kernel this beats drawing
           // at every slot first, which the grid path does for rows longer than
           // kDrawFirstDeg
           bool fired = false;
           int cpos = 0;
-          for (; cpos < hdeg && !fired && remaining > 0; cpos += 32 * kHeavyUnroll) {
-            uint32_t wv[kHeavyUnroll];
+          for (; cpos < hdeg && !fired && remaining > 0; cpos += 32 * kResHeavyUnroll) {
+            uint32_t wv[kResHeavyUnroll];
 #pragma unroll
-            for (int u = 0; u < kHeavyUnroll; ++u) {
+            for (int u = 0; u < kResHeavyUnroll; ++u) {
               const int slot = cpos + 32 * u + lane;
               wv[u] = slot < hdeg ? ld_col(adj, hrow + slot) : kTag;
             }
             bool hit = false;
             int seen = 0;
 #pragma unroll
-            for (int u = 0; u < kHeavyUnroll; ++u) {
+            for (int u = 0; u < kResHeavyUnroll; ++u) {
               const int slot = cpos + 32 * u + lane;
               if (slot < hdeg && (sw[wv[u] & kIdx] & 3u) == kI) {
                 ++seen;
