@@ -444,3 +444,29 @@ def test_sir_run_from_host_needs_the_resident_path(cuda):
     b = ensemble.SIRBatch(g, st, [0.1], [0.1], [1], 10, resident=False)
     with pytest.raises(ValueError):
         b.run_from_host(torch.zeros(1), torch.zeros(1), torch.zeros(1))
+
+
+def test_sir_resident_member_order_never_changes_results(cuda):
+    """The resident kernel takes members in the batch's order (longest predicted time
+    first); any other order -- reversed, shuffled -- gives bit-identical counts and final
+    compartments, since each member runs alone on its CTA."""
+    from jaxabm_gb300 import ensemble
+    spec = ensemble.ensemble_spec(4096)
+    idx = list(range(0, 4096, 97))
+    sub = {k: v[idx] for k, v in spec.items()}
+    graphs, inits = ensemble.build_instances(sub)
+    b = ensemble.SIRBatch(graphs, inits, sub["beta"], sub["gamma"], sub["seed"], 365,
+                          resident=True)
+    order0 = b.order.cpu().numpy()
+    assert np.array_equal(order0, np.argsort(-b.cost, kind="stable"))
+    b.run()
+    ref_counts = b.counts.cpu().numpy().copy()
+    ref_states = [b.final_state(k).cpu().numpy().copy() for k in range(len(idx))]
+    rs = np.random.RandomState(5)
+    for order in (order0[::-1], rs.permutation(len(idx))):
+        b.order.copy_(torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)))
+        b.reset()
+        b.run()
+        assert np.array_equal(b.counts.cpu().numpy(), ref_counts)
+        for k in range(len(idx)):
+            assert np.array_equal(b.final_state(k).cpu().numpy(), ref_states[k])
