@@ -171,9 +171,11 @@ def chunk_ranges(nbytes, chunks):
 
 
 # Fixed cost of one step of a member on the resident path (its three barriers and the
-# dependent loads of its phases), counted in list entries: fitted per-member device times
-# give ~10 us per active step and a few hundredths of a microsecond per list entry.
-STEP_COST_ENTRIES = 256
+# dependent loads of its phases), counted in list entries: per-member device times give
+# ~10 us per active step against ~10 ns of CTA time per list entry, and replays of the
+# 4,096-member ensemble are fastest with 4,096-16,384 here (65,536 puts large members too
+# late and is slower than ordering by size).
+STEP_COST_ENTRIES = 4096
 
 
 def excess_degrees(row_ptrs):
