@@ -1265,7 +1265,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
       }
     }
-    auto row_at = [&](int k) { return staged ? srp[k] : __ldcs(rp + k); };
+    // (row offsets not staged are read through L1: neighbouring entries share lines)
+    auto row_at = [&](int k) { return staged ? srp[k] : __ldca(rp + k); };
     if (threadIdx.x == 0) {
       const uint2 rng = make_uint2(I->rng[0], I->rng[1]);
       const uint2 c = step_key_of(I, t_begin, rng);
