@@ -1097,14 +1097,15 @@ __device__ __forceinline__ void push_rows_shared(const int32_t* __restrict__ adj
 }
 
 // Entry k of a CTA list: the first scap entries are in shared memory (sl), the rest in the
-// CTA's global list (gl, indexed from 0 like the shared part).
+// CTA's global list (gl, indexed from 0 like the shared part; streaming stores and loads,
+// which leave the small L1 to row offsets and columns).
 __device__ __forceinline__ void list_put(uint32_t* sl, uint32_t* gl, int scap, int k, uint32_t v) {
   if (k < scap) sl[k] = v;
-  else gl[k] = v;
+  else __stcs(gl + k, v);
 }
 __device__ __forceinline__ uint32_t list_get(const uint32_t* sl, const uint32_t* gl, int scap,
                                              int k) {
-  return k < scap ? sl[k] : gl[k];
+  return k < scap ? sl[k] : __ldcs(gl + k);
 }
 
 // Appends (agent << 2 | new compartment) of the lanes with `changed` to the change list.
