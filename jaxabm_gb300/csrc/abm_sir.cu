@@ -1108,19 +1108,23 @@ __device__ __forceinline__ uint32_t list_get(const uint32_t* sl, const uint32_t*
   return k < scap ? sl[k] : __ldcs(gl + k);
 }
 
-// Appends (agent << 2 | new compartment) of the lanes with `changed` to the change list.
-__device__ __forceinline__ void res_record(bool changed, int agent, uint32_t comp_new,
-                                           uint32_t* s_changes, uint32_t* changes, int scap,
-                                           int* count, int lane) {
-  const unsigned m = __ballot_sync(kFull, changed);
-  if (!m) return;
-  int base = 0;
-  const int leader = __ffs(m) - 1;
-  if (lane == leader) base = atomicAdd(count, __popc(m));
-  base = __shfl_sync(kFull, base, leader);
-  if (changed)
-    list_put(s_changes, changes, scap, base + __popc(m & ((1u << lane) - 1u)),
-             (static_cast<uint32_t>(agent) << 2) | comp_new);
+// Appends (agent << 2 | new compartment) of the round's changes to the change list, the
+// recoveries (lanes with rec, agent ei) then the infections (lanes with inf, agent e),
+// with one counter atomic per warp.
+__device__ __forceinline__ void res_record(bool rec, int ei, bool inf, int e, uint32_t* s_changes,
+                                           uint32_t* changes, int scap, int* count, int lane) {
+  const unsigned m1 = __ballot_sync(kFull, rec), m2 = __ballot_sync(kFull, inf);
+  if (!(m1 | m2)) return;
+  const int c1 = __popc(m1);
+  int at = 0;
+  if (lane == 0) at = atomicAdd(count, c1 + __popc(m2));
+  at = __shfl_sync(kFull, at, 0);
+  const unsigned below = (1u << lane) - 1u;
+  if (rec)
+    list_put(s_changes, changes, scap, at + __popc(m1 & below), (static_cast<uint32_t>(ei) << 2) | 2u);
+  if (inf)
+    list_put(s_changes, changes, scap, at + c1 + __popc(m2 & below),
+             (static_cast<uint32_t>(e) << 2) | kI);
 }
 
 __global__ void __launch_bounds__(kResThreads, 2)
@@ -1295,7 +1299,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         S.next_group = 0;
       }
       // ---- sweep: lists of susceptible agents with infected neighbours, infected agents
-      unsigned long long my_cands = 0;
+      int my_cands = 0;
       for (;;) {
         int c = 0;
         if (lane == 0) c = atomicAdd(&S.next_chunk, 1);
@@ -1336,9 +1340,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         for (unsigned m = need_s; m; m &= m - 1) list_put(s_slist, slist, scap, bs++, base + __ffs(m) - 1);
         for (unsigned m = need_i; m; m &= m - 1) list_put(s_ilist, ilist, scap, bi++, base + __ffs(m) - 1);
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) my_cands += __shfl_down_sync(kFull, my_cands, o);
-      if (lane == 0 && my_cands) atomicAdd(&S.cands, my_cands);
+      my_cands = __reduce_add_sync(kFull, my_cands);
+      if (lane == 0 && my_cands) atomicAdd(&S.cands, static_cast<unsigned long long>(my_cands));
       __syncthreads();
       // ---- decide: paired rounds taken from a round counter -----------------------------
       // Round p holds susceptible entries 32p..32p+31 and infected entries 32p..32p+31, one
@@ -1354,7 +1357,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       const uint2 coll = make_uint2(S.coll0, S.coll1);
       const int ns = S.ns, ni = S.ni;
       const int rounds = max((ns + 31) >> 5, (ni + 31) >> 5);
-      unsigned long long my_scanned = 0;
+      int my_scanned = 0;
       int my_si = 0, my_ir = 0, my_draws = 0;
       auto take = [&]() {
         int r = 0;
@@ -1505,18 +1508,16 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         }
         my_scanned += scanned;
         my_si += infected;
-        res_record(rec, ei, 2u, s_changes, changes, scap, &S.nchanges, lane);
-        res_record(infected, e, kI, s_changes, changes, scap, &S.nchanges, lane);
+        res_record(rec, ei, infected, e, s_changes, changes, scap, &S.nchanges, lane);
       }
       my_si = __reduce_add_sync(kFull, my_si);
       my_ir = __reduce_add_sync(kFull, my_ir);
       my_draws = __reduce_add_sync(kFull, my_draws);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) my_scanned += __shfl_down_sync(kFull, my_scanned, o);
+      my_scanned = __reduce_add_sync(kFull, my_scanned);
       if (lane == 0) {
         if (my_si) atomicAdd(&S.si, my_si);
         if (my_ir) atomicAdd(&S.ir, my_ir);
-        if (my_scanned) atomicAdd(&S.scanned, my_scanned);
+        if (my_scanned) atomicAdd(&S.scanned, static_cast<unsigned long long>(my_scanned));
         if (my_draws) atomicAdd(&S.draws, static_cast<unsigned long long>(my_draws));
       }
       __syncthreads();
