@@ -1032,6 +1032,7 @@ struct ResState {
   int num_s, num_i, num_r;
   uint32_t rng0, rng1, coll0, coll1;
   unsigned long long scanned, pushed, cands, draws;
+  uint32_t st_scanned, st_pushed, st_cands, st_draws;  // this step's, folded by thread 0
 };
 
 // First lane whose inclusive prefix sum `incl` exceeds f (f below the warp total), by a
@@ -1287,6 +1288,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       S.nchanges = 0;
       S.next_chunk = S.next_round = S.next_group = 0;
       S.scanned = S.pushed = S.cands = S.draws = 0;
+      S.st_scanned = S.st_pushed = S.st_cands = S.st_draws = 0;
     }
     __syncthreads();
     const int nchunks = (n + kResChunk - 1) / kResChunk;
@@ -1297,6 +1299,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       if (threadIdx.x == 0) {
         S.nchanges = 0;
         S.next_group = 0;
+        S.pushed += S.st_pushed;
+        S.st_pushed = 0;
       }
       // ---- sweep: lists of susceptible agents with infected neighbours, infected agents
       int my_cands = 0;
@@ -1341,7 +1345,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         for (unsigned m = need_i; m; m &= m - 1) list_put(s_ilist, ilist, scap, bi++, base + __ffs(m) - 1);
       }
       my_cands = __reduce_add_sync(kFull, my_cands);
-      if (lane == 0 && my_cands) atomicAdd(&S.cands, static_cast<unsigned long long>(my_cands));
+      if (lane == 0 && my_cands) atomicAdd(&S.st_cands, static_cast<uint32_t>(my_cands));
       __syncthreads();
       // ---- decide: paired rounds taken from a round counter -----------------------------
       // Round p holds susceptible entries 32p..32p+31 and infected entries 32p..32p+31, one
@@ -1517,8 +1521,8 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       if (lane == 0) {
         if (my_si) atomicAdd(&S.si, my_si);
         if (my_ir) atomicAdd(&S.ir, my_ir);
-        if (my_scanned) atomicAdd(&S.scanned, static_cast<unsigned long long>(my_scanned));
-        if (my_draws) atomicAdd(&S.draws, static_cast<unsigned long long>(my_draws));
+        if (my_scanned) atomicAdd(&S.st_scanned, static_cast<uint32_t>(my_scanned));
+        if (my_draws) atomicAdd(&S.st_draws, static_cast<uint32_t>(my_draws));
       }
       __syncthreads();
       // ---- apply: groups of 32 changes, taken from a group counter ------------------------
@@ -1538,6 +1542,10 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         S.si = S.ir = 0;
         S.ns = S.ni = 0;
         S.next_round = 0;
+        S.scanned += S.st_scanned;
+        S.cands += S.st_cands;
+        S.draws += S.st_draws;
+        S.st_scanned = S.st_cands = S.st_draws = 0;
         S.rng0 = next_rng.x;
         S.rng1 = next_rng.y;
         S.coll0 = next_coll.x;
@@ -1564,7 +1572,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         push_rows_shared(adj, sw, hubs, up, r0, len, lane);
       }
       my_pushed = __reduce_add_sync(kFull, my_pushed);
-      if (lane == 0 && my_pushed) atomicAdd(&S.pushed, static_cast<unsigned long long>(my_pushed));
+      if (lane == 0 && my_pushed) atomicAdd(&S.st_pushed, static_cast<uint32_t>(my_pushed));
       __syncthreads();
     }
     // steps without an infected agent: constant counts, the key chain still advances
@@ -1607,7 +1615,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       I->step_si = 0;
       I->step_ir = 0;
       I->edges_scanned += S.scanned;
-      I->edges_pushed += S.pushed;
+      I->edges_pushed += S.pushed + S.st_pushed;
       I->candidates += S.cands;
       I->draws += S.draws;
       if (t_end == I->steps && I->done_flag) {
