@@ -993,7 +993,7 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 // counts come from global memory, and the row offsets of a member whose words leave room
 // for them are staged in shared memory too.  A step is three phases separated by
 // __syncthreads:
-//   sweep     warps take 1024-agent chunks of the words from a chunk counter and append
+//   sweep     warp w takes the 1024-agent chunks w, w + 16, ... of the words and appends
 //             the susceptible agents with infected neighbours (and every susceptible hub,
 //             whose count only its decision reads) and the infected agents to two lists
 //             (their first entries in shared memory after the words, as many as fit
@@ -1023,7 +1023,6 @@ constexpr int kResChunk = 1024;  // agents per warp chunk, 32 per lane
 
 struct ResState {
   int inst;        // queue position taken by the CTA
-  int next_chunk;  // chunk counter of the step's sweep
   int next_round;  // round counter of the step's decisions
   int next_group;  // group counter of the step's count updates
   int ns, ni;      // entries in the candidate and infected lists
@@ -1286,7 +1285,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       S.si = S.ir = 0;
       S.ns = S.ni = 0;
       S.nchanges = 0;
-      S.next_chunk = S.next_round = S.next_group = 0;
+      S.next_round = S.next_group = 0;
       S.scanned = S.pushed = S.cands = S.draws = 0;
       S.st_scanned = S.st_pushed = S.st_cands = S.st_draws = 0;
     }
@@ -1304,11 +1303,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       }
       // ---- sweep: lists of susceptible agents with infected neighbours, infected agents
       int my_cands = 0;
-      for (;;) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(&S.next_chunk, 1);
-        c = __shfl_sync(kFull, c, 0);
-        if (c >= nchunks) break;
+      for (int c = static_cast<int>(threadIdx.x >> 5); c < nchunks; c += kResThreads / 32) {
         const int base = c * kResChunk + 32 * lane;
         uint32_t qw[8];
 #pragma unroll
@@ -1354,7 +1349,6 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       // and row offsets one round ahead.
       uint2 next_rng = make_uint2(0, 0), next_coll = make_uint2(0, 0);
       if (threadIdx.x == 0) {
-        S.next_chunk = 0;  // the sweep is over
         next_rng = abm::split_at(make_uint2(S.rng0, S.rng1), 0);
         if (t + 1 < I->steps) next_coll = step_key_of(I, t + 1, next_rng);
       }
