@@ -1347,11 +1347,6 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
       // of each per lane: the infected entry's recovery chain and the susceptible entry's
       // key derivation run while its row is in flight.  Entries are loaded two rounds ahead
       // and row offsets one round ahead.
-      uint2 next_rng = make_uint2(0, 0), next_coll = make_uint2(0, 0);
-      if (threadIdx.x == 0) {
-        next_rng = abm::split_at(make_uint2(S.rng0, S.rng1), 0);
-        if (t + 1 < I->steps) next_coll = step_key_of(I, t + 1, next_rng);
-      }
       const uint2 coll = make_uint2(S.coll0, S.coll1);
       const int ns = S.ns, ni = S.ni;
       const int rounds = max((ns + 31) >> 5, (ni + 31) >> 5);
@@ -1540,6 +1535,9 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         S.cands += S.st_cands;
         S.draws += S.st_draws;
         S.st_scanned = S.st_cands = S.st_draws = 0;
+        const uint2 next_rng = abm::split_at(make_uint2(S.rng0, S.rng1), 0);
+        uint2 next_coll = make_uint2(0, 0);
+        if (t + 1 < I->steps) next_coll = step_key_of(I, t + 1, next_rng);
         S.rng0 = next_rng.x;
         S.rng1 = next_rng.y;
         S.coll0 = next_coll.x;
