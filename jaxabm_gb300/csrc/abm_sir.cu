@@ -1008,8 +1008,8 @@ __global__ void sir_setup_single_kernel(abm_sir_instance* d, int4* work, int nti
 //   apply     warps take groups of 32 changes: +1 on each changed agent's compartment
 //             field and +-1 on its neighbours' counts (push of the concatenated rows);
 //             meanwhile thread 0 records the step's S/I/R counts and advances the keys.
-// Rounds are taken two ahead, so that the list entries and row offsets of the next
-// rounds are in flight while one is decided.  Draws compare the 23 random mantissa bits
+// In steps with more rounds than warps, rounds are taken two ahead, so that the list
+// entries and row offsets of the next rounds are in flight while one is decided.  Draws compare the 23 random mantissa bits
 // with an integer threshold, which equals the float comparison of jax.random.uniform.
 // An instance at step 0 may build its words in the kernel from the int8 compartments
 // (hub marks, column hub tags, initial counts) instead of reading packed words.  The
@@ -1365,7 +1365,10 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         const int f = 32 * r + lane;
         return r < rounds && f < ni ? static_cast<int>(list_get(s_ilist, ilist, scap, f)) : -1;
       };
-      int r_cur = take(), r_nxt = take();
+      // rounds are taken one ahead only when there are more rounds than warps: with fewer,
+      // a warp holding two rounds would leave another warp without one
+      const bool ahead = rounds > kResThreads / 32;
+      int r_cur = take(), r_nxt = ahead ? take() : rounds;
       int es_cur = s_entry(r_cur), ei_cur = i_entry(r_cur);
       int es_nxt = s_entry(r_nxt), ei_nxt = i_entry(r_nxt);
       int a_cur = 0, b_cur = 0;
@@ -1384,7 +1387,7 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         r_cur = r_nxt;
         es_cur = es_nxt;
         ei_cur = ei_nxt;
-        r_nxt = take();
+        r_nxt = ahead ? take() : rounds;
         es_nxt = s_entry(r_nxt);
         ei_nxt = i_entry(r_nxt);
         // susceptible entry (a susceptible agent with infected neighbours): the first
