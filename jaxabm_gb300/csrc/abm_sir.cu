@@ -1366,7 +1366,9 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
         return r < rounds && f < ni ? static_cast<int>(list_get(s_ilist, ilist, scap, f)) : -1;
       };
       // rounds are taken one ahead only when there are more rounds than warps: with fewer,
-      // a warp holding two rounds would leave another warp without one
+      // a warp holding two rounds would leave another warp without one.  Without taking
+      // ahead each warp takes exactly one round index (0..15 over the 16 warps), which
+      // covers every round only because the threshold is the warp count.
       const bool ahead = rounds > kResThreads / 32;
       int r_cur = take(), r_nxt = ahead ? take() : rounds;
       int es_cur = s_entry(r_cur), ei_cur = i_entry(r_cur);
