@@ -1443,19 +1443,15 @@ sir_resident_kernel(abm_sir_instance* __restrict__ insts, int ninst,
             scanned = min(k1, deg);
           }
         }
-        // draws at the infected slots in row order, two per pass; the first that fires
+        // draws at the infected slots in row order, one per pass; the first that fires
         // infects (the outcome is the OR over the slots, the count is the sequential one)
         while (__any_sync(kFull, imask != 0)) {
           if (imask) {
             const int s1 = __ffs(imask) - 1;
             imask &= imask - 1;
-            const bool two = imask != 0;
-            const int s2 = two ? __ffs(imask) - 1 : s1;
-            if (two) imask &= imask - 1;
             const bool f1 = abm::unit_below(abm::bits_at(kinf, (uint64_t)s1), tbeta);
-            const bool f2 = two && abm::unit_below(abm::bits_at(kinf, (uint64_t)s2), tbeta);
-            my_draws += (f1 || !two) ? 1 : 2;
-            if (f1 || f2) {
+            ++my_draws;
+            if (f1) {
               infected = true;
               imask = 0;
             }
