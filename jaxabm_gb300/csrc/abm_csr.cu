@@ -148,7 +148,7 @@ csr_scatter_kernel(const int32_t* __restrict__ keys, const int32_t* __restrict__
         wcount[w][dd] = acc;
         acc += c;
       }
-      // base[dd] is read below by this round's edges before it advances
+      // base[dd] is read below by this sub-round's edges before it advances
       __syncthreads();
       if (valid) {
         const int32_t pos = base[d] + wcount[warp][d] + rank;
